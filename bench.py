@@ -1,0 +1,328 @@
+#!/usr/bin/env python
+"""Benchmark of the node-relaxation hot path on GB300.
+
+A step is one batched relaxation launch: every open B&B node of a synthetic
+batch (uneven fixings, depth-dependent FW tolerances) is relaxed by FW/DICG
+for up to --iters iterations. value = node relaxations per second with the
+batch resident in HBM; e2e = the same through the C ABI with the node data
+in pinned host memory (H2D and D2H inside the timed region).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time to certified 1e-6 gap & B&B nodes/s: batched+learned vs plain, 1 GB300"
+
+WORKLOADS = {
+    # name: (instance builder, order, nodes per batch, algorithm, line search)
+    "birkhoff_gnp36": dict(order=36, nodes=256, alg=1, ls=4, iters=100),
+    "birkhoff_regular120": dict(order=120, nodes=256, alg=1, ls=4, iters=20),
+}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def make_workload(name, nodes, rank):
+    from gpuboscia_gb300 import instances
+    w = WORKLOADS[name]
+    order = w["order"]
+    if name.startswith("birkhoff_gnp"):
+        inst = instances.birkhoff_gnp(order=order)
+    else:
+        inst = instances.birkhoff_regular_perturbed(order=order)
+    lb, ub = instances.birkhoff_node_batch(order, nodes, seed=4242 + rank)
+    rng = np.random.Generator(np.random.PCG64(77 + rank))
+    depth = rng.integers(0, 13, nodes)
+    eps = np.maximum(1e-6, 1e-3 * 0.8 ** depth)
+    return inst, lb, ub, eps
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.text = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.text, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.text, _ = self.proc.communicate()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (getattr(self, "text", "") or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(inst, lb, ub, eps, alg_kind, ls, iters, budget_s=12.0):
+    """The oracle on the machine's host cores over a bounded sample of the batch."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle as O
+    threads = os.cpu_count() or 1
+    n = lb.shape[1]
+    flags = np.ones(n, np.uint8)
+    alg = O.algorithm(alg_kind, ls)
+    count = min(len(lb), max(threads, 8))
+    t0 = time.perf_counter()
+    O.relax(inst.objective, inst.lmo, alg, lb[:count].copy(), lb[:count], ub[:count], eps[:count],
+            max_iters=iters, flags=flags, threads=threads)
+    dt = time.perf_counter() - t0
+    done = count
+    while dt < budget_s and done < len(lb):
+        c2 = min(len(lb) - done, count)
+        t1 = time.perf_counter()
+        O.relax(inst.objective, inst.lmo, alg, lb[done:done + c2].copy(), lb[done:done + c2], ub[done:done + c2],
+                eps[done:done + c2], max_iters=iters, flags=flags, threads=threads)
+        dt += time.perf_counter() - t1
+        done += c2
+    return done / dt, threads, done, dt
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the oracle port of the reference's relaxation on the host cores."""
+    if rank != 0:
+        return
+    inst, lb, ub, eps = make_workload(args.workload, args.nodes, 0)
+    w = WORKLOADS[args.workload]
+    for _ in range(args.warmup):
+        cpu_sample(inst, lb, ub, eps, w["alg"], w["ls"], args.iters, budget_s=0.0)
+    vals, times = [], []
+    for _ in range(args.steps):
+        v, threads, done, dt = cpu_sample(inst, lb, ub, eps, w["alg"], w["ls"], args.iters, budget_s=args.ref_budget)
+        vals.append(v)
+        times.append(dt)
+    value = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * statistics.mean(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_dict(args),
+            "cpu_baseline": {"value": value, "unit": "nodes/s", "cores": threads, "kind": "port",
+                             "sample": f"{done} of {args.nodes} nodes per step, {args.iters} iterations max"},
+            "e2e": {"value": value, "unit": "nodes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args):
+    w = WORKLOADS[args.workload]
+    return {"workload": args.workload, "order": w["order"], "variables": w["order"] ** 2,
+            "nodes_per_batch": args.nodes, "max_iters_per_dispatch": args.iters,
+            "algorithm": "DICG", "line_search": "quadratic_exact",
+            "precision": args.precision, "l2": "flushed between timed steps (256 MiB write)"}
+
+
+def run_gpu(args, rank, world):
+    import torch
+    from gpuboscia_gb300 import _abi as A
+    from gpuboscia_gb300 import api
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device("cuda")
+    inst, lb, ub, eps = make_workload(args.workload, args.nodes, rank)
+    w = WORKLOADS[args.workload]
+    order = w["order"]
+    N, n = lb.shape
+    prec = A.PRECISION_MIXED if args.precision == "mixed" else A.PRECISION_FP64
+    alg = A.Algorithm(w["alg"], w["ls"], 4, 1e-10, 1e-14, prec)
+    T = lambda a, t=None: torch.from_numpy(np.ascontiguousarray(a if t is None else np.asarray(a, t))).to(dev)
+    d_lb, d_ub, d_eps = T(lb), T(ub), T(eps)
+    d_flags = T(np.ones(n), np.uint8)
+    x0 = d_lb.clone()
+    x = torch.empty_like(x0)
+    it = torch.zeros(N, dtype=torch.int32, device=dev)
+    st = torch.zeros(N, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    relaxer = api.BatchRelaxer(inst.objective, inst.lmo, alg, x, d_lb, d_ub, d_eps, it, st, args.iters, d_flags,
+                               1e-6, stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        x.copy_(x0)
+        it.zero_()
+        st.zero_()
+        relaxer.launch()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            x.copy_(x0)
+            it.zero_()
+            st.zero_()
+            ev[k][0].record(stream)
+            relaxer.launch()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    times = [a.elapsed_time(b) for a, b in ev]
+    kernel_ms = sum(times) / len(times)
+    node_iters = int(it.sum().item())
+    statuses = st.cpu().numpy()
+    t_local = torch.tensor([sum(times)], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
+    total_ms = float(t_local.item())
+    value = N * args.steps * world / (total_ms / 1000.0)
+
+    # e2e through the C ABI with pinned host buffers
+    h = {k: v.pin_memory() for k, v in dict(x=torch.from_numpy(lb.copy()), lb=torch.from_numpy(lb),
+                                                 ub=torch.from_numpy(ub), eps=torch.from_numpy(eps),
+                                                 it=torch.zeros(N, dtype=torch.int32),
+                                                 st=torch.zeros(N, dtype=torch.uint8)).items()}
+    ho = {k: torch.empty(s, dtype=dt).pin_memory() for k, s, dt in
+          (("x", (N, n), torch.float64), ("gap", (N,), torch.float64), ("value", (N,), torch.float64),
+           ("bvv", (N,), torch.float64), ("bv", (N, n), torch.float64), ("it", (N,), torch.int32),
+           ("st", (N,), torch.uint8))}
+    h2d = sum(v.numel() * v.element_size() for v in h.values())
+    d2h = sum(v.numel() * v.element_size() for v in ho.values())
+
+    def e2e_step():
+        x.copy_(h["x"], non_blocking=True)
+        d_lb.copy_(h["lb"], non_blocking=True)
+        d_ub.copy_(h["ub"], non_blocking=True)
+        d_eps.copy_(h["eps"], non_blocking=True)
+        it.copy_(h["it"], non_blocking=True)
+        st.copy_(h["st"], non_blocking=True)
+        relaxer.launch()
+        ho["x"].copy_(x, non_blocking=True)
+        ho["gap"].copy_(relaxer.gap, non_blocking=True)
+        ho["value"].copy_(relaxer.value, non_blocking=True)
+        ho["bvv"].copy_(relaxer.best_vertex_val, non_blocking=True)
+        ho["bv"].copy_(relaxer.best_vertex, non_blocking=True)
+        ho["it"].copy_(it, non_blocking=True)
+        ho["st"].copy_(st, non_blocking=True)
+        stream.synchronize()
+
+    e2e_step()
+    e2e_times = []
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_local = torch.tensor([sum(e2e_times)], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(e2e_local, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = N * args.steps * world / float(e2e_local.item())
+
+    if rank != 0:
+        return
+    hbm_peak, bf16_peak, peak_kind = load_peaks()
+    grads = node_iters + N  # iterations plus the final certificate gradient of each node
+    flops = grads * 8.0 * order ** 3
+    achieved_tf = flops / (kernel_ms / 1000.0) / 1e12
+    roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": achieved_tf / bf16_peak, "traffic": None, "peak_kind": peak_kind,
+                "kernel": "relax_kernel<GRAPH_MATCHING,BIRKHOFF>",
+                "work": f"{grads} gradients x 8*{order}^3 flop per launch"}
+    cpu_v, cores, done, dt = cpu_sample(inst, lb, ub, eps, w["alg"], w["ls"], args.iters, budget_s=args.cpu_budget)
+    line = {"metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == A.PRECISION_FP64 else "bf16+f64",
+            "data": "synthetic", "config": config_dict(args),
+            "e2e": {"value": e2e_value, "unit": "nodes/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": roofline,
+            "cpu_baseline": {"value": cpu_v, "unit": "nodes/s", "cores": cores, "kind": "port",
+                             "sample": f"{done} of {N} nodes of the same batch, {args.iters} iterations max, "
+                                       f"{dt:.1f} s"},
+            "clocks": clk.summary(), "gpu_launches": args.steps,
+            "node_iterations_per_step": node_iters,
+            "status_counts": {str(s): int((statuses == s).sum()) for s in np.unique(statuses)}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="birkhoff_gnp36", choices=sorted(WORKLOADS))
+    ap.add_argument("--nodes", type=int, default=None)
+    ap.add_argument("--iters", type=int, default=None)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--ref-budget", type=float, default=8.0)
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    args.nodes = args.nodes or w["nodes"]
+    args.iters = args.iters or w["iters"]
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "gb300":
+        import torch
+        torch.distributed.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        from gpuboscia_gb300 import build
+        if rank == 0:
+            build.build()
+        if world > 1:
+            import torch
+            torch.distributed.barrier()
+        run_gpu(args, rank, world)
+    if world > 1 and args.impl == "gb300":
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

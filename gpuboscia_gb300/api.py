@@ -1,0 +1,360 @@
+"""Python mirror of the reference's public API over the C ABI.
+
+Objectives and LMOs keep their data as float64 numpy arrays and produce the C
+descriptors of include/gpuboscia_gb300.h either over host arrays (``where="host"``)
+or over device copies (``where="cuda"``, torch tensors). ``solve`` runs the whole
+branch and bound in the library (gbx_solve); ``relax_batch`` / ``lmo_batch`` /
+``node_feasible_batch`` expose the batched GPU kernels over torch tensors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _abi as A
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+class _Keep:
+    """Holds the arrays a descriptor points at."""
+
+    def __init__(self):
+        self.items = []
+
+    def ptr(self, arr, where: str):
+        if arr is None:
+            return None
+        if where == "host":
+            a = np.ascontiguousarray(arr)
+            self.items.append(a)
+            return a.ctypes.data
+        import torch
+        if isinstance(arr, torch.Tensor):
+            t = arr.contiguous()
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(arr)).to("cuda")
+        self.items.append(t)
+        return t.data_ptr()
+
+
+# ---------------------------------------------------------------- objectives
+@dataclasses.dataclass
+class DenseQuadraticObjective:
+    """f(x) = 0.5*s*x'Qx + s*l*c'x + k (GlobalCachedDenseQuadraticObjective,
+    dense_quadratic_objectives.cuh:18-112). ``Q`` is given in the usual
+    orientation; it is stored transposed for the kernel (a symmetric Q is
+    unchanged)."""
+    Q: np.ndarray
+    c: Optional[np.ndarray] = None
+    scale: float = 1.0
+    linear_scale: float = 1.0
+    constant: float = 0.0
+
+    @property
+    def n(self) -> int:
+        return int(np.asarray(self.Q).shape[0])
+
+    def to_c(self, where: str, keep: _Keep) -> A.Objective:
+        Q = _f64(self.Q)
+        o = A.Objective()
+        o.kind = A.OBJ_DENSE_QUADRATIC
+        o.n = Q.shape[0]
+        o.Q = keep.ptr(_f64(Q.T), where)
+        o.c = keep.ptr(_f64(self.c) if self.c is not None else None, where)
+        o.scale, o.linear_scale, o.constant = self.scale, self.linear_scale, self.constant
+        return o
+
+
+def ILSObjective(AtA, Atb, btb: float) -> DenseQuadraticObjective:
+    """||Ax - b||^2 from A'A, A'b, b'b (ILSGlobalCachedObjective, dense_quadratic_objectives.cuh:114-124)."""
+    return DenseQuadraticObjective(AtA, Atb, 2.0, -1.0, btb)
+
+
+@dataclasses.dataclass
+class GraphMatchingObjective:
+    """f(X) = scale*||A X - X B||_F^2 over order x order X (row-major)."""
+    A: np.ndarray
+    B: np.ndarray
+    scale: float = 1.0
+
+    @property
+    def order(self) -> int:
+        return int(np.asarray(self.A).shape[0])
+
+    @property
+    def n(self) -> int:
+        return self.order ** 2
+
+    def to_c(self, where: str, keep: _Keep) -> A.Objective:
+        o = A.Objective()
+        o.kind = A.OBJ_GRAPH_MATCHING
+        o.order = self.order
+        o.n = self.n
+        o.A = keep.ptr(_f64(self.A), where)
+        o.B = keep.ptr(_f64(self.B), where)
+        o.scale = self.scale
+        o.linear_scale = 1.0
+        return o
+
+
+# ---------------------------------------------------------------- LMOs
+@dataclasses.dataclass
+class BoxLMO:
+    supports_dicg = True
+
+    def to_c(self, n: int, where: str, keep: _Keep) -> A.LMO:
+        return A.LMO(A.LMO_BOX, n, 1.0, None, 0)
+
+    def relaxation_feasible(self, x, lb, ub, tol) -> bool:
+        return True
+
+
+@dataclasses.dataclass
+class UnitSimplexLMO:
+    right_side: float = 1.0
+    int_vars: Sequence[int] = ()
+    equality: bool = False
+    supports_dicg = True
+
+    def to_c(self, n: int, where: str, keep: _Keep) -> A.LMO:
+        flags = np.zeros(n, dtype=np.uint8)
+        for j in self.int_vars:
+            if 0 <= j < n:
+                flags[j] = 1
+        kind = A.LMO_EQUALITY_SIMPLEX if self.equality else A.LMO_SIMPLEX
+        return A.LMO(kind, n, float(self.right_side), keep.ptr(flags, where), 0)
+
+    def relaxation_feasible(self, x, lb, ub, tol) -> bool:
+        x = np.asarray(x, dtype=np.float64)
+        if self.equality:
+            return bool((x >= -tol).all() and math.isfinite(x.sum()) and abs(x.sum() - self.right_side) <= tol)
+        return bool((x >= 0).all() and x.sum() <= self.right_side + tol)
+
+
+def EqualitySimplexLMO(right_side=1.0, int_vars=()) -> UnitSimplexLMO:
+    return UnitSimplexLMO(right_side, int_vars, True)
+
+
+@dataclasses.dataclass
+class BirkhoffLMO:
+    order: int
+    supports_dicg = True
+
+    def to_c(self, n: int, where: str, keep: _Keep) -> A.LMO:
+        return A.LMO(A.LMO_BIRKHOFF, n, 1.0, None, self.order)
+
+
+# ---------------------------------------------------------------- problem / settings
+@dataclasses.dataclass
+class Problem:
+    n_vars: int
+    lb: np.ndarray
+    ub: np.ndarray
+    int_vars: Sequence[int] = ()
+
+
+@dataclasses.dataclass
+class Settings:
+    """gpuboscia::Settings + DeviceResidentConfig (gpuboscia.cuh:21-32, device_resident_solver.cuh:1004-1025)."""
+    gpu_batch_size: int = 1024
+    num_streams: int = 8
+    gpu_max_iters: int = 20000
+    gpu_eps: float = 1e-3
+    gpu_eps_decay: float = 0.8
+    gpu_eps_min: float = 1e-6
+    integer_tol: float = 1e-6
+    abs_gap_tol: float = 1e-6
+    rel_gap_tol: float = 1e-2
+    algorithm: int = A.ALG_DICG
+    line_search: int = A.LS_SECANT
+    secant_iters: int = 4
+    secant_tol: float = 1e-10
+    secant_denom_eps: float = 1e-14
+    precision: int = A.PRECISION_FP64
+    time_limit_seconds: float = math.inf
+    natural_lower_bound: float = -math.inf
+    root_initial_point: Optional[np.ndarray] = None
+    branch_k: int = 3
+    use_cuda_graph: int = 1
+
+    def algorithm_c(self) -> A.Algorithm:
+        return A.Algorithm(self.algorithm, self.line_search, self.secant_iters, self.secant_tol,
+                           self.secant_denom_eps, self.precision)
+
+    def to_c(self, keep: _Keep) -> A.Settings:
+        s = A.Settings()
+        for f in ("gpu_batch_size", "num_streams", "gpu_max_iters", "gpu_eps", "gpu_eps_decay", "gpu_eps_min",
+                  "integer_tol", "abs_gap_tol", "rel_gap_tol", "time_limit_seconds", "natural_lower_bound",
+                  "branch_k", "use_cuda_graph"):
+            setattr(s, f, getattr(self, f))
+        s.algorithm = self.algorithm_c()
+        s.root_initial_point = keep.ptr(_f64(self.root_initial_point) if self.root_initial_point is not None
+                                        else None, "host")
+        return s
+
+
+@dataclasses.dataclass
+class Result:
+    objective: float
+    x: np.ndarray
+    dual_bound: float
+    nodes_processed: int
+    elapsed_seconds: float
+    reached_tolerance: bool
+    reached_time_limit: bool
+
+
+def problem_to_c(p: Problem, keep: _Keep) -> A.Problem:
+    iv = np.ascontiguousarray(np.asarray(list(p.int_vars), dtype=np.int32))
+    return A.Problem(p.n_vars, keep.ptr(_f64(p.lb), "host"), keep.ptr(_f64(p.ub), "host"),
+                     keep.ptr(iv, "host") if len(iv) else None, len(iv))
+
+
+def solve(problem: Problem, objective, lmo, settings: Optional[Settings] = None) -> Result:
+    """gpuboscia::solve on the GPU (gbx_solve)."""
+    lib = A.load()
+    settings = settings or Settings()
+    keep = _Keep()
+    n = problem.n_vars
+    o = objective.to_c("cuda", keep)
+    lm = lmo.to_c(n, "cuda", keep)
+    s = settings.to_c(keep)
+    pr = problem_to_c(problem, keep)
+    x = np.zeros(n, dtype=np.float64)
+    r = A.Result()
+    r.x = x.ctypes.data
+    rc = lib.gbx_solve(C.byref(pr), C.byref(o), C.byref(lm), C.byref(s), C.byref(r))
+    if rc == A.ERR_INVALID:
+        raise ValueError(lib.gbx_last_error().decode())
+    A.check(lib, rc, "gbx_solve")
+    return Result(r.objective, x if r.has_incumbent else np.zeros(0), r.dual_bound, r.nodes_processed,
+                  r.elapsed_seconds, bool(r.reached_tolerance), bool(r.reached_time_limit))
+
+
+# ---------------------------------------------------------------- batched kernels
+class RelaxWorkspace:
+    """Caller-owned device scratch for gbx_relax_batch (grows on demand)."""
+
+    def __init__(self):
+        self.buf = None
+
+    def get(self, nbytes: int):
+        import torch
+        if self.buf is None or self.buf.numel() < nbytes:
+            self.buf = torch.empty(max(nbytes, 256), dtype=torch.uint8, device="cuda")
+        return self.buf
+
+
+def _stream_ptr(stream) -> int:
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def relax_batch(objective, lmo, algorithm: A.Algorithm, x, lb, ub, eps, iterations, status,
+                max_iters: int, integer_flags=None, candidate_tol: float = 1e-6,
+                workspace: Optional[RelaxWorkspace] = None, stream=None, keep: Optional[_Keep] = None):
+    """Run gbx_relax_batch over device tensors (x, iterations, status updated in place).
+
+    Returns dict(gap, value, best_vertex, best_vertex_val) of new device tensors.
+    """
+    import torch
+    lib = A.load()
+    keep = keep or _Keep()
+    N, n = x.shape
+    o = objective.to_c("cuda", keep)
+    lm = lmo.to_c(n, "cuda", keep)
+    dev = x.device
+    out = dict(gap=torch.empty(N, dtype=torch.float64, device=dev),
+               value=torch.empty(N, dtype=torch.float64, device=dev),
+               best_vertex=torch.zeros(N, n, dtype=torch.float64, device=dev),
+               best_vertex_val=torch.empty(N, dtype=torch.float64, device=dev))
+    b = A.NodeBatch(N, max_iters, candidate_tol, x.data_ptr(), lb.data_ptr(), ub.data_ptr(), eps.data_ptr(),
+                    iterations.data_ptr(), status.data_ptr(), out["gap"].data_ptr(), out["value"].data_ptr(),
+                    out["best_vertex"].data_ptr(), out["best_vertex_val"].data_ptr(),
+                    integer_flags.data_ptr() if integer_flags is not None else None)
+    need = lib.gbx_relax_workspace_bytes(C.byref(o), C.byref(lm), C.byref(algorithm), N)
+    if need == 0:
+        A.check(lib, A.ERR_INVALID, "gbx_relax_workspace_bytes")
+    ws = (workspace or RelaxWorkspace()).get(need)
+    rc = lib.gbx_relax_batch(C.byref(o), C.byref(lm), C.byref(algorithm), C.byref(b), ws.data_ptr(), need,
+                             _stream_ptr(stream))
+    A.check(lib, rc, "gbx_relax_batch")
+    out["_keep"] = (keep, ws)
+    return out
+
+
+def lmo_batch(lmo, mode: int, direction, lb, ub, x=None, want_step: bool = False, stream=None):
+    """Batched forward (mode 0) or in-face (mode 1) oracle over device tensors [cases, n]."""
+    import torch
+    lib = A.load()
+    keep = _Keep()
+    cases, n = direction.shape
+    lm = lmo.to_c(n, "cuda", keep)
+    out = torch.zeros(cases, n, dtype=torch.float64, device=direction.device)
+    step = torch.zeros(cases, dtype=torch.float64, device=direction.device) if want_step else None
+    rc = lib.gbx_lmo_batch(C.byref(lm), cases, mode, direction.data_ptr(), x.data_ptr() if x is not None else None,
+                           lb.data_ptr(), ub.data_ptr(), out.data_ptr(), step.data_ptr() if step is not None else None,
+                           _stream_ptr(stream))
+    A.check(lib, rc, "gbx_lmo_batch")
+    torch.cuda.current_stream().synchronize()
+    return out, step
+
+
+def node_feasible_batch(lmo, lb, ub, integer_flags=None, stream=None):
+    import torch
+    lib = A.load()
+    keep = _Keep()
+    cases, n = lb.shape
+    lm = lmo.to_c(n, "cuda", keep)
+    out = torch.zeros(cases, dtype=torch.uint8, device=lb.device)
+    rc = lib.gbx_node_feasible_batch(C.byref(lm), cases, lb.data_ptr(), ub.data_ptr(),
+                                     integer_flags.data_ptr() if integer_flags is not None else None,
+                                     out.data_ptr(), _stream_ptr(stream))
+    A.check(lib, rc, "gbx_node_feasible_batch")
+    torch.cuda.current_stream().synchronize()
+    return out
+
+
+class BatchRelaxer:
+    """A fixed batch shape with descriptors, outputs and workspace built once;
+    launch() is a single gbx_relax_batch call on the given stream."""
+
+    def __init__(self, objective, lmo, algorithm: A.Algorithm, x, lb, ub, eps, iterations, status,
+                 max_iters: int, integer_flags=None, candidate_tol: float = 1e-6, stream=None):
+        import torch
+        self.lib = A.load()
+        self.keep = _Keep()
+        N, n = x.shape
+        self.obj = objective.to_c("cuda", self.keep)
+        self.lmo = lmo.to_c(n, "cuda", self.keep)
+        self.alg = algorithm
+        dev = x.device
+        self.gap = torch.empty(N, dtype=torch.float64, device=dev)
+        self.value = torch.empty(N, dtype=torch.float64, device=dev)
+        self.best_vertex = torch.zeros(N, n, dtype=torch.float64, device=dev)
+        self.best_vertex_val = torch.empty(N, dtype=torch.float64, device=dev)
+        self.tensors = (x, lb, ub, eps, iterations, status, integer_flags)
+        self.batch = A.NodeBatch(N, max_iters, candidate_tol, x.data_ptr(), lb.data_ptr(), ub.data_ptr(),
+                                 eps.data_ptr(), iterations.data_ptr(), status.data_ptr(), self.gap.data_ptr(),
+                                 self.value.data_ptr(), self.best_vertex.data_ptr(), self.best_vertex_val.data_ptr(),
+                                 integer_flags.data_ptr() if integer_flags is not None else None)
+        self.ws_bytes = self.lib.gbx_relax_workspace_bytes(C.byref(self.obj), C.byref(self.lmo), C.byref(self.alg), N)
+        if self.ws_bytes == 0:
+            A.check(self.lib, A.ERR_INVALID, "gbx_relax_workspace_bytes")
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=dev)
+        self.stream = _stream_ptr(stream)
+        self._args = (C.byref(self.obj), C.byref(self.lmo), C.byref(self.alg), C.byref(self.batch),
+                      C.c_void_p(self.ws.data_ptr()), C.c_size_t(self.ws_bytes), C.c_void_p(self.stream))
+
+    def launch(self) -> None:
+        rc = self.lib.gbx_relax_batch(*self._args)
+        if rc != A.OK:
+            A.check(self.lib, rc, "gbx_relax_batch")

@@ -1,0 +1,124 @@
+// capi.cu -- extern "C" entry points of libgpuboscia_gb300 (include/gpuboscia_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+
+#include "relax.cuh"
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int rc, const std::string& msg) {
+    g_err = msg;
+    return rc;
+}
+
+int validate(const gbx_objective* o, const gbx_lmo* l, const gbx_algorithm* a) {
+    if (!o || !l || !a) return fail(GBX_ERR_INVALID, "null descriptor");
+    if (o->n <= 0) return fail(GBX_ERR_INVALID, "objective n must be positive");
+    if (l->n != o->n) return fail(GBX_ERR_INVALID, "objective and LMO sizes differ");
+    if (o->kind == GBX_OBJ_DENSE_QUADRATIC) {
+        if (!o->Q) return fail(GBX_ERR_INVALID, "dense quadratic needs Q");
+    } else if (o->kind == GBX_OBJ_GRAPH_MATCHING) {
+        if (o->order <= 0 || o->order * o->order != o->n || !o->A || !o->B)
+            return fail(GBX_ERR_INVALID, "graph matching needs order*order == n and A, B");
+    } else {
+        return fail(GBX_ERR_UNSUPPORTED, "unknown objective kind");
+    }
+    if (l->kind == GBX_LMO_BIRKHOFF && l->order * l->order != l->n)
+        return fail(GBX_ERR_INVALID, "Birkhoff LMO needs order*order == n");
+    if (l->kind < GBX_LMO_BOX || l->kind > GBX_LMO_BIRKHOFF)
+        return fail(GBX_ERR_UNSUPPORTED, "unknown LMO kind");
+    if (a->kind != GBX_ALG_FRANK_WOLFE && a->kind != GBX_ALG_DICG)
+        return fail(GBX_ERR_INVALID, "unknown algorithm");
+    if (a->line_search < GBX_LS_OPEN_LOOP || a->line_search > GBX_LS_QUADRATIC_EXACT)
+        return fail(GBX_ERR_INVALID, "unknown line search");
+    if (a->line_search == GBX_LS_SECANT && a->secant_iters < 0)
+        return fail(GBX_ERR_INVALID, "secant_iters must be non-negative");
+    if (a->precision != GBX_PRECISION_FP64 && a->precision != GBX_PRECISION_MIXED)
+        return fail(GBX_ERR_INVALID, "unknown precision");
+    return GBX_OK;
+}
+}  // namespace
+
+namespace gbx {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace gbx
+
+extern "C" {
+
+int gbx_abi_version(void) { return GBX_ABI_VERSION; }
+
+const char* gbx_last_error(void) { return g_err.c_str(); }
+
+size_t gbx_relax_workspace_bytes(const gbx_objective* obj, const gbx_lmo* lmo,
+                                 const gbx_algorithm* alg, int n_nodes) {
+    if (validate(obj, lmo, alg) != GBX_OK || n_nodes < 0) return 0;
+    gbx::Layout L;
+    std::string err;
+    if (gbx::make_layout(*obj, *lmo, *alg, n_nodes, &L, &err) != GBX_OK) {
+        g_err = err;
+        return 0;
+    }
+    return gbx::workspace_bytes(L, n_nodes);
+}
+
+int gbx_relax_batch(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
+                    const gbx_node_batch* b, void* workspace, size_t workspace_bytes,
+                    void* stream) {
+    int rc = validate(obj, lmo, alg);
+    if (rc) return rc;
+    if (!b || b->n_nodes < 0 || b->max_iters < 0)
+        return fail(GBX_ERR_INVALID, "batch: n_nodes and max_iters must be non-negative");
+    if (b->n_nodes > 0 && (!b->x || !b->lb || !b->ub || !b->eps || !b->iterations
+                           || !b->status || !b->gap || !b->value || !b->best_vertex
+                           || !b->best_vertex_val))
+        return fail(GBX_ERR_INVALID, "batch: null node buffer");
+    if (!(b->candidate_tol >= 0.0)) return fail(GBX_ERR_INVALID, "candidate_tol must be >= 0");
+    gbx::Params p{};
+    p.obj = *obj;
+    p.lmo = *lmo;
+    p.alg = *alg;
+    p.b = *b;
+    std::string err;
+    rc = gbx::make_layout(*obj, *lmo, *alg, b->n_nodes, &p.L, &err);
+    if (rc) return fail(rc, err);
+    const size_t need = gbx::workspace_bytes(p.L, b->n_nodes);
+    if (need > 256 && (!workspace || workspace_bytes < need))
+        return fail(GBX_ERR_WORKSPACE, "workspace smaller than gbx_relax_workspace_bytes()");
+    p.ws = static_cast<double*>(workspace);
+    p.mixed = nullptr;
+    rc = gbx::launch_relax(p, stream, &err);
+    if (rc) return fail(rc, err);
+    return GBX_OK;
+}
+
+int gbx_lmo_batch(const gbx_lmo* lmo, int cases, int mode, const double* direction,
+                  const double* x, const double* lb, const double* ub, double* out,
+                  double* out_step, void* stream) {
+    if (!lmo || cases < 0 || lmo->n <= 0) return fail(GBX_ERR_INVALID, "lmo batch arguments");
+    if (mode != 0 && mode != 1) return fail(GBX_ERR_INVALID, "mode must be 0 or 1");
+    if (cases > 0 && (!direction || !lb || !ub || !out || (mode == 1 && !x)))
+        return fail(GBX_ERR_INVALID, "null LMO buffer");
+    if (lmo->kind == GBX_LMO_BIRKHOFF && lmo->order * lmo->order != lmo->n)
+        return fail(GBX_ERR_INVALID, "Birkhoff LMO needs order*order == n");
+    std::string err;
+    const int rc = gbx::launch_lmo_batch(*lmo, cases, mode, direction, x, lb, ub, out,
+                                         out_step, stream, &err);
+    if (rc) return fail(rc, err);
+    return GBX_OK;
+}
+
+int gbx_node_feasible_batch(const gbx_lmo* lmo, int cases, const double* lb,
+                            const double* ub, const uint8_t* integer_flags, uint8_t* out,
+                            void* stream) {
+    if (!lmo || cases < 0 || lmo->n <= 0) return fail(GBX_ERR_INVALID, "feasibility arguments");
+    if (cases > 0 && (!lb || !ub || !out)) return fail(GBX_ERR_INVALID, "null buffer");
+    std::string err;
+    const int rc = gbx::launch_node_feasible(*lmo, cases, lb, ub, integer_flags, out, stream, &err);
+    if (rc) return fail(rc, err);
+    return GBX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,1206 @@
+// relax.cu -- FP64 Frank-Wolfe / DICG node relaxation for sm_103a.
+//
+// One 256-thread CTA relaxes one B&B node (the reference's node-per-block
+// decomposition, device_resident_solver.cuh:631-660), but the node's working
+// set (iterate, gradient, vertices, bounds, residual, objective matrices) is
+// staged in shared memory whenever it fits, so an iteration touches HBM only
+// for the objective data of large instances. The Birkhoff oracle runs as a
+// warp-level Hungarian (shuffle argmin, no block barriers per Dijkstra step),
+// and the DICG forward and in-face oracles run concurrently on warps 0 and 1.
+//
+// Arithmetic follows a fixed order so results are reproducible on any GPU and
+// by the oracle: block reductions are 256 lanes folded by the warp shuffle
+// tree; products marked fma() are fused, nothing else is (-fmad=false).
+//
+// Reference semantics restated: drs_fw_relax_node (device_resident_solver.cuh:
+// 337-629), SecantLS / QuadraticExactLS (algorithms.cuh:121-296), BoxLMO /
+// UnitSimplexLMO / BirkhoffLMO (lmo.cuh:212-1417), drs_integer_value and the
+// rounding heuristic (device_resident_solver.cuh:295-335, heuristics.h:23-35).
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#include <algorithm>
+#include <cstdio>
+
+#include "relax.cuh"
+
+namespace gbx {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// ------------------------------------------------------------------ layout
+__host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
+
+__host__ __device__ inline size_t hung_ws_bytes(int m) {
+    size_t b = 0;
+    b += align16(3 * (size_t)(m + 1) * sizeof(double));     // u, pv, minv
+    b += align16(2 * (size_t)(m + 1) * sizeof(int));        // p, way
+    b += align16(6 * (size_t)m * sizeof(int));              // fcol frow rows cols pi pinv
+    b += align16(8 * sizeof(int));                          // scalars
+    b += align16((size_t)(m + 1));                          // used
+    return b;
+}
+
+struct HW {
+    double *u, *pv, *minv;
+    int *p, *way, *fcol, *frow, *rows, *cols, *pi, *pinv, *scal;
+    uint8_t* used;
+};
+
+__device__ inline HW hw_at(unsigned char* base, int m) {
+    HW w;
+    size_t o = 0;
+    w.u = reinterpret_cast<double*>(base + o);
+    w.pv = w.u + (m + 1);
+    w.minv = w.pv + (m + 1);
+    o += align16(3 * (size_t)(m + 1) * sizeof(double));
+    w.p = reinterpret_cast<int*>(base + o);
+    w.way = w.p + (m + 1);
+    o += align16(2 * (size_t)(m + 1) * sizeof(int));
+    w.fcol = reinterpret_cast<int*>(base + o);
+    w.frow = w.fcol + m;
+    w.rows = w.frow + m;
+    w.cols = w.rows + m;
+    w.pi = w.cols + m;
+    w.pinv = w.pi + m;
+    o += align16(6 * (size_t)m * sizeof(int));
+    w.scal = reinterpret_cast<int*>(base + o);
+    o += align16(8 * sizeof(int));
+    w.used = base + o;
+    return w;
+}
+
+// ------------------------------------------------------------------ reductions
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = v + __shfl_down_sync(kFull, v, off);
+    return v;
+}
+__device__ __forceinline__ double warp_min(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fmin(v, __shfl_down_sync(kFull, v, off));
+    return v;
+}
+
+// 256-lane sum, result broadcast to every thread.
+__device__ double bsum(double v, double* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double r = lane < kWarps ? red[lane] : 0.0;
+        r = warp_sum(r);
+        if (lane == 0) red[32] = r;
+    }
+    __syncthreads();
+    return red[32];
+}
+// 256-lane min; lanes past the warp count read 1.0 (drs_block_min).
+__device__ double bmin(double v, double* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = warp_min(v);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double r = lane < kWarps ? red[lane] : 1.0;
+        r = warp_min(r);
+        if (lane == 0) red[33] = r;
+    }
+    __syncthreads();
+    return red[33];
+}
+
+// ------------------------------------------------------------------ context
+struct Ctx {
+    int n, tid;
+    double* red;          // >= 40 doubles
+    int* flag;            // shared ints
+    // objective
+    int ok;               // objective kind
+    int m;                // graph order
+    const double* Q;
+    const double* c;
+    double s, ls, k0;
+    const double* A;
+    const double* B;
+    double* R;
+    // lmo
+    int lk;
+    double rhs;
+    const uint8_t* is_int;
+    int lorder;
+    int S;
+    double* keys;
+    double* prefix;
+    int* idx;
+    uint8_t* fixed;
+    unsigned char* hung[2];
+    size_t hung_bytes;
+    // problem
+    const uint8_t* flags;
+    double tol;
+};
+
+// ------------------------------------------------------------------ objective
+__device__ void residual(const Ctx& c, const double* X, double* R) {
+    const int m = c.m;
+    for (int e = c.tid; e < c.n; e += kThreads) {
+        const int i = e / m, j = e - (e / m) * m;
+        double r = 0.0;
+        for (int k = 0; k < m; ++k) {
+            r = fma(c.A[i * m + k], X[k * m + j], r);
+            r = fma(-X[i * m + k], c.B[k * m + j], r);
+        }
+        R[e] = r;
+    }
+}
+
+// g = grad f(x). Graph matching leaves the residual of x in c.R.
+__device__ void obj_grad(const Ctx& c, const double* x, double* g) {
+    const int n = c.n;
+    if (c.ok == GBX_OBJ_GRAPH_MATCHING) {
+        residual(c, x, c.R);
+        __syncthreads();
+        const int m = c.m;
+        const double two_s = 2.0 * c.s;
+        for (int e = c.tid; e < n; e += kThreads) {
+            const int p = e / m, q = e - (e / m) * m;
+            double acc = 0.0;
+            for (int r = 0; r < m; ++r) acc = fma(c.A[r * m + p], c.R[r * m + q], acc);
+            for (int k = 0; k < m; ++k) acc = fma(-c.R[p * m + k], c.B[q * m + k], acc);
+            g[e] = two_s * acc;
+        }
+    } else {
+        for (int j = c.tid; j < n; j += kThreads) {
+            double acc = 0.0;
+            for (int k = 0; k < n; ++k) acc = fma(c.Q[(size_t)k * n + j], x[k], acc);
+            const double lin = c.c ? c.ls * c.c[j] : 0.0;
+            g[j] = c.s * (acc + lin);
+        }
+    }
+    __syncthreads();
+}
+
+__device__ double value_from_residual(const Ctx& c) {
+    double loc = 0.0;
+    for (int e = c.tid; e < c.n; e += kThreads) loc = fma(c.R[e], c.R[e], loc);
+    return c.s * bsum(loc, c.red);
+}
+
+__device__ double obj_value(const Ctx& c, const double* x) {
+    const int n = c.n;
+    if (c.ok == GBX_OBJ_GRAPH_MATCHING) {
+        residual(c, x, c.R);
+        __syncthreads();
+        return value_from_residual(c);
+    }
+    const double a = 0.5 * c.s, b = c.s * c.ls;
+    double quad = 0.0, lin = 0.0;
+    for (int j = c.tid; j < n; j += kThreads) {
+        double qx = 0.0;
+        for (int k = 0; k < n; ++k) qx = fma(c.Q[(size_t)k * n + j], x[k], qx);
+        quad = fma(x[j], qx, quad);
+        if (c.c) lin = fma(c.c[j], x[j], lin);
+    }
+    double val = a * quad + b * lin;
+    if (c.tid == 0) val += c.k0;
+    return bsum(val, c.red);
+}
+
+__device__ double obj_curvature(const Ctx& c, const double* d) {
+    const int n = c.n;
+    if (c.ok == GBX_OBJ_GRAPH_MATCHING) {
+        residual(c, d, c.R);
+        __syncthreads();
+        double loc = 0.0;
+        for (int e = c.tid; e < n; e += kThreads) loc = fma(c.R[e], c.R[e], loc);
+        return (2.0 * c.s) * bsum(loc, c.red);
+    }
+    double curv = 0.0;
+    for (int j = c.tid; j < n; j += kThreads) {
+        double prod = 0.0;
+        for (int k = 0; k < n; ++k) prod = fma(c.Q[(size_t)k * n + j], d[k], prod);
+        curv = fma(c.s * d[j], prod, curv);
+    }
+    return bsum(curv, c.red);
+}
+
+// Value of a permutation vertex of the graph-matching objective in O(m^2):
+// with exactly one unit per row and column, every residual entry of the
+// generic O(m^3) loop reduces to one rounding of A[i,pinv(j)] - B[pi(i),j],
+// so this is bit-identical to obj_value on the same vertex.
+__device__ double perm_value(const Ctx& c, const int* pi, int* pinv) {
+    const int m = c.m;
+    for (int r = c.tid; r < m; r += kThreads) pinv[pi[r]] = r;
+    __syncthreads();
+    double loc = 0.0;
+    for (int e = c.tid; e < c.n; e += kThreads) {
+        const int i = e / m, j = e - (e / m) * m;
+        const double r = c.A[i * m + pinv[j]] - c.B[pi[i] * m + j];
+        loc = fma(r, r, loc);
+    }
+    return c.s * bsum(loc, c.red);
+}
+
+// ------------------------------------------------------------------ Hungarian
+// Exact min-cost assignment over the Birkhoff order-m polytope with forced
+// (lb > 1/2), forbidden (ub < 1/2) and face restrictions, ties to the lowest
+// column (lmo.cuh:1239-1417). Executed by ONE warp; `out` must be zeroed and
+// visible. cost may be null (zero costs); the cost of edge e is sign*cost[e].
+// Returns a warp-uniform success flag and leaves the row->column map in w.pi.
+__device__ bool hungarian_warp(const HW& w, int m, const double* cost, double sign,
+                               const double* lb, const double* ub, const double* face,
+                               double* out) {
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < m; i += 32) { w.fcol[i] = -1; w.frow[i] = -1; }
+    __syncwarp();
+    bool ok = true;
+    const int nn = m * m;
+    for (int e = lane; e < nn; e += 32) {
+        const double le = lb[e], ue = ub[e];
+        if (le > ue + 1e-9) ok = false;
+        const bool forced = le > 0.5 || (face && face[e] >= 1.0 - 1e-9);
+        if (forced) {
+            const int r = e / m, col = e - r * m;
+            if (ue < 0.5) ok = false;
+            if (atomicCAS(&w.fcol[r], -1, col) != -1) ok = false;
+            if (atomicCAS(&w.frow[col], -1, r) != -1) ok = false;
+        }
+    }
+    ok = __all_sync(kFull, ok);
+    __syncwarp();
+    if (!ok) return false;
+    int k = 0, kc = 0;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int base = 0; base < m; base += 32) {
+        const int i = base + lane;
+        const bool fr = i < m && w.fcol[i] < 0;
+        const bool fc = i < m && w.frow[i] < 0;
+        const unsigned mr = __ballot_sync(kFull, fr), mc = __ballot_sync(kFull, fc);
+        if (fr) w.rows[k + __popc(mr & lt)] = i;
+        if (fc) w.cols[kc + __popc(mc & lt)] = i;
+        k += __popc(mr);
+        kc += __popc(mc);
+    }
+    if (k != kc) return false;
+    for (int i = lane; i < m; i += 32)
+        if (w.fcol[i] >= 0) { out[i * m + w.fcol[i]] = 1.0; w.pi[i] = w.fcol[i]; }
+    for (int j = lane; j <= k; j += 32) { w.u[j] = 0.0; w.pv[j] = 0.0; w.p[j] = 0; w.way[j] = 0; }
+    __syncwarp();
+    for (int i = 1; i <= k; ++i) {
+        for (int j = lane; j <= k; j += 32) { w.minv[j] = kNone; w.used[j] = 0; }
+        if (lane == 0) w.p[0] = i;
+        __syncwarp();
+        int j0 = 0;
+        for (int step = 0; step <= k; ++step) {
+            if (lane == 0) w.used[j0] = 1;
+            __syncwarp();
+            const int i0 = w.p[j0];
+            const double ui0 = w.u[i0];
+            const int rb = w.rows[i0 - 1] * m;
+            double bv = kNone;
+            int bj = -1;
+            for (int j = lane + 1; j <= k; j += 32) {
+                if (w.used[j]) continue;
+                const int e = rb + w.cols[j - 1];
+                double mv = w.minv[j];
+                if (ub[e] >= 0.5 && (!face || face[e] > 1e-9)) {
+                    const double ce = cost ? sign * cost[e] : 0.0;
+                    const double cur = ce - ui0 - w.pv[j];
+                    if (cur < mv) { mv = cur; w.minv[j] = cur; w.way[j] = j0; }
+                }
+                if (mv < kNone && (bj < 0 || mv < bv)) { bv = mv; bj = j; }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const double ov = __shfl_down_sync(kFull, bv, off);
+                const int oj = __shfl_down_sync(kFull, bj, off);
+                if (oj >= 0 && (bj < 0 || ov < bv || (ov == bv && oj < bj))) { bv = ov; bj = oj; }
+            }
+            bv = __shfl_sync(kFull, bv, 0);
+            bj = __shfl_sync(kFull, bj, 0);
+            if (bj < 0 || !isfinite(bv)) return false;
+            __syncwarp();
+            for (int j = lane; j <= k; j += 32) {
+                if (w.used[j]) { w.u[w.p[j]] += bv; w.pv[j] -= bv; }
+                else w.minv[j] -= bv;
+            }
+            __syncwarp();
+            j0 = bj;
+            if (w.p[j0] == 0) break;
+        }
+        if (w.p[j0] != 0) return false;  // no augmenting path within k+1 steps
+        if (lane == 0) {
+            int jj = j0;
+            for (int guard = 0; guard <= k && jj != 0; ++guard) {
+                const int j1 = w.way[jj];
+                w.p[jj] = w.p[j1];
+                jj = j1;
+            }
+        }
+        __syncwarp();
+    }
+    for (int j = lane + 1; j <= k; j += 32) {
+        const int r = w.rows[w.p[j] - 1], col = w.cols[j - 1];
+        out[r * m + col] = 1.0;
+        w.pi[r] = col;
+    }
+    __syncwarp();
+    return true;
+}
+
+// ------------------------------------------------------------------ simplex
+// parallel_greedy_allocate_cooperative (lmo.cuh:529-618); key of j is sign*g[j].
+__device__ void simplex_greedy(const Ctx& c, const double* g, double sign, const double* ub,
+                               double* out, const uint8_t* fixed, double remaining,
+                               bool force_full, bool floor_int) {
+    const int S = c.S, n = c.n, tid = c.tid;
+    const bool eq = c.lk == GBX_LMO_EQUALITY_SIMPLEX;
+    for (int pos = tid; pos < S; pos += kThreads) {
+        bool el = pos < n && (!fixed || !fixed[pos]);
+        double key = CUDART_INF;
+        if (el) {
+            key = sign * g[pos];
+            el = force_full || key <= 0.0;
+        }
+        c.keys[pos] = el ? key : CUDART_INF;
+        c.idx[pos] = el ? pos : -1;
+    }
+    __syncthreads();
+    for (int width = 2; width <= S; width <<= 1)
+        for (int stride = width >> 1; stride > 0; stride >>= 1) {
+            for (int left = tid; left < S; left += kThreads) {
+                const int right = left ^ stride;
+                if (right <= left) continue;
+                const double lk = c.keys[left], rk = c.keys[right];
+                const int li = c.idx[left], ri = c.idx[right];
+                const bool after = rk < lk || (rk == lk && ri >= 0 && (li < 0 || ri < li));
+                const bool asc = (left & width) == 0;
+                if (after == asc) {
+                    c.keys[left] = rk; c.keys[right] = lk;
+                    c.idx[left] = ri; c.idx[right] = li;
+                }
+            }
+            __syncthreads();
+        }
+    const uint8_t* isint = c.is_int;
+    for (int pos = tid; pos < S; pos += kThreads) {
+        const int j = c.idx[pos];
+        c.prefix[pos] = j < 0 ? 0.0
+            : ((isint && isint[j]) ? fmax(ub[j] - out[j], 0.0) : remaining);
+    }
+    __syncthreads();
+    for (int off = 1; off < S; off <<= 1) {
+        for (int op = tid; op < S / (off << 1); op += kThreads) {
+            const int right = (op + 1) * (off << 1) - 1;
+            c.prefix[right] += c.prefix[right - off];
+        }
+        __syncthreads();
+    }
+    if (tid == 0) c.prefix[S - 1] = 0.0;
+    __syncthreads();
+    for (int off = S >> 1; off > 0; off >>= 1) {
+        for (int op = tid; op < S / (off << 1); op += kThreads) {
+            const int right = (op + 1) * (off << 1) - 1;
+            const double ls = c.prefix[right - off];
+            c.prefix[right - off] = c.prefix[right];
+            c.prefix[right] += ls;
+        }
+        __syncthreads();
+    }
+    for (int pos = tid; pos < S; pos += kThreads) {
+        const int j = c.idx[pos];
+        if (j < 0) continue;
+        const bool ij = isint && isint[j];
+        double add = fmax(remaining - c.prefix[pos], 0.0);
+        const double cap = ij ? fmax(ub[j] - out[j], 0.0) : remaining;
+        add = fmin(add, cap);
+        if (floor_int && ij) add = floor(add + (eq ? 1e-9 : 0.0));
+        out[j] += add;
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------------ LMOs
+template <int LK>
+__device__ bool lmo_forward(const Ctx& c, const double* g, const double* lb,
+                            const double* ub, double* v) {
+    const int n = c.n;
+    if constexpr (LK == GBX_LMO_BOX) {
+        for (int j = c.tid; j < n; j += kThreads) v[j] = g[j] > 0.0 ? lb[j] : ub[j];
+        __syncthreads();
+        return false;
+    } else if constexpr (LK == GBX_LMO_BIRKHOFF) {
+        for (int j = c.tid; j < n; j += kThreads) v[j] = 0.0;
+        __syncthreads();
+        if (n != c.lorder * c.lorder) return false;
+        if (threadIdx.x < 32) {
+            const HW w = hw_at(c.hung[0], c.lorder);
+            const bool ok = hungarian_warp(w, c.lorder, g, 1.0, lb, ub, nullptr, v);
+            if (threadIdx.x == 0) c.flag[0] = ok;
+        }
+        __syncthreads();
+        return c.flag[0] != 0;
+    } else {
+        double loc = 0.0;
+        for (int j = c.tid; j < n; j += kThreads) {
+            if (c.is_int && c.is_int[j]) { v[j] = lb[j]; loc += v[j]; }
+            else v[j] = 0.0;
+        }
+        const double mass = bsum(loc, c.red);
+        const bool eq = LK == GBX_LMO_EQUALITY_SIMPLEX;
+        simplex_greedy(c, g, 1.0, ub, v, nullptr, c.rhs - mass, eq, eq);
+        return false;
+    }
+}
+
+// In-face away oracle on the direction sign*g over the minimal face of x.
+template <int LK>
+__device__ bool lmo_inface(const Ctx& c, const double* g, double sign, const double* x,
+                           const double* lb, const double* ub, double* a, int hw_slot) {
+    const int n = c.n;
+    const double atol = 1e-6, rtol = 1e-4;
+    if constexpr (LK == GBX_LMO_BOX) {
+        for (int j = c.tid; j < n; j += kThreads) {
+            const double ut = atol + rtol * fabs(ub[j]);
+            const double lt = atol + rtol * fabs(lb[j]);
+            if (fabs(x[j] - ub[j]) <= ut) a[j] = ub[j];
+            else if (fabs(x[j] - lb[j]) <= lt) a[j] = lb[j];
+            else a[j] = sign * g[j] > 0.0 ? lb[j] : ub[j];
+        }
+        __syncthreads();
+        return false;
+    } else if constexpr (LK == GBX_LMO_BIRKHOFF) {
+        // caller zeroes `a` and runs this on one warp
+        const HW w = hw_at(c.hung[hw_slot], c.lorder);
+        return hungarian_warp(w, c.lorder, g, sign, lb, ub, x, a);
+    } else {
+        double lm = 0.0, lx = 0.0;
+        for (int j = c.tid; j < n; j += kThreads) {
+            const bool ij = c.is_int && c.is_int[j];
+            c.fixed[j] = 0;
+            a[j] = ij ? lb[j] : 0.0;
+            const double lower = ij ? lb[j] : 0.0;
+            const double ltol = atol + rtol * fmax(fabs(x[j]), fabs(lower));
+            if (fabs(x[j] - lower) <= ltol) {
+                c.fixed[j] = 1;
+                a[j] = lower;
+            } else if (ij) {
+                const double utol = atol + rtol * fmax(fabs(x[j]), fabs(ub[j]));
+                if (fabs(x[j] - ub[j]) <= utol) { c.fixed[j] = 1; a[j] = ub[j]; }
+            }
+            lm += a[j];
+            lx += x[j];
+        }
+        const double mass = bsum(lm, c.red);
+        const double xmass = bsum(lx, c.red);
+        const bool eq = LK == GBX_LMO_EQUALITY_SIMPLEX;
+        const bool force = eq || fabs(xmass - c.rhs) <= atol + rtol * fmax(fabs(xmass), fabs(c.rhs));
+        simplex_greedy(c, g, sign, ub, a, c.fixed, c.rhs - mass, force, true);
+        return false;
+    }
+}
+
+// max(0, min(coordinate step, aggregate step)) for x - gamma*d.
+template <int LK>
+__device__ double lmo_max_step(const Ctx& c, const double* d, const double* x,
+                               const double* lb, const double* ub) {
+    const int n = c.n;
+    double res = 1.0;
+    for (int j = c.tid; j < n; j += kThreads) {
+        const double dj = d[j];
+        if constexpr (LK == GBX_LMO_BOX) {
+            if (dj < 0.0) res = fmin(res, (ub[j] - x[j]) / -dj);
+            else if (dj > 0.0) res = fmin(res, (x[j] - lb[j]) / dj);
+        } else if constexpr (LK == GBX_LMO_BIRKHOFF) {
+            if (dj > 0.0) res = fmin(res, (x[j] - lb[j]) / dj);
+            else if (dj < 0.0) res = fmin(res, (ub[j] - x[j]) / -dj);
+        } else {
+            const bool ij = c.is_int && c.is_int[j];
+            if (dj > 1e-6) res = fmin(res, (x[j] - (ij ? lb[j] : 0.0)) / dj);
+            else if (dj < -1e-6) res = fmin(res, ((ij ? ub[j] : c.rhs) - x[j]) / -dj);
+        }
+    }
+    const double coord = bmin(res, c.red);
+    double agg = 1.0;
+    if constexpr (LK == GBX_LMO_SIMPLEX || LK == GBX_LMO_EQUALITY_SIMPLEX) {
+        double sx = 0.0, sd = 0.0;
+        for (int j = c.tid; j < n; j += kThreads) { sx += x[j]; sd += d[j]; }
+        const double sum_x = bsum(sx, c.red);
+        const double sum_d = bsum(sd, c.red);
+        if (LK == GBX_LMO_EQUALITY_SIMPLEX && fabs(sum_d) > 1e-9) agg = 0.0;
+        else agg = sum_d < 0.0 ? fmin(1.0, (sum_x - c.rhs) / sum_d) : 1.0;
+    }
+    return fmax(0.0, fmin(coord, agg));
+}
+
+// drs_node_feasible (device_resident_solver.cuh:206-217) + LMO check.
+template <int LK>
+__device__ bool node_feasible(const Ctx& c, const double* lb, const double* ub,
+                              double* scratch) {
+    const int n = c.n;
+    bool valid = true;
+    for (int j = c.tid; j < n; j += kThreads)
+        if (isnan(lb[j]) || isnan(ub[j]) || lb[j] > ub[j]
+                || (c.flags && c.flags[j] && ceil(lb[j]) > floor(ub[j])))
+            valid = false;
+    if (!__syncthreads_and(valid)) return false;
+    if constexpr (LK == GBX_LMO_BOX) {
+        return true;
+    } else if constexpr (LK == GBX_LMO_BIRKHOFF) {
+        if (n != c.lorder * c.lorder) return false;
+        for (int j = c.tid; j < n; j += kThreads) scratch[j] = 0.0;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            const HW w = hw_at(c.hung[0], c.lorder);
+            const bool ok = hungarian_warp(w, c.lorder, nullptr, 1.0, lb, ub, nullptr, scratch);
+            if (threadIdx.x == 0) c.flag[1] = ok;
+        }
+        __syncthreads();
+        return c.flag[1] != 0;
+    } else {
+        bool v2 = true, cont = false;
+        double mand = 0.0, cap = 0.0;
+        for (int j = c.tid; j < n; j += kThreads) {
+            const bool integer = c.flags ? c.flags[j] != 0 : (c.is_int && c.is_int[j]);
+            const double lo = integer ? ceil(fmax(0.0, lb[j])) : fmax(0.0, lb[j]);
+            const double hi = integer ? floor(ub[j]) : ub[j];
+            v2 = v2 && lo <= hi;
+            mand += lo;
+            cap += hi;
+            cont = cont || !integer;
+        }
+        const bool iv = __syncthreads_and(v2);
+        const double ms = bsum(mand, c.red);
+        bool feas = iv && ms <= c.rhs + 1e-9;
+        if (LK == GBX_LMO_EQUALITY_SIMPLEX) {
+            const double cs = bsum(cap, c.red);
+            const bool hc = __syncthreads_or(cont);
+            feas = feas && cs >= c.rhs - 1e-9
+                && (hc || fabs(c.rhs - round(c.rhs)) <= 1e-9);
+        }
+        return feas;
+    }
+}
+
+template <int LK>
+__device__ bool rounded_feasible(const Ctx& c, const double* x) {
+    const int n = c.n;
+    const double tol = c.tol;
+    if constexpr (LK == GBX_LMO_BOX) {
+        return true;
+    } else if constexpr (LK == GBX_LMO_BIRKHOFF) {
+        const int m = c.lorder;
+        if (n != m * m) return false;
+        bool valid = true;
+        for (int i = c.tid; i < m; i += kThreads) {
+            double row = 0.0, col = 0.0;
+            for (int j = 0; j < m; ++j) {
+                if (x[i * m + j] < -tol) valid = false;
+                row += x[i * m + j];
+                col += x[j * m + i];
+            }
+            if (fabs(row - 1.0) > tol || fabs(col - 1.0) > tol) valid = false;
+        }
+        return __syncthreads_and(valid);
+    } else {
+        bool valid = true;
+        double s = 0.0;
+        for (int j = c.tid; j < n; j += kThreads) { valid = valid && x[j] >= -tol; s += x[j]; }
+        const bool nn = __syncthreads_and(valid);
+        const double sum = bsum(s, c.red);
+        return nn && (LK == GBX_LMO_EQUALITY_SIMPLEX ? fabs(sum - c.rhs) <= tol
+                                                    : sum <= c.rhs + tol);
+    }
+}
+
+// drs_integer_value: score of an LMO vertex or rounded candidate.
+__device__ double integer_value(const Ctx& c, const double* x, const double* lb,
+                                const double* ub, const int* pi, int* pinv) {
+    bool valid = true;
+    const double tol = c.tol;
+    for (int j = c.tid; j < c.n; j += kThreads)
+        if (!isfinite(x[j]) || x[j] < lb[j] - tol || x[j] > ub[j] + tol
+                || (c.flags && c.flags[j] && x[j] != round(x[j])))
+            valid = false;
+    if (!__syncthreads_and(valid)) return kNone;
+    const double val = pi ? perm_value(c, pi, pinv) : obj_value(c, x);
+    return isfinite(val) ? val : kNone;
+}
+
+// ------------------------------------------------------------------ kernel
+struct Scalars {
+    double red[40];
+    int flag[8];
+};
+
+__device__ inline double* vecp(double* base, const Layout& L, int b) {
+    return L.off[b] >= 0 ? base + L.off[b] : nullptr;
+}
+
+template <int OK, int LK>
+__global__ void __launch_bounds__(kThreads, 1) relax_kernel(const __grid_constant__ Params P) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ Scalars sh;
+    const int node = blockIdx.x;
+    if (node >= P.b.n_nodes) return;
+    const int tid = threadIdx.x;
+    const int n = P.obj.n;
+    const Layout& L = P.L;
+
+    double* vb = L.vec_smem ? reinterpret_cast<double*>(dsm + L.sm_vec)
+                            : P.ws + (size_t)node * L.node_stride;
+    double* X = vecp(vb, L, B_X);
+    double* G = vecp(vb, L, B_G);
+    double* V = vecp(vb, L, B_V);
+    double* AW = vecp(vb, L, B_AW);
+    double* TX = vecp(vb, L, B_TX);
+    double* TG = vecp(vb, L, B_TG);
+    double* LB = vecp(vb, L, B_LB);
+    double* UB = vecp(vb, L, B_UB);
+    double* CAND = vecp(vb, L, B_CAND);
+
+    const size_t off = (size_t)node * n;
+    double* gx = P.b.x + off;
+    double* best = P.b.best_vertex + off;
+
+    Ctx c;
+    c.n = n;
+    c.tid = tid;
+    c.red = sh.red;
+    c.flag = sh.flag;
+    c.ok = OK;
+    c.m = P.obj.order;
+    c.c = P.obj.c;
+    c.s = P.obj.scale;
+    c.ls = P.obj.linear_scale;
+    c.k0 = P.obj.constant;
+    c.R = vecp(vb, L, B_R);
+    c.lk = LK;
+    c.rhs = P.lmo.right_side;
+    c.is_int = P.lmo.is_int;
+    c.lorder = P.lmo.order;
+    c.S = L.sort_size;
+    c.keys = reinterpret_cast<double*>(dsm + L.sm_keys);
+    c.prefix = reinterpret_cast<double*>(dsm + L.sm_prefix);
+    c.idx = reinterpret_cast<int*>(dsm + L.sm_idx);
+    c.fixed = dsm + L.sm_fixed;
+    c.hung[0] = dsm + L.sm_hung;
+    c.hung[1] = dsm + L.sm_hung + L.hung_bytes;
+    c.hung_bytes = L.hung_bytes;
+    c.flags = P.b.integer_flags;
+    c.tol = P.b.candidate_tol;
+
+    // stage node data and objective matrices
+    for (int j = tid; j < n; j += kThreads) {
+        X[j] = gx[j];
+        LB[j] = P.b.lb[off + j];
+        UB[j] = P.b.ub[off + j];
+    }
+    if (OK == GBX_OBJ_GRAPH_MATCHING) {
+        if (L.obj_smem) {
+            double* As = reinterpret_cast<double*>(dsm + L.sm_obj);
+            double* Bs = As + (size_t)c.m * c.m;
+            for (int e = tid; e < c.m * c.m; e += kThreads) { As[e] = P.obj.A[e]; Bs[e] = P.obj.B[e]; }
+            c.A = As;
+            c.B = Bs;
+        } else {
+            c.A = P.obj.A;
+            c.B = P.obj.B;
+        }
+        c.Q = nullptr;
+    } else {
+        if (L.obj_smem) {
+            double* Qs = reinterpret_cast<double*>(dsm + L.sm_obj);
+            for (size_t e = tid; e < (size_t)n * n; e += kThreads) Qs[e] = P.obj.Q[e];
+            c.Q = Qs;
+        } else {
+            c.Q = P.obj.Q;
+        }
+        c.A = c.B = nullptr;
+    }
+    const double eps = P.b.eps[node];
+    const int it0 = P.b.iterations[node];
+    const bool supplied = (P.b.status[node] & GBX_NODE_INITIAL_POINT_SUPPLIED) != 0;
+    __syncthreads();
+    if (tid == 0) P.b.best_vertex_val[node] = kNone;
+    double best_val = kNone;
+
+    if (!node_feasible<LK>(c, LB, UB, V)) {
+        if (tid == 0) {
+            P.b.status[node] = GBX_NODE_INFEASIBLE;
+            P.b.value[node] = CUDART_INF;
+            P.b.gap[node] = 0.0;
+            P.b.iterations[node] = it0;
+        }
+        return;
+    }
+
+    const bool dicg = P.alg.kind == GBX_ALG_DICG;
+    const int ls = P.alg.line_search;
+    const bool search = ls == GBX_LS_SECANT || ls == GBX_LS_QUADRATIC_EXACT;
+    const HW hw0 = hw_at(c.hung[0], LK == GBX_LMO_BIRKHOFF ? c.lorder : 0);
+    const HW hw1 = hw_at(c.hung[1], LK == GBX_LMO_BIRKHOFF ? c.lorder : 0);
+    const bool graph_perm = OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF;
+
+    if (it0 == 0 && !supplied) {
+        for (int j = tid; j < n; j += kThreads) G[j] = -1.0 - static_cast<double>(j) / (n + 1.0);
+        __syncthreads();
+        lmo_forward<LK>(c, G, LB, UB, V);
+        for (int j = tid; j < n; j += kThreads) X[j] = V[j];
+        __syncthreads();
+    }
+
+    // score an integral vertex (drs_integer_value + best-vertex bookkeeping)
+    auto score = [&](const double* vert, const int* pi, int* pinv) {
+        const double fv = integer_value(c, vert, LB, UB, pi, pinv);
+        if (fv < best_val) {
+            best_val = fv;
+            if (tid == 0) P.b.best_vertex_val[node] = fv;
+        }
+        if (fv < 1e299 && fv == best_val)
+            for (int j = tid; j < n; j += kThreads) best[j] = vert[j];
+        __syncthreads();
+    };
+
+    // line searches (SecantLS::search, QuadraticExactLS::search)
+    auto line_search = [&](double gap, double maxg, const double* dir) -> double {
+        if (ls == GBX_LS_QUADRATIC_EXACT) {
+            const double curv = obj_curvature(c, dir);
+            if (maxg <= 0.0) return 0.0;
+            if (curv > 0.0) {
+                if (gap <= 0.0) return 0.0;
+                const double st = gap / curv;
+                return st < maxg ? st : maxg;
+            }
+            return -gap + 0.5 * curv * maxg < 0.0 ? maxg : 0.0;
+        }
+        const double tol = P.alg.secant_tol, deps = P.alg.secant_denom_eps;
+        const double f_base = obj_value(c, X);
+        double lo = 0.0, hi = maxg, best_f = f_base, best_gamma = 0.0;
+        double phi_lo = -gap, phi_hi = 0.0, gamma = 0.0;
+        bool done = phi_lo >= -tol;
+        const double f_abs = f_base >= 0.0 ? f_base : -f_base;
+        const double allow = tol * (1.0 + f_abs);
+        auto probe = [&](double gm, double& phi, double& f) {
+            for (int j = tid; j < n; j += kThreads) TX[j] = fma(gm, dir[j], X[j]);
+            __syncthreads();
+            obj_grad(c, TX, TG);
+            double loc = 0.0;
+            for (int j = tid; j < n; j += kThreads) loc = fma(TG[j], dir[j], loc);
+            phi = bsum(loc, c.red);
+            f = OK == GBX_OBJ_GRAPH_MATCHING ? value_from_residual(c) : obj_value(c, TX);
+        };
+        double f_hi;
+        probe(maxg, phi_hi, f_hi);
+        if (f_hi < best_f || (best_gamma == 0.0 && f_hi <= f_base + allow)) { best_f = f_hi; best_gamma = maxg; }
+        if (!done && phi_hi <= tol && f_hi <= f_base + allow) { gamma = maxg; done = true; }
+        for (int it = 0; it < P.alg.secant_iters; ++it) {
+            if (done) break;
+            const double denom = phi_hi - phi_lo;
+            double gm = (denom > deps || denom < -deps) ? hi - phi_hi * (hi - lo) / denom : 0.5 * (lo + hi);
+            if (!(gm > lo && gm < hi)) gm = 0.5 * (lo + hi);
+            gamma = gm;
+            double phi, ft;
+            probe(gamma, phi, ft);
+            if (ft < best_f || (best_gamma == 0.0 && ft <= f_base + allow)) { best_f = ft; best_gamma = gamma; }
+            if (phi < 0.0) { lo = gamma; phi_lo = phi; }
+            else { hi = gamma; phi_hi = phi; }
+            if ((phi <= tol && phi >= -tol) || (hi - lo) <= tol) { gamma = 0.5 * (lo + hi); done = true; }
+        }
+        if (best_gamma > 0.0 && best_f <= f_base + allow) gamma = best_gamma;
+        else if (!done) gamma = 0.0;
+        return gamma;
+    };
+
+    int iters = it0;
+    for (int iter = 0; iter < P.b.max_iters; ++iter) {
+        iters = it0 + iter + 1;
+        obj_grad(c, X, G);
+        bool fwd_perm = false, away_perm = false;
+        if constexpr (LK == GBX_LMO_BIRKHOFF) {
+            // forward oracle on warp 0, DICG away oracle on warp 1
+            for (int j = tid; j < n; j += kThreads) { V[j] = 0.0; if (dicg) AW[j] = 0.0; }
+            __syncthreads();
+            if (n == c.lorder * c.lorder) {
+                if (threadIdx.x < 32) {
+                    const bool ok = hungarian_warp(hw0, c.lorder, G, 1.0, LB, UB, nullptr, V);
+                    if (threadIdx.x == 0) sh.flag[0] = ok;
+                } else if (dicg && threadIdx.x < 64) {
+                    const bool ok = hungarian_warp(hw1, c.lorder, G, -1.0, LB, UB, X, AW);
+                    if (threadIdx.x == 32) sh.flag[2] = ok;
+                }
+            } else if (tid == 0) {
+                sh.flag[0] = 0;
+                sh.flag[2] = 0;
+            }
+            __syncthreads();
+            fwd_perm = graph_perm && sh.flag[0];
+            away_perm = graph_perm && dicg && sh.flag[2];
+        } else {
+            lmo_forward<LK>(c, G, LB, UB, V);
+        }
+        score(V, fwd_perm ? hw0.pi : nullptr, hw0.pinv);
+        double loc = 0.0;
+        for (int j = tid; j < n; j += kThreads) loc = fma(G[j], X[j] - V[j], loc);
+        const double gap = bsum(loc, c.red);
+        if (gap >= 0.0 && gap < eps) break;
+
+        if (!dicg) {
+            if (search) {
+                for (int j = tid; j < n; j += kThreads) V[j] -= X[j];
+                __syncthreads();
+                const double gm = line_search(gap, 1.0, V);
+                for (int j = tid; j < n; j += kThreads) X[j] = fma(gm, V[j], X[j]);
+            } else {
+                const double gm = 2.0 / (double)(it0 + iter + 2);
+                for (int j = tid; j < n; j += kThreads) X[j] = fma(gm, V[j] - X[j], X[j]);
+            }
+            __syncthreads();
+            continue;
+        }
+        if constexpr (LK != GBX_LMO_BIRKHOFF) lmo_inface<LK>(c, G, -1.0, X, LB, UB, AW, 1);
+        score(AW, away_perm ? hw1.pi : nullptr, hw1.pinv);
+        for (int j = tid; j < n; j += kThreads) AW[j] -= V[j];
+        __syncthreads();
+        const double gmax = lmo_max_step<LK>(c, AW, X, LB, UB);
+        if (search) {
+            for (int j = tid; j < n; j += kThreads) AW[j] = -AW[j];
+            __syncthreads();
+            double pl = 0.0;
+            for (int j = tid; j < n; j += kThreads) pl = fma(-G[j], AW[j], pl);
+            const double pgap = bsum(pl, c.red);
+            const double gm = line_search(pgap, gmax, AW);
+            for (int j = tid; j < n; j += kThreads) X[j] = fma(gm, AW[j], X[j]);
+        } else {
+            const double open = 2.0 / (double)(it0 + iter + 2);
+            double gm;
+            if (ls == GBX_LS_SAFEGUARDED_SCALED_OPEN_LOOP) gm = gmax <= open ? gmax : gmax * open;
+            else if (ls == GBX_LS_SCALED_OPEN_LOOP) gm = gmax * open;
+            else gm = fmin(gmax, open);
+            for (int j = tid; j < n; j += kThreads) X[j] = fma(-gm, AW[j], X[j]);
+        }
+        __syncthreads();
+    }
+
+    // certificate at the returned iterate
+    obj_grad(c, X, G);
+    const bool fok = lmo_forward<LK>(c, G, LB, UB, V);
+    score(V, (graph_perm && fok) ? hw0.pi : nullptr, hw0.pinv);
+    double loc = 0.0;
+    for (int j = tid; j < n; j += kThreads) loc = fma(G[j], X[j] - V[j], loc);
+    const double fgap = bsum(loc, c.red);
+    const double fval = obj_value(c, X);
+    int st = (fgap >= 0.0 && fgap < eps) ? 1 : 0;
+    if (c.flags) {
+        for (int j = tid; j < n; j += kThreads) CAND[j] = c.flags[j] ? round(X[j]) : X[j];
+        __syncthreads();
+        if (rounded_feasible<LK>(c, CAND)) {
+            const double cv = integer_value(c, CAND, LB, UB, nullptr, nullptr);
+            if (cv < best_val) {
+                for (int j = tid; j < n; j += kThreads) best[j] = CAND[j];
+                if (tid == 0) P.b.best_vertex_val[node] = cv;
+            }
+        }
+    }
+    bool integral = true;
+    for (int j = tid; j < n; j += kThreads)
+        if (!isfinite(X[j]) || (c.flags && c.flags[j] && fabs(X[j] - round(X[j])) > c.tol))
+            integral = false;
+    if (__syncthreads_and(integral)) st = st ? GBX_NODE_INTEGRAL_CONVERGED : GBX_NODE_INTEGRAL_UNCONVERGED;
+    for (int j = tid; j < n; j += kThreads) gx[j] = X[j];
+    if (tid == 0) {
+        P.b.value[node] = fval;
+        P.b.gap[node] = fgap;
+        P.b.status[node] = (uint8_t)st;
+        P.b.iterations[node] = iters;
+    }
+}
+
+// ------------------------------------------------------------------ LMO probes
+template <int LK>
+__global__ void __launch_bounds__(kThreads, 1) lmo_probe_kernel(
+    gbx_lmo lmo, Layout L, int cases, int mode, const double* dir, const double* x,
+    const double* lb, const double* ub, double* out, double* out_step, double* ws) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ Scalars sh;
+    const int cs = blockIdx.x;
+    if (cs >= cases) return;
+    const int n = lmo.n, tid = threadIdx.x;
+    const size_t off = (size_t)cs * n;
+    Ctx c;
+    c.n = n;
+    c.tid = tid;
+    c.red = sh.red;
+    c.flag = sh.flag;
+    c.lk = LK;
+    c.rhs = lmo.right_side;
+    c.is_int = lmo.is_int;
+    c.lorder = lmo.order;
+    c.S = L.sort_size;
+    c.keys = reinterpret_cast<double*>(dsm + L.sm_keys);
+    c.prefix = reinterpret_cast<double*>(dsm + L.sm_prefix);
+    c.idx = reinterpret_cast<int*>(dsm + L.sm_idx);
+    c.fixed = dsm + L.sm_fixed;
+    c.hung[0] = dsm + L.sm_hung;
+    c.hung[1] = dsm + L.sm_hung + L.hung_bytes;
+    c.flags = nullptr;
+    c.tol = 0.0;
+    double* o = out + off;
+    if (mode == 0) {
+        lmo_forward<LK>(c, dir + off, lb + off, ub + off, o);
+        return;
+    }
+    if constexpr (LK == GBX_LMO_BIRKHOFF) {
+        for (int j = tid; j < n; j += kThreads) o[j] = 0.0;
+        __syncthreads();
+        if (n == c.lorder * c.lorder && threadIdx.x < 32) lmo_inface<LK>(c, dir + off, 1.0, x + off, lb + off, ub + off, o, 0);
+        __syncthreads();
+    } else {
+        lmo_inface<LK>(c, dir + off, 1.0, x + off, lb + off, ub + off, o, 0);
+    }
+    if (!out_step) return;
+    // forward vertex of -direction, then the DICG maximum step
+    double* fwd = ws + off * 2;
+    double* d = fwd + n;
+    double* neg = ws + (size_t)cases * n * 2 + off;
+    for (int j = tid; j < n; j += kThreads) neg[j] = -dir[off + j];
+    __syncthreads();
+    lmo_forward<LK>(c, neg, lb + off, ub + off, fwd);
+    for (int j = tid; j < n; j += kThreads) d[j] = o[j] - fwd[j];
+    __syncthreads();
+    const double st = lmo_max_step<LK>(c, d, x + off, lb + off, ub + off);
+    if (tid == 0) out_step[cs] = st;
+}
+
+template <int LK>
+__global__ void __launch_bounds__(kThreads, 1) feasible_kernel(
+    gbx_lmo lmo, Layout L, int cases, const double* lb, const double* ub,
+    const uint8_t* flags, uint8_t* out, double* ws) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ Scalars sh;
+    const int cs = blockIdx.x;
+    if (cs >= cases) return;
+    const int n = lmo.n;
+    Ctx c;
+    c.n = n;
+    c.tid = threadIdx.x;
+    c.red = sh.red;
+    c.flag = sh.flag;
+    c.lk = LK;
+    c.rhs = lmo.right_side;
+    c.is_int = lmo.is_int;
+    c.lorder = lmo.order;
+    c.S = L.sort_size;
+    c.hung[0] = dsm + L.sm_hung;
+    c.hung[1] = dsm + L.sm_hung + L.hung_bytes;
+    c.flags = flags;
+    c.tol = 0.0;
+    const bool ok = node_feasible<LK>(c, lb + (size_t)cs * n, ub + (size_t)cs * n, ws + (size_t)cs * n);
+    if (threadIdx.x == 0) out[cs] = ok ? 1 : 0;
+}
+
+// ------------------------------------------------------------------ host side
+namespace {
+int next_pow2(int v) { int r = 1; while (r < v) r <<= 1; return r; }
+constexpr size_t kSmemBudget = 220 * 1024;
+}
+
+int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a,
+                int n_nodes, Layout* out, std::string* err) {
+    (void)n_nodes;
+    Layout L{};
+    const int n = o.n;
+    for (int& v : L.off) v = -1;
+    const bool dicg = a.kind == GBX_ALG_DICG;
+    const bool secant = a.line_search == GBX_LS_SECANT;
+    int cnt = 0;
+    auto add = [&](int b) { L.off[b] = cnt * n; ++cnt; };
+    add(B_X); add(B_G); add(B_V);
+    if (dicg) add(B_AW);
+    if (secant) { add(B_TX); add(B_TG); }
+    if (o.kind == GBX_OBJ_GRAPH_MATCHING) add(B_R);
+    add(B_LB); add(B_UB);
+    if (secant) L.off[B_CAND] = L.off[B_TX]; else add(B_CAND);
+    L.nvec = cnt;
+
+    size_t fixed_bytes = 0;
+    if (l.kind == GBX_LMO_SIMPLEX || l.kind == GBX_LMO_EQUALITY_SIMPLEX) {
+        if (n > 8192) { *err = "simplex LMO supports n <= 8192"; return GBX_ERR_UNSUPPORTED; }
+        L.sort_size = next_pow2(n);
+        fixed_bytes += align16((size_t)L.sort_size * 8) * 2 + align16((size_t)L.sort_size * 4)
+                       + align16((size_t)n);
+    }
+    if (l.kind == GBX_LMO_BIRKHOFF) {
+        if (l.order <= 0 || l.order > 1024) { *err = "Birkhoff order out of range"; return GBX_ERR_UNSUPPORTED; }
+        L.hung_order = l.order;
+        L.hung_warps = 2;
+        L.hung_bytes = hung_ws_bytes(l.order);
+        fixed_bytes += 2 * L.hung_bytes;
+    }
+    const size_t vec_bytes = align16((size_t)cnt * n * sizeof(double));
+    size_t obj_doubles = o.kind == GBX_OBJ_GRAPH_MATCHING ? 2 * (size_t)o.order * o.order
+                                                          : (size_t)n * n;
+    const size_t obj_bytes = align16(obj_doubles * sizeof(double));
+    L.obj_doubles = obj_doubles;
+    if (vec_bytes + obj_bytes + fixed_bytes <= kSmemBudget) {
+        L.vec_smem = 1; L.obj_smem = 1;
+    } else if (vec_bytes + fixed_bytes <= kSmemBudget) {
+        L.vec_smem = 1; L.obj_smem = 0;
+    } else if (obj_bytes + fixed_bytes <= kSmemBudget) {
+        L.vec_smem = 0; L.obj_smem = 1;
+    } else {
+        L.vec_smem = 0; L.obj_smem = 0;
+    }
+    if (fixed_bytes > kSmemBudget) { *err = "LMO workspace exceeds shared memory"; return GBX_ERR_UNSUPPORTED; }
+    L.node_stride = L.vec_smem ? 0 : (size_t)cnt * n;
+    size_t p = 0;
+    L.sm_vec = p; if (L.vec_smem) p += vec_bytes;
+    L.sm_obj = p; if (L.obj_smem) p += obj_bytes;
+    L.sm_keys = p; L.sm_prefix = p; L.sm_idx = p; L.sm_fixed = p;
+    if (L.sort_size) {
+        L.sm_keys = p; p += align16((size_t)L.sort_size * 8);
+        L.sm_prefix = p; p += align16((size_t)L.sort_size * 8);
+        L.sm_idx = p; p += align16((size_t)L.sort_size * 4);
+        L.sm_fixed = p; p += align16((size_t)n);
+    }
+    L.sm_hung = p; p += 2 * L.hung_bytes;
+    L.sm_total = p;
+    L.mixed_node_bytes = 0;
+    *out = L;
+    return GBX_OK;
+}
+
+size_t workspace_bytes(const Layout& L, int n_nodes) {
+    size_t b = L.vec_smem ? 0 : L.node_stride * sizeof(double) * (size_t)n_nodes;
+    b += L.mixed_node_bytes * (size_t)n_nodes;
+    return b + 256;
+}
+
+template <int OK, int LK>
+static int launch_one(const Params& p, cudaStream_t st, std::string* err) {
+    auto k = relax_kernel<OK, LK>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)std::max<size_t>(p.L.sm_total, 1));
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    k<<<p.b.n_nodes, kThreads, p.L.sm_total, st>>>(p);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    return GBX_OK;
+}
+
+int launch_relax(const Params& p, void* stream, std::string* err) {
+    if (p.b.n_nodes == 0) return GBX_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int ok = p.obj.kind, lk = p.lmo.kind;
+#define GBX_CASE(O, LMOK) if (ok == O && lk == LMOK) return launch_one<O, LMOK>(p, st, err);
+    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_BOX)
+    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_SIMPLEX)
+    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_EQUALITY_SIMPLEX)
+    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_BIRKHOFF)
+    GBX_CASE(GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BIRKHOFF)
+    GBX_CASE(GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BOX)
+#undef GBX_CASE
+    *err = "unsupported objective/LMO combination";
+    return GBX_ERR_UNSUPPORTED;
+}
+
+template <int LK>
+static int probe_one(const gbx_lmo& l, const Layout& L, int cases, int mode, const double* dir,
+                     const double* x, const double* lb, const double* ub, double* out,
+                     double* out_step, cudaStream_t st, std::string* err) {
+    double* ws = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (out_step) {
+        e = cudaMallocAsync(&ws, (size_t)cases * l.n * 3 * sizeof(double), st);
+        if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    }
+    auto k = lmo_probe_kernel<LK>;
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(L.sm_total, 1));
+    if (e == cudaSuccess) {
+        k<<<cases, kThreads, L.sm_total, st>>>(l, L, cases, mode, dir, x, lb, ub, out, out_step, ws);
+        e = cudaGetLastError();
+    }
+    if (ws) cudaFreeAsync(ws, st);
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    return GBX_OK;
+}
+
+static int probe_layout(const gbx_lmo& l, Layout* L, std::string* err) {
+    gbx_objective o{};
+    o.kind = GBX_OBJ_DENSE_QUADRATIC;
+    o.n = l.n;
+    gbx_algorithm a{};
+    a.kind = GBX_ALG_DICG;
+    const int rc = make_layout(o, l, a, 1, L, err);
+    if (rc) return rc;
+    // probes only need the LMO scratch: rebuild offsets without node vectors
+    size_t p = 0;
+    Layout& M = *L;
+    M.sm_keys = M.sm_prefix = M.sm_idx = M.sm_fixed = 0;
+    if (M.sort_size) {
+        M.sm_keys = p; p += align16((size_t)M.sort_size * 8);
+        M.sm_prefix = p; p += align16((size_t)M.sort_size * 8);
+        M.sm_idx = p; p += align16((size_t)M.sort_size * 4);
+        M.sm_fixed = p; p += align16((size_t)l.n);
+    }
+    M.sm_hung = p; p += 2 * M.hung_bytes;
+    M.sm_total = p;
+    return GBX_OK;
+}
+
+int launch_lmo_batch(const gbx_lmo& l, int cases, int mode, const double* dir,
+                     const double* x, const double* lb, const double* ub, double* out,
+                     double* out_step, void* stream, std::string* err) {
+    if (cases == 0) return GBX_OK;
+    Layout L;
+    int rc = probe_layout(l, &L, err);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (l.kind) {
+    case GBX_LMO_BOX: return probe_one<GBX_LMO_BOX>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
+    case GBX_LMO_SIMPLEX: return probe_one<GBX_LMO_SIMPLEX>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
+    case GBX_LMO_EQUALITY_SIMPLEX: return probe_one<GBX_LMO_EQUALITY_SIMPLEX>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
+    case GBX_LMO_BIRKHOFF: return probe_one<GBX_LMO_BIRKHOFF>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
+    default: *err = "lmo kind"; return GBX_ERR_UNSUPPORTED;
+    }
+}
+
+template <int LK>
+static int feas_one(const gbx_lmo& l, const Layout& L, int cases, const double* lb,
+                    const double* ub, const uint8_t* flags, uint8_t* out, cudaStream_t st,
+                    std::string* err) {
+    double* ws = nullptr;
+    cudaError_t e = cudaMallocAsync(&ws, (size_t)cases * l.n * sizeof(double), st);
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    auto k = feasible_kernel<LK>;
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(L.sm_total, 1));
+    if (e == cudaSuccess) {
+        k<<<cases, kThreads, L.sm_total, st>>>(l, L, cases, lb, ub, flags, out, ws);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(ws, st);
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    return GBX_OK;
+}
+
+int launch_node_feasible(const gbx_lmo& l, int cases, const double* lb, const double* ub,
+                         const uint8_t* flags, uint8_t* out, void* stream, std::string* err) {
+    if (cases == 0) return GBX_OK;
+    Layout L;
+    int rc = probe_layout(l, &L, err);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (l.kind) {
+    case GBX_LMO_BOX: return feas_one<GBX_LMO_BOX>(l, L, cases, lb, ub, flags, out, st, err);
+    case GBX_LMO_SIMPLEX: return feas_one<GBX_LMO_SIMPLEX>(l, L, cases, lb, ub, flags, out, st, err);
+    case GBX_LMO_EQUALITY_SIMPLEX: return feas_one<GBX_LMO_EQUALITY_SIMPLEX>(l, L, cases, lb, ub, flags, out, st, err);
+    case GBX_LMO_BIRKHOFF: return feas_one<GBX_LMO_BIRKHOFF>(l, L, cases, lb, ub, flags, out, st, err);
+    default: *err = "lmo kind"; return GBX_ERR_UNSUPPORTED;
+    }
+}
+
+}  // namespace gbx

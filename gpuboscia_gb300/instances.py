@@ -1,0 +1,188 @@
+"""Seeded synthetic instances of the five benchmark configurations.
+
+Every draw comes from numpy's PCG64 generator (bit-stable across platforms);
+normals use an explicit Box-Muller transform so no library sampler decides
+the values. The generators return plain numpy arrays plus the objective /
+LMO / problem objects of gpuboscia_gb300.api.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+from . import api
+
+SEEDS = {1: 1001, 2: 1002, 3: 1003, 4: 1004, 5: 1005}
+
+
+def _rng(seed: int) -> np.random.Generator:
+    return np.random.Generator(np.random.PCG64(seed))
+
+
+def normal(rng: np.random.Generator, size, mean=0.0, std=1.0) -> np.ndarray:
+    """Box-Muller over the generator's uniform doubles."""
+    count = int(np.prod(size))
+    m = (count + 1) // 2
+    u1 = 1.0 - rng.random(m)          # (0, 1]
+    u2 = rng.random(m)
+    r = np.sqrt(-2.0 * np.log(u1))
+    z = np.concatenate([r * np.cos(2.0 * np.pi * u2), r * np.sin(2.0 * np.pi * u2)])[:count]
+    return (mean + std * z).reshape(size)
+
+
+def permutation(rng: np.random.Generator, n: int) -> np.ndarray:
+    """Fisher-Yates over the generator's integers."""
+    p = np.arange(n)
+    for i in range(n - 1, 0, -1):
+        j = int(rng.integers(0, i + 1))
+        p[i], p[j] = p[j], p[i]
+    return p
+
+
+def gnp_graph(rng: np.random.Generator, n: int, p: float) -> np.ndarray:
+    u = rng.random((n, n))
+    A = (np.triu(u, 1) < p).astype(np.float64)
+    A = np.triu(A, 1)
+    return A + A.T
+
+
+def random_regular(rng: np.random.Generator, n: int, d: int, mixing: int = 10) -> np.ndarray:
+    """Random simple d-regular graph: the circulant graph (i ~ i +- 1..d/2, plus
+    the antipode when d is odd) randomised by mixing*|E| degree-preserving swaps."""
+    assert n * d % 2 == 0 and d < n
+    A = np.zeros((n, n))
+    for i in range(n):
+        for k in range(1, d // 2 + 1):
+            A[i, (i + k) % n] = A[(i + k) % n, i] = 1.0
+        if d % 2:
+            A[i, (i + n // 2) % n] = A[(i + n // 2) % n, i] = 1.0
+    return double_edge_swaps(rng, A, mixing * (n * d // 2))
+
+
+def double_edge_swaps(rng: np.random.Generator, A: np.ndarray, swaps: int) -> np.ndarray:
+    """Degree-preserving swaps (a-b, c-d) -> (a-d, c-b) keeping the graph simple."""
+    A = A.copy()
+    edges = np.argwhere(np.triu(A, 1) > 0)
+    m = len(edges)
+    done = 0
+    while done < swaps:
+        i = int(rng.integers(0, m))
+        j = int(rng.integers(0, m))
+        a, b = edges[i]
+        c, d = edges[j]
+        if rng.random() < 0.5:
+            c, d = d, c
+        if len({a, b, c, d}) < 4 or A[a, d] or A[c, b]:
+            continue
+        A[a, b] = A[b, a] = A[c, d] = A[d, c] = 0.0
+        A[a, d] = A[d, a] = A[c, b] = A[b, c] = 1.0
+        edges[i] = (a, d)
+        edges[j] = (c, b)
+        done += 1
+    return A
+
+
+def permute(A: np.ndarray, p: np.ndarray) -> np.ndarray:
+    """B = P A P' with P[i, p[i]] = 1, i.e. B[i, j] = A[p[i], p[j]]."""
+    return A[np.ix_(p, p)]
+
+
+@dataclasses.dataclass
+class Instance:
+    name: str
+    problem: api.Problem
+    objective: object
+    lmo: object
+    settings: api.Settings
+    known_optimum: float | None = None
+    solution: np.ndarray | None = None
+
+
+def box_qp(n: int = 64, seed: int = SEEDS[1]) -> Instance:
+    """Config 1: f = x'Qx/2 + c'x, Q = M'M/64 + 0.1 I, x binary in [0,1]^n."""
+    rng = _rng(seed)
+    M = normal(rng, (n, n))
+    Q = M.T @ M / 64.0 + 0.1 * np.eye(n)
+    Q = 0.5 * (Q + Q.T)
+    c = rng.random(n) * 2.0 - 1.0
+    prob = api.Problem(n, np.zeros(n), np.ones(n), list(range(n)))
+    s = api.Settings(algorithm=0, line_search=4, rel_gap_tol=1e-6, abs_gap_tol=1e-6)
+    return Instance("box_bqp_n64", prob, api.DenseQuadraticObjective(Q, c), api.BoxLMO(), s)
+
+
+def graph_matching(order: int, A: np.ndarray, B: np.ndarray, name: str, known=None, solution=None) -> Instance:
+    n = order * order
+    prob = api.Problem(n, np.zeros(n), np.ones(n), list(range(n)))
+    s = api.Settings(algorithm=1, line_search=0, natural_lower_bound=0.0, rel_gap_tol=1e-6, abs_gap_tol=1e-6)
+    return Instance(name, prob, api.GraphMatchingObjective(A, B, 1.0), api.BirkhoffLMO(order), s, known, solution)
+
+
+def birkhoff_gnp(order: int = 36, seed: int = SEEDS[2]) -> Instance:
+    """Config 2: A = G(order, 1/2), B = P A P', optimum 0 at X = P'."""
+    rng = _rng(seed)
+    A = gnp_graph(rng, order, 0.5)
+    p = permutation(rng, order)
+    B = permute(A, p)
+    X = np.zeros((order, order))
+    X[p, np.arange(order)] = 1.0   # X = P': AX = XB
+    return graph_matching(order, A, B, f"birkhoff_gnp_n{order}", 0.0, X.ravel())
+
+
+def birkhoff_regular_perturbed(order: int = 120, degree: int = 8, swaps: int = 20,
+                               seed: int = SEEDS[4]) -> Instance:
+    """Config 4: A d-regular, B = A after `swaps` double-edge swaps, then permuted (optimum > 0)."""
+    rng = _rng(seed)
+    A = random_regular(rng, order, degree)
+    B = permute(double_edge_swaps(rng, A, swaps), permutation(rng, order))
+    return graph_matching(order, A, B, f"birkhoff_regular_n{order}_perturbed")
+
+
+def birkhoff_regular_isomorphic(order: int = 400, degree: int = 10, seed: int = SEEDS[5]) -> Instance:
+    """Config 5: A d-regular, B = P A P' (optimum 0)."""
+    rng = _rng(seed)
+    A = random_regular(rng, order, degree)
+    p = permutation(rng, order)
+    X = np.zeros((order, order))
+    X[p, np.arange(order)] = 1.0
+    return graph_matching(order, A, permute(A, p), f"birkhoff_regular_n{order}", 0.0, X.ravel())
+
+
+def birkhoff_node_batch(order: int, nodes: int, seed: int, max_forced: int | None = None,
+                        forbid_frac: float = 0.05):
+    """Open B&B nodes with uneven fixings over the order x order Birkhoff
+    polytope: node i forces a random number of edges of its own random
+    permutation and forbids a random subset of the others, so every node is
+    feasible but nodes differ in size and active set. Returns (lb, ub) [nodes, n]."""
+    rng = _rng(seed)
+    n = order * order
+    max_forced = order // 3 if max_forced is None else max_forced
+    lb = np.zeros((nodes, n))
+    ub = np.ones((nodes, n))
+    for i in range(nodes):
+        p = permutation(rng, order)
+        keep = np.zeros((order, order), dtype=bool)
+        keep[np.arange(order), p] = True
+        forced = int(rng.integers(0, max_forced + 1))
+        rows = permutation(rng, order)[:forced]
+        L = np.zeros((order, order))
+        L[rows, p[rows]] = 1.0
+        U = np.where((rng.random((order, order)) < forbid_frac) & ~keep, 0.0, 1.0)
+        lb[i] = L.ravel()
+        ub[i] = U.ravel()
+    return lb, ub
+
+
+def box_node_batch(n: int, nodes: int, seed: int, max_fixed: int | None = None):
+    """Open B&B nodes of a binary box problem with uneven numbers of fixed variables."""
+    rng = _rng(seed)
+    max_fixed = n // 4 if max_fixed is None else max_fixed
+    lb = np.zeros((nodes, n))
+    ub = np.ones((nodes, n))
+    for i in range(nodes):
+        k = int(rng.integers(0, max_fixed + 1))
+        idx = permutation(rng, n)[:k]
+        val = (rng.random(k) < 0.5).astype(np.float64)
+        lb[i, idx] = val
+        ub[i, idx] = val
+    return lb, ub

@@ -1,0 +1,95 @@
+// lmo.h -- the built-in linear minimization oracles (reference: include/gpuboscia/lmo.cuh).
+//
+// These are host-side descriptors: the oracles themselves run inside the
+// GB300 relaxation kernel (libgpuboscia_gb300). Each type keeps the reference
+// name, its supports_dicg flag and relaxation_feasible_cpu, and describes
+// itself to the C ABI through spec().
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#include "../gpuboscia_gb300.h"
+
+namespace gpuboscia {
+// What the relaxation kernel needs to know about an LMO (host data).
+struct LMOSpec {
+    int kind = GBX_LMO_BOX;
+    double right_side = 1.0;
+    std::vector<uint8_t> is_int;  // simplex integer flags, empty = none
+    int order = 0;
+};
+}  // namespace gpuboscia
+
+// argmin over the box [lb, ub] (lmo.cuh:212-321)
+struct BoxLMO {
+    static constexpr bool supports_dicg = true;
+    bool relaxation_feasible_cpu(const std::vector<double>&, const std::vector<double>&,
+                                 const std::vector<double>&, double) const {
+        return true;  // the public API checks the box bounds itself
+    }
+    gpuboscia::LMOSpec spec(int) const { return {GBX_LMO_BOX, 1.0, {}, 0}; }
+};
+
+// Bounded simplex {x >= 0, sum x <= right_side} (== with RequireEquality),
+// integer coordinates capped by their branch interval (lmo.cuh:335-912).
+template <int MaxN, bool RequireEquality = false>
+struct UnitSimplexLMO {
+    static constexpr bool supports_dicg = true;
+    double right_side = 1.0;
+    unsigned char is_int[MaxN]{};
+
+    UnitSimplexLMO() = default;
+    UnitSimplexLMO(double rhs, int n, const std::vector<int>& int_vars) : right_side(rhs) {
+        set_integer_vars(n, int_vars);
+    }
+    void set_integer_vars(int n, const std::vector<int>& int_vars) {
+        std::fill(is_int, is_int + MaxN, (unsigned char)0);
+        const int capped = std::min(n, MaxN);
+        for (int idx : int_vars)
+            if (idx >= 0 && idx < capped) is_int[idx] = 1;
+    }
+    bool relaxation_feasible_cpu(const std::vector<double>& x, const std::vector<double>&,
+                                 const std::vector<double>&, double tol) const {
+        double mass = 0.0;
+        if (RequireEquality) {
+            for (double v : x) { if (v < -tol) return false; mass += v; }
+            return std::isfinite(mass) && std::abs(mass - right_side) <= tol;
+        }
+        for (double v : x) { if (v < 0.0) return false; mass += v; }
+        return mass <= right_side + tol;
+    }
+    gpuboscia::LMOSpec spec(int n) const {
+        gpuboscia::LMOSpec s;
+        s.kind = RequireEquality ? GBX_LMO_EQUALITY_SIMPLEX : GBX_LMO_SIMPLEX;
+        s.right_side = right_side;
+        s.is_int.assign(n, 0);
+        for (int j = 0; j < std::min(n, MaxN); ++j) s.is_int[j] = is_int[j];
+        return s;
+    }
+};
+
+template <int MaxN>
+using EqualitySimplexLMO = UnitSimplexLMO<MaxN, true>;
+
+// Order x Order Birkhoff polytope, row-major; lb > 1/2 forces an edge,
+// ub < 1/2 forbids it; exact Hungarian assignment (lmo.cuh:918-1419).
+template <int Order>
+struct BirkhoffLMO {
+    static_assert(Order > 0, "Birkhoff order must be positive");
+    static constexpr bool supports_dicg = true;
+    static constexpr int variable_count = Order * Order;
+    bool relaxation_feasible_cpu(const std::vector<double>& x, const std::vector<double>&,
+                                 const std::vector<double>&, double tol) const {
+        if (x.size() != static_cast<size_t>(variable_count)) return false;
+        for (double v : x) if (v < -tol || v > 1 + tol) return false;
+        for (int i = 0; i < Order; ++i) {
+            double row = 0, col = 0;
+            for (int j = 0; j < Order; ++j) { row += x[i * Order + j]; col += x[j * Order + i]; }
+            if (std::abs(row - 1) > tol || std::abs(col - 1) > tol) return false;
+        }
+        return true;
+    }
+    gpuboscia::LMOSpec spec(int) const { return {GBX_LMO_BIRKHOFF, 1.0, {}, Order}; }
+};

@@ -1,0 +1,229 @@
+/*
+ * gpuboscia_gb300.h -- C ABI of the GB300 node-relaxation library.
+ *
+ * The reference library (GPUBoscia) is header-only C++/CUDA: its hot path is
+ * the template kernel drs_fw_relax_batch_kernel<Objective, Algorithm, LMO>
+ * (include/gpuboscia/device_resident_solver.cuh:631-660) launched by
+ * DeviceResidentHybridSolver::run_slot (device_resident_solver.cuh:1775-1863).
+ * This header replaces that launch with plain extern "C" entry points over
+ * caller-owned device buffers, so any host language can bind the path.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (GBX_OK == 0, negative on error)
+ *     and never throws; gbx_last_error() gives a thread-local message.
+ *   - Pointers named d_* / documented "device" are CUDA device pointers owned
+ *     by the caller; "host" pointers are ordinary host memory.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *   - Node vectors are node-major, row-major: x[node * n + j]. Birkhoff
+ *     variables are e = r * order + c (lmo.cuh:914-917).
+ */
+#ifndef GPUBOSCIA_GB300_H
+#define GPUBOSCIA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBX_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    GBX_OK = 0,
+    GBX_ERR_INVALID = -1,      /* bad sizes, null pointers, bad enums        */
+    GBX_ERR_UNSUPPORTED = -2,  /* objective/LMO/algorithm combination        */
+    GBX_ERR_CUDA = -3,         /* a CUDA runtime call failed                 */
+    GBX_ERR_WORKSPACE = -4,    /* workspace too small                        */
+    GBX_ERR_TIMEOUT = -5       /* a bounded device wait gave up              */
+};
+
+/* ---- per-node status byte (device_resident_solver.cuh:192-202) --------- */
+enum {
+    GBX_NODE_FRACTIONAL_UNCONVERGED = 0,
+    GBX_NODE_FRACTIONAL_CONVERGED = 1,
+    GBX_NODE_INFEASIBLE = 2,
+    GBX_NODE_INTEGRAL_UNCONVERGED = 3,
+    GBX_NODE_INTEGRAL_CONVERGED = 4,
+    /* input-only flag: x holds a caller-supplied start (DRSInitialPointSupplied) */
+    GBX_NODE_INITIAL_POINT_SUPPLIED = 0x80
+};
+
+/* ---- objectives --------------------------------------------------------- */
+enum {
+    /* f(x) = 0.5*scale*x'Qx + scale*linear_scale*c'x + constant; Q symmetric
+     * (GlobalCachedDenseQuadraticObjective, dense_quadratic_objectives.cuh:18-112) */
+    GBX_OBJ_DENSE_QUADRATIC = 1,
+    /* f(X) = scale*||A X - X B||_F^2 over order x order X
+     * (GraphIsoObjective, examples/main.cu:131-181, is scale=0.5 with A,B swapped) */
+    GBX_OBJ_GRAPH_MATCHING = 2
+};
+
+typedef struct gbx_objective {
+    int kind;             /* GBX_OBJ_*                                        */
+    int n;                /* number of variables                              */
+    /* dense quadratic */
+    const double* Q;      /* device, n*n; Q[k*n + j] multiplies x_k in grad_j
+                           * (the transposed storage of
+                           * dense_quadratic_objectives.cuh:22-23; a
+                           * symmetric matrix needs no care)                */
+    const double* c;      /* device, n (may be NULL)                          */
+    double scale;         /* grad_scale                                       */
+    double linear_scale;
+    double constant;
+    /* graph matching */
+    int order;            /* n == order*order                                 */
+    const double* A;      /* device, order*order row-major                    */
+    const double* B;      /* device, order*order row-major                    */
+} gbx_objective;
+
+/* ---- linear minimization oracles (lmo.cuh) ----------------------------- */
+enum {
+    GBX_LMO_BOX = 1,                /* BoxLMO, lmo.cuh:212-321                        */
+    GBX_LMO_SIMPLEX = 2,            /* UnitSimplexLMO<n,false>, lmo.cuh:335-907       */
+    GBX_LMO_EQUALITY_SIMPLEX = 3,   /* EqualitySimplexLMO<n>, lmo.cuh:911-912         */
+    GBX_LMO_BIRKHOFF = 4            /* BirkhoffLMO<order>, lmo.cuh:918-1419           */
+};
+
+typedef struct gbx_lmo {
+    int kind;                 /* GBX_LMO_*                                    */
+    int n;                    /* number of variables                          */
+    double right_side;        /* simplex mass                                 */
+    const uint8_t* is_int;    /* device, n: the simplex LMO's integer flags   */
+    int order;                /* Birkhoff order                               */
+} gbx_lmo;
+
+/* ---- algorithm policy (algorithms.cuh, line_search_options.h) ---------- */
+enum { GBX_ALG_FRANK_WOLFE = 0, GBX_ALG_DICG = 1 };
+enum {                        /* same order as LineSearchKind                */
+    GBX_LS_OPEN_LOOP = 0,
+    GBX_LS_SCALED_OPEN_LOOP = 1,
+    GBX_LS_SAFEGUARDED_SCALED_OPEN_LOOP = 2,
+    GBX_LS_SECANT = 3,
+    GBX_LS_QUADRATIC_EXACT = 4
+};
+enum {
+    GBX_PRECISION_FP64 = 0,   /* plain FP64 method (the drop-in)              */
+    GBX_PRECISION_MIXED = 1   /* BF16 split tensor-core gradient, FP64 certificate */
+};
+
+typedef struct gbx_algorithm {
+    int kind;                 /* GBX_ALG_*                                    */
+    int line_search;          /* GBX_LS_*                                     */
+    int secant_iters;         /* SecantLS::max_iters (default 4)              */
+    double secant_tol;        /* SecantLS::tolerance (default 1e-10)          */
+    double secant_denom_eps;  /* SecantLS::denom_eps (default 1e-14)          */
+    int precision;            /* GBX_PRECISION_*                              */
+} gbx_algorithm;
+
+/* ---- one batch of B&B nodes (the arguments of drs_fw_relax_batch_kernel,
+ *      device_resident_solver.cuh:634-654) -------------------------------- */
+typedef struct gbx_node_batch {
+    int n_nodes;
+    int max_iters;            /* FW iteration budget of this dispatch         */
+    double candidate_tol;     /* integer tolerance for vertex scoring         */
+    double* x;                /* device [n_nodes*n] in: start/resume, out: iterate */
+    const double* lb;         /* device [n_nodes*n]                           */
+    const double* ub;         /* device [n_nodes*n]                           */
+    const double* eps;        /* device [n_nodes] FW gap tolerance per node   */
+    int* iterations;          /* device [n_nodes] in: done so far, out: total */
+    uint8_t* status;          /* device [n_nodes] in: 0 or 0x80, out: GBX_NODE_* */
+    double* gap;              /* device [n_nodes] out: FW gap at returned x   */
+    double* value;            /* device [n_nodes] out: f(x)                   */
+    double* best_vertex;      /* device [n_nodes*n] out: best integral point  */
+    double* best_vertex_val;  /* device [n_nodes] out: its value (1e300 none) */
+    const uint8_t* integer_flags; /* device [n] problem integer flags         */
+} gbx_node_batch;
+
+/* Library identity. */
+int gbx_abi_version(void);
+const char* gbx_last_error(void);
+
+/* Bytes of device scratch gbx_relax_batch needs for this batch (node vectors
+ * that do not fit in shared memory, Hungarian state, split-precision tiles).
+ * Replaces the slot workspace sizing of DRSStreamSlot::alloc
+ * (device_resident_solver.cuh:1094-1128). */
+size_t gbx_relax_workspace_bytes(const gbx_objective* obj, const gbx_lmo* lmo,
+                                 const gbx_algorithm* alg, int n_nodes);
+
+/* Relax every node of the batch with FW/DICG on the GPU (one launch on
+ * `stream`; asynchronous). Replaces drs_fw_relax_batch_kernel<<<N,...>>>
+ * (device_resident_solver.cuh:1834-1851). `workspace` is caller-owned device
+ * memory of at least gbx_relax_workspace_bytes() bytes. */
+int gbx_relax_batch(const gbx_objective* obj, const gbx_lmo* lmo,
+                    const gbx_algorithm* alg, const gbx_node_batch* batch,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
+/* Batched LMO calls, one case per row (the probes of tests/test_pipeline.cu:
+ * 96-163). mode 0: forward v = argmin <direction, v> over the node's set
+ * (LMO::compute_v); mode 1: in-face away oracle (LMO::compute_inface_v) on
+ * the minimal face of x. All arrays are device [cases*n]; x may be NULL for
+ * mode 0. out_step (device [cases], may be NULL) receives, for mode 1, the
+ * DICG maximum step of x - gamma*(out - fwd) where fwd is the forward vertex
+ * of -direction (dicg_maximum_step_local + dicg_sum_maximum_step). */
+int gbx_lmo_batch(const gbx_lmo* lmo, int cases, int mode,
+                  const double* direction, const double* x,
+                  const double* lb, const double* ub, double* out,
+                  double* out_step, void* stream);
+
+/* Node feasibility before any objective work (drs_node_feasible,
+ * device_resident_solver.cuh:206-217): out[case] = 1 feasible, 0 infeasible. */
+int gbx_node_feasible_batch(const gbx_lmo* lmo, int cases, const double* lb,
+                            const double* ub, const uint8_t* integer_flags,
+                            uint8_t* out, void* stream);
+
+/* ---- whole branch-and-bound solve (gpuboscia::solve, gpuboscia.cuh:108-170)
+ * for callers without the C++ headers. Objective/LMO data are device pointers
+ * owned by the caller (as in the reference); problem data are host arrays. */
+typedef struct gbx_problem {
+    int n_vars;
+    const double* lb;         /* host [n_vars] */
+    const double* ub;         /* host [n_vars] */
+    const int* int_vars;      /* host [n_int]  */
+    int n_int;
+} gbx_problem;
+
+typedef struct gbx_settings {
+    /* DeviceResidentConfig (device_resident_solver.cuh:1004-1025) */
+    int gpu_batch_size;       /* 1024 */
+    int num_streams;          /* 8    */
+    int gpu_max_iters;        /* 20000 */
+    double gpu_eps;           /* 1e-3 */
+    double gpu_eps_decay;     /* 0.8  */
+    double gpu_eps_min;       /* 1e-6 */
+    double integer_tol;       /* 1e-6 */
+    double abs_gap_tol;       /* 1e-6 */
+    double rel_gap_tol;       /* 1e-2 */
+    /* Settings (gpuboscia.cuh:21-32) */
+    gbx_algorithm algorithm;
+    double time_limit_seconds;   /* +inf */
+    double natural_lower_bound;  /* -inf */
+    const double* root_initial_point; /* host [n_vars] or NULL */
+    int branch_k;             /* branch_pow2 k (3) */
+    int use_cuda_graph;       /* capture the relax launch (1) */
+} gbx_settings;
+
+typedef struct gbx_result {
+    double objective;         /* +inf when no incumbent                       */
+    double dual_bound;
+    int nodes_processed;
+    double elapsed_seconds;
+    int reached_tolerance;
+    int reached_time_limit;
+    int has_incumbent;
+    double* x;                /* host [n_vars], caller-owned, filled when has_incumbent */
+} gbx_result;
+
+/* Fill *s with the reference defaults (create_default_settings). */
+void gbx_default_settings(gbx_settings* s);
+
+int gbx_solve(const gbx_problem* problem, const gbx_objective* obj,
+              const gbx_lmo* lmo, const gbx_settings* settings,
+              gbx_result* result);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPUBOSCIA_GB300_H */

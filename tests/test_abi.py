@@ -1,0 +1,124 @@
+"""The C-ABI library loads on a CPU-only machine, exports every entry point the
+header declares, and its structures have the layout the ctypes mirror uses.
+No compute call is made here."""
+import ctypes as C
+import pathlib
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from gpuboscia_gb300 import _abi as A
+from gpuboscia_gb300 import api, build
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "gpuboscia_gb300.h"
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return A.load()
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbx_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_header_declares_the_exported_set():
+    assert declared_functions() == sorted(A.EXPORTED_SYMBOLS)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(A.LIB_PATH)], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(re.findall(r" T (gbx_\w+)", out))
+    missing = [f for f in declared_functions() if f not in exported]
+    assert not missing, missing
+    for f in declared_functions():
+        assert hasattr(lib, f)
+    assert lib.gbx_abi_version() == 1
+
+
+_LAYOUT_C = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "gpuboscia_gb300.h"
+#define S(T) printf(#T " %zu\n", sizeof(T));
+#define O(T, f) printf(#T "." #f " %zu\n", offsetof(T, f));
+int main(void) {
+  S(gbx_objective) O(gbx_objective, Q) O(gbx_objective, constant) O(gbx_objective, B)
+  S(gbx_lmo) O(gbx_lmo, is_int) O(gbx_lmo, order)
+  S(gbx_algorithm) O(gbx_algorithm, secant_tol) O(gbx_algorithm, precision)
+  S(gbx_node_batch) O(gbx_node_batch, x) O(gbx_node_batch, integer_flags)
+  S(gbx_problem) O(gbx_problem, n_int)
+  S(gbx_settings) O(gbx_settings, algorithm) O(gbx_settings, time_limit_seconds) O(gbx_settings, use_cuda_graph)
+  S(gbx_result) O(gbx_result, x)
+  return 0;
+}
+"""
+
+
+def test_struct_layouts_match_ctypes(tmp_path):
+    src = tmp_path / "layout.c"
+    src.write_text(_LAYOUT_C)
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                       check=True).stdout.splitlines())
+    M = {"gbx_objective": A.Objective, "gbx_lmo": A.LMO, "gbx_algorithm": A.Algorithm,
+         "gbx_node_batch": A.NodeBatch, "gbx_problem": A.Problem, "gbx_settings": A.Settings,
+         "gbx_result": A.Result}
+    for key, val in got.items():
+        if "." in key:
+            t, f = key.split(".")
+            assert getattr(M[t], f).offset == int(val), key
+        else:
+            assert C.sizeof(M[key]) == int(val), key
+
+
+def test_default_settings_match_reference_defaults(lib):
+    s = A.Settings()
+    lib.gbx_default_settings(C.byref(s))
+    d = A.default_settings()
+    for f, _ in A.Settings._fields_:
+        if f == "algorithm":
+            for g, _ in A.Algorithm._fields_:
+                assert getattr(s.algorithm, g) == getattr(d.algorithm, g), g
+        elif f != "root_initial_point":
+            assert getattr(s, f) == getattr(d, f), f
+
+
+def test_workspace_sizing_is_host_only(lib):
+    """gbx_relax_workspace_bytes runs without a GPU; invalid descriptors give 0."""
+    keep = api._Keep()
+    inst_A = np.zeros((36, 36))
+    obj = api.GraphMatchingObjective(inst_A, inst_A).to_c("host", keep)
+    lmo = api.BirkhoffLMO(36).to_c(36 * 36, "host", keep)
+    alg = A.Algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT, 4, 1e-10, 1e-14, A.PRECISION_FP64)
+    assert lib.gbx_relax_workspace_bytes(C.byref(obj), C.byref(lmo), C.byref(alg), 256) > 0
+    big = api.GraphMatchingObjective(np.zeros((120, 120)), np.zeros((120, 120))).to_c("host", keep)
+    blmo = api.BirkhoffLMO(120).to_c(120 * 120, "host", keep)
+    # order 120 node vectors spill to the global workspace: it scales with the batch
+    w1 = lib.gbx_relax_workspace_bytes(C.byref(big), C.byref(blmo), C.byref(alg), 1)
+    w8 = lib.gbx_relax_workspace_bytes(C.byref(big), C.byref(blmo), C.byref(alg), 8)
+    assert w8 > w1 > 120 * 120 * 8
+    bad = A.LMO(A.LMO_BIRKHOFF, 36 * 36, 1.0, None, 35)
+    assert lib.gbx_relax_workspace_bytes(C.byref(obj), C.byref(bad), C.byref(alg), 4) == 0
+    assert b"order" in lib.gbx_last_error()
+
+
+def test_relax_rejects_bad_arguments_without_launching(lib):
+    keep = api._Keep()
+    obj = api.DenseQuadraticObjective(np.eye(4)).to_c("host", keep)
+    lmo = api.BoxLMO().to_c(4, "host", keep)
+    alg = A.Algorithm(A.ALG_FRANK_WOLFE, 9, 4, 1e-10, 1e-14, A.PRECISION_FP64)
+    b = A.NodeBatch()
+    assert lib.gbx_relax_batch(C.byref(obj), C.byref(lmo), C.byref(alg), C.byref(b), None, 0, None) == A.ERR_INVALID
+    alg.line_search = A.LS_OPEN_LOOP
+    b.n_nodes = 2
+    assert lib.gbx_relax_batch(C.byref(obj), C.byref(lmo), C.byref(alg), C.byref(b), None, 0, None) == A.ERR_INVALID
+    assert b"null" in lib.gbx_last_error()
