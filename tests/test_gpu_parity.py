@@ -238,3 +238,19 @@ def test_node_feasibility_matches_oracle(cuda_lib):
     g = api.node_feasible_batch(lmo, _t(lb), _t(ub), _t(np.ones(n, np.uint8)))
     o = O.feasible(lmo, lb, ub, np.ones(n, np.uint8))
     assert np.array_equal(g.cpu().numpy(), o)
+
+
+def test_birkhoff_order64_workspace_path_bitwise(cuda_lib):
+    """Order 64 (4096 variables): the node vectors exceed shared memory and live in the
+    caller's global workspace; results stay bit-identical to the oracle."""
+    import ctypes as C
+    inst = instances.birkhoff_gnp(order=64, seed=13)
+    keep = api._Keep()
+    o = inst.objective.to_c("host", keep)
+    lm = inst.lmo.to_c(64 * 64, "host", keep)
+    alg = O.algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT)
+    per_node = cuda_lib.gbx_relax_workspace_bytes(C.byref(o), C.byref(lm), C.byref(alg), 1)
+    assert per_node > 4096 * 8 * 4, "order 64 should spill node vectors to the workspace"
+    lb, ub = instances.birkhoff_node_batch(64, 4, seed=3)
+    g, o_ = run_both(inst.objective, inst.lmo, alg, lb.copy(), lb, ub, 1e-6, 6, np.ones(4096, np.uint8))
+    assert_same(g, o_)
