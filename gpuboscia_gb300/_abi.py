@@ -140,10 +140,13 @@ def default_settings() -> Settings:
     return s
 
 
+# bytes of the library-owned scratch of gbx_relax_batch_static (GBX_STATIC_SCRATCH_BYTES)
+STATIC_SCRATCH_BYTES = 32 << 20
+
 # exported symbols of the CUDA library, as declared in include/gpuboscia_gb300.h
 EXPORTED_SYMBOLS = (
     "gbx_abi_version", "gbx_last_error", "gbx_relax_workspace_bytes",
-    "gbx_relax_batch", "gbx_lmo_batch", "gbx_node_feasible_batch",
+    "gbx_relax_batch", "gbx_relax_batch_static", "gbx_lmo_batch", "gbx_node_feasible_batch",
     "gbx_default_settings", "gbx_solve",
 )
 
@@ -169,6 +172,8 @@ def load(path: os.PathLike | str | None = None) -> C.CDLL:
     lib.gbx_relax_batch.restype = C.c_int
     lib.gbx_relax_batch.argtypes = [P(Objective), P(LMO), P(Algorithm), P(NodeBatch),
                                     C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.gbx_relax_batch_static.restype = C.c_int
+    lib.gbx_relax_batch_static.argtypes = [P(Objective), P(LMO), P(Algorithm), P(NodeBatch), C.c_void_p]
     lib.gbx_lmo_batch.restype = C.c_int
     lib.gbx_lmo_batch.argtypes = [P(LMO), C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]

@@ -155,6 +155,20 @@ int gbx_relax_batch(const gbx_objective* obj, const gbx_lmo* lmo,
                     const gbx_algorithm* alg, const gbx_node_batch* batch,
                     void* workspace, size_t workspace_bytes, void* stream);
 
+/* The same relaxation for callers that cannot allocate device memory (a host
+ * language without a CUDA allocator, memory owned by another runtime's pool, a
+ * loop where allocation is not allowed). No counterpart in the reference: the
+ * scratch lives in a library-owned __device__ array of GBX_STATIC_SCRATCH_BYTES
+ * (32 MiB, held on every GPU that loads the library until exit); batches that
+ * need more are rejected with GBX_ERR_WORKSPACE. The first call on a device
+ * looks the array up and should come before any stream capture. Calls share
+ * the array, so calls that overlap on the GPU race: issue them on one stream.
+ * Allocates nothing. */
+#define GBX_STATIC_SCRATCH_BYTES (32u << 20)
+int gbx_relax_batch_static(const gbx_objective* obj, const gbx_lmo* lmo,
+                           const gbx_algorithm* alg, const gbx_node_batch* batch,
+                           void* stream);
+
 /* Batched LMO calls, one case per row (the probes of tests/test_pipeline.cu:
  * 96-163). mode 0: forward v = argmin <direction, v> over the node's set
  * (LMO::compute_v); mode 1: in-face away oracle (LMO::compute_inface_v) on
