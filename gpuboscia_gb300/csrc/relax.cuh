@@ -30,7 +30,11 @@ struct Layout {
     size_t hung_bytes;      // bytes per Hungarian workspace
     // byte offsets inside dynamic shared memory
     size_t sm_vec, sm_obj, sm_keys, sm_prefix, sm_idx, sm_fixed, sm_hung, sm_total;
-    // bytes of the mixed-precision scratch (per node, global)
+    // mixed precision (GBX_PRECISION_MIXED, Birkhoff graph matching): FP32
+    // x, gradient, residual, A, B, B' [6 n floats], edge / face code bytes
+    // [2 n], and two integer Hungarian workspaces with warm state
+    int mixed;
+    size_t sm_mx, sm_code, sm_ihw, ihw_bytes;
     size_t mixed_node_bytes;
 };
 
@@ -43,6 +47,35 @@ struct Params {
     double* ws;             // global workspace (node vectors when not in smem)
     unsigned char* mixed;   // mixed-precision scratch
 };
+
+#ifdef __CUDACC__
+#define GBX_HD __host__ __device__
+#else
+#define GBX_HD
+#endif
+
+GBX_HD inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
+
+// bytes of one FP64 Hungarian workspace (potentials, minv, path, forced maps)
+GBX_HD inline size_t hung_ws_bytes(int m) {
+    size_t b = 0;
+    b += align16(3 * (size_t)(m + 1) * sizeof(double));     // u, pv, minv
+    b += align16(2 * (size_t)(m + 1) * sizeof(int));        // p, way
+    b += align16(6 * (size_t)m * sizeof(int));              // fcol frow rows cols pi pinv
+    b += align16(8 * sizeof(int));                          // scalars
+    b += align16((size_t)(m + 1));                          // used
+    return b;
+}
+
+// bytes of one integer Hungarian workspace of the mixed path (with warm state)
+GBX_HD inline size_t ihw_bytes(int m) {
+    size_t b = 0;
+    b += align16(5 * (size_t)(m + 1) * sizeof(int));   // u pv minv p way
+    b += align16(9 * (size_t)m * sizeof(int));         // rows cols rowpos fcol frow pi colpot match pinv
+    b += align16((size_t)(m + 1) * 2);                 // used, rmatch
+    b += align16(8 * sizeof(int));                     // scalars
+    return b;
+}
 
 // thread-local message returned by gbx_last_error() (capi.cu)
 void set_last_error(const std::string& msg);

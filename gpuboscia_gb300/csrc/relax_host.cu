@@ -1,0 +1,192 @@
+// relax_host.cu -- launch planning (shared-memory layout, workspace sizing)
+// and dispatch of the node-relaxation kernels over the objective / LMO kinds.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+
+#include "relax.cuh"
+
+namespace gbx {
+
+template <int OK, int LK>
+int launch_one(const Params& p, cudaStream_t st, std::string* err);
+template <int LK>
+int probe_one(const gbx_lmo& l, const Layout& L, int cases, int mode, const double* dir, const double* x,
+              const double* lb, const double* ub, double* out, double* out_step, cudaStream_t st,
+              std::string* err);
+template <int LK>
+int feas_one(const gbx_lmo& l, const Layout& L, int cases, const double* lb, const double* ub,
+             const uint8_t* flags, uint8_t* out, cudaStream_t st, std::string* err);
+
+namespace {
+int next_pow2(int v) { int r = 1; while (r < v) r <<= 1; return r; }
+constexpr size_t kSmemBudget = 220 * 1024;
+}
+
+int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a,
+                int n_nodes, Layout* out, std::string* err) {
+    (void)n_nodes;
+    Layout L{};
+    const int n = o.n;
+    for (int& v : L.off) v = -1;
+    const bool dicg = a.kind == GBX_ALG_DICG;
+    const bool secant = a.line_search == GBX_LS_SECANT;
+    const bool mixed = a.precision == GBX_PRECISION_MIXED;
+    if (mixed) {
+        if (o.kind != GBX_OBJ_GRAPH_MATCHING || l.kind != GBX_LMO_BIRKHOFF) {
+            *err = "mixed precision covers the graph-matching objective over the Birkhoff polytope";
+            return GBX_ERR_UNSUPPORTED;
+        }
+        if (secant) {
+            *err = "the secant line search is not available in mixed precision";
+            return GBX_ERR_UNSUPPORTED;
+        }
+    }
+    int cnt = 0;
+    auto add = [&](int b) { L.off[b] = cnt * n; ++cnt; };
+    add(B_X); add(B_G); add(B_V);
+    if (dicg && !mixed) add(B_AW);
+    if (secant) { add(B_TX); add(B_TG); }
+    if (o.kind == GBX_OBJ_GRAPH_MATCHING) add(B_R);
+    add(B_LB); add(B_UB);
+    if (secant) L.off[B_CAND] = L.off[B_TX]; else add(B_CAND);
+    L.nvec = cnt;
+
+    size_t fixed_bytes = 0;
+    if (l.kind == GBX_LMO_SIMPLEX || l.kind == GBX_LMO_EQUALITY_SIMPLEX) {
+        if (n > 8192) { *err = "simplex LMO supports n <= 8192"; return GBX_ERR_UNSUPPORTED; }
+        L.sort_size = next_pow2(n);
+        fixed_bytes += align16((size_t)L.sort_size * 8) * 2 + align16((size_t)L.sort_size * 4)
+                       + align16((size_t)n);
+    }
+    if (l.kind == GBX_LMO_BIRKHOFF) {
+        if (l.order <= 0 || l.order > 1024) { *err = "Birkhoff order out of range"; return GBX_ERR_UNSUPPORTED; }
+        L.hung_order = l.order;
+        L.hung_warps = 2;
+        L.hung_bytes = hung_ws_bytes(l.order);
+        fixed_bytes += 2 * L.hung_bytes;
+    }
+    L.mixed = mixed ? 1 : 0;
+    size_t mx_bytes = 0, code_bytes = 0;
+    if (mixed) {
+        mx_bytes = align16(6 * (size_t)n * sizeof(float));
+        code_bytes = align16(2 * (size_t)n);
+        L.ihw_bytes = ihw_bytes(l.order);
+        fixed_bytes += mx_bytes + code_bytes + 2 * L.ihw_bytes;
+    }
+    const size_t vec_bytes = align16((size_t)cnt * n * sizeof(double));
+    size_t obj_doubles = o.kind == GBX_OBJ_GRAPH_MATCHING ? 2 * (size_t)o.order * o.order
+                                                          : (size_t)n * n;
+    const size_t obj_bytes = align16(obj_doubles * sizeof(double));
+    L.obj_doubles = obj_doubles;
+    if (vec_bytes + obj_bytes + fixed_bytes <= kSmemBudget) {
+        L.vec_smem = 1; L.obj_smem = 1;
+    } else if (vec_bytes + fixed_bytes <= kSmemBudget) {
+        L.vec_smem = 1; L.obj_smem = 0;
+    } else if (obj_bytes + fixed_bytes <= kSmemBudget) {
+        L.vec_smem = 0; L.obj_smem = 1;
+    } else {
+        L.vec_smem = 0; L.obj_smem = 0;
+    }
+    if (fixed_bytes > kSmemBudget) { *err = "LMO workspace exceeds shared memory"; return GBX_ERR_UNSUPPORTED; }
+    L.node_stride = L.vec_smem ? 0 : (size_t)cnt * n;
+    size_t p = 0;
+    L.sm_vec = p; if (L.vec_smem) p += vec_bytes;
+    L.sm_obj = p; if (L.obj_smem) p += obj_bytes;
+    L.sm_keys = p; L.sm_prefix = p; L.sm_idx = p; L.sm_fixed = p;
+    if (L.sort_size) {
+        L.sm_keys = p; p += align16((size_t)L.sort_size * 8);
+        L.sm_prefix = p; p += align16((size_t)L.sort_size * 8);
+        L.sm_idx = p; p += align16((size_t)L.sort_size * 4);
+        L.sm_fixed = p; p += align16((size_t)n);
+    }
+    L.sm_hung = p; p += 2 * L.hung_bytes;
+    L.sm_mx = p; p += mx_bytes;
+    L.sm_code = p; p += code_bytes;
+    L.sm_ihw = p; p += mixed ? 2 * L.ihw_bytes : 0;
+    L.sm_total = p;
+    L.mixed_node_bytes = 0;
+    *out = L;
+    return GBX_OK;
+}
+
+size_t workspace_bytes(const Layout& L, int n_nodes) {
+    size_t b = L.vec_smem ? 0 : L.node_stride * sizeof(double) * (size_t)n_nodes;
+    b += L.mixed_node_bytes * (size_t)n_nodes;
+    return b + 256;
+}
+
+int launch_relax(const Params& p, void* stream, std::string* err) {
+    if (p.b.n_nodes == 0) return GBX_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int ok = p.obj.kind, lk = p.lmo.kind;
+#define GBX_CASE(O, LMOK) if (ok == O && lk == LMOK) return launch_one<O, LMOK>(p, st, err);
+    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_BOX)
+    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_SIMPLEX)
+    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_EQUALITY_SIMPLEX)
+    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_BIRKHOFF)
+    GBX_CASE(GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BIRKHOFF)
+    GBX_CASE(GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BOX)
+#undef GBX_CASE
+    *err = "unsupported objective/LMO combination";
+    return GBX_ERR_UNSUPPORTED;
+}
+
+static int probe_layout(const gbx_lmo& l, Layout* L, std::string* err) {
+    gbx_objective o{};
+    o.kind = GBX_OBJ_DENSE_QUADRATIC;
+    o.n = l.n;
+    gbx_algorithm a{};
+    a.kind = GBX_ALG_DICG;
+    const int rc = make_layout(o, l, a, 1, L, err);
+    if (rc) return rc;
+    // probes only need the LMO scratch: rebuild offsets without node vectors
+    size_t p = 0;
+    Layout& M = *L;
+    M.sm_keys = M.sm_prefix = M.sm_idx = M.sm_fixed = 0;
+    if (M.sort_size) {
+        M.sm_keys = p; p += align16((size_t)M.sort_size * 8);
+        M.sm_prefix = p; p += align16((size_t)M.sort_size * 8);
+        M.sm_idx = p; p += align16((size_t)M.sort_size * 4);
+        M.sm_fixed = p; p += align16((size_t)l.n);
+    }
+    M.sm_hung = p; p += 2 * M.hung_bytes;
+    M.sm_total = p;
+    return GBX_OK;
+}
+
+int launch_lmo_batch(const gbx_lmo& l, int cases, int mode, const double* dir,
+                     const double* x, const double* lb, const double* ub, double* out,
+                     double* out_step, void* stream, std::string* err) {
+    if (cases == 0) return GBX_OK;
+    Layout L;
+    int rc = probe_layout(l, &L, err);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (l.kind) {
+    case GBX_LMO_BOX: return probe_one<GBX_LMO_BOX>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
+    case GBX_LMO_SIMPLEX: return probe_one<GBX_LMO_SIMPLEX>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
+    case GBX_LMO_EQUALITY_SIMPLEX: return probe_one<GBX_LMO_EQUALITY_SIMPLEX>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
+    case GBX_LMO_BIRKHOFF: return probe_one<GBX_LMO_BIRKHOFF>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
+    default: *err = "lmo kind"; return GBX_ERR_UNSUPPORTED;
+    }
+}
+
+int launch_node_feasible(const gbx_lmo& l, int cases, const double* lb, const double* ub,
+                         const uint8_t* flags, uint8_t* out, void* stream, std::string* err) {
+    if (cases == 0) return GBX_OK;
+    Layout L;
+    int rc = probe_layout(l, &L, err);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (l.kind) {
+    case GBX_LMO_BOX: return feas_one<GBX_LMO_BOX>(l, L, cases, lb, ub, flags, out, st, err);
+    case GBX_LMO_SIMPLEX: return feas_one<GBX_LMO_SIMPLEX>(l, L, cases, lb, ub, flags, out, st, err);
+    case GBX_LMO_EQUALITY_SIMPLEX: return feas_one<GBX_LMO_EQUALITY_SIMPLEX>(l, L, cases, lb, ub, flags, out, st, err);
+    case GBX_LMO_BIRKHOFF: return feas_one<GBX_LMO_BIRKHOFF>(l, L, cases, lb, ub, flags, out, st, err);
+    default: *err = "lmo kind"; return GBX_ERR_UNSUPPORTED;
+    }
+}
+
+}  // namespace gbx

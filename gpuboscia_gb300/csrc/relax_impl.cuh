@@ -1,4 +1,6 @@
-// relax.cu -- FP64 Frank-Wolfe / DICG node relaxation for sm_103a.
+#pragma once
+// relax_impl.cuh -- device code of the node relaxation (FW / DICG) for sm_103a,
+// shared by the translation units that instantiate its kernels.
 //
 // One 256-thread CTA relaxes one B&B node (the reference's node-per-block
 // decomposition, device_resident_solver.cuh:631-660), but the node's working
@@ -29,17 +31,6 @@ namespace gbx {
 constexpr unsigned kFull = 0xffffffffu;
 
 // ------------------------------------------------------------------ layout
-__host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
-
-__host__ __device__ inline size_t hung_ws_bytes(int m) {
-    size_t b = 0;
-    b += align16(3 * (size_t)(m + 1) * sizeof(double));     // u, pv, minv
-    b += align16(2 * (size_t)(m + 1) * sizeof(int));        // p, way
-    b += align16(6 * (size_t)m * sizeof(int));              // fcol frow rows cols pi pinv
-    b += align16(8 * sizeof(int));                          // scalars
-    b += align16((size_t)(m + 1));                          // used
-    return b;
-}
 
 struct HW {
     double *u, *pv, *minv;
@@ -83,7 +74,7 @@ __device__ __forceinline__ double warp_min(double v) {
 }
 
 // 256-lane sum, result broadcast to every thread.
-__device__ double bsum(double v, double* red) {
+static __device__ double bsum(double v, double* red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     v = warp_sum(v);
     __syncthreads();
@@ -98,7 +89,7 @@ __device__ double bsum(double v, double* red) {
     return red[32];
 }
 // 256-lane min; lanes past the warp count read 1.0 (drs_block_min).
-__device__ double bmin(double v, double* red) {
+static __device__ double bmin(double v, double* red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     v = warp_min(v);
     __syncthreads();
@@ -145,7 +136,7 @@ struct Ctx {
 };
 
 // ------------------------------------------------------------------ objective
-__device__ void residual(const Ctx& c, const double* X, double* R) {
+static __device__ void residual(const Ctx& c, const double* X, double* R) {
     const int m = c.m;
     for (int e = c.tid; e < c.n; e += kThreads) {
         const int i = e / m, j = e - (e / m) * m;
@@ -159,7 +150,7 @@ __device__ void residual(const Ctx& c, const double* X, double* R) {
 }
 
 // g = grad f(x). Graph matching leaves the residual of x in c.R.
-__device__ void obj_grad(const Ctx& c, const double* x, double* g) {
+static __device__ void obj_grad(const Ctx& c, const double* x, double* g) {
     const int n = c.n;
     if (c.ok == GBX_OBJ_GRAPH_MATCHING) {
         residual(c, x, c.R);
@@ -184,13 +175,13 @@ __device__ void obj_grad(const Ctx& c, const double* x, double* g) {
     __syncthreads();
 }
 
-__device__ double value_from_residual(const Ctx& c) {
+static __device__ double value_from_residual(const Ctx& c) {
     double loc = 0.0;
     for (int e = c.tid; e < c.n; e += kThreads) loc = fma(c.R[e], c.R[e], loc);
     return c.s * bsum(loc, c.red);
 }
 
-__device__ double obj_value(const Ctx& c, const double* x) {
+static __device__ double obj_value(const Ctx& c, const double* x) {
     const int n = c.n;
     if (c.ok == GBX_OBJ_GRAPH_MATCHING) {
         residual(c, x, c.R);
@@ -210,7 +201,7 @@ __device__ double obj_value(const Ctx& c, const double* x) {
     return bsum(val, c.red);
 }
 
-__device__ double obj_curvature(const Ctx& c, const double* d) {
+static __device__ double obj_curvature(const Ctx& c, const double* d) {
     const int n = c.n;
     if (c.ok == GBX_OBJ_GRAPH_MATCHING) {
         residual(c, d, c.R);
@@ -232,7 +223,7 @@ __device__ double obj_curvature(const Ctx& c, const double* d) {
 // with exactly one unit per row and column, every residual entry of the
 // generic O(m^3) loop reduces to one rounding of A[i,pinv(j)] - B[pi(i),j],
 // so this is bit-identical to obj_value on the same vertex.
-__device__ double perm_value(const Ctx& c, const int* pi, int* pinv) {
+static __device__ double perm_value(const Ctx& c, const int* pi, int* pinv) {
     const int m = c.m;
     for (int r = c.tid; r < m; r += kThreads) pinv[pi[r]] = r;
     __syncthreads();
@@ -245,13 +236,17 @@ __device__ double perm_value(const Ctx& c, const int* pi, int* pinv) {
     return c.s * bsum(loc, c.red);
 }
 
+}  // namespace gbx
+#include "mixed.cuh"
+namespace gbx {
+
 // ------------------------------------------------------------------ Hungarian
 // Exact min-cost assignment over the Birkhoff order-m polytope with forced
 // (lb > 1/2), forbidden (ub < 1/2) and face restrictions, ties to the lowest
 // column (lmo.cuh:1239-1417). Executed by ONE warp; `out` must be zeroed and
 // visible. cost may be null (zero costs); the cost of edge e is sign*cost[e].
 // Returns a warp-uniform success flag and leaves the row->column map in w.pi.
-__device__ bool hungarian_warp(const HW& w, int m, const double* cost, double sign,
+static __device__ bool hungarian_warp(const HW& w, int m, const double* cost, double sign,
                                const double* lb, const double* ub, const double* face,
                                double* out) {
     const int lane = threadIdx.x & 31;
@@ -354,7 +349,7 @@ __device__ bool hungarian_warp(const HW& w, int m, const double* cost, double si
 
 // ------------------------------------------------------------------ simplex
 // parallel_greedy_allocate_cooperative (lmo.cuh:529-618); key of j is sign*g[j].
-__device__ void simplex_greedy(const Ctx& c, const double* g, double sign, const double* ub,
+static __device__ void simplex_greedy(const Ctx& c, const double* g, double sign, const double* ub,
                                double* out, const uint8_t* fixed, double remaining,
                                bool force_full, bool floor_int) {
     const int S = c.S, n = c.n, tid = c.tid;
@@ -426,7 +421,7 @@ __device__ void simplex_greedy(const Ctx& c, const double* g, double sign, const
 
 // ------------------------------------------------------------------ LMOs
 template <int LK>
-__device__ bool lmo_forward(const Ctx& c, const double* g, const double* lb,
+static __device__ bool lmo_forward(const Ctx& c, const double* g, const double* lb,
                             const double* ub, double* v) {
     const int n = c.n;
     if constexpr (LK == GBX_LMO_BOX) {
@@ -459,7 +454,7 @@ __device__ bool lmo_forward(const Ctx& c, const double* g, const double* lb,
 
 // In-face away oracle on the direction sign*g over the minimal face of x.
 template <int LK>
-__device__ bool lmo_inface(const Ctx& c, const double* g, double sign, const double* x,
+static __device__ bool lmo_inface(const Ctx& c, const double* g, double sign, const double* x,
                            const double* lb, const double* ub, double* a, int hw_slot) {
     const int n = c.n;
     const double atol = 1e-6, rtol = 1e-4;
@@ -506,7 +501,7 @@ __device__ bool lmo_inface(const Ctx& c, const double* g, double sign, const dou
 
 // max(0, min(coordinate step, aggregate step)) for x - gamma*d.
 template <int LK>
-__device__ double lmo_max_step(const Ctx& c, const double* d, const double* x,
+static __device__ double lmo_max_step(const Ctx& c, const double* d, const double* x,
                                const double* lb, const double* ub) {
     const int n = c.n;
     double res = 1.0;
@@ -539,7 +534,7 @@ __device__ double lmo_max_step(const Ctx& c, const double* d, const double* x,
 
 // drs_node_feasible (device_resident_solver.cuh:206-217) + LMO check.
 template <int LK>
-__device__ bool node_feasible(const Ctx& c, const double* lb, const double* ub,
+static __device__ bool node_feasible(const Ctx& c, const double* lb, const double* ub,
                               double* scratch) {
     const int n = c.n;
     bool valid = true;
@@ -587,7 +582,7 @@ __device__ bool node_feasible(const Ctx& c, const double* lb, const double* ub,
 }
 
 template <int LK>
-__device__ bool rounded_feasible(const Ctx& c, const double* x) {
+static __device__ bool rounded_feasible(const Ctx& c, const double* x) {
     const int n = c.n;
     const double tol = c.tol;
     if constexpr (LK == GBX_LMO_BOX) {
@@ -618,7 +613,7 @@ __device__ bool rounded_feasible(const Ctx& c, const double* x) {
 }
 
 // drs_integer_value: score of an LMO vertex or rounded candidate.
-__device__ double integer_value(const Ctx& c, const double* x, const double* lb,
+static __device__ double integer_value(const Ctx& c, const double* x, const double* lb,
                                 const double* ub, const int* pi, int* pinv) {
     bool valid = true;
     const double tol = c.tol;
@@ -629,6 +624,183 @@ __device__ double integer_value(const Ctx& c, const double* x, const double* lb,
     if (!__syncthreads_and(valid)) return kNone;
     const double val = pi ? perm_value(c, pi, pinv) : obj_value(c, x);
     return isfinite(val) ? val : kNone;
+}
+
+
+// ------------------------------------------------------------------ mixed loop
+// Score of a permutation vertex pi (drs_integer_value on a 0/1 point): bounds
+// are checked through the per-edge code bytes, the value through perm_value.
+static __device__ double perm_score(const Ctx& c, const uint8_t* code, const int* pi, int* pinv) {
+    bool valid = true;
+    for (int e = c.tid; e < c.n; e += kThreads) {
+        const int i = e / c.m, j = e - (e / c.m) * c.m;
+        if (!(code[e] & (pi[i] == j ? kOneOk : kZeroOk))) valid = false;
+    }
+    if (!__syncthreads_and(valid)) return kNone;
+    const double val = perm_value(c, pi, pinv);
+    return isfinite(val) ? val : kNone;
+}
+
+// Mixed-precision DICG / FW iterations (see mixed.cuh). Works on the FP64
+// iterate X in place and returns the cumulative iteration count; the caller
+// then computes the FP64 certificate at the returned iterate.
+static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, int node, double* X,
+                          const double* LB, const double* UB, double* best, double& best_val,
+                          double eps, int it0, bool dicg, int ls) {
+    const Layout& L = P.L;
+    const int n = c.n, m = c.m, tid = c.tid;
+    float* xf = reinterpret_cast<float*>(dsm + L.sm_mx);
+    float* gf = xf + n;
+    float* Rf = gf + n;
+    float* Af = Rf + n;
+    float* Bf = Af + n;
+    float* Btf = Bf + n;
+    uint8_t* code = dsm + L.sm_code;
+    uint8_t* face = code + n;
+    const IHW w0 = ihw_at(dsm + L.sm_ihw, m);
+    const IHW w1 = ihw_at(dsm + L.sm_ihw + L.ihw_bytes, m);
+    const double tol = c.tol;
+    for (int e = tid; e < n; e += kThreads) {
+        const int i = e / m, j = e - (e / m) * m;
+        Af[e] = (float)c.A[e];
+        Bf[e] = (float)c.B[e];
+        Btf[e] = (float)c.B[j * m + i];
+        const double lo = LB[e], up = UB[e];
+        uint8_t cd = 0;
+        if (lo > 0.5) cd |= kForced;
+        if (up >= 0.5) cd |= kAllowed;
+        if (lo > up + 1e-9) cd |= kBad;
+        if (!(0.0 < lo - tol) && !(0.0 > up + tol)) cd |= kZeroOk;
+        if (!(1.0 < lo - tol) && !(1.0 > up + tol)) cd |= kOneOk;
+        code[e] = cd;
+        const double xe = X[e];
+        xf[e] = (float)xe;
+        face[e] = (uint8_t)((xe > 1e-9 ? kFaceIn : 0) | (xe >= 1.0 - 1e-9 ? kFaceOne : 0));
+    }
+    if (tid == 0) { w0.scal[0] = 0; w0.scal[1] = 0; }
+    if (tid == 32) { w1.scal[0] = 0; w1.scal[1] = 0; }
+    __syncthreads();
+
+    auto take = [&](const int* pi, double fv) {
+        if (fv < best_val) {
+            best_val = fv;
+            if (tid == 0) P.b.best_vertex_val[node] = fv;
+        }
+        if (fv < 1e299 && fv == best_val)
+            for (int e = tid; e < n; e += kThreads) best[e] = pi[e / m] == e - (e / m) * m ? 1.0 : 0.0;
+        __syncthreads();
+    };
+
+    const float two_s = (float)(2.0 * c.s);
+    const float limit = 16777216.0f / (float)m;  // integer costs stay below 2^24 / m
+    int iters = it0;
+    for (int iter = 0; iter < P.b.max_iters; ++iter) {
+        iters = it0 + iter + 1;
+        grad_f32(m, two_s, Af, Bf, Btf, xf, Rf, gf);
+        const float gmx = bmax_abs(gf, n, c.red);
+        int shift = 0;
+        if (gmx > 0.f) {
+            int ex = 0;
+            frexpf(limit / gmx, &ex);
+            shift = max(-120, min(120, ex - 1));
+        }
+        if (threadIdx.x < 32) {
+            const bool ok = int_hungarian_warp(w0, m, gf, 1.f, shift, code, nullptr);
+            if (threadIdx.x == 0) c.flag[0] = ok;
+        } else if (dicg && threadIdx.x < 64) {
+            const bool ok = int_hungarian_warp(w1, m, gf, -1.f, shift, code, face);
+            if (threadIdx.x == 32) c.flag[2] = ok;
+        }
+        __syncthreads();
+        if (!c.flag[0] || (dicg && !c.flag[2])) break;
+        take(w0.pi, perm_score(c, code, w0.pi, w0.pinv));
+        double loc = 0.0;
+        for (int e = tid; e < n; e += kThreads) {
+            const double ve = w0.pi[e / m] == e - (e / m) * m ? 1.0 : 0.0;
+            loc = fma((double)gf[e], X[e] - ve, loc);
+        }
+        const double gap = bsum(loc, c.red);
+        if (gap >= 0.0 && gap < eps) break;
+
+        if (!dicg) {
+            double gm;
+            if (ls == GBX_LS_QUADRATIC_EXACT) {
+                for (int r = tid; r < m; r += kThreads) w0.pinv[w0.pi[r]] = r;
+                __syncthreads();
+                double cl = 0.0;
+                for (int e = tid; e < n; e += kThreads) {
+                    const int i = e / m, j = e - (e / m) * m;
+                    const double rv = c.A[i * m + w0.pinv[j]] - c.B[w0.pi[i] * m + j];
+                    const double d = rv - (double)Rf[e];
+                    cl = fma(d, d, cl);
+                }
+                const double curv = (2.0 * c.s) * bsum(cl, c.red);
+                if (curv > 0.0) gm = gap <= 0.0 ? 0.0 : fmin(gap / curv, 1.0);
+                else gm = -gap + 0.5 * curv * 1.0 < 0.0 ? 1.0 : 0.0;
+            } else {
+                gm = 2.0 / (double)(it0 + iter + 2);
+            }
+            for (int e = tid; e < n; e += kThreads) {
+                const double ve = w0.pi[e / m] == e - (e / m) * m ? 1.0 : 0.0;
+                X[e] = fma(gm, ve - X[e], X[e]);
+                xf[e] = (float)X[e];
+            }
+            __syncthreads();
+            continue;
+        }
+        take(w1.pi, perm_score(c, code, w1.pi, w1.pinv));
+        for (int r = tid; r < m; r += kThreads) {
+            w0.pinv[w0.pi[r]] = r;
+            w1.pinv[w1.pi[r]] = r;
+        }
+        __syncthreads();
+        double res = 1.0;
+        for (int i = tid; i < m; i += kThreads) {
+            const int pa = w1.pi[i], pv = w0.pi[i];
+            if (pa == pv) continue;
+            const int ea = i * m + pa, ev = i * m + pv;
+            res = fmin(res, (X[ea] - LB[ea]) / 1.0);
+            res = fmin(res, (UB[ev] - X[ev]) / 1.0);
+        }
+        const double gmax = fmax(0.0, fmin(bmin(res, c.red), 1.0));
+        double gm;
+        if (ls == GBX_LS_QUADRATIC_EXACT) {
+            double pl = 0.0, cl = 0.0;
+            for (int i = tid; i < m; i += kThreads) {
+                const int pa = w1.pi[i], pv = w0.pi[i];
+                if (pa != pv) pl += (double)gf[i * m + pa] - (double)gf[i * m + pv];
+            }
+            for (int e = tid; e < n; e += kThreads) {
+                const int i = e / m, j = e - (e / m) * m;
+                const double rd = (c.A[i * m + w1.pinv[j]] - c.A[i * m + w0.pinv[j]])
+                                - (c.B[w1.pi[i] * m + j] - c.B[w0.pi[i] * m + j]);
+                cl = fma(rd, rd, cl);
+            }
+            const double pgap = bsum(pl, c.red);
+            const double curv = (2.0 * c.s) * bsum(cl, c.red);
+            if (gmax <= 0.0) gm = 0.0;
+            else if (curv > 0.0) gm = pgap <= 0.0 ? 0.0 : fmin(pgap / curv, gmax);
+            else gm = -pgap + 0.5 * curv * gmax < 0.0 ? gmax : 0.0;
+        } else {
+            const double open = 2.0 / (double)(it0 + iter + 2);
+            if (ls == GBX_LS_SAFEGUARDED_SCALED_OPEN_LOOP) gm = gmax <= open ? gmax : gmax * open;
+            else if (ls == GBX_LS_SCALED_OPEN_LOOP) gm = gmax * open;
+            else gm = fmin(gmax, open);
+        }
+        for (int i = tid; i < m; i += kThreads) {
+            const int pa = w1.pi[i], pv = w0.pi[i];
+            if (pa == pv) continue;
+            const int ea = i * m + pa, ev = i * m + pv;
+            X[ea] = fma(-gm, 1.0, X[ea]);
+            X[ev] = fma(-gm, -1.0, X[ev]);
+            xf[ea] = (float)X[ea];
+            xf[ev] = (float)X[ev];
+            face[ea] = (uint8_t)((X[ea] > 1e-9 ? kFaceIn : 0) | (X[ea] >= 1.0 - 1e-9 ? kFaceOne : 0));
+            face[ev] = (uint8_t)((X[ev] > 1e-9 ? kFaceIn : 0) | (X[ev] >= 1.0 - 1e-9 ? kFaceOne : 0));
+        }
+        __syncthreads();
+    }
+    return iters;
 }
 
 // ------------------------------------------------------------------ kernel
@@ -817,7 +989,14 @@ __global__ void __launch_bounds__(kThreads, 1) relax_kernel(const __grid_constan
     };
 
     int iters = it0;
-    for (int iter = 0; iter < P.b.max_iters; ++iter) {
+    bool mixed_done = false;
+    if constexpr (OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF) {
+        if (L.mixed) {
+            iters = mixed_loop(c, P, dsm, node, X, LB, UB, best, best_val, eps, it0, dicg, ls);
+            mixed_done = true;
+        }
+    }
+    for (int iter = 0; !mixed_done && iter < P.b.max_iters; ++iter) {
         iters = it0 + iter + 1;
         obj_grad(c, X, G);
         bool fwd_perm = false, away_perm = false;
@@ -1003,85 +1182,10 @@ __global__ void __launch_bounds__(kThreads, 1) feasible_kernel(
     if (threadIdx.x == 0) out[cs] = ok ? 1 : 0;
 }
 
-// ------------------------------------------------------------------ host side
-namespace {
-int next_pow2(int v) { int r = 1; while (r < v) r <<= 1; return r; }
-constexpr size_t kSmemBudget = 220 * 1024;
-}
 
-int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a,
-                int n_nodes, Layout* out, std::string* err) {
-    (void)n_nodes;
-    Layout L{};
-    const int n = o.n;
-    for (int& v : L.off) v = -1;
-    const bool dicg = a.kind == GBX_ALG_DICG;
-    const bool secant = a.line_search == GBX_LS_SECANT;
-    int cnt = 0;
-    auto add = [&](int b) { L.off[b] = cnt * n; ++cnt; };
-    add(B_X); add(B_G); add(B_V);
-    if (dicg) add(B_AW);
-    if (secant) { add(B_TX); add(B_TG); }
-    if (o.kind == GBX_OBJ_GRAPH_MATCHING) add(B_R);
-    add(B_LB); add(B_UB);
-    if (secant) L.off[B_CAND] = L.off[B_TX]; else add(B_CAND);
-    L.nvec = cnt;
-
-    size_t fixed_bytes = 0;
-    if (l.kind == GBX_LMO_SIMPLEX || l.kind == GBX_LMO_EQUALITY_SIMPLEX) {
-        if (n > 8192) { *err = "simplex LMO supports n <= 8192"; return GBX_ERR_UNSUPPORTED; }
-        L.sort_size = next_pow2(n);
-        fixed_bytes += align16((size_t)L.sort_size * 8) * 2 + align16((size_t)L.sort_size * 4)
-                       + align16((size_t)n);
-    }
-    if (l.kind == GBX_LMO_BIRKHOFF) {
-        if (l.order <= 0 || l.order > 1024) { *err = "Birkhoff order out of range"; return GBX_ERR_UNSUPPORTED; }
-        L.hung_order = l.order;
-        L.hung_warps = 2;
-        L.hung_bytes = hung_ws_bytes(l.order);
-        fixed_bytes += 2 * L.hung_bytes;
-    }
-    const size_t vec_bytes = align16((size_t)cnt * n * sizeof(double));
-    size_t obj_doubles = o.kind == GBX_OBJ_GRAPH_MATCHING ? 2 * (size_t)o.order * o.order
-                                                          : (size_t)n * n;
-    const size_t obj_bytes = align16(obj_doubles * sizeof(double));
-    L.obj_doubles = obj_doubles;
-    if (vec_bytes + obj_bytes + fixed_bytes <= kSmemBudget) {
-        L.vec_smem = 1; L.obj_smem = 1;
-    } else if (vec_bytes + fixed_bytes <= kSmemBudget) {
-        L.vec_smem = 1; L.obj_smem = 0;
-    } else if (obj_bytes + fixed_bytes <= kSmemBudget) {
-        L.vec_smem = 0; L.obj_smem = 1;
-    } else {
-        L.vec_smem = 0; L.obj_smem = 0;
-    }
-    if (fixed_bytes > kSmemBudget) { *err = "LMO workspace exceeds shared memory"; return GBX_ERR_UNSUPPORTED; }
-    L.node_stride = L.vec_smem ? 0 : (size_t)cnt * n;
-    size_t p = 0;
-    L.sm_vec = p; if (L.vec_smem) p += vec_bytes;
-    L.sm_obj = p; if (L.obj_smem) p += obj_bytes;
-    L.sm_keys = p; L.sm_prefix = p; L.sm_idx = p; L.sm_fixed = p;
-    if (L.sort_size) {
-        L.sm_keys = p; p += align16((size_t)L.sort_size * 8);
-        L.sm_prefix = p; p += align16((size_t)L.sort_size * 8);
-        L.sm_idx = p; p += align16((size_t)L.sort_size * 4);
-        L.sm_fixed = p; p += align16((size_t)n);
-    }
-    L.sm_hung = p; p += 2 * L.hung_bytes;
-    L.sm_total = p;
-    L.mixed_node_bytes = 0;
-    *out = L;
-    return GBX_OK;
-}
-
-size_t workspace_bytes(const Layout& L, int n_nodes) {
-    size_t b = L.vec_smem ? 0 : L.node_stride * sizeof(double) * (size_t)n_nodes;
-    b += L.mixed_node_bytes * (size_t)n_nodes;
-    return b + 256;
-}
-
+// ------------------------------------------------------------------ launchers
 template <int OK, int LK>
-static int launch_one(const Params& p, cudaStream_t st, std::string* err) {
+int launch_one(const Params& p, cudaStream_t st, std::string* err) {
     auto k = relax_kernel<OK, LK>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::max<size_t>(p.L.sm_total, 1));
@@ -1092,24 +1196,8 @@ static int launch_one(const Params& p, cudaStream_t st, std::string* err) {
     return GBX_OK;
 }
 
-int launch_relax(const Params& p, void* stream, std::string* err) {
-    if (p.b.n_nodes == 0) return GBX_OK;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int ok = p.obj.kind, lk = p.lmo.kind;
-#define GBX_CASE(O, LMOK) if (ok == O && lk == LMOK) return launch_one<O, LMOK>(p, st, err);
-    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_BOX)
-    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_SIMPLEX)
-    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_EQUALITY_SIMPLEX)
-    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_BIRKHOFF)
-    GBX_CASE(GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BIRKHOFF)
-    GBX_CASE(GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BOX)
-#undef GBX_CASE
-    *err = "unsupported objective/LMO combination";
-    return GBX_ERR_UNSUPPORTED;
-}
-
 template <int LK>
-static int probe_one(const gbx_lmo& l, const Layout& L, int cases, int mode, const double* dir,
+int probe_one(const gbx_lmo& l, const Layout& L, int cases, int mode, const double* dir,
                      const double* x, const double* lb, const double* ub, double* out,
                      double* out_step, cudaStream_t st, std::string* err) {
     double* ws = nullptr;
@@ -1129,48 +1217,8 @@ static int probe_one(const gbx_lmo& l, const Layout& L, int cases, int mode, con
     return GBX_OK;
 }
 
-static int probe_layout(const gbx_lmo& l, Layout* L, std::string* err) {
-    gbx_objective o{};
-    o.kind = GBX_OBJ_DENSE_QUADRATIC;
-    o.n = l.n;
-    gbx_algorithm a{};
-    a.kind = GBX_ALG_DICG;
-    const int rc = make_layout(o, l, a, 1, L, err);
-    if (rc) return rc;
-    // probes only need the LMO scratch: rebuild offsets without node vectors
-    size_t p = 0;
-    Layout& M = *L;
-    M.sm_keys = M.sm_prefix = M.sm_idx = M.sm_fixed = 0;
-    if (M.sort_size) {
-        M.sm_keys = p; p += align16((size_t)M.sort_size * 8);
-        M.sm_prefix = p; p += align16((size_t)M.sort_size * 8);
-        M.sm_idx = p; p += align16((size_t)M.sort_size * 4);
-        M.sm_fixed = p; p += align16((size_t)l.n);
-    }
-    M.sm_hung = p; p += 2 * M.hung_bytes;
-    M.sm_total = p;
-    return GBX_OK;
-}
-
-int launch_lmo_batch(const gbx_lmo& l, int cases, int mode, const double* dir,
-                     const double* x, const double* lb, const double* ub, double* out,
-                     double* out_step, void* stream, std::string* err) {
-    if (cases == 0) return GBX_OK;
-    Layout L;
-    int rc = probe_layout(l, &L, err);
-    if (rc) return rc;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    switch (l.kind) {
-    case GBX_LMO_BOX: return probe_one<GBX_LMO_BOX>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
-    case GBX_LMO_SIMPLEX: return probe_one<GBX_LMO_SIMPLEX>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
-    case GBX_LMO_EQUALITY_SIMPLEX: return probe_one<GBX_LMO_EQUALITY_SIMPLEX>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
-    case GBX_LMO_BIRKHOFF: return probe_one<GBX_LMO_BIRKHOFF>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
-    default: *err = "lmo kind"; return GBX_ERR_UNSUPPORTED;
-    }
-}
-
 template <int LK>
-static int feas_one(const gbx_lmo& l, const Layout& L, int cases, const double* lb,
+int feas_one(const gbx_lmo& l, const Layout& L, int cases, const double* lb,
                     const double* ub, const uint8_t* flags, uint8_t* out, cudaStream_t st,
                     std::string* err) {
     double* ws = nullptr;
@@ -1185,22 +1233,6 @@ static int feas_one(const gbx_lmo& l, const Layout& L, int cases, const double* 
     cudaFreeAsync(ws, st);
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
     return GBX_OK;
-}
-
-int launch_node_feasible(const gbx_lmo& l, int cases, const double* lb, const double* ub,
-                         const uint8_t* flags, uint8_t* out, void* stream, std::string* err) {
-    if (cases == 0) return GBX_OK;
-    Layout L;
-    int rc = probe_layout(l, &L, err);
-    if (rc) return rc;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    switch (l.kind) {
-    case GBX_LMO_BOX: return feas_one<GBX_LMO_BOX>(l, L, cases, lb, ub, flags, out, st, err);
-    case GBX_LMO_SIMPLEX: return feas_one<GBX_LMO_SIMPLEX>(l, L, cases, lb, ub, flags, out, st, err);
-    case GBX_LMO_EQUALITY_SIMPLEX: return feas_one<GBX_LMO_EQUALITY_SIMPLEX>(l, L, cases, lb, ub, flags, out, st, err);
-    case GBX_LMO_BIRKHOFF: return feas_one<GBX_LMO_BIRKHOFF>(l, L, cases, lb, ub, flags, out, st, err);
-    default: *err = "lmo kind"; return GBX_ERR_UNSUPPORTED;
-    }
 }
 
 }  // namespace gbx
