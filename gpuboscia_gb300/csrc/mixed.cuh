@@ -35,21 +35,19 @@ constexpr uint8_t kFaceIn = 1;     // x > 1e-9
 constexpr uint8_t kFaceOne = 2;    // x >= 1 - 1e-9
 
 struct IHW {
-    int *u, *pv, *minv, *p, *way;
-    int *rows, *cols, *rowpos, *fcol, *frow, *pi, *colpot, *match, *pinv;
-    uint8_t *used, *rmatch;
-    int* scal;   // [0] warm state valid, [1] shift of the stored potentials
+    int *u, *rowb, *pvs;                         // [m+1] row potentials, row offsets r*m, column potentials
+    int *rows, *cols, *rowpos, *fcol, *frow, *pi, *colpot, *match, *pinv;  // [m]
+    uint8_t* rmatch;                             // [m+1]
+    int* scal;   // [0] warm state valid, [1] shift of the stored potentials, [2] k+1 of the cached restriction (0: none)
 };
 
 __device__ inline IHW ihw_at(unsigned char* base, int m) {
     IHW w;
     size_t o = 0;
     w.u = reinterpret_cast<int*>(base);
-    w.pv = w.u + (m + 1);
-    w.minv = w.pv + (m + 1);
-    w.p = w.minv + (m + 1);
-    w.way = w.p + (m + 1);
-    o += align16(5 * (size_t)(m + 1) * sizeof(int));
+    w.rowb = w.u + (m + 1);
+    w.pvs = w.rowb + (m + 1);
+    o += align16(3 * (size_t)(m + 1) * sizeof(int));
     w.rows = reinterpret_cast<int*>(base + o);
     w.cols = w.rows + m;
     w.rowpos = w.cols + m;
@@ -60,175 +58,244 @@ __device__ inline IHW ihw_at(unsigned char* base, int m) {
     w.match = w.colpot + m;
     w.pinv = w.match + m;
     o += align16(9 * (size_t)m * sizeof(int));
-    w.used = base + o;
-    w.rmatch = w.used + (m + 1);
-    o += align16((size_t)(m + 1) * 2);
+    w.rmatch = base + o;
+    o += align16((size_t)(m + 1));
     w.scal = reinterpret_cast<int*>(base + o);
     return w;
 }
 
-__device__ __forceinline__ int scaled_cost(const float* g, int e, float sign, int shift) {
-    return __float2int_rn(scalbnf(sign * g[e], shift));
+template <int CPL>
+__device__ __forceinline__ int lane_slot(const int (&a)[CPL], int slot) {
+    int v = 0;
+#pragma unroll
+    for (int t = 0; t < CPL; ++t)
+        if (t == slot) v = a[t];
+    return v;
 }
 
-// Exact assignment on the integer costs round(sign*g*2^shift) over the
-// Birkhoff polytope restricted by the edge codes (and the face of x when
-// `face` is given). One warp. Leaves the row->column map in w.pi and keeps
-// column potentials / matching for the next call. Returns a warp-uniform flag.
-static __device__ bool int_hungarian_warp(const IHW& w, int m, const float* g, float sign, int shift,
-                                   const uint8_t* code, const uint8_t* face) {
+// Slacks below this bound travel as one packed 32-bit key (slack << 10 | column)
+// through a single warp min-reduction; larger ones take the two-reduction path.
+constexpr int kPackLimit = 1 << 21;
+
+// Exact assignment on integer costs over the Birkhoff polytope. `cost` holds
+// round(sign*g*2^shift) for allowed edges and kIntInf for excluded ones; the
+// forced / face-forced pre-pass reads the edge codes and is skipped when
+// `restrict_same` says the restrictions equal those of the previous call. One
+// warp; lane l owns the compacted columns l+1, l+33, ... and keeps, per column,
+// its potential, slack, predecessor, matched row and that row's potential and
+// offset in registers (CPL columns per lane: the compacted order k must not
+// exceed 32*CPL). Shortest augmenting paths use lazy potentials: slacks are
+// stored offset by the running path length D, a column remembers the D at
+// which it joined the tree, and potentials are applied once per path; the
+// reached row's potential is still its value from the path's start when it is
+// relaxed, so the integer arithmetic equals the eager update exactly. Column
+// potentials and the matching persist in `w`. Ties go to the lowest column.
+// Returns a warp-uniform success flag; the row->column map is left in w.pi.
+template <int CPL>
+__device__ bool int_hungarian_warp(const IHW& w, int m, const int* cost, int shift, const uint8_t* code,
+                                   const uint8_t* face, bool restrict_same) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    for (int i = lane; i < m; i += 32) { w.fcol[i] = -1; w.frow[i] = -1; }
-    __syncwarp();
-    bool ok = true;
-    const int nn = m * m;
-    for (int e = lane; e < nn; e += 32) {
-        const uint8_t c = code[e];
-        if (c & kBad) ok = false;
-        const bool forced = (c & kForced) || (face && (face[e] & kFaceOne));
-        if (forced) {
-            const int r = e / m, col = e - r * m;
-            if (!(c & kAllowed)) ok = false;
-            if (atomicCAS(&w.fcol[r], -1, col) != -1) ok = false;
-            if (atomicCAS(&w.frow[col], -1, r) != -1) ok = false;
-        }
-    }
-    ok = __all_sync(kFull, ok);
-    __syncwarp();
-    if (!ok) return false;
-    int k = 0, kc = 0;
-    for (int base = 0; base < m; base += 32) {
-        const int i = base + lane;
-        const bool fr = i < m && w.fcol[i] < 0;
-        const bool fc = i < m && w.frow[i] < 0;
-        const unsigned mr = __ballot_sync(kFull, fr), mc = __ballot_sync(kFull, fc);
-        if (fr) { w.rows[k + __popc(mr & lt)] = i; }
-        if (i < m) w.rowpos[i] = fr ? k + __popc(mr & lt) + 1 : 0;
-        if (fc) w.cols[kc + __popc(mc & lt)] = i;
-        k += __popc(mr);
-        kc += __popc(mc);
-    }
-    if (k != kc) return false;
-    __syncwarp();
-    const bool warm = w.scal[0] != 0;
-    const int old_shift = w.scal[1];
-    // column potentials: kept (rescaled to this call's cost scale) or zero
-    for (int j = lane + 1; j <= k; j += 32) {
-        int v = 0;
-        if (warm) {
-            long long t = w.colpot[w.cols[j - 1]];
-            const int d = shift - old_shift;
-            if (d > 0) t = d >= 24 ? 0 : t * (1ll << d);
-            else if (d < 0) t = -d >= 40 ? 0 : (t >> (-d));
-            v = (int)max(-kPotLimit, min(kPotLimit, t));
-        }
-        w.pv[j] = v;
-        w.p[j] = 0;
-        w.way[j] = 0;
-    }
-    if (lane == 0) { w.pv[0] = 0; w.p[0] = 0; }
-    __syncwarp();
-    // row potentials u_i = min_j (c_ij - v_j): dual feasible for the new costs
-    for (int i = 1; i <= k; ++i) {
-        const int rb = w.rows[i - 1] * m;
-        int best = kIntInf;
-        for (int j = lane + 1; j <= k; j += 32) {
-            const int e = rb + w.cols[j - 1];
-            if ((code[e] & kAllowed) && (!face || (face[e] & kFaceIn))) {
-                const int r = scaled_cost(g, e, sign, shift) - w.pv[j];
-                best = r < best ? r : best;
+    int k;
+    if (restrict_same && w.scal[2] > 0) {
+        k = w.scal[2] - 1;
+    } else {
+        for (int i = lane; i < m; i += 32) { w.fcol[i] = -1; w.frow[i] = -1; }
+        __syncwarp();
+        bool ok = true;
+        const int nn = m * m;
+        for (int e = lane; e < nn; e += 32) {
+            const uint8_t c = code[e];
+            if (c & kBad) ok = false;
+            const bool forced = (c & kForced) || (face && (face[e] & kFaceOne));
+            if (forced) {
+                const int r = e / m, col = e - r * m;
+                if (!(c & kAllowed)) ok = false;
+                if (atomicCAS(&w.fcol[r], -1, col) != -1) ok = false;
+                if (atomicCAS(&w.frow[col], -1, r) != -1) ok = false;
             }
         }
-        best = __reduce_min_sync(kFull, best);
-        if (best >= kIntInf) return false;
-        if (lane == 0) { w.u[i] = best; w.rmatch[i] = 0; }
+        ok = __all_sync(kFull, ok);
+        __syncwarp();
+        if (!ok) return false;
+        k = 0;
+        int kc = 0;
+        for (int base = 0; base < m; base += 32) {
+            const int i = base + lane;
+            const bool fr = i < m && w.fcol[i] < 0;
+            const bool fc = i < m && w.frow[i] < 0;
+            const unsigned mr = __ballot_sync(kFull, fr), mc = __ballot_sync(kFull, fc);
+            if (fr) w.rows[k + __popc(mr & lt)] = i;
+            if (i < m) w.rowpos[i] = fr ? k + __popc(mr & lt) + 1 : 0;
+            if (fc) w.cols[kc + __popc(mc & lt)] = i;
+            k += __popc(mr);
+            kc += __popc(mc);
+        }
+        if (k != kc || k > 32 * CPL) return false;
+        for (int i = lane + 1; i <= k; i += 32) w.rowb[i] = w.rows[i - 1] * m;
+        if (lane == 0) w.scal[2] = k + 1;
+        __syncwarp();
     }
+    const bool warm = w.scal[0] != 0;
+    const int dshift = shift - w.scal[1];
+    int colE[CPL], pv[CPL], mraw[CPL], way[CPL], pj[CPL], usedAt[CPL], ur[CPL], rbr[CPL];
+    bool valid[CPL];
+#pragma unroll
+    for (int t = 0; t < CPL; ++t) {
+        const int j = lane + 1 + 32 * t;
+        valid[t] = j <= k;
+        colE[t] = valid[t] ? w.cols[j - 1] : 0;
+        long long v = 0;
+        if (valid[t] && warm) {
+            v = w.colpot[colE[t]];
+            if (dshift > 0) v = dshift >= 24 ? 0 : v * (1ll << dshift);
+            else if (dshift < 0) v = -dshift >= 40 ? 0 : (v >> (-dshift));
+            v = max(-kPotLimit, min(kPotLimit, v));
+        }
+        pv[t] = (int)v;
+        pj[t] = 0;
+        ur[t] = 0;
+        rbr[t] = 0;
+        if (valid[t]) w.pvs[j] = pv[t];
+    }
+    __syncwarp();
+    // row potentials u_i = min_j (c_ij - v_j), one row per lane
+    bool rows_ok = true;
+    for (int i = lane + 1; i <= k; i += 32) {
+        const int rb = w.rowb[i];
+        int best = kIntInf;
+        for (int j = 1; j <= k; ++j) {
+            const int c = cost[rb + w.cols[j - 1]];
+            if (c < kIntInf) best = min(best, c - w.pvs[j]);
+        }
+        if (best >= kIntInf) rows_ok = false;
+        w.u[i] = best;
+        w.rmatch[i] = 0;
+    }
+    if (!__all_sync(kFull, rows_ok)) return false;
     __syncwarp();
     // keep the previous matching where its edge is still allowed and tight
     if (warm) {
-        for (int j = lane + 1; j <= k; j += 32) {
-            const int c = w.cols[j - 1];
-            const int r = w.match[c];
+#pragma unroll
+        for (int t = 0; t < CPL; ++t) {
+            if (!valid[t]) continue;
+            const int r = w.match[colE[t]];
             if (r < 0 || r >= m) continue;
             const int i = w.rowpos[r];
             if (i <= 0) continue;
-            const int e = r * m + c;
-            if ((code[e] & kAllowed) && (!face || (face[e] & kFaceIn))
-                    && scaled_cost(g, e, sign, shift) - w.u[i] - w.pv[j] == 0) {
-                w.p[j] = i;
+            const int c = cost[r * m + colE[t]];
+            const int ui = w.u[i];
+            if (c < kIntInf && c - ui - pv[t] == 0) {
+                pj[t] = i;
+                ur[t] = ui;
+                rbr[t] = w.rowb[i];
                 w.rmatch[i] = 1;
             }
         }
     }
     __syncwarp();
-    // augment every unmatched row along a shortest path
-    for (int i = 1; i <= k; ++i) {
+    bool feasible = true;
+    for (int i = 1; i <= k && feasible; ++i) {
         if (w.rmatch[i]) continue;
-        for (int j = lane; j <= k; j += 32) { w.minv[j] = kIntInf; w.used[j] = 0; }
-        if (lane == 0) w.p[0] = i;
-        __syncwarp();
-        int j0 = 0;
-        int step = 0;
-        for (; step <= k; ++step) {
-            if (lane == 0) w.used[j0] = 1;
-            __syncwarp();
-            const int i0 = w.p[j0];
-            const int ui0 = w.u[i0];
-            const int rb = w.rows[i0 - 1] * m;
+#pragma unroll
+        for (int t = 0; t < CPL; ++t) {
+            mraw[t] = kIntInf;
+            way[t] = 0;
+            usedAt[t] = -1;
+        }
+        int j0 = 0, D = 0;
+        int ui0 = w.u[i], rb = w.rowb[i];
+        bool augmented = false;
+        for (int step = 0; step <= k; ++step) {
             int bv = kIntInf, bj = 0x7fffffff;
-            for (int j = lane + 1; j <= k; j += 32) {
-                if (w.used[j]) continue;
-                const int e = rb + w.cols[j - 1];
-                int mv = w.minv[j];
-                if ((code[e] & kAllowed) && (!face || (face[e] & kFaceIn))) {
-                    const int cur = scaled_cost(g, e, sign, shift) - ui0 - w.pv[j];
-                    if (cur < mv) { mv = cur; w.minv[j] = cur; w.way[j] = j0; }
+#pragma unroll
+            for (int t = 0; t < CPL; ++t) {
+                if (!valid[t] || usedAt[t] >= 0) continue;
+                const int c = cost[rb + colE[t]];
+                if (c < kIntInf) {
+                    const int cur = c - ui0 - pv[t] + D;
+                    if (cur < mraw[t]) { mraw[t] = cur; way[t] = j0; }
                 }
-                if (mv < bv) { bv = mv; bj = j; }
+                if (mraw[t] < bv) { bv = mraw[t]; bj = lane + 1 + 32 * t; }
             }
-            const int gmin = __reduce_min_sync(kFull, bv);
-            if (gmin >= kIntInf) return false;
-            const int j1 = __reduce_min_sync(kFull, bv == gmin ? bj : 0x7fffffff);
-            __syncwarp();
-            for (int j = lane; j <= k; j += 32) {
-                if (w.used[j]) { w.u[w.p[j]] += gmin; w.pv[j] -= gmin; }
-                else if (w.minv[j] < kIntInf) w.minv[j] -= gmin;
+            int gmin, j1;
+            const int key = bv < kPackLimit ? (bv << 10) | bj : 0x7fffffff;
+            const int kmin = __reduce_min_sync(kFull, key);
+            if (kmin != 0x7fffffff) {
+                gmin = kmin >> 10;
+                j1 = kmin & 1023;
+            } else {
+                gmin = __reduce_min_sync(kFull, bv);
+                if (gmin >= kIntInf) { feasible = false; break; }
+                j1 = __reduce_min_sync(kFull, bv == gmin ? bj : 0x7fffffff);
             }
-            __syncwarp();
+            D = gmin;
+            const int owner = (j1 - 1) & 31, slot = (j1 - 1) >> 5;
+            const int pnext = __shfl_sync(kFull, lane_slot<CPL>(pj, slot), owner);
+            const int unext = __shfl_sync(kFull, lane_slot<CPL>(ur, slot), owner);
+            const int rnext = __shfl_sync(kFull, lane_slot<CPL>(rbr, slot), owner);
+            if (lane == owner) {
+#pragma unroll
+                for (int t = 0; t < CPL; ++t)
+                    if (t == slot) usedAt[t] = D;
+            }
             j0 = j1;
-            if (w.p[j0] == 0) break;
+            if (pnext == 0) { augmented = true; break; }
+            ui0 = unext;
+            rb = rnext;
         }
-        if (w.p[j0] != 0) return false;
-        if (lane == 0) {
-            int jj = j0;
-            for (int guard = 0; guard <= k && jj != 0; ++guard) {
-                const int jp = w.way[jj];
-                w.p[jj] = w.p[jp];
-                jj = jp;
+        if (!feasible || !augmented) { feasible = false; break; }
+        // apply the potentials of this path (before the matching flips)
+        const int uroot = w.u[i] + D;
+#pragma unroll
+        for (int t = 0; t < CPL; ++t) {
+            if (usedAt[t] < 0) continue;
+            const int d = D - usedAt[t];
+            pv[t] -= d;
+            ur[t] += d;
+        }
+        // flip the path: column j takes the row (and its potential / offset) of way[j]
+        int j = j0;
+        for (int guard = 0; guard <= k && j != 0; ++guard) {
+            const int owner = (j - 1) & 31, slot = (j - 1) >> 5;
+            const int jp = __shfl_sync(kFull, lane_slot<CPL>(way, slot), owner);
+            int np = i, nu = uroot, nr = w.rowb[i];
+            if (jp != 0) {
+                const int po = (jp - 1) & 31, ps = (jp - 1) >> 5;
+                np = __shfl_sync(kFull, lane_slot<CPL>(pj, ps), po);
+                nu = __shfl_sync(kFull, lane_slot<CPL>(ur, ps), po);
+                nr = __shfl_sync(kFull, lane_slot<CPL>(rbr, ps), po);
             }
+            if (lane == owner) {
+#pragma unroll
+                for (int t = 0; t < CPL; ++t)
+                    if (t == slot) { pj[t] = np; ur[t] = nu; rbr[t] = nr; }
+            }
+            j = jp;
         }
         __syncwarp();
     }
+    if (!__all_sync(kFull, feasible)) return false;
     // outputs and the warm state for the next call (original indices)
-    for (int i = lane; i < m; i += 32) {
+    for (int i = lane; i < m; i += 32)
         if (w.fcol[i] >= 0) { w.pi[i] = w.fcol[i]; w.match[w.fcol[i]] = i; }
-    }
-    for (int j = lane + 1; j <= k; j += 32) {
-        const int r = w.rows[w.p[j] - 1], c = w.cols[j - 1];
-        w.pi[r] = c;
-        w.match[c] = r;
-        w.colpot[c] = w.pv[j];
-    }
-    __syncwarp();
     int lo = kIntInf;
-    for (int j = lane + 1; j <= k; j += 32) lo = min(lo, w.pv[j]);
+#pragma unroll
+    for (int t = 0; t < CPL; ++t) {
+        if (!valid[t]) continue;
+        const int r = w.rows[pj[t] - 1];
+        w.pi[r] = colE[t];
+        w.match[colE[t]] = r;
+        lo = min(lo, pv[t]);
+    }
     lo = __reduce_min_sync(kFull, lo);
     if (lo >= kIntInf) lo = 0;
     bool sane = true;
-    for (int j = lane + 1; j <= k; j += 32) {
-        const int v = w.colpot[w.cols[j - 1]] - lo;
-        w.colpot[w.cols[j - 1]] = v;
+#pragma unroll
+    for (int t = 0; t < CPL; ++t) {
+        if (!valid[t]) continue;
+        const int v = pv[t] - lo;
+        w.colpot[colE[t]] = v;
         sane = sane && v <= kPotLimit;
     }
     sane = __all_sync(kFull, sane);

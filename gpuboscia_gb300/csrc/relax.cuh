@@ -18,9 +18,10 @@ enum Buf { B_X, B_G, B_V, B_AW, B_TX, B_TG, B_R, B_LB, B_UB, B_CAND, B_COUNT };
 
 // Where every buffer of a node lives; computed once per launch on the host.
 struct Layout {
-    int off[B_COUNT];       // offset in doubles inside the node-vector block (-1: absent)
+    int off[B_COUNT];       // offset in doubles inside the buffer's region (-1: absent)
+    int in_smem[B_COUNT];   // 1: the buffer lives in dynamic shared memory, 0: global workspace
     int nvec;
-    int vec_smem;           // node vectors in dynamic shared memory
+    int vec_smem;           // every present node vector is in shared memory
     size_t node_stride;     // doubles per node in the global workspace
     int obj_smem;           // objective matrices staged in shared memory
     size_t obj_doubles;
@@ -31,7 +32,8 @@ struct Layout {
     // byte offsets inside dynamic shared memory
     size_t sm_vec, sm_obj, sm_keys, sm_prefix, sm_idx, sm_fixed, sm_hung, sm_total;
     // mixed precision (GBX_PRECISION_MIXED, Birkhoff graph matching): FP32
-    // x, gradient, residual, A, B, B' [6 n floats], edge / face code bytes
+    // x, gradient, residual, A, B, B' [6 n floats], forward / in-face integer
+    // oracle costs [2 n ints], edge / face code bytes
     // [2 n], and two integer Hungarian workspaces with warm state
     int mixed;
     size_t sm_mx, sm_code, sm_ihw, ihw_bytes;
@@ -70,9 +72,9 @@ GBX_HD inline size_t hung_ws_bytes(int m) {
 // bytes of one integer Hungarian workspace of the mixed path (with warm state)
 GBX_HD inline size_t ihw_bytes(int m) {
     size_t b = 0;
-    b += align16(5 * (size_t)(m + 1) * sizeof(int));   // u pv minv p way
+    b += align16(3 * (size_t)(m + 1) * sizeof(int));   // u rowb pvs
     b += align16(9 * (size_t)m * sizeof(int));         // rows cols rowpos fcol frow pi colpot match pinv
-    b += align16((size_t)(m + 1) * 2);                 // used, rmatch
+    b += align16((size_t)(m + 1));                     // rmatch
     b += align16(8 * sizeof(int));                     // scalars
     return b;
 }

@@ -43,14 +43,15 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
             return GBX_ERR_UNSUPPORTED;
         }
     }
+    // which node vectors exist
+    bool need[B_COUNT] = {};
+    need[B_X] = need[B_G] = need[B_V] = need[B_LB] = need[B_UB] = true;
+    need[B_AW] = dicg && !mixed;
+    need[B_TX] = need[B_TG] = secant;
+    need[B_R] = o.kind == GBX_OBJ_GRAPH_MATCHING;
+    need[B_CAND] = !secant;  // with the secant search the candidate reuses the trial point
     int cnt = 0;
-    auto add = [&](int b) { L.off[b] = cnt * n; ++cnt; };
-    add(B_X); add(B_G); add(B_V);
-    if (dicg && !mixed) add(B_AW);
-    if (secant) { add(B_TX); add(B_TG); }
-    if (o.kind == GBX_OBJ_GRAPH_MATCHING) add(B_R);
-    add(B_LB); add(B_UB);
-    if (secant) L.off[B_CAND] = L.off[B_TX]; else add(B_CAND);
+    for (int b = 0; b < B_COUNT; ++b) cnt += need[b];
     L.nvec = cnt;
 
     size_t fixed_bytes = 0;
@@ -70,29 +71,54 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
     L.mixed = mixed ? 1 : 0;
     size_t mx_bytes = 0, code_bytes = 0;
     if (mixed) {
-        mx_bytes = align16(6 * (size_t)n * sizeof(float));
+        if (l.order > 256) {
+            *err = "mixed precision supports Birkhoff orders up to 256";
+            return GBX_ERR_UNSUPPORTED;
+        }
+        mx_bytes = align16(6 * (size_t)n * sizeof(float) + 2 * (size_t)n * sizeof(int)
+                           + 2 * align16((size_t)n));
         code_bytes = align16(2 * (size_t)n);
         L.ihw_bytes = ihw_bytes(l.order);
         fixed_bytes += mx_bytes + code_bytes + 2 * L.ihw_bytes;
     }
-    const size_t vec_bytes = align16((size_t)cnt * n * sizeof(double));
     size_t obj_doubles = o.kind == GBX_OBJ_GRAPH_MATCHING ? 2 * (size_t)o.order * o.order
                                                           : (size_t)n * n;
     const size_t obj_bytes = align16(obj_doubles * sizeof(double));
     L.obj_doubles = obj_doubles;
-    if (vec_bytes + obj_bytes + fixed_bytes <= kSmemBudget) {
-        L.vec_smem = 1; L.obj_smem = 1;
-    } else if (vec_bytes + fixed_bytes <= kSmemBudget) {
-        L.vec_smem = 1; L.obj_smem = 0;
-    } else if (obj_bytes + fixed_bytes <= kSmemBudget) {
-        L.vec_smem = 0; L.obj_smem = 1;
-    } else {
-        L.vec_smem = 0; L.obj_smem = 0;
-    }
     if (fixed_bytes > kSmemBudget) { *err = "LMO workspace exceeds shared memory"; return GBX_ERR_UNSUPPORTED; }
-    L.node_stride = L.vec_smem ? 0 : (size_t)cnt * n;
+    // Placement. The mixed loop touches only x and the bounds among the FP64
+    // vectors, so those stay in shared memory and the certificate's vectors and
+    // the FP64 objective matrices go to the workspace (two nodes per SM fit).
+    // The FP64 path keeps everything in shared memory when it fits.
+    bool smem[B_COUNT] = {};
+    const size_t vec_all = align16((size_t)cnt * n * sizeof(double));
+    if (mixed) {
+        smem[B_X] = smem[B_LB] = smem[B_UB] = true;
+        L.obj_smem = 0;
+        if (align16(3 * (size_t)n * sizeof(double)) + fixed_bytes > kSmemBudget)
+            smem[B_X] = smem[B_LB] = smem[B_UB] = false;
+    } else if (vec_all + obj_bytes + fixed_bytes <= kSmemBudget) {
+        for (int b = 0; b < B_COUNT; ++b) smem[b] = need[b];
+        L.obj_smem = 1;
+    } else if (vec_all + fixed_bytes <= kSmemBudget) {
+        for (int b = 0; b < B_COUNT; ++b) smem[b] = need[b];
+        L.obj_smem = 0;
+    } else {
+        L.obj_smem = obj_bytes + fixed_bytes <= kSmemBudget ? 1 : 0;
+    }
+    int sc = 0, gc = 0;
+    L.vec_smem = 1;
+    for (int b = 0; b < B_COUNT; ++b) {
+        L.off[b] = -1;
+        L.in_smem[b] = 0;
+        if (!need[b]) continue;
+        if (smem[b]) { L.in_smem[b] = 1; L.off[b] = sc++ * n; }
+        else { L.off[b] = gc++ * n; L.vec_smem = 0; }
+    }
+    if (secant) { L.off[B_CAND] = L.off[B_TX]; L.in_smem[B_CAND] = L.in_smem[B_TX]; }
+    L.node_stride = (size_t)gc * n;
     size_t p = 0;
-    L.sm_vec = p; if (L.vec_smem) p += vec_bytes;
+    L.sm_vec = p; p += align16((size_t)sc * n * sizeof(double));
     L.sm_obj = p; if (L.obj_smem) p += obj_bytes;
     L.sm_keys = p; L.sm_prefix = p; L.sm_idx = p; L.sm_fixed = p;
     if (L.sort_size) {
@@ -112,7 +138,7 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
 }
 
 size_t workspace_bytes(const Layout& L, int n_nodes) {
-    size_t b = L.vec_smem ? 0 : L.node_stride * sizeof(double) * (size_t)n_nodes;
+    size_t b = L.node_stride * sizeof(double) * (size_t)n_nodes;
     b += L.mixed_node_bytes * (size_t)n_nodes;
     return b + 256;
 }

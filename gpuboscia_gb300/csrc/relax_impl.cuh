@@ -655,16 +655,25 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
     float* Af = Rf + n;
     float* Bf = Af + n;
     float* Btf = Bf + n;
+    int* costf = reinterpret_cast<int*>(Btf + n);   // forward oracle costs
+    int* costa = costf + n;                          // in-face oracle costs (negated, face only)
+    int8_t* Ai = reinterpret_cast<int8_t*>(costa + n);   // A, B as small integers when they are
+    int8_t* Bi = Ai + align16((size_t)n);                 // (exact integer scores and curvature)
     uint8_t* code = dsm + L.sm_code;
     uint8_t* face = code + n;
     const IHW w0 = ihw_at(dsm + L.sm_ihw, m);
     const IHW w1 = ihw_at(dsm + L.sm_ihw + L.ihw_bytes, m);
     const double tol = c.tol;
+    bool int_ok = true;
     for (int e = tid; e < n; e += kThreads) {
         const int i = e / m, j = e - (e / m) * m;
         Af[e] = (float)c.A[e];
         Bf[e] = (float)c.B[e];
         Btf[e] = (float)c.B[j * m + i];
+        const double ae = c.A[e], be = c.B[e];
+        if (!(ae == rint(ae) && fabs(ae) <= 127.0 && be == rint(be) && fabs(be) <= 127.0)) int_ok = false;
+        Ai[e] = (int8_t)(fabs(ae) <= 127.0 ? (int)ae : 0);
+        Bi[e] = (int8_t)(fabs(be) <= 127.0 ? (int)be : 0);
         const double lo = LB[e], up = UB[e];
         uint8_t cd = 0;
         if (lo > 0.5) cd |= kForced;
@@ -677,9 +686,31 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
         xf[e] = (float)xe;
         face[e] = (uint8_t)((xe > 1e-9 ? kFaceIn : 0) | (xe >= 1.0 - 1e-9 ? kFaceOne : 0));
     }
-    if (tid == 0) { w0.scal[0] = 0; w0.scal[1] = 0; }
-    if (tid == 32) { w1.scal[0] = 0; w1.scal[1] = 0; }
-    __syncthreads();
+    if (tid == 0) { w0.scal[0] = 0; w0.scal[1] = 0; w0.scal[2] = 0; }
+    if (tid == 32) { w1.scal[0] = 0; w1.scal[1] = 0; w1.scal[2] = 0; }
+    if (tid == 0) c.flag[4] = 0;  // set when a face-forced bit of x changes
+    // small-integer A and B (graph adjacency): permutation residuals are
+    // integers, so scores and curvatures are exact integer sums (the FP64 sums
+    // of the same integers are exact too, hence bit-identical)
+    const bool ints = __syncthreads_and(int_ok) != 0;
+
+    auto score = [&](const int* pi, int* pinv) -> double {
+        if (!ints) return perm_score(c, code, pi, pinv);
+        bool valid = true;
+        for (int r = tid; r < m; r += kThreads) pinv[pi[r]] = r;
+        for (int e = tid; e < n; e += kThreads) {
+            const int i = e / m, j = e - (e / m) * m;
+            if (!(code[e] & (pi[i] == j ? kOneOk : kZeroOk))) valid = false;
+        }
+        if (!__syncthreads_and(valid)) return kNone;
+        int acc = 0;
+        for (int e = tid; e < n; e += kThreads) {
+            const int i = e / m, j = e - (e / m) * m;
+            const int r = (int)Ai[i * m + pinv[j]] - (int)Bi[pi[i] * m + j];
+            acc += r * r;
+        }
+        return c.s * bsum((double)acc, c.red);
+    };
 
     auto take = [&](const int* pi, double fv) {
         if (fv < best_val) {
@@ -704,16 +735,29 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
             frexpf(limit / gmx, &ex);
             shift = max(-120, min(120, ex - 1));
         }
-        if (threadIdx.x < 32) {
-            const bool ok = int_hungarian_warp(w0, m, gf, 1.f, shift, code, nullptr);
-            if (threadIdx.x == 0) c.flag[0] = ok;
-        } else if (dicg && threadIdx.x < 64) {
-            const bool ok = int_hungarian_warp(w1, m, gf, -1.f, shift, code, face);
-            if (threadIdx.x == 32) c.flag[2] = ok;
+        for (int e = tid; e < n; e += kThreads) {
+            const int ci = __float2int_rn(scalbnf(gf[e], shift));
+            const bool allowed = (code[e] & kAllowed) != 0;
+            costf[e] = allowed ? ci : kIntInf;
+            if (dicg) costa[e] = (allowed && (face[e] & kFaceIn)) ? -ci : kIntInf;
         }
         __syncthreads();
+        if (threadIdx.x < 64 && (threadIdx.x < 32 || dicg)) {
+            const bool fwd = threadIdx.x < 32;
+            const IHW& w = fwd ? w0 : w1;
+            const int* cst = fwd ? costf : costa;
+            const uint8_t* fc = fwd ? nullptr : face;
+            const bool same = fwd || c.flag[4] == 0;
+            bool ok;
+            if (m <= 64) ok = int_hungarian_warp<2>(w, m, cst, shift, code, fc, same);
+            else if (m <= 128) ok = int_hungarian_warp<4>(w, m, cst, shift, code, fc, same);
+            else ok = int_hungarian_warp<8>(w, m, cst, shift, code, fc, same);
+            if ((threadIdx.x & 31) == 0) c.flag[fwd ? 0 : 2] = ok;
+        }
+        __syncthreads();
+        if (tid == 0) c.flag[4] = 0;
         if (!c.flag[0] || (dicg && !c.flag[2])) break;
-        take(w0.pi, perm_score(c, code, w0.pi, w0.pinv));
+        take(w0.pi, score(w0.pi, w0.pinv));
         double loc = 0.0;
         for (int e = tid; e < n; e += kThreads) {
             const double ve = w0.pi[e / m] == e - (e / m) * m ? 1.0 : 0.0;
@@ -748,7 +792,7 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
             __syncthreads();
             continue;
         }
-        take(w1.pi, perm_score(c, code, w1.pi, w1.pinv));
+        take(w1.pi, score(w1.pi, w1.pinv));
         for (int r = tid; r < m; r += kThreads) {
             w0.pinv[w0.pi[r]] = r;
             w1.pinv[w1.pi[r]] = r;
@@ -770,11 +814,22 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
                 const int pa = w1.pi[i], pv = w0.pi[i];
                 if (pa != pv) pl += (double)gf[i * m + pa] - (double)gf[i * m + pv];
             }
-            for (int e = tid; e < n; e += kThreads) {
-                const int i = e / m, j = e - (e / m) * m;
-                const double rd = (c.A[i * m + w1.pinv[j]] - c.A[i * m + w0.pinv[j]])
-                                - (c.B[w1.pi[i] * m + j] - c.B[w0.pi[i] * m + j]);
-                cl = fma(rd, rd, cl);
+            if (ints) {
+                int acc = 0;
+                for (int e = tid; e < n; e += kThreads) {
+                    const int i = e / m, j = e - (e / m) * m;
+                    const int rd = ((int)Ai[i * m + w1.pinv[j]] - (int)Ai[i * m + w0.pinv[j]])
+                                 - ((int)Bi[w1.pi[i] * m + j] - (int)Bi[w0.pi[i] * m + j]);
+                    acc += rd * rd;
+                }
+                cl = (double)acc;
+            } else {
+                for (int e = tid; e < n; e += kThreads) {
+                    const int i = e / m, j = e - (e / m) * m;
+                    const double rd = (c.A[i * m + w1.pinv[j]] - c.A[i * m + w0.pinv[j]])
+                                    - (c.B[w1.pi[i] * m + j] - c.B[w0.pi[i] * m + j]);
+                    cl = fma(rd, rd, cl);
+                }
             }
             const double pgap = bsum(pl, c.red);
             const double curv = (2.0 * c.s) * bsum(cl, c.red);
@@ -795,8 +850,11 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
             X[ev] = fma(-gm, -1.0, X[ev]);
             xf[ea] = (float)X[ea];
             xf[ev] = (float)X[ev];
-            face[ea] = (uint8_t)((X[ea] > 1e-9 ? kFaceIn : 0) | (X[ea] >= 1.0 - 1e-9 ? kFaceOne : 0));
-            face[ev] = (uint8_t)((X[ev] > 1e-9 ? kFaceIn : 0) | (X[ev] >= 1.0 - 1e-9 ? kFaceOne : 0));
+            const uint8_t fa = (uint8_t)((X[ea] > 1e-9 ? kFaceIn : 0) | (X[ea] >= 1.0 - 1e-9 ? kFaceOne : 0));
+            const uint8_t fv = (uint8_t)((X[ev] > 1e-9 ? kFaceIn : 0) | (X[ev] >= 1.0 - 1e-9 ? kFaceOne : 0));
+            if (((fa ^ face[ea]) | (fv ^ face[ev])) & kFaceOne) c.flag[4] = 1;
+            face[ea] = fa;
+            face[ev] = fv;
         }
         __syncthreads();
     }
@@ -809,12 +867,13 @@ struct Scalars {
     int flag[8];
 };
 
-__device__ inline double* vecp(double* base, const Layout& L, int b) {
-    return L.off[b] >= 0 ? base + L.off[b] : nullptr;
+__device__ inline double* vecp(double* sbase, double* gbase, const Layout& L, int b) {
+    if (L.off[b] < 0) return nullptr;
+    return (L.in_smem[b] ? sbase : gbase) + L.off[b];
 }
 
-template <int OK, int LK>
-__global__ void __launch_bounds__(kThreads, 1) relax_kernel(const __grid_constant__ Params P) {
+template <int OK, int LK, bool MIX>
+__global__ void __launch_bounds__(kThreads, MIX ? 2 : 1) relax_kernel(const __grid_constant__ Params P) {
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ Scalars sh;
     const int node = blockIdx.x;
@@ -823,17 +882,17 @@ __global__ void __launch_bounds__(kThreads, 1) relax_kernel(const __grid_constan
     const int n = P.obj.n;
     const Layout& L = P.L;
 
-    double* vb = L.vec_smem ? reinterpret_cast<double*>(dsm + L.sm_vec)
-                            : P.ws + (size_t)node * L.node_stride;
-    double* X = vecp(vb, L, B_X);
-    double* G = vecp(vb, L, B_G);
-    double* V = vecp(vb, L, B_V);
-    double* AW = vecp(vb, L, B_AW);
-    double* TX = vecp(vb, L, B_TX);
-    double* TG = vecp(vb, L, B_TG);
-    double* LB = vecp(vb, L, B_LB);
-    double* UB = vecp(vb, L, B_UB);
-    double* CAND = vecp(vb, L, B_CAND);
+    double* sb = reinterpret_cast<double*>(dsm + L.sm_vec);
+    double* gb = P.ws + (size_t)node * L.node_stride;
+    double* X = vecp(sb, gb, L, B_X);
+    double* G = vecp(sb, gb, L, B_G);
+    double* V = vecp(sb, gb, L, B_V);
+    double* AW = vecp(sb, gb, L, B_AW);
+    double* TX = vecp(sb, gb, L, B_TX);
+    double* TG = vecp(sb, gb, L, B_TG);
+    double* LB = vecp(sb, gb, L, B_LB);
+    double* UB = vecp(sb, gb, L, B_UB);
+    double* CAND = vecp(sb, gb, L, B_CAND);
 
     const size_t off = (size_t)node * n;
     double* gx = P.b.x + off;
@@ -850,7 +909,7 @@ __global__ void __launch_bounds__(kThreads, 1) relax_kernel(const __grid_constan
     c.s = P.obj.scale;
     c.ls = P.obj.linear_scale;
     c.k0 = P.obj.constant;
-    c.R = vecp(vb, L, B_R);
+    c.R = vecp(sb, gb, L, B_R);
     c.lk = LK;
     c.rhs = P.lmo.right_side;
     c.is_int = P.lmo.is_int;
@@ -989,14 +1048,10 @@ __global__ void __launch_bounds__(kThreads, 1) relax_kernel(const __grid_constan
     };
 
     int iters = it0;
-    bool mixed_done = false;
-    if constexpr (OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF) {
-        if (L.mixed) {
-            iters = mixed_loop(c, P, dsm, node, X, LB, UB, best, best_val, eps, it0, dicg, ls);
-            mixed_done = true;
-        }
-    }
-    for (int iter = 0; !mixed_done && iter < P.b.max_iters; ++iter) {
+    constexpr bool kMixedLoop = MIX && OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF;
+    if constexpr (kMixedLoop)
+        iters = mixed_loop(c, P, dsm, node, X, LB, UB, best, best_val, eps, it0, dicg, ls);
+    for (int iter = 0; !kMixedLoop && iter < P.b.max_iters; ++iter) {
         iters = it0 + iter + 1;
         obj_grad(c, X, G);
         bool fwd_perm = false, away_perm = false;
@@ -1186,7 +1241,9 @@ __global__ void __launch_bounds__(kThreads, 1) feasible_kernel(
 // ------------------------------------------------------------------ launchers
 template <int OK, int LK>
 int launch_one(const Params& p, cudaStream_t st, std::string* err) {
-    auto k = relax_kernel<OK, LK>;
+    auto k = relax_kernel<OK, LK, false>;
+    if constexpr (OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF)
+        if (p.L.mixed) k = relax_kernel<OK, LK, true>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::max<size_t>(p.L.sm_total, 1));
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
