@@ -162,6 +162,62 @@ def config_dict(args):
             "precision": args.precision, "l2": "flushed between timed steps (256 MiB write)"}
 
 
+def time_plain(args, inst, lb, x0, d_lb, d_ub, d_eps, d_flags, flush, w, stream):
+    """The plain method (FP64 gradient and Hungarian) on the same batch, for the ratio."""
+    import torch
+    from gpuboscia_gb300 import _abi as A
+    from gpuboscia_gb300 import api
+    N = lb.shape[0]
+    alg = A.Algorithm(w["alg"], w["ls"], 4, 1e-10, 1e-14, A.PRECISION_FP64)
+    x = torch.empty_like(x0)
+    it = torch.zeros(N, dtype=torch.int32, device=x0.device)
+    st = torch.zeros(N, dtype=torch.uint8, device=x0.device)
+    relaxer = api.BatchRelaxer(inst.objective, inst.lmo, alg, x, d_lb, d_ub, d_eps, it, st, args.iters, d_flags,
+                               1e-6, stream)
+    x.copy_(x0)
+    relaxer.launch()
+    times = []
+    for k in range(args.plain_steps):
+        flush.fill_(float(k))
+        x.copy_(x0)
+        it.zero_()
+        st.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        relaxer.launch()
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    ms = sum(times) / len(times)
+    return {"value": N / (ms / 1000.0), "unit": "nodes/s", "ms_per_step": ms, "steps": len(times),
+            "node_iterations_per_step": int(it.sum().item())}
+
+
+def time_to_gap(args, inst):
+    """Wall time of gpuboscia::solve (through gbx_solve) from entry to the certified
+    1e-6 gap, plain FP64 against mixed precision, on the workload's instance."""
+    from gpuboscia_gb300 import _abi as A
+    from gpuboscia_gb300 import api
+    out = {}
+    for name, prec in (("plain_fp64", A.PRECISION_FP64), ("mixed", A.PRECISION_MIXED)):
+        s = inst.settings
+        s.gpu_batch_size = 256
+        s.num_streams = 2
+        s.gpu_max_iters = 400
+        s.line_search = A.LS_QUADRATIC_EXACT
+        s.abs_gap_tol = 1e-6
+        s.rel_gap_tol = 1e-6
+        s.time_limit_seconds = args.ttg_limit
+        s.precision = prec
+        t0 = time.perf_counter()
+        r = api.solve(inst.problem, inst.objective, inst.lmo, s)
+        wall = time.perf_counter() - t0
+        out[name] = {"seconds": wall, "nodes": r.nodes_processed, "objective": r.objective,
+                     "dual_bound": r.dual_bound, "certified": bool(r.reached_tolerance),
+                     "time_limit": bool(r.reached_time_limit)}
+    return out
+
+
 def run_gpu(args, rank, world):
     import torch
     from gpuboscia_gb300 import _abi as A
@@ -262,6 +318,10 @@ def run_gpu(args, rank, world):
         torch.distributed.all_reduce(e2e_local, op=torch.distributed.ReduceOp.MAX)
     e2e_value = N * args.steps * world / float(e2e_local.item())
 
+    plain = None
+    if args.plain_steps > 0 and prec != A.PRECISION_FP64:
+        plain = time_plain(args, inst, lb, x0, d_lb, d_ub, d_eps, d_flags, flush, w, stream)
+    ttg = time_to_gap(args, inst) if rank == 0 and args.ttg_limit > 0 else None
     if rank != 0:
         return
     hbm_peak, bf16_peak, peak_kind = load_peaks()
@@ -284,6 +344,7 @@ def run_gpu(args, rank, world):
                                        f"{dt:.1f} s"},
             "clocks": clk.summary(), "gpu_launches": args.steps,
             "node_iterations_per_step": node_iters,
+            "plain_fp64": plain, "time_to_gap": ttg,
             "status_counts": {str(s): int((statuses == s).sum()) for s in np.unique(statuses)}}
     print(json.dumps(line), flush=True)
 
@@ -297,7 +358,11 @@ def main():
     ap.add_argument("--workload", default="birkhoff_gnp36", choices=sorted(WORKLOADS))
     ap.add_argument("--nodes", type=int, default=None)
     ap.add_argument("--iters", type=int, default=None)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--plain-steps", type=int, default=2,
+                    help="timed steps of the plain FP64 method on the same batch (0 skips it)")
+    ap.add_argument("--ttg-limit", type=float, default=30.0,
+                    help="time limit of each time-to-gap solve in seconds (0 skips them)")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-budget", type=float, default=8.0)
     args = ap.parse_args()

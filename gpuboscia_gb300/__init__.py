@@ -8,10 +8,10 @@ include/gpuboscia/gpuboscia.h instead.
 from . import _abi
 from .api import (BirkhoffLMO, BoxLMO, DenseQuadraticObjective, EqualitySimplexLMO, GraphMatchingObjective,
                   ILSObjective, Problem, RelaxWorkspace, Result, Settings, UnitSimplexLMO, lmo_batch,
-                  node_feasible_batch, relax_batch, solve)
+                  node_feasible_batch, objective_gradient_batch, relax_batch, solve)
 
 __all__ = [
     "BirkhoffLMO", "BoxLMO", "DenseQuadraticObjective", "EqualitySimplexLMO", "GraphMatchingObjective",
     "ILSObjective", "Problem", "RelaxWorkspace", "Result", "Settings", "UnitSimplexLMO", "lmo_batch",
-    "node_feasible_batch", "relax_batch", "solve", "_abi",
+    "node_feasible_batch", "objective_gradient_batch", "relax_batch", "solve", "_abi",
 ]

@@ -146,7 +146,8 @@ STATIC_SCRATCH_BYTES = 32 << 20
 # exported symbols of the CUDA library, as declared in include/gpuboscia_gb300.h
 EXPORTED_SYMBOLS = (
     "gbx_abi_version", "gbx_last_error", "gbx_relax_workspace_bytes",
-    "gbx_relax_batch", "gbx_relax_batch_static", "gbx_lmo_batch", "gbx_node_feasible_batch",
+    "gbx_relax_batch", "gbx_relax_batch_static", "gbx_lmo_batch", "gbx_objective_gradient_batch",
+    "gbx_node_feasible_batch",
     "gbx_default_settings", "gbx_solve",
 )
 
@@ -177,6 +178,9 @@ def load(path: os.PathLike | str | None = None) -> C.CDLL:
     lib.gbx_lmo_batch.restype = C.c_int
     lib.gbx_lmo_batch.argtypes = [P(LMO), C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.gbx_objective_gradient_batch.restype = C.c_int
+    lib.gbx_objective_gradient_batch.argtypes = [P(Objective), C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                                 C.c_void_p]
     lib.gbx_node_feasible_batch.restype = C.c_int
     lib.gbx_node_feasible_batch.argtypes = [P(LMO), C.c_int, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.c_void_p]

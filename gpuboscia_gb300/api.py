@@ -308,6 +308,21 @@ def lmo_batch(lmo, mode: int, direction, lb, ub, x=None, want_step: bool = False
     return out, step
 
 
+def objective_gradient_batch(objective, x, precision: int = A.PRECISION_FP64, stream=None):
+    """Gradients of the objective at the rows of the device tensor x [cases, n]."""
+    import torch
+    lib = A.load()
+    keep = _Keep()
+    cases, n = x.shape
+    o = objective.to_c("cuda", keep)
+    g = torch.empty(cases, n, dtype=torch.float64, device=x.device)
+    rc = lib.gbx_objective_gradient_batch(C.byref(o), precision, cases, x.data_ptr(), g.data_ptr(),
+                                          _stream_ptr(stream))
+    A.check(lib, rc, "gbx_objective_gradient_batch")
+    torch.cuda.current_stream().synchronize()
+    return g
+
+
 def node_feasible_batch(lmo, lb, ub, integer_flags=None, stream=None):
     import torch
     lib = A.load()

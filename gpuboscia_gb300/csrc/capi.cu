@@ -88,7 +88,15 @@ int gbx_relax_batch(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algo
     if (need > 256 && (!workspace || workspace_bytes < need))
         return fail(GBX_ERR_WORKSPACE, "workspace smaller than gbx_relax_workspace_bytes()");
     p.ws = static_cast<double*>(workspace);
-    p.mixed = nullptr;
+    p.mixed = p.L.mixed_node_bytes
+                  ? static_cast<unsigned char*>(workspace) + gbx::mixed_region_offset(p.L, b->n_nodes)
+                  : nullptr;
+    p.sparse = nullptr;
+    if (p.L.sparse_bytes && b->n_nodes > 0) {
+        p.sparse = static_cast<unsigned char*>(workspace) + gbx::sparse_region_offset(p.L, b->n_nodes);
+        rc = gbx::launch_sparse_build(*obj, p.L, p.sparse, static_cast<cudaStream_t>(stream), &err);
+        if (rc) return fail(rc, err);
+    }
     rc = gbx::launch_relax(p, stream, &err);
     if (rc) return fail(rc, err);
     return GBX_OK;
@@ -106,6 +114,29 @@ int gbx_lmo_batch(const gbx_lmo* lmo, int cases, int mode, const double* directi
     std::string err;
     const int rc = gbx::launch_lmo_batch(*lmo, cases, mode, direction, x, lb, ub, out,
                                          out_step, stream, &err);
+    if (rc) return fail(rc, err);
+    return GBX_OK;
+}
+
+int gbx_objective_gradient_batch(const gbx_objective* obj, int precision, int cases,
+                                 const double* x, double* g, void* stream) {
+    if (!obj || cases < 0 || obj->n <= 0) return fail(GBX_ERR_INVALID, "gradient batch arguments");
+    if (cases > 0 && (!x || !g)) return fail(GBX_ERR_INVALID, "null gradient buffer");
+    if (obj->kind == GBX_OBJ_DENSE_QUADRATIC) {
+        if (!obj->Q) return fail(GBX_ERR_INVALID, "dense quadratic needs Q");
+    } else if (obj->kind == GBX_OBJ_GRAPH_MATCHING) {
+        if (obj->order <= 0 || obj->order * obj->order != obj->n || !obj->A || !obj->B)
+            return fail(GBX_ERR_INVALID, "graph matching needs order*order == n and A, B");
+    } else {
+        return fail(GBX_ERR_UNSUPPORTED, "unknown objective kind");
+    }
+    if (precision != GBX_PRECISION_FP64 && precision != GBX_PRECISION_MIXED)
+        return fail(GBX_ERR_INVALID, "unknown precision");
+    if (precision == GBX_PRECISION_MIXED && (obj->kind != GBX_OBJ_GRAPH_MATCHING || obj->order > 128))
+        return fail(GBX_ERR_UNSUPPORTED, "the mixed gradient covers graph matching up to order 128");
+    std::string err;
+    const int rc = gbx::launch_gradient_batch(*obj, precision, cases, x, g,
+                                              static_cast<cudaStream_t>(stream), &err);
     if (rc) return fail(rc, err);
     return GBX_OK;
 }

@@ -1,6 +1,8 @@
 // relax.cuh -- shared declarations of the node-relaxation kernels.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstddef>
 #include <cstdint>
 #include <string>
@@ -32,12 +34,20 @@ struct Layout {
     // byte offsets inside dynamic shared memory
     size_t sm_vec, sm_obj, sm_keys, sm_prefix, sm_idx, sm_fixed, sm_hung, sm_total;
     // mixed precision (GBX_PRECISION_MIXED, Birkhoff graph matching): FP32
-    // x, gradient, residual, A, B, B' [6 n floats], forward / in-face integer
-    // oracle costs [2 n ints], edge / face code bytes
-    // [2 n], and two integer Hungarian workspaces with warm state
+    // x, gradient, residual, A, B, B' [6 n floats] and A, B as int8 [2 n]
+    // (shared memory, or per node in the workspace when mx_global), forward /
+    // in-face integer oracle costs [2 n ints], edge / face code bytes [2 n],
+    // and two integer Hungarian workspaces with warm state
     int mixed;
-    size_t sm_mx, sm_code, sm_ihw, ihw_bytes;
-    size_t mixed_node_bytes;
+    int mx_global;
+    int tc;                   // gradient on the tensor cores (orders 65..128); the
+                              // operand images share the cost matrices' memory
+    size_t sm_mx, sm_cost, sm_code, sm_ihw, ihw_bytes;
+    size_t mixed_node_bytes;  // bytes per node of the workspace's mixed region
+    // graph matching: nonzero lists of A and B (rows and columns), built once
+    // per launch at the end of the workspace; up to sparse_cap entries each
+    int sparse_cap;
+    size_t sparse_bytes;
 };
 
 struct Params {
@@ -48,6 +58,7 @@ struct Params {
     Layout L;
     double* ws;             // global workspace (node vectors when not in smem)
     unsigned char* mixed;   // mixed-precision scratch
+    unsigned char* sparse;  // nonzero lists of A and B (graph matching), or null
 };
 
 #ifdef __CUDACC__
@@ -57,6 +68,36 @@ struct Params {
 #endif
 
 GBX_HD inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
+
+// Nonzero lists of the graph-matching matrices, CSR-like per line:
+// list 0 = rows of A, 1 = columns of B, 2 = columns of A, 3 = rows of B;
+// entries of a line in increasing index. ok[l] = 0 when list l overflowed.
+struct SparseAB {
+    int* ok;        // [4]
+    int* ptr[4];    // [m + 1]
+    int* idx[4];    // [cap]
+    double* val[4]; // [cap]
+};
+
+GBX_HD inline size_t sparse_list_bytes(int m, int cap) {
+    return align16((size_t)(m + 1) * sizeof(int)) + align16((size_t)cap * sizeof(int))
+         + align16((size_t)cap * sizeof(double));
+}
+
+GBX_HD inline SparseAB sparse_at(unsigned char* base, int m, int cap) {
+    SparseAB S;
+    S.ok = reinterpret_cast<int*>(base);
+    size_t o = 16;
+    for (int l = 0; l < 4; ++l) {
+        S.ptr[l] = reinterpret_cast<int*>(base + o);
+        o += align16((size_t)(m + 1) * sizeof(int));
+        S.idx[l] = reinterpret_cast<int*>(base + o);
+        o += align16((size_t)cap * sizeof(int));
+        S.val[l] = reinterpret_cast<double*>(base + o);
+        o += align16((size_t)cap * sizeof(double));
+    }
+    return S;
+}
 
 // bytes of one FP64 Hungarian workspace (potentials, minv, path, forced maps)
 GBX_HD inline size_t hung_ws_bytes(int m) {
@@ -68,6 +109,15 @@ GBX_HD inline size_t hung_ws_bytes(int m) {
     b += align16((size_t)(m + 1));                          // used
     return b;
 }
+
+// bytes of the mixed path's FP32 / int8 node arrays (xf gf Rf Af Bf Btf, Ai Bi)
+GBX_HD inline size_t mixed_array_bytes(int n) {
+    return align16(6 * (size_t)n * sizeof(float)) + 2 * align16((size_t)n);
+}
+
+// bytes of a node's A / -B operand images of the tensor-core gradient
+constexpr size_t kTcImageBytes = 2 * 128 * 128 * 2;
+constexpr size_t kTcOperandBytes = 4 * 128 * 128 * 2;  // A, -B, two halves of X or R
 
 // bytes of one integer Hungarian workspace of the mixed path (with warm state)
 GBX_HD inline size_t ihw_bytes(int m) {
@@ -86,10 +136,16 @@ void set_last_error(const std::string& msg);
 int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a,
                 int n_nodes, Layout* L, std::string* err);
 size_t workspace_bytes(const Layout& L, int n_nodes);
+size_t mixed_region_offset(const Layout& L, int n_nodes);  // bytes from the workspace start
+size_t sparse_region_offset(const Layout& L, int n_nodes);
+int launch_sparse_build(const gbx_objective& o, const Layout& L, unsigned char* base, cudaStream_t st,
+                        std::string* err);
 int launch_relax(const Params& p, void* stream, std::string* err);
 int launch_lmo_batch(const gbx_lmo& l, int cases, int mode, const double* dir,
                      const double* x, const double* lb, const double* ub, double* out,
                      double* out_step, void* stream, std::string* err);
+int launch_gradient_batch(const gbx_objective& o, int precision, int cases, const double* x, double* g,
+                          cudaStream_t st, std::string* err);
 int launch_node_feasible(const gbx_lmo& l, int cases, const double* lb, const double* ub,
                          const uint8_t* flags, uint8_t* out, void* stream, std::string* err);
 

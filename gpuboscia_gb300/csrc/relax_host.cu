@@ -69,17 +69,19 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
         fixed_bytes += 2 * L.hung_bytes;
     }
     L.mixed = mixed ? 1 : 0;
-    size_t mx_bytes = 0, code_bytes = 0;
+    size_t mx_bytes = 0, cost_bytes = 0, code_bytes = 0;
     if (mixed) {
         if (l.order > 256) {
             *err = "mixed precision supports Birkhoff orders up to 256";
             return GBX_ERR_UNSUPPORTED;
         }
-        mx_bytes = align16(6 * (size_t)n * sizeof(float) + 2 * (size_t)n * sizeof(int)
-                           + 2 * align16((size_t)n));
+        mx_bytes = mixed_array_bytes(n);
+        cost_bytes = align16(2 * (size_t)n * sizeof(int));
+        L.tc = l.order > 64 && l.order <= 128 ? 1 : 0;
+        if (L.tc) cost_bytes = std::max(cost_bytes, kTcOperandBytes);
         code_bytes = align16(2 * (size_t)n);
         L.ihw_bytes = ihw_bytes(l.order);
-        fixed_bytes += mx_bytes + code_bytes + 2 * L.ihw_bytes;
+        fixed_bytes += cost_bytes + code_bytes + 2 * L.ihw_bytes;
     }
     size_t obj_doubles = o.kind == GBX_OBJ_GRAPH_MATCHING ? 2 * (size_t)o.order * o.order
                                                           : (size_t)n * n;
@@ -93,10 +95,13 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
     bool smem[B_COUNT] = {};
     const size_t vec_all = align16((size_t)cnt * n * sizeof(double));
     if (mixed) {
-        smem[B_X] = smem[B_LB] = smem[B_UB] = true;
+        // the FP32 arrays go to the workspace when they do not fit beside
+        // the oracle costs (orders above ~90); x and the bounds follow them
         L.obj_smem = 0;
-        if (align16(3 * (size_t)n * sizeof(double)) + fixed_bytes > kSmemBudget)
-            smem[B_X] = smem[B_LB] = smem[B_UB] = false;
+        L.mx_global = (L.tc || mx_bytes + fixed_bytes > kSmemBudget) ? 1 : 0;
+        if (!L.mx_global) fixed_bytes += mx_bytes;
+        const bool xs = align16(3 * (size_t)n * sizeof(double)) + fixed_bytes <= kSmemBudget;
+        smem[B_X] = smem[B_LB] = smem[B_UB] = xs;
     } else if (vec_all + obj_bytes + fixed_bytes <= kSmemBudget) {
         for (int b = 0; b < B_COUNT; ++b) smem[b] = need[b];
         L.obj_smem = 1;
@@ -128,19 +133,35 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
         L.sm_fixed = p; p += align16((size_t)n);
     }
     L.sm_hung = p; p += 2 * L.hung_bytes;
-    L.sm_mx = p; p += mx_bytes;
+    L.sm_mx = p; if (mixed && !L.mx_global) p += mx_bytes;
+    L.sm_cost = p; p += cost_bytes;
     L.sm_code = p; p += code_bytes;
     L.sm_ihw = p; p += mixed ? 2 * L.ihw_bytes : 0;
     L.sm_total = p;
-    L.mixed_node_bytes = 0;
+    L.mixed_node_bytes = L.mx_global ? (mx_bytes + 255) / 256 * 256 : 0;
+    if (L.tc) L.mixed_node_bytes += kTcImageBytes;
+    L.sparse_cap = 0;
+    L.sparse_bytes = 0;
+    if (o.kind == GBX_OBJ_GRAPH_MATCHING && o.order >= 16) {
+        // zero-skipping products pay off below a quarter density
+        const int m = o.order;
+        L.sparse_cap = m * m / 4;
+        L.sparse_bytes = 16 + 4 * sparse_list_bytes(m, L.sparse_cap);
+    }
     *out = L;
     return GBX_OK;
 }
 
+size_t mixed_region_offset(const Layout& L, int n_nodes) {
+    return (L.node_stride * sizeof(double) * (size_t)n_nodes + 255) / 256 * 256;
+}
+
+size_t sparse_region_offset(const Layout& L, int n_nodes) {
+    return (mixed_region_offset(L, n_nodes) + L.mixed_node_bytes * (size_t)n_nodes + 255) / 256 * 256;
+}
+
 size_t workspace_bytes(const Layout& L, int n_nodes) {
-    size_t b = L.node_stride * sizeof(double) * (size_t)n_nodes;
-    b += L.mixed_node_bytes * (size_t)n_nodes;
-    return b + 256;
+    return sparse_region_offset(L, n_nodes) + L.sparse_bytes + 256;
 }
 
 int launch_relax(const Params& p, void* stream, std::string* err) {

@@ -118,6 +118,8 @@ struct Ctx {
     const double* A;
     const double* B;
     double* R;
+    SparseAB sp;          // nonzero lists of A and B (valid when use_sp)
+    bool use_sp;
     // lmo
     int lk;
     double rhs;
@@ -136,8 +138,33 @@ struct Ctx {
 };
 
 // ------------------------------------------------------------------ objective
+static __device__ bool all_finite(const Ctx& c, const double* v) {
+    bool f = true;
+    for (int e = c.tid; e < c.n; e += kThreads) f = f && isfinite(v[e]);
+    return __syncthreads_and(f) != 0;
+}
+
+// R = A X - X B. With the nonzero lists the terms of zero coefficients are
+// skipped, in the same order as the dense loop (bit-identical for finite X).
 static __device__ void residual(const Ctx& c, const double* X, double* R) {
     const int m = c.m;
+    if (c.use_sp && all_finite(c, X)) {
+        const SparseAB& S = c.sp;
+        for (int e = c.tid; e < c.n; e += kThreads) {
+            const int i = e / m, j = e - (e / m) * m;
+            int ia = S.ptr[0][i], ib = S.ptr[1][j];
+            const int ea = S.ptr[0][i + 1], eb = S.ptr[1][j + 1];
+            double r = 0.0;
+            while (ia < ea || ib < eb) {
+                const int ka = ia < ea ? S.idx[0][ia] : m;
+                const int kb = ib < eb ? S.idx[1][ib] : m;
+                if (ka <= kb) { r = fma(S.val[0][ia], X[ka * m + j], r); ++ia; }
+                else { r = fma(-X[i * m + kb], S.val[1][ib], r); ++ib; }
+            }
+            R[e] = r;
+        }
+        return;
+    }
     for (int e = c.tid; e < c.n; e += kThreads) {
         const int i = e / m, j = e - (e / m) * m;
         double r = 0.0;
@@ -157,12 +184,25 @@ static __device__ void obj_grad(const Ctx& c, const double* x, double* g) {
         __syncthreads();
         const int m = c.m;
         const double two_s = 2.0 * c.s;
-        for (int e = c.tid; e < n; e += kThreads) {
-            const int p = e / m, q = e - (e / m) * m;
-            double acc = 0.0;
-            for (int r = 0; r < m; ++r) acc = fma(c.A[r * m + p], c.R[r * m + q], acc);
-            for (int k = 0; k < m; ++k) acc = fma(-c.R[p * m + k], c.B[q * m + k], acc);
-            g[e] = two_s * acc;
+        if (c.use_sp && all_finite(c, c.R)) {
+            const SparseAB& S = c.sp;
+            for (int e = c.tid; e < n; e += kThreads) {
+                const int p = e / m, q = e - (e / m) * m;
+                double acc = 0.0;
+                for (int t = S.ptr[2][p]; t < S.ptr[2][p + 1]; ++t)
+                    acc = fma(S.val[2][t], c.R[S.idx[2][t] * m + q], acc);
+                for (int t = S.ptr[3][q]; t < S.ptr[3][q + 1]; ++t)
+                    acc = fma(-c.R[p * m + S.idx[3][t]], S.val[3][t], acc);
+                g[e] = two_s * acc;
+            }
+        } else {
+            for (int e = c.tid; e < n; e += kThreads) {
+                const int p = e / m, q = e - (e / m) * m;
+                double acc = 0.0;
+                for (int r = 0; r < m; ++r) acc = fma(c.A[r * m + p], c.R[r * m + q], acc);
+                for (int k = 0; k < m; ++k) acc = fma(-c.R[p * m + k], c.B[q * m + k], acc);
+                g[e] = two_s * acc;
+            }
         }
     } else {
         for (int j = c.tid; j < n; j += kThreads) {
@@ -238,6 +278,7 @@ static __device__ double perm_value(const Ctx& c, const int* pi, int* pinv) {
 
 }  // namespace gbx
 #include "mixed.cuh"
+#include "tc_grad.cuh"
 namespace gbx {
 
 // ------------------------------------------------------------------ Hungarian
@@ -345,6 +386,72 @@ static __device__ bool hungarian_warp(const HW& w, int m, const double* cost, do
     }
     __syncwarp();
     return true;
+}
+
+// Perfect matching by greedy lowest-column choice, for the feasibility test of
+// a Birkhoff node. Executed by ONE warp; `out` must be zeroed and visible.
+// Returns 0 when the bounds are contradictory (the Hungarian's pre-pass fails
+// on exactly these), 1 when every row found a free allowed column (a perfect
+// matching honouring the forced edges, left in out and w.pi), and 2 when the
+// greedy choice got stuck -- only then is the full Hungarian needed to decide.
+static __device__ int greedy_matching_warp(const HW& w, int m, const double* lb, const double* ub,
+                                           double* out) {
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < m; i += 32) { w.fcol[i] = -1; w.frow[i] = -1; }
+    __syncwarp();
+    bool ok = true;
+    const int nn = m * m;
+    for (int e = lane; e < nn; e += 32) {
+        const double le = lb[e], ue = ub[e];
+        if (le > ue + 1e-9) ok = false;
+        if (le > 0.5) {
+            const int r = e / m, col = e - r * m;
+            if (ue < 0.5) ok = false;
+            if (atomicCAS(&w.fcol[r], -1, col) != -1) ok = false;
+            if (atomicCAS(&w.frow[col], -1, r) != -1) ok = false;
+        }
+    }
+    ok = __all_sync(kFull, ok);
+    __syncwarp();
+    if (!ok) return 0;
+    int k = 0, kc = 0;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int base = 0; base < m; base += 32) {
+        const int i = base + lane;
+        const bool fr = i < m && w.fcol[i] < 0;
+        const bool fc = i < m && w.frow[i] < 0;
+        const unsigned mr = __ballot_sync(kFull, fr), mc = __ballot_sync(kFull, fc);
+        if (fr) w.rows[k + __popc(mr & lt)] = i;
+        if (fc) w.cols[kc + __popc(mc & lt)] = i;
+        k += __popc(mr);
+        kc += __popc(mc);
+    }
+    if (k != kc) return 0;
+    for (int j = lane; j < k; j += 32) w.used[j] = 0;   // free column position taken
+    __syncwarp();
+    int first = 0;  // lowest position that may still be free
+    for (int t = 0; t < k; ++t) {
+        const int r = w.rows[t];
+        int pick = -1;
+        for (int base = first & ~31; base < k && pick < 0; base += 32) {
+            const int pos = base + lane;
+            const bool cand = pos < k && !w.used[pos] && ub[r * m + w.cols[pos]] >= 0.5;
+            const unsigned b = __ballot_sync(kFull, cand);
+            if (b) pick = base + __ffs(b) - 1;
+        }
+        if (pick < 0) return 2;
+        if (lane == 0) {
+            w.used[pick] = 1;
+            w.pi[r] = w.cols[pick];
+            out[r * m + w.cols[pick]] = 1.0;
+        }
+        __syncwarp();
+        while (first < k && w.used[first]) ++first;
+    }
+    for (int i = lane; i < m; i += 32)
+        if (w.fcol[i] >= 0) { out[i * m + w.fcol[i]] = 1.0; w.pi[i] = w.fcol[i]; }
+    __syncwarp();
+    return 1;
 }
 
 // ------------------------------------------------------------------ simplex
@@ -549,10 +656,17 @@ static __device__ bool node_feasible(const Ctx& c, const double* lb, const doubl
         if (n != c.lorder * c.lorder) return false;
         for (int j = c.tid; j < n; j += kThreads) scratch[j] = 0.0;
         __syncthreads();
+        // a perfect matching of the allowed edges exists (the reference runs the
+        // Hungarian on zero costs); the greedy matching settles almost every node
         if (threadIdx.x < 32) {
             const HW w = hw_at(c.hung[0], c.lorder);
-            const bool ok = hungarian_warp(w, c.lorder, nullptr, 1.0, lb, ub, nullptr, scratch);
-            if (threadIdx.x == 0) c.flag[1] = ok;
+            int r = greedy_matching_warp(w, c.lorder, lb, ub, scratch);
+            if (r == 2) {
+                for (int j = threadIdx.x; j < n; j += 32) scratch[j] = 0.0;
+                __syncwarp();
+                r = hungarian_warp(w, c.lorder, nullptr, 1.0, lb, ub, nullptr, scratch) ? 1 : 0;
+            }
+            if (threadIdx.x == 0) c.flag[1] = r;
         }
         __syncthreads();
         return c.flag[1] != 0;
@@ -644,32 +758,66 @@ static __device__ double perm_score(const Ctx& c, const uint8_t* code, const int
 // Mixed-precision DICG / FW iterations (see mixed.cuh). Works on the FP64
 // iterate X in place and returns the cumulative iteration count; the caller
 // then computes the FP64 certificate at the returned iterate.
+template <bool TC>
 static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, int node, double* X,
                           const double* LB, const double* UB, double* best, double& best_val,
                           double eps, int it0, bool dicg, int ls) {
     const Layout& L = P.L;
     const int n = c.n, m = c.m, tid = c.tid;
-    float* xf = reinterpret_cast<float*>(dsm + L.sm_mx);
+    unsigned char* mx = L.mx_global ? P.mixed + (size_t)node * L.mixed_node_bytes : dsm + L.sm_mx;
+    float* xf = reinterpret_cast<float*>(mx);
     float* gf = xf + n;
     float* Rf = gf + n;
     float* Af = Rf + n;
     float* Bf = Af + n;
     float* Btf = Bf + n;
-    int* costf = reinterpret_cast<int*>(Btf + n);   // forward oracle costs
-    int* costa = costf + n;                          // in-face oracle costs (negated, face only)
-    int8_t* Ai = reinterpret_cast<int8_t*>(costa + n);   // A, B as small integers when they are
-    int8_t* Bi = Ai + align16((size_t)n);                 // (exact integer scores and curvature)
+    int8_t* Ai = reinterpret_cast<int8_t*>(mx + align16(6 * (size_t)n * sizeof(float)));  // A, B as small
+    int8_t* Bi = Ai + align16((size_t)n);      // integers when they are (exact integer scores, curvature)
+    int* costf = reinterpret_cast<int*>(dsm + L.sm_cost);   // forward oracle costs
+    int* costa = costf + n;                                  // in-face oracle costs (negated, face only)
     uint8_t* code = dsm + L.sm_code;
     uint8_t* face = code + n;
     const IHW w0 = ihw_at(dsm + L.sm_ihw, m);
     const IHW w1 = ihw_at(dsm + L.sm_ihw + L.ihw_bytes, m);
     const double tol = c.tol;
+    // tensor-core gradient: operand images in the cost matrices' shared memory,
+    // the node's A / -B images after its FP32 arrays in the workspace
+    constexpr bool tcg = TC;
+    __shared__ uint64_t tc_bars[2];
+    __shared__ uint32_t tc_slot;
+    tc::Grad tg;
+    if constexpr (tcg) {
+        unsigned char* un = dsm + L.sm_cost;
+        tg.opA = un;
+        tg.opB = un + tc::kImgBytes;
+        tg.op0 = un + 2 * tc::kImgBytes;
+        tg.op1 = un + 3 * tc::kImgBytes;
+        tg.bar_tma = &tc_bars[0];
+        tg.bar_mma = &tc_bars[1];
+        tg.tmem_slot = &tc_slot;
+        unsigned char* img = mx + (mixed_array_bytes(n) + 255) / 256 * 256;
+        tg.img = img;
+        tg.ph_tma = tg.ph_mma = 0;
+        tc::build_images(img, c.A, c.B, m);
+        tc::fence_async_all();
+        if (tid < 32) tc::tmem_alloc(&tc_slot);
+        if (tid == 0) {
+            tc::bar_init(&tc_bars[0], 1);
+            tc::bar_init(&tc_bars[1], 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        tc::fence_before();
+        __syncthreads();
+        tc::fence_after();
+    }
     bool int_ok = true;
     for (int e = tid; e < n; e += kThreads) {
         const int i = e / m, j = e - (e / m) * m;
-        Af[e] = (float)c.A[e];
-        Bf[e] = (float)c.B[e];
-        Btf[e] = (float)c.B[j * m + i];
+        if (!tcg) {
+            Af[e] = (float)c.A[e];
+            Bf[e] = (float)c.B[e];
+            Btf[e] = (float)c.B[j * m + i];
+        }
         const double ae = c.A[e], be = c.B[e];
         if (!(ae == rint(ae) && fabs(ae) <= 127.0 && be == rint(be) && fabs(be) <= 127.0)) int_ok = false;
         Ai[e] = (int8_t)(fabs(ae) <= 127.0 ? (int)ae : 0);
@@ -689,6 +837,7 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
     if (tid == 0) { w0.scal[0] = 0; w0.scal[1] = 0; w0.scal[2] = 0; }
     if (tid == 32) { w1.scal[0] = 0; w1.scal[1] = 0; w1.scal[2] = 0; }
     if (tid == 0) c.flag[4] = 0;  // set when a face-forced bit of x changes
+    if (tid == 0) c.flag[5] = 0;  // set when a tensor-core wait timed out
     // small-integer A and B (graph adjacency): permutation residuals are
     // integers, so scores and curvatures are exact integer sums (the FP64 sums
     // of the same integers are exact too, hence bit-identical)
@@ -727,7 +876,16 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
     int iters = it0;
     for (int iter = 0; iter < P.b.max_iters; ++iter) {
         iters = it0 + iter + 1;
-        grad_f32(m, two_s, Af, Bf, Btf, xf, Rf, gf);
+        if constexpr (tcg) {
+            if (!tc::gradient(tg, m, xf, two_s, gf, dicg ? nullptr : Rf)) {
+                iters = it0 + iter;  // the iteration did not happen
+                if (tid == 0) c.flag[5] = 1;
+                __syncthreads();
+                break;
+            }
+        } else {
+            grad_f32(m, two_s, Af, Bf, Btf, xf, Rf, gf);
+        }
         const float gmx = bmax_abs(gf, n, c.red);
         int shift = 0;
         if (gmx > 0.f) {
@@ -858,6 +1016,15 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
         }
         __syncthreads();
     }
+    if constexpr (tcg) {
+        // a gradient that timed out may still have MMAs in flight: wait (bounded)
+        // for them before the accumulator columns are released
+        if (c.flag[5] && tid == 0) tc::bar_wait(tg.bar_mma, tg.ph_mma);
+        tc::fence_before();
+        __syncthreads();
+        tc::fence_after();
+        if (tid < 32) tc::tmem_dealloc(tc_slot);
+    }
     return iters;
 }
 
@@ -872,8 +1039,10 @@ __device__ inline double* vecp(double* sbase, double* gbase, const Layout& L, in
     return (L.in_smem[b] ? sbase : gbase) + L.off[b];
 }
 
-template <int OK, int LK, bool MIX>
-__global__ void __launch_bounds__(kThreads, MIX ? 2 : 1) relax_kernel(const __grid_constant__ Params P) {
+// MIX: 0 FP64 iterations, 1 mixed precision with the FP32 SIMT gradient (two
+// nodes per SM), 2 mixed precision with the tensor-core gradient
+template <int OK, int LK, int MIX>
+__global__ void __launch_bounds__(kThreads, MIX == 1 ? 2 : 1) relax_kernel(const __grid_constant__ Params P) {
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ Scalars sh;
     const int node = blockIdx.x;
@@ -910,6 +1079,11 @@ __global__ void __launch_bounds__(kThreads, MIX ? 2 : 1) relax_kernel(const __gr
     c.ls = P.obj.linear_scale;
     c.k0 = P.obj.constant;
     c.R = vecp(sb, gb, L, B_R);
+    c.use_sp = false;
+    if (OK == GBX_OBJ_GRAPH_MATCHING && P.sparse) {
+        c.sp = sparse_at(P.sparse, P.obj.order, L.sparse_cap);
+        c.use_sp = c.sp.ok[0] && c.sp.ok[1] && c.sp.ok[2] && c.sp.ok[3];
+    }
     c.lk = LK;
     c.rhs = P.lmo.right_side;
     c.is_int = P.lmo.is_int;
@@ -978,9 +1152,14 @@ __global__ void __launch_bounds__(kThreads, MIX ? 2 : 1) relax_kernel(const __gr
     const bool graph_perm = OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF;
 
     if (it0 == 0 && !supplied) {
-        for (int j = tid; j < n; j += kThreads) G[j] = -1.0 - static_cast<double>(j) / (n + 1.0);
-        __syncthreads();
-        lmo_forward<LK>(c, G, LB, UB, V);
+        // the reference starts at the vertex of the direction -1 - j/(n+1); the
+        // mixed-precision iterations start at the feasibility test's matching
+        // (any vertex is a valid start, and this one costs no oracle call)
+        if constexpr (MIX == 0) {
+            for (int j = tid; j < n; j += kThreads) G[j] = -1.0 - static_cast<double>(j) / (n + 1.0);
+            __syncthreads();
+            lmo_forward<LK>(c, G, LB, UB, V);
+        }
         for (int j = tid; j < n; j += kThreads) X[j] = V[j];
         __syncthreads();
     }
@@ -1048,9 +1227,9 @@ __global__ void __launch_bounds__(kThreads, MIX ? 2 : 1) relax_kernel(const __gr
     };
 
     int iters = it0;
-    constexpr bool kMixedLoop = MIX && OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF;
+    constexpr bool kMixedLoop = MIX != 0 && OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF;
     if constexpr (kMixedLoop)
-        iters = mixed_loop(c, P, dsm, node, X, LB, UB, best, best_val, eps, it0, dicg, ls);
+        iters = mixed_loop<MIX == 2>(c, P, dsm, node, X, LB, UB, best, best_val, eps, it0, dicg, ls);
     for (int iter = 0; !kMixedLoop && iter < P.b.max_iters; ++iter) {
         iters = it0 + iter + 1;
         obj_grad(c, X, G);
@@ -1120,20 +1299,36 @@ __global__ void __launch_bounds__(kThreads, MIX ? 2 : 1) relax_kernel(const __gr
         __syncthreads();
     }
 
-    // certificate at the returned iterate
+    // certificate at the returned iterate (the graph-matching value comes from
+    // the residual the gradient leaves behind: the same sums as obj_value)
     obj_grad(c, X, G);
+    double fval = 0.0;
+    if constexpr (OK == GBX_OBJ_GRAPH_MATCHING) fval = value_from_residual(c);
     const bool fok = lmo_forward<LK>(c, G, LB, UB, V);
     score(V, (graph_perm && fok) ? hw0.pi : nullptr, hw0.pinv);
     double loc = 0.0;
     for (int j = tid; j < n; j += kThreads) loc = fma(G[j], X[j] - V[j], loc);
     const double fgap = bsum(loc, c.red);
-    const double fval = obj_value(c, X);
+    if constexpr (OK != GBX_OBJ_GRAPH_MATCHING) fval = obj_value(c, X);
     int st = (fgap >= 0.0 && fgap < eps) ? 1 : 0;
     if (c.flags) {
-        for (int j = tid; j < n; j += kThreads) CAND[j] = c.flags[j] ? round(X[j]) : X[j];
+        bool zero_one = true;
+        for (int j = tid; j < n; j += kThreads) {
+            const double r = c.flags[j] ? round(X[j]) : X[j];
+            CAND[j] = r;
+            if (r != 0.0 && r != 1.0) zero_one = false;
+        }
         __syncthreads();
         if (rounded_feasible<LK>(c, CAND)) {
-            const double cv = integer_value(c, CAND, LB, UB, nullptr, nullptr);
+            // a 0/1 point with unit row and column sums is a permutation: its
+            // value in O(m^2) is bit-identical to the generic one
+            const bool perm = graph_perm && c.tol < 0.5 && __syncthreads_and(zero_one);
+            if (perm) {
+                for (int j = tid; j < n; j += kThreads)
+                    if (CAND[j] == 1.0) hw1.pi[j / c.m] = j - (j / c.m) * c.m;
+                __syncthreads();
+            }
+            const double cv = integer_value(c, CAND, LB, UB, perm ? hw1.pi : nullptr, hw1.pinv);
             if (cv < best_val) {
                 for (int j = tid; j < n; j += kThreads) best[j] = CAND[j];
                 if (tid == 0) P.b.best_vertex_val[node] = cv;
@@ -1166,6 +1361,7 @@ __global__ void __launch_bounds__(kThreads, 1) lmo_probe_kernel(
     const int n = lmo.n, tid = threadIdx.x;
     const size_t off = (size_t)cs * n;
     Ctx c;
+    c.use_sp = false;
     c.n = n;
     c.tid = tid;
     c.red = sh.red;
@@ -1220,6 +1416,7 @@ __global__ void __launch_bounds__(kThreads, 1) feasible_kernel(
     if (cs >= cases) return;
     const int n = lmo.n;
     Ctx c;
+    c.use_sp = false;
     c.n = n;
     c.tid = threadIdx.x;
     c.red = sh.red;
@@ -1241,9 +1438,9 @@ __global__ void __launch_bounds__(kThreads, 1) feasible_kernel(
 // ------------------------------------------------------------------ launchers
 template <int OK, int LK>
 int launch_one(const Params& p, cudaStream_t st, std::string* err) {
-    auto k = relax_kernel<OK, LK, false>;
+    auto k = relax_kernel<OK, LK, 0>;
     if constexpr (OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF)
-        if (p.L.mixed) k = relax_kernel<OK, LK, true>;
+        if (p.L.mixed) k = p.L.tc ? relax_kernel<OK, LK, 2> : relax_kernel<OK, LK, 1>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::max<size_t>(p.L.sm_total, 1));
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }

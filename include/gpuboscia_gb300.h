@@ -181,6 +181,17 @@ int gbx_lmo_batch(const gbx_lmo* lmo, int cases, int mode,
                   const double* lb, const double* ub, double* out,
                   double* out_step, void* stream);
 
+/* Batched objective gradients g = grad f(x), one point per row of x and g
+ * (device [cases*n]); replaces Objective::grad
+ * (dense_quadratic_objectives.cuh:43-60; the graph-matching gradient of
+ * examples/main.cu:131-181). precision GBX_PRECISION_FP64: the relaxation's own
+ * FP64 gradient, bit-identical to it; GBX_PRECISION_MIXED (graph matching
+ * only): the gradient of the mixed-precision relaxation, BF16 tensor-core
+ * products with FP32 accumulation for orders 65..128, FP32 below, widened to
+ * double. */
+int gbx_objective_gradient_batch(const gbx_objective* obj, int precision, int cases,
+                                 const double* x, double* g, void* stream);
+
 /* Node feasibility before any objective work (drs_node_feasible,
  * device_resident_solver.cuh:206-217): out[case] = 1 feasible, 0 infeasible. */
 int gbx_node_feasible_batch(const gbx_lmo* lmo, int cases, const double* lb,

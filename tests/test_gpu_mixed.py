@@ -56,6 +56,24 @@ def test_mixed_certificate_is_exact_fp64(cuda_lib, kind, ls, order):
         assert O.value(inst.objective, g["best_vertex"][i]) == g["best_vertex_val"][i]
 
 
+def test_mixed_order120_workspace_arrays(cuda_lib):
+    """Order 120: the FP32 arrays and the FP64 vectors live in the workspace."""
+    inst = instances.birkhoff_regular_perturbed(order=120)
+    order, n, N = 120, 120 * 120, 6
+    lb, ub = instances.birkhoff_node_batch(order, N, seed=5)
+    flags = np.ones(n, np.uint8)
+    g = gpu_relax(inst.objective, inst.lmo, mixed(), lb.copy(), lb, ub, 1e-6, np.zeros(N, np.int32),
+                  np.zeros(N, np.uint8), 12, flags)
+    assert (g["iterations"] > 0).all()
+    o = O.relax(inst.objective, inst.lmo, O.algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT), g["x"], lb, ub, 1e-6,
+                g["iterations"], np.full(N, A.NODE_INITIAL_POINT_SUPPLIED, np.uint8), 0, flags)
+    assert np.array_equal(g["gap"], o["gap"])
+    assert np.array_equal(g["value"], o["value"])
+    assert np.array_equal(g["status"], o["status"])
+    X = g["x"].reshape(N, order, order)
+    assert np.allclose(X.sum(1), 1.0, atol=1e-9) and np.allclose(X.sum(2), 1.0, atol=1e-9)
+
+
 def test_mixed_and_fp64_bounds_overlap(cuda_lib):
     inst = instances.birkhoff_gnp()
     N = 12
@@ -98,6 +116,42 @@ def test_mixed_solve_reaches_fp64_optimum(cuda_lib, inst):
     X = fast.x.reshape(order, order)
     assert (X.sum(0) == 1).all() and (X.sum(1) == 1).all()
     assert fast.dual_bound <= fast.objective + 1e-9
+
+
+@pytest.mark.parametrize("order", [72, 96])
+def test_mixed_tensor_core_bounds_overlap(cuda_lib, order):
+    """Orders 65..128 take the tensor-core gradient; certified intervals still overlap FP64's."""
+    inst = instances.birkhoff_gnp(order=order, seed=order)
+    N = 6
+    lb, ub = instances.birkhoff_node_batch(order, N, seed=order + 1)
+    flags = np.ones(order * order, np.uint8)
+    z = np.zeros(N, np.int32), np.zeros(N, np.uint8)
+    m = gpu_relax(inst.objective, inst.lmo, mixed(), lb.copy(), lb, ub, 1e-7, *z, 150, flags)
+    f = gpu_relax(inst.objective, inst.lmo, O.algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT), lb.copy(), lb, ub, 1e-7,
+                  *z, 150, flags)
+    o = O.relax(inst.objective, inst.lmo, O.algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT), m["x"], lb, ub, 1e-7,
+                m["iterations"], np.full(N, A.NODE_INITIAL_POINT_SUPPLIED, np.uint8), 0, flags)
+    assert np.array_equal(m["gap"], o["gap"]) and np.array_equal(m["value"], o["value"])
+    for i in range(N):
+        lo_m, hi_m = m["value"][i] - m["gap"][i], m["value"][i]
+        lo_f, hi_f = f["value"][i] - f["gap"][i], f["value"][i]
+        assert max(lo_m, lo_f) <= min(hi_m, hi_f) + 1e-9 * max(1.0, abs(hi_f)), (i, lo_m, hi_m, lo_f, hi_f)
+
+
+def test_mixed_tensor_core_solve_isomorphic72(cuda_lib):
+    inst = instances.birkhoff_gnp(order=72, seed=11)
+    s = inst.settings
+    s.gpu_batch_size = 32
+    s.num_streams = 1
+    s.gpu_max_iters = 300
+    s.line_search = A.LS_QUADRATIC_EXACT
+    s.time_limit_seconds = 120
+    s.precision = A.PRECISION_MIXED
+    r = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert not r.reached_time_limit
+    assert r.objective == 0.0
+    X = r.x.reshape(72, 72)
+    assert (X.sum(0) == 1).all() and (X.sum(1) == 1).all()
 
 
 def test_mixed_rejects_other_kinds(cuda_lib):

@@ -81,8 +81,9 @@ def test_static_scratch_rejects_oversized_batches():
     obj = inst.objective.to_c("cuda", keep)
     lmo = inst.lmo.to_c(64 * 64, "cuda", keep)
     alg = A.Algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT, 4, 1e-10, 1e-14, A.PRECISION_FP64)
-    per_node = lib.gbx_relax_workspace_bytes(C.byref(obj), C.byref(lmo), C.byref(alg), 1)
-    too_many = A.STATIC_SCRATCH_BYTES // max(per_node - 256, 1) + 2
+    one = lib.gbx_relax_workspace_bytes(C.byref(obj), C.byref(lmo), C.byref(alg), 1)
+    per_node = lib.gbx_relax_workspace_bytes(C.byref(obj), C.byref(lmo), C.byref(alg), 2) - one
+    too_many = A.STATIC_SCRATCH_BYTES // max(per_node, 1) + 2
     b = A.NodeBatch()
     b.n_nodes = int(too_many)
     rc = lib.gbx_relax_batch_static(C.byref(obj), C.byref(lmo), C.byref(alg), C.byref(b), None)
