@@ -5,7 +5,7 @@ the C ABI of include/gpuboscia_gb300.h). This package builds it in-tree and
 mirrors the reference's public API in Python; C++ users include
 include/gpuboscia/gpuboscia.h instead.
 """
-from . import _abi
+from . import _abi, scorer
 from .api import (BirkhoffLMO, BoxLMO, DenseQuadraticObjective, EqualitySimplexLMO, GraphMatchingObjective,
                   ILSObjective, Problem, RelaxWorkspace, Result, Settings, UnitSimplexLMO, lmo_batch,
                   node_feasible_batch, objective_gradient_batch, relax_batch, solve)
@@ -13,5 +13,5 @@ from .api import (BirkhoffLMO, BoxLMO, DenseQuadraticObjective, EqualitySimplexL
 __all__ = [
     "BirkhoffLMO", "BoxLMO", "DenseQuadraticObjective", "EqualitySimplexLMO", "GraphMatchingObjective",
     "ILSObjective", "Problem", "RelaxWorkspace", "Result", "Settings", "UnitSimplexLMO", "lmo_batch",
-    "node_feasible_batch", "objective_gradient_batch", "relax_batch", "solve", "_abi",
+    "node_feasible_batch", "objective_gradient_batch", "relax_batch", "solve", "scorer", "_abi",
 ]

@@ -97,6 +97,16 @@ class Problem(C.Structure):
     ]
 
 
+SCORER_FEATURES = 16
+
+
+class Scorer(C.Structure):
+    _fields_ = [
+        ("n_features", C.c_int), ("hidden", C.c_int),
+        ("params", C.c_void_p), ("params_bf16", C.c_void_p),
+    ]
+
+
 class Settings(C.Structure):
     _fields_ = [
         ("gpu_batch_size", C.c_int), ("num_streams", C.c_int), ("gpu_max_iters", C.c_int),
@@ -106,6 +116,7 @@ class Settings(C.Structure):
         ("time_limit_seconds", C.c_double), ("natural_lower_bound", C.c_double),
         ("root_initial_point", C.c_void_p),
         ("branch_k", C.c_int), ("use_cuda_graph", C.c_int),
+        ("scorer", C.c_void_p),
     ]
 
 
@@ -137,6 +148,7 @@ def default_settings() -> Settings:
     s.root_initial_point = None
     s.branch_k = 3
     s.use_cuda_graph = 1
+    s.scorer = None
     return s
 
 
@@ -149,6 +161,8 @@ EXPORTED_SYMBOLS = (
     "gbx_relax_batch", "gbx_relax_batch_static", "gbx_lmo_batch", "gbx_objective_gradient_batch",
     "gbx_node_feasible_batch",
     "gbx_default_settings", "gbx_solve",
+    "gbx_scorer_param_count", "gbx_branch_features", "gbx_scorer_forward", "gbx_scorer_workspace_bytes",
+    "gbx_scorer_gradient", "gbx_scorer_adam",
 )
 
 _lib = None
@@ -184,6 +198,21 @@ def load(path: os.PathLike | str | None = None) -> C.CDLL:
     lib.gbx_node_feasible_batch.restype = C.c_int
     lib.gbx_node_feasible_batch.argtypes = [P(LMO), C.c_int, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.gbx_scorer_param_count.restype = C.c_int
+    lib.gbx_scorer_param_count.argtypes = [C.c_int, C.c_int]
+    lib.gbx_branch_features.restype = None
+    lib.gbx_branch_features.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                        C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p]
+    lib.gbx_scorer_forward.restype = C.c_int
+    lib.gbx_scorer_forward.argtypes = [P(Scorer), C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    lib.gbx_scorer_workspace_bytes.restype = C.c_size_t
+    lib.gbx_scorer_workspace_bytes.argtypes = [P(Scorer), C.c_int]
+    lib.gbx_scorer_gradient.restype = C.c_int
+    lib.gbx_scorer_gradient.argtypes = [P(Scorer), C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.gbx_scorer_adam.restype = C.c_int
+    lib.gbx_scorer_adam.argtypes = [P(Scorer), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float,
+                                    C.c_void_p]
     lib.gbx_default_settings.restype = None
     lib.gbx_default_settings.argtypes = [P(Settings)]
     lib.gbx_solve.restype = C.c_int

@@ -183,6 +183,7 @@ class Settings:
     root_initial_point: Optional[np.ndarray] = None
     branch_k: int = 3
     use_cuda_graph: int = 1
+    scorer: Optional[object] = None   # gpuboscia_gb300.scorer.Scorer: learned branching
 
     def algorithm_c(self) -> A.Algorithm:
         return A.Algorithm(self.algorithm, self.line_search, self.secant_iters, self.secant_tol,
@@ -197,6 +198,10 @@ class Settings:
         s.algorithm = self.algorithm_c()
         s.root_initial_point = keep.ptr(_f64(self.root_initial_point) if self.root_initial_point is not None
                                         else None, "host")
+        if self.scorer is not None:
+            sc = self.scorer.to_c()
+            keep.items.append(sc)
+            s.scorer = C.addressof(sc)
         return s
 
 

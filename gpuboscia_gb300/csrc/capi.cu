@@ -141,6 +141,39 @@ int gbx_objective_gradient_batch(const gbx_objective* obj, int precision, int ca
     return GBX_OK;
 }
 
+int gbx_scorer_param_count(int n_features, int hidden) {
+    if (n_features <= 0 || hidden <= 0) return 0;
+    return gbx::scorer_param_count(n_features, hidden);
+}
+
+int gbx_scorer_forward(const gbx_scorer* s, int rows, const float* features, float* scores, int bf16,
+                       void* stream) {
+    if (rows < 0 || (rows > 0 && (!features || !scores))) return fail(GBX_ERR_INVALID, "scorer forward arguments");
+    std::string err;
+    const int rc = gbx::scorer_forward(s, rows, features, scores, bf16, static_cast<cudaStream_t>(stream), &err);
+    if (rc) return fail(rc, err);
+    return GBX_OK;
+}
+
+size_t gbx_scorer_workspace_bytes(const gbx_scorer* s, int rows) { return gbx::scorer_workspace_bytes(s, rows); }
+
+int gbx_scorer_gradient(const gbx_scorer* s, int rows, const float* features, int groups,
+                        const int* group_ptr, const float* target, float* grad, float* loss,
+                        void* workspace, size_t workspace_bytes, void* stream) {
+    std::string err;
+    const int rc = gbx::scorer_gradient(s, rows, features, groups, group_ptr, target, grad, loss, workspace,
+                                        workspace_bytes, static_cast<cudaStream_t>(stream), &err);
+    if (rc) return fail(rc, err);
+    return GBX_OK;
+}
+
+int gbx_scorer_adam(gbx_scorer* s, const float* grad, float* m, float* v, int step, float lr, void* stream) {
+    std::string err;
+    const int rc = gbx::scorer_adam(s, grad, m, v, step, lr, static_cast<cudaStream_t>(stream), &err);
+    if (rc) return fail(rc, err);
+    return GBX_OK;
+}
+
 int gbx_node_feasible_batch(const gbx_lmo* lmo, int cases, const double* lb,
                             const double* ub, const uint8_t* integer_flags, uint8_t* out,
                             void* stream) {

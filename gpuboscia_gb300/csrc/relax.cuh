@@ -146,6 +146,14 @@ int launch_lmo_batch(const gbx_lmo& l, int cases, int mode, const double* dir,
                      double* out_step, void* stream, std::string* err);
 int launch_gradient_batch(const gbx_objective& o, int precision, int cases, const double* x, double* g,
                           cudaStream_t st, std::string* err);
+int scorer_param_count(int F, int H);
+int scorer_forward(const gbx_scorer* s, int rows, const float* X, float* z, int bf16, cudaStream_t st,
+                   std::string* err);
+size_t scorer_workspace_bytes(const gbx_scorer* s, int rows);
+int scorer_gradient(const gbx_scorer* s, int rows, const float* X, int groups, const int* gp, const float* target,
+                    float* grad, float* loss, void* ws, size_t ws_bytes, cudaStream_t st, std::string* err);
+int scorer_adam(gbx_scorer* s, const float* g, float* m, float* v, int step, float lr, cudaStream_t st,
+                std::string* err);
 int launch_node_feasible(const gbx_lmo& l, int cases, const double* lb, const double* ub,
                          const uint8_t* flags, uint8_t* out, void* stream, std::string* err);
 

@@ -6,8 +6,11 @@
 #include <cmath>
 #include <exception>
 #include <limits>
+#include <memory>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "../../include/gpuboscia/device_resident_solver.h"
@@ -37,6 +40,100 @@ bool relaxation_feasible(const gbx_lmo& l, const std::vector<double>& x, double 
     }
     return true;
 }
+// Learned branching (branch_pow2 over the k candidates the scorer ranks
+// highest). Every completed batch is scored in one device call; a node without
+// scores (or with a non-finite score) falls back to the k most fractional
+// variables, and the FW dual bound alone still decides pruning.
+class LearnedBrancher {
+public:
+    LearnedBrancher(const gbx_scorer* s, int k, double tol, int order, const Problem& prob)
+        : s_(s), k_(k), tol_(tol), order_(order), prob_(prob) {
+        GBX_CUDA_CHECK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    }
+    ~LearnedBrancher() {
+        if (d_feat_) cudaFree(d_feat_);
+        if (d_score_) cudaFree(d_score_);
+        if (st_) cudaStreamDestroy(st_);
+    }
+
+    void prepare(int N, const Node* nodes, const double* x, const double* gap, const double* value,
+                 const uint8_t* status) {
+        const int n = prob_.n_vars;
+        const int F = GBX_SCORER_FEATURES;
+        std::vector<int> who, vars, start;
+        for (int i = 0; i < N; ++i) {
+            if (status[i] >= GBX_NODE_INTEGRAL_UNCONVERGED || cache_.count(nodes[i].id)) continue;
+            const double* xi = x + (size_t)i * n;
+            const int b = (int)vars.size();
+            for (int v : prob_.int_vars) {
+                const double fr = xi[v] - std::floor(xi[v]);
+                if (std::isfinite(xi[v]) && std::min(fr, 1.0 - fr) > tol_) vars.push_back(v);
+            }
+            if ((int)vars.size() == b) continue;
+            who.push_back(i);
+            start.push_back(b);
+        }
+        if (vars.empty()) return;
+        start.push_back((int)vars.size());
+        const size_t R = vars.size();
+        h_feat_.resize(R * F);
+        for (size_t w = 0; w < who.size(); ++w) {
+            const int i = who[w];
+            const Node& nd = nodes[i];
+            gbx_branch_features(n, x + (size_t)i * n, nd.lb.data(), nd.ub.data(), order_, nd.depth, gap[i],
+                                value[i], start[w + 1] - start[w], vars.data() + start[w],
+                                h_feat_.data() + (size_t)start[w] * F);
+        }
+        if (R > cap_) {
+            if (d_feat_) cudaFree(d_feat_);
+            if (d_score_) cudaFree(d_score_);
+            cap_ = R * 2;
+            GBX_CUDA_CHECK(cudaMalloc(&d_feat_, cap_ * F * sizeof(float)));
+            GBX_CUDA_CHECK(cudaMalloc(&d_score_, cap_ * sizeof(float)));
+        }
+        GBX_CUDA_CHECK(cudaMemcpyAsync(d_feat_, h_feat_.data(), R * F * sizeof(float), cudaMemcpyHostToDevice, st_));
+        if (gbx_scorer_forward(s_, (int)R, d_feat_, d_score_, s_->params_bf16 ? 1 : 0, st_) != GBX_OK)
+            throw std::runtime_error(std::string("scorer: ") + gbx_last_error());
+        h_score_.resize(R);
+        GBX_CUDA_CHECK(cudaMemcpyAsync(h_score_.data(), d_score_, R * sizeof(float), cudaMemcpyDeviceToHost, st_));
+        GBX_CUDA_CHECK(cudaStreamSynchronize(st_));
+        for (size_t w = 0; w < who.size(); ++w) {
+            auto& c = cache_[nodes[who[w]].id];
+            for (int r = start[w]; r < start[w + 1]; ++r) c.push_back({vars[r], h_score_[r]});
+        }
+    }
+
+    std::vector<Node> branch(const Node& p, int& id, const std::vector<double>& x, const std::vector<int>& iv) {
+        std::vector<int> pick;
+        auto it = cache_.find(p.id);
+        if (it != cache_.end()) {
+            auto c = std::move(it->second);
+            cache_.erase(it);
+            bool finite = true;
+            for (auto& e : c) finite = finite && std::isfinite(e.second);
+            if (finite && !c.empty()) {
+                std::stable_sort(c.begin(), c.end(), [](const std::pair<int, float>& a,
+                                                        const std::pair<int, float>& b) { return a.second > b.second; });
+                for (int t = 0; t < (int)c.size() && t < k_; ++t) pick.push_back(c[t].first);
+            }
+        }
+        if (pick.empty()) pick = top_k_infeasible(x, iv, k_, tol_);
+        return branch_on_vars(p, id, x, pick);
+    }
+
+private:
+    const gbx_scorer* s_;
+    int k_;
+    double tol_;
+    int order_;
+    const Problem& prob_;
+    cudaStream_t st_ = nullptr;
+    float* d_feat_ = nullptr;
+    float* d_score_ = nullptr;
+    size_t cap_ = 0;
+    std::vector<float> h_feat_, h_score_;
+    std::unordered_map<int, std::vector<std::pair<int, float>>> cache_;
+};
 }  // namespace
 
 extern "C" {
@@ -118,8 +215,26 @@ int gbx_solve(const gbx_problem* problem, const gbx_objective* obj, const gbx_lm
         const int k = s->branch_k;
         BranchStrategy branch = [tol, k](const Node& p, int& id, const std::vector<double>& x,
                                          const std::vector<int>& iv) { return branch_pow2(p, id, x, iv, k, tol); };
+        std::unique_ptr<LearnedBrancher> learned;
+        if (s->scorer) {
+            if (!s->scorer->params || s->scorer->n_features != GBX_SCORER_FEATURES)
+                throw std::invalid_argument("scorer: invalid descriptor");
+            learned.reset(new LearnedBrancher(s->scorer, k, tol, lmo->kind == GBX_LMO_BIRKHOFF ? lmo->order : 0,
+                                              prob));
+            LearnedBrancher* lb = learned.get();
+            branch = [lb](const Node& p, int& id, const std::vector<double>& x, const std::vector<int>& iv) {
+                return lb->branch(p, id, x, iv);
+            };
+        }
         gpuboscia::detail::BnBEngine engine(prob, *obj, spec, s->algorithm, branch, cfg, s->time_limit_seconds);
         engine.set_child_id_stride(std::max(8, 1 << k));
+        if (learned) {
+            LearnedBrancher* lb = learned.get();
+            engine.set_branch_batch_hook([lb](int N, const Node* nd, const double* x, const double* gap,
+                                              const double* val, const uint8_t* st) {
+                lb->prepare(N, nd, x, gap, val, st);
+            });
+        }
         Node root(0, -1, 0, prob.lb, prob.ub);
         root.dual_bound = s->natural_lower_bound;
         root.relaxation_x = root_x;

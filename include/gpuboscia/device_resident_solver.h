@@ -171,6 +171,12 @@ public:
     void set_scheduling_callback(std::function<void(const DRSSchedulingEvent&)> cb) { scheduling_cb_ = std::move(cb); }
     // Children get ids next_id .. next_id + stride - 1 per expansion (8 in the reference).
     void set_child_id_stride(int s) { id_stride_ = std::max(1, s); }
+    // Called with every completed batch before any of its nodes is branched
+    // (nodes, x [N*n], gap, value, status), so that a branching rule can score
+    // all candidates of the batch in one device call.
+    using BranchBatchHook = std::function<void(int, const Node*, const double*, const double*, const double*,
+                                               const uint8_t*)>;
+    void set_branch_batch_hook(BranchBatchHook h) { branch_hook_ = std::move(h); }
 
     void solve() {
         solve_started_ = Clock::now();
@@ -428,7 +434,14 @@ private:
         return r;
     }
 
+    void call_branch_hook(const Completed& b) {
+        if (branch_hook_ && !b.nodes.empty())
+            branch_hook_((int)b.nodes.size(), b.nodes.data(), b.x.data(), b.gap.data(), b.value.data(),
+                         b.status.data());
+    }
+
     void branch_starved_batches(std::vector<Completed>& batches) {
+        for (const auto& b : batches) call_branch_hook(b);
         struct Cand { size_t batch; int node; double bound; };
         std::vector<Cand> cands;
         for (size_t b = 0; b < batches.size(); ++b)
@@ -465,6 +478,7 @@ private:
     void process_completed_batch(Completed& batch) {
         const int n = prob_.n_vars;
         const int N = (int)batch.nodes.size();
+        call_branch_hook(batch);
         emit_scheduling_event(DRSSchedulingEventType::PostprocessStarted, batch.slot_id, batch.generation, N);
         for (int i = 0; i < N; ++i) {
             if (finish_if_time_limit_reached()) return;
@@ -596,6 +610,7 @@ private:
     Clock::time_point solve_started_{};
     std::function<void(int, int, double, double, bool)> progress_cb_;
     std::function<void(const DRSSchedulingEvent&)> scheduling_cb_;
+    BranchBatchHook branch_hook_;
 
     std::vector<Slot> slots_;
     size_t ws_bytes_ = 0;

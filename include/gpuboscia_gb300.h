@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GBX_ABI_VERSION 1
+#define GBX_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------ */
 enum {
@@ -209,6 +209,52 @@ typedef struct gbx_problem {
     int n_int;
 } gbx_problem;
 
+/* ---------------------------------------------------------------------------
+ * Learned branching scorer (no counterpart in the reference; it only changes
+ * which fractional variables branch_pow2 splits on -- most-fractional stays the
+ * fallback and the FW dual bound alone decides pruning and optimality).
+ * An MLP n_features -> hidden -> hidden -> 1 with ReLU, parameters in one FP32
+ * device array in the order W1[hidden][n_features], b1[hidden],
+ * W2[hidden][hidden], b2[hidden], w3[hidden], b3; params_bf16 (optional) is the
+ * BF16 copy used for inference.
+ * ------------------------------------------------------------------------- */
+#define GBX_SCORER_FEATURES 16
+typedef struct gbx_scorer {
+    int n_features;             /* GBX_SCORER_FEATURES */
+    int hidden;                 /* 8..128, a multiple of 8 */
+    float* params;              /* device [gbx_scorer_param_count] */
+    unsigned short* params_bf16;/* device [gbx_scorer_param_count] or NULL */
+} gbx_scorer;
+
+int gbx_scorer_param_count(int n_features, int hidden);
+
+/* Features of the branching candidates vars[0..n_cand) of one node (host
+ * arrays [n]): distance to integrality, value and fractional part, the node's
+ * depth and relative gap, and for Birkhoff orders > 0 the candidate's row and
+ * column structure. Writes n_cand rows of GBX_SCORER_FEATURES floats to out. */
+void gbx_branch_features(int n, const double* x, const double* lb, const double* ub, int order,
+                         int depth, double gap, double value, int n_cand, const int* vars, float* out);
+
+/* scores[r] = MLP(features[r]) for rows of device features [rows][n_features];
+ * bf16 != 0 uses params_bf16 (FP32 accumulation). */
+int gbx_scorer_forward(const gbx_scorer* s, int rows, const float* features, float* scores, int bf16,
+                       void* stream);
+
+/* Listwise loss over groups (one group = the candidates of one node, rows
+ * group_ptr[g] .. group_ptr[g+1]-1): L = sum_g -sum_r target[r] log softmax_g(z)[r]
+ * with target summing to 1 per group. Writes dL/dparams (device
+ * [param_count], deterministic order) and, if loss != NULL, L (device, 1 float).
+ * workspace: device, gbx_scorer_workspace_bytes(rows) bytes. */
+size_t gbx_scorer_workspace_bytes(const gbx_scorer* s, int rows);
+int gbx_scorer_gradient(const gbx_scorer* s, int rows, const float* features, int groups,
+                        const int* group_ptr, const float* target, float* grad, float* loss,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* Adam step on params (m, v: device moment arrays, step >= 1), then refresh
+ * params_bf16 when it is set. */
+int gbx_scorer_adam(gbx_scorer* s, const float* grad, float* m, float* v, int step, float lr,
+                    void* stream);
+
 typedef struct gbx_settings {
     /* DeviceResidentConfig (device_resident_solver.cuh:1004-1025) */
     int gpu_batch_size;       /* 1024 */
@@ -227,6 +273,7 @@ typedef struct gbx_settings {
     const double* root_initial_point; /* host [n_vars] or NULL */
     int branch_k;             /* branch_pow2 k (3) */
     int use_cuda_graph;       /* capture the relax launch (1) */
+    const gbx_scorer* scorer; /* learned branching (NULL: most fractional) */
 } gbx_settings;
 
 typedef struct gbx_result {
