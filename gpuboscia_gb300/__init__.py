@@ -6,12 +6,12 @@ mirrors the reference's public API in Python; C++ users include
 include/gpuboscia/gpuboscia.h instead.
 """
 from . import _abi, scorer
-from .api import (BirkhoffLMO, BoxLMO, DenseQuadraticObjective, EqualitySimplexLMO, GraphMatchingObjective,
+from .api import (BirkhoffLMO, BoxLMO, CardinalityLMO, DenseQuadraticObjective, EqualitySimplexLMO, GraphMatchingObjective,
                   ILSObjective, Problem, RelaxWorkspace, Result, Settings, UnitSimplexLMO, lmo_batch,
                   node_feasible_batch, objective_gradient_batch, relax_batch, solve)
 
 __all__ = [
-    "BirkhoffLMO", "BoxLMO", "DenseQuadraticObjective", "EqualitySimplexLMO", "GraphMatchingObjective",
+    "BirkhoffLMO", "BoxLMO", "CardinalityLMO", "DenseQuadraticObjective", "EqualitySimplexLMO", "GraphMatchingObjective",
     "ILSObjective", "Problem", "RelaxWorkspace", "Result", "Settings", "UnitSimplexLMO", "lmo_batch",
     "node_feasible_batch", "objective_gradient_batch", "relax_batch", "solve", "scorer", "_abi",
 ]

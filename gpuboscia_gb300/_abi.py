@@ -38,6 +38,7 @@ LMO_BOX = 1
 LMO_SIMPLEX = 2
 LMO_EQUALITY_SIMPLEX = 3
 LMO_BIRKHOFF = 4
+LMO_CARDINALITY = 5
 
 ALG_FRANK_WOLFE = 0
 ALG_DICG = 1

@@ -151,6 +151,19 @@ class BirkhoffLMO:
         return A.LMO(A.LMO_BIRKHOFF, n, 1.0, None, self.order)
 
 
+@dataclasses.dataclass
+class CardinalityLMO:
+    """x = (w, z): sum w = 1, 0 <= w <= z, sum z <= cardinality, z in [0, 1]
+    (GBX_LMO_CARDINALITY; Frank-Wolfe only)."""
+    assets: int
+    cardinality: int
+    supports_dicg = False
+
+    def to_c(self, n: int, where: str, keep: _Keep) -> A.LMO:
+        assert n == 2 * self.assets
+        return A.LMO(A.LMO_CARDINALITY, n, float(self.cardinality), None, 0)
+
+
 # ---------------------------------------------------------------- problem / settings
 @dataclasses.dataclass
 class Problem:

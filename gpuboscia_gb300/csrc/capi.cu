@@ -28,8 +28,14 @@ int validate(const gbx_objective* o, const gbx_lmo* l, const gbx_algorithm* a) {
     }
     if (l->kind == GBX_LMO_BIRKHOFF && l->order * l->order != l->n)
         return fail(GBX_ERR_INVALID, "Birkhoff LMO needs order*order == n");
-    if (l->kind < GBX_LMO_BOX || l->kind > GBX_LMO_BIRKHOFF)
+    if (l->kind < GBX_LMO_BOX || l->kind > GBX_LMO_CARDINALITY)
         return fail(GBX_ERR_UNSUPPORTED, "unknown LMO kind");
+    if (l->kind == GBX_LMO_CARDINALITY) {
+        if (l->n % 2 || !(l->right_side >= 1.0))
+            return fail(GBX_ERR_INVALID, "cardinality LMO needs n = 2 * assets and a cardinality >= 1");
+        if (a->kind == GBX_ALG_DICG)
+            return fail(GBX_ERR_UNSUPPORTED, "the cardinality LMO supports Frank-Wolfe only");
+    }
     if (a->kind != GBX_ALG_FRANK_WOLFE && a->kind != GBX_ALG_DICG)
         return fail(GBX_ERR_INVALID, "unknown algorithm");
     if (a->line_search < GBX_LS_OPEN_LOOP || a->line_search > GBX_LS_QUADRATIC_EXACT)

@@ -526,6 +526,106 @@ static __device__ void simplex_greedy(const Ctx& c, const double* g, double sign
     __syncthreads();
 }
 
+// ------------------------------------------------------------------ cardinality LMO
+// 256-lane min padded with +inf (bmin pads with 1.0 for step sizes).
+static __device__ double bmin_inf(double v, double* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = warp_min(v);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double r = lane < kWarps ? red[lane] : CUDART_INF;
+        r = warp_min(r);
+        if (lane == 0) red[34] = r;
+    }
+    __syncthreads();
+    return red[34];
+}
+
+// min <g, (w, z)> over {sum w = 1, 0 <= w <= z, sum z <= K, 0 <= z <= 1} with z
+// forced (lb > 1/2) or forbidden (ub < 1/2). A vertex puts w = e_a on one asset
+// a (z_a = 1) and switches on z for the forced assets and for the most negative
+// remaining z-costs while slots are left. With L = free assets of negative
+// z-cost sorted by (cost, index) and P its prefix sums (left to right), base =
+// sum of forced z-costs (index order), r0 = K - #forced, r1 = r0 - 1:
+//   a forced:              (g_w[a] + base) + P[r0]
+//   a among first r1 of L: (g_w[a] + base) + P[r1 + 1]
+//   otherwise:             (g_w[a] + base) + (g_z[a] + P[r1])
+// (P clamped at |L|); the minimum, lowest asset on ties, is the vertex.
+static __device__ bool card_forward(const Ctx& c, const double* g, const double* lb, const double* ub,
+                                    double* v) {
+    __shared__ int s_arg;
+    const int n = c.n, N = n / 2, tid = c.tid;
+    const int K = (int)floor(c.rhs + 1e-9);
+    int* pos = reinterpret_cast<int*>(c.keys);
+    int* ord = c.idx;
+    double* P = c.prefix;
+    for (int j = tid; j < n; j += kThreads) v[j] = 0.0;
+    for (int j = tid; j < N; j += kThreads) {
+        const double gz = g[N + j];
+        int rank = -1;
+        if (!(lb[N + j] > 0.5) && !(ub[N + j] < 0.5) && gz < 0.0) {
+            rank = 0;
+            for (int k = 0; k < N; ++k) {
+                const double gk = g[N + k];
+                if (lb[N + k] > 0.5 || ub[N + k] < 0.5 || !(gk < 0.0)) continue;
+                if (gk < gz || (gk == gz && k < j)) ++rank;
+            }
+            ord[rank] = j;
+        }
+        pos[j] = rank;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int nf = 0, nl = 0;
+        double base = 0.0;
+        for (int j = 0; j < N; ++j) {
+            if (lb[N + j] > 0.5) { ++nf; base = base + g[N + j]; }
+            if (pos[j] >= 0) ++nl;
+        }
+        P[0] = 0.0;
+        for (int t = 0; t < nl; ++t) P[t + 1] = P[t] + g[N + ord[t]];
+        c.flag[6] = nf;
+        c.flag[7] = nl;
+        c.red[38] = base;
+        s_arg = 0x7fffffff;
+    }
+    __syncthreads();
+    const int nf = c.flag[6], nl = c.flag[7];
+    const double base = c.red[38];
+    if (nf > K) return false;
+    const int r0 = K - nf, r1 = K - nf - 1;
+    auto value = [&](int a) -> double {
+        if (ub[N + a] < 0.5) return CUDART_INF;
+        const double head = g[a] + base;
+        double val;
+        if (lb[N + a] > 0.5) val = head + P[min(r0, nl)];
+        else if (r1 < 0) return CUDART_INF;
+        else if (pos[a] >= 0 && pos[a] < r1) val = head + P[min(r1 + 1, nl)];
+        else val = head + (g[N + a] + P[min(r1, nl)]);
+        return val < CUDART_INF ? val : CUDART_INF;
+    };
+    double best = CUDART_INF;
+    for (int a = tid; a < N; a += kThreads) best = fmin(best, value(a));
+    const double vmin = bmin_inf(best, c.red);
+    if (!(vmin < CUDART_INF)) return false;
+    for (int a = tid; a < N; a += kThreads)
+        if (value(a) == vmin) { atomicMin(&s_arg, a); break; }
+    __syncthreads();
+    const int a = s_arg;
+    const bool af = lb[N + a] > 0.5;
+    int limit;
+    if (af) limit = min(r0, nl);
+    else if (pos[a] >= 0 && pos[a] < r1) limit = min(r1 + 1, nl);
+    else limit = min(r1, nl);
+    for (int j = tid; j < N; j += kThreads)
+        if (lb[N + j] > 0.5 || (pos[j] >= 0 && pos[j] < limit) || j == a) v[N + j] = 1.0;
+    if (tid == 0) v[a] = 1.0;
+    __syncthreads();
+    return true;
+}
+
 // ------------------------------------------------------------------ LMOs
 template <int LK>
 static __device__ bool lmo_forward(const Ctx& c, const double* g, const double* lb,
@@ -546,6 +646,9 @@ static __device__ bool lmo_forward(const Ctx& c, const double* g, const double* 
         }
         __syncthreads();
         return c.flag[0] != 0;
+    } else if constexpr (LK == GBX_LMO_CARDINALITY) {
+        card_forward(c, g, lb, ub, v);
+        return false;
     } else {
         double loc = 0.0;
         for (int j = c.tid; j < n; j += kThreads) {
@@ -579,6 +682,11 @@ static __device__ bool lmo_inface(const Ctx& c, const double* g, double sign, co
         // caller zeroes `a` and runs this on one warp
         const HW w = hw_at(c.hung[hw_slot], c.lorder);
         return hungarian_warp(w, c.lorder, g, sign, lb, ub, x, a);
+    } else if constexpr (LK == GBX_LMO_CARDINALITY) {
+        // Frank-Wolfe only: the host rejects DICG and in-face probes for this set
+        for (int j = c.tid; j < n; j += kThreads) a[j] = x[j];
+        __syncthreads();
+        return false;
     } else {
         double lm = 0.0, lx = 0.0;
         for (int j = c.tid; j < n; j += kThreads) {
@@ -617,7 +725,7 @@ static __device__ double lmo_max_step(const Ctx& c, const double* d, const doubl
         if constexpr (LK == GBX_LMO_BOX) {
             if (dj < 0.0) res = fmin(res, (ub[j] - x[j]) / -dj);
             else if (dj > 0.0) res = fmin(res, (x[j] - lb[j]) / dj);
-        } else if constexpr (LK == GBX_LMO_BIRKHOFF) {
+        } else if constexpr (LK == GBX_LMO_BIRKHOFF || LK == GBX_LMO_CARDINALITY) {
             if (dj > 0.0) res = fmin(res, (x[j] - lb[j]) / dj);
             else if (dj < 0.0) res = fmin(res, (ub[j] - x[j]) / -dj);
         } else {
@@ -670,6 +778,18 @@ static __device__ bool node_feasible(const Ctx& c, const double* lb, const doubl
         }
         __syncthreads();
         return c.flag[1] != 0;
+    } else if constexpr (LK == GBX_LMO_CARDINALITY) {
+        const int N = n / 2;
+        const int K = (int)floor(c.rhs + 1e-9);
+        int forced = 0;
+        bool open = false;
+        for (int j = c.tid; j < N; j += kThreads) {
+            forced += lb[N + j] > 0.5 ? 1 : 0;
+            open = open || !(ub[N + j] < 0.5);
+        }
+        const int nf = (int)bsum((double)forced, c.red);
+        const bool any_open = __syncthreads_or(open) != 0;
+        return nf <= K && (nf >= 1 || (K >= 1 && any_open));
     } else {
         bool v2 = true, cont = false;
         double mand = 0.0, cap = 0.0;
@@ -715,6 +835,20 @@ static __device__ bool rounded_feasible(const Ctx& c, const double* x) {
             if (fabs(row - 1.0) > tol || fabs(col - 1.0) > tol) valid = false;
         }
         return __syncthreads_and(valid);
+    } else if constexpr (LK == GBX_LMO_CARDINALITY) {
+        const int N = n / 2;
+        bool valid = true;
+        double sw = 0.0, sz = 0.0;
+        for (int j = c.tid; j < N; j += kThreads) {
+            const double w = x[j], z = x[N + j];
+            valid = valid && w >= -tol && z >= -tol && z <= 1.0 + tol && w <= z + tol;
+            sw += w;
+            sz += z;
+        }
+        const bool nn = __syncthreads_and(valid);
+        const double SW = bsum(sw, c.red);
+        const double SZ = bsum(sz, c.red);
+        return nn && fabs(SW - 1.0) <= tol && SZ <= floor(c.rhs + 1e-9) + tol;
     } else {
         bool valid = true;
         double s = 0.0;

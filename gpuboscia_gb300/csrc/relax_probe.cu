@@ -12,5 +12,6 @@ GBX_PROBE(GBX_LMO_BOX)
 GBX_PROBE(GBX_LMO_SIMPLEX)
 GBX_PROBE(GBX_LMO_EQUALITY_SIMPLEX)
 GBX_PROBE(GBX_LMO_BIRKHOFF)
+GBX_PROBE(GBX_LMO_CARDINALITY)
 #undef GBX_PROBE
 }  // namespace gbx

@@ -30,6 +30,17 @@ bool relaxation_feasible(const gbx_lmo& l, const std::vector<double>& x, double 
         for (double v : x) { if (v < 0.0) return false; mass += v; }
         return mass <= l.right_side + tol;
     }
+    if (l.kind == GBX_LMO_CARDINALITY) {
+        const int N = (int)x.size() / 2;
+        double sw = 0.0, sz = 0.0;
+        for (int j = 0; j < N; ++j) {
+            const double w = x[j], z = x[N + j];
+            if (w < -tol || z < -tol || z > 1 + tol || w > z + tol) return false;
+            sw += w;
+            sz += z;
+        }
+        return std::abs(sw - 1.0) <= tol && sz <= std::floor(l.right_side + 1e-9) + tol;
+    }
     const int m = l.order;
     if ((int)x.size() != m * m) return false;
     for (double v : x) if (v < -tol || v > 1 + tol) return false;

@@ -111,6 +111,49 @@ def box_qp(n: int = 64, seed: int = SEEDS[1]) -> Instance:
     return Instance("box_bqp_n64", prob, api.DenseQuadraticObjective(Q, c), api.BoxLMO(), s)
 
 
+def portfolio(assets: int = 100, months: int = 600, cardinality: int = 10, seed: int = SEEDS[3]) -> Instance:
+    """Config 3: cardinality-constrained mean-variance portfolio.
+
+    Returns of a 3-factor model: factor returns N(0.5 %, 4 %) per month, betas
+    N(1, 0.3), idiosyncratic volatility U[4 %, 10 %]. Sigma and mu are the sample
+    covariance and mean. min w'Sigma w - 0.5 mu'w over x = (w, z) with
+    sum w = 1, 0 <= w <= z, sum z <= cardinality, z binary: f = x'Qx/2 + c'x with
+    Q = diag(2 Sigma, 0) and c = (-0.5 mu, 0)."""
+    rng = _rng(seed)
+    f = normal(rng, (months, 3), 0.005, 0.04)
+    beta = normal(rng, (assets, 3), 1.0, 0.3)
+    vol = 0.04 + 0.06 * rng.random(assets)
+    eps = normal(rng, (months, assets)) * vol[None, :]
+    R = f @ beta.T + eps
+    mu = R.mean(0)
+    D = R - mu
+    Sigma = D.T @ D / (months - 1)
+    n = 2 * assets
+    Q = np.zeros((n, n))
+    Q[:assets, :assets] = 2.0 * Sigma
+    c = np.zeros(n)
+    c[:assets] = -0.5 * mu
+    prob = api.Problem(n, np.zeros(n), np.ones(n), list(range(assets, n)))
+    s = api.Settings(algorithm=0, line_search=4, rel_gap_tol=1e-6, abs_gap_tol=1e-6, gpu_batch_size=64)
+    return Instance(f"portfolio_n{assets}_k{cardinality}", prob, api.DenseQuadraticObjective(Q, c),
+                    api.CardinalityLMO(assets, cardinality), s)
+
+
+def portfolio_node_batch(assets: int, cardinality: int, nodes: int, seed: int = 7):
+    """Open nodes with uneven fixings of z: some forced in (at most cardinality),
+    some forced out."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = 2 * assets
+    lb = np.zeros((nodes, n))
+    ub = np.ones((nodes, n))
+    for k in range(nodes):
+        ins = rng.choice(assets, int(rng.integers(0, cardinality + 1)), replace=False)
+        outs = rng.choice(np.setdiff1d(np.arange(assets), ins), int(rng.integers(0, assets // 3)), replace=False)
+        lb[k, assets + ins] = 1.0
+        ub[k, assets + outs] = 0.0
+    return lb, ub
+
+
 def graph_matching(order: int, A: np.ndarray, B: np.ndarray, name: str, known=None, solution=None) -> Instance:
     n = order * order
     prob = api.Problem(n, np.zeros(n), np.ones(n), list(range(n)))

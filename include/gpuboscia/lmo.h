@@ -93,3 +93,28 @@ struct BirkhoffLMO {
     }
     gpuboscia::LMOSpec spec(int) const { return {GBX_LMO_BIRKHOFF, 1.0, {}, Order}; }
 };
+
+// Cardinality-linked simplex over x = (w, z), n = 2*Assets:
+// sum w = 1, 0 <= w <= z, sum z <= cardinality, 0 <= z <= 1. Branching fixes z;
+// Frank-Wolfe only (no in-face oracle). No counterpart in the reference (its
+// LinkedCardinalityLMO, examples/sparse_sharpe.cu:266-546, lacks sum w = 1).
+template <int Assets>
+struct LinkedCardinalityLMO {
+    static_assert(Assets > 0, "asset count must be positive");
+    static constexpr bool supports_dicg = false;
+    static constexpr int variable_count = 2 * Assets;
+    int cardinality = 1;
+    bool relaxation_feasible_cpu(const std::vector<double>& x, const std::vector<double>&,
+                                 const std::vector<double>&, double tol) const {
+        if (x.size() != static_cast<size_t>(variable_count)) return false;
+        double sw = 0, sz = 0;
+        for (int j = 0; j < Assets; ++j) {
+            const double w = x[j], z = x[Assets + j];
+            if (w < -tol || z < -tol || z > 1 + tol || w > z + tol) return false;
+            sw += w;
+            sz += z;
+        }
+        return std::abs(sw - 1) <= tol && sz <= cardinality + tol;
+    }
+    gpuboscia::LMOSpec spec(int) const { return {GBX_LMO_CARDINALITY, double(cardinality), {}, 0}; }
+};

@@ -83,7 +83,12 @@ enum {
     GBX_LMO_BOX = 1,                /* BoxLMO, lmo.cuh:212-321                        */
     GBX_LMO_SIMPLEX = 2,            /* UnitSimplexLMO<n,false>, lmo.cuh:335-907       */
     GBX_LMO_EQUALITY_SIMPLEX = 3,   /* EqualitySimplexLMO<n>, lmo.cuh:911-912         */
-    GBX_LMO_BIRKHOFF = 4            /* BirkhoffLMO<order>, lmo.cuh:918-1419           */
+    GBX_LMO_BIRKHOFF = 4,           /* BirkhoffLMO<order>, lmo.cuh:918-1419           */
+    GBX_LMO_CARDINALITY = 5         /* x = (w, z), n = 2N: sum w = 1, 0 <= w <= z,
+                                       sum z <= right_side, 0 <= z <= 1; node bounds on z
+                                       (lb > 1/2 forced, ub < 1/2 forbidden); Frank-Wolfe
+                                       only (no counterpart in the reference; the pattern
+                                       of examples/sparse_sharpe.cu:266-546 plus sum w = 1) */
 };
 
 typedef struct gbx_lmo {

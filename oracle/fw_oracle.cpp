@@ -345,8 +345,62 @@ struct LMO {
         return true;
     }
 
+    // ---- cardinality-linked simplex (config 3; no reference counterpart):
+    // x = (w, z), sum w = 1, 0 <= w <= z, sum z <= K. Vertex = w on one asset a
+    // plus z on the forced assets and on the most negative free z-costs while
+    // slots remain; values summed in the kernel's order (base over forced
+    // assets by index, prefix sums over the sorted free negatives).
+    bool card_forward(const double* g, const double* lb, const double* ub, double* v) const {
+        const int N = n / 2;
+        const int K = (int)std::floor(l->right_side + 1e-9);
+        for (int j = 0; j < n; ++j) v[j] = 0.0;
+        std::vector<int> ord, pos(N, -1);
+        int nf = 0;
+        double base = 0.0;
+        for (int j = 0; j < N; ++j) {
+            if (lb[N + j] > 0.5) { ++nf; base = base + g[N + j]; }
+            else if (!(ub[N + j] < 0.5) && g[N + j] < 0.0) ord.push_back(j);
+        }
+        std::sort(ord.begin(), ord.end(), [&](int a, int b) {
+            return g[N + a] < g[N + b] || (g[N + a] == g[N + b] && a < b);
+        });
+        const int nl = (int)ord.size();
+        for (int t = 0; t < nl; ++t) pos[ord[t]] = t;
+        std::vector<double> P(nl + 1, 0.0);
+        for (int t = 0; t < nl; ++t) P[t + 1] = P[t] + g[N + ord[t]];
+        if (nf > K) return false;
+        const int r0 = K - nf, r1 = K - nf - 1;
+        auto value = [&](int a) -> double {
+            if (ub[N + a] < 0.5) return kInf;
+            const double head = g[a] + base;
+            double val;
+            if (lb[N + a] > 0.5) val = head + P[std::min(r0, nl)];
+            else if (r1 < 0) return kInf;
+            else if (pos[a] >= 0 && pos[a] < r1) val = head + P[std::min(r1 + 1, nl)];
+            else val = head + (g[N + a] + P[std::min(r1, nl)]);
+            return val < kInf ? val : kInf;
+        };
+        double vmin = kInf;
+        int a = -1;
+        for (int i = 0; i < N; ++i) {
+            const double val = value(i);
+            if (val < vmin) { vmin = val; a = i; }
+        }
+        if (a < 0) return false;
+        int limit;
+        if (lb[N + a] > 0.5) limit = std::min(r0, nl);
+        else if (pos[a] >= 0 && pos[a] < r1) limit = std::min(r1 + 1, nl);
+        else limit = std::min(r1, nl);
+        for (int j = 0; j < N; ++j)
+            if (lb[N + j] > 0.5 || (pos[j] >= 0 && pos[j] < limit) || j == a) v[N + j] = 1.0;
+        v[a] = 1.0;
+        return true;
+    }
+
     void forward(const double* g, const double* lb, const double* ub, double* v) const {
-        if (l->kind == GBX_LMO_BOX) {
+        if (l->kind == GBX_LMO_CARDINALITY) {
+            card_forward(g, lb, ub, v);
+        } else if (l->kind == GBX_LMO_BOX) {
             for (int j = 0; j < n; ++j) v[j] = g[j] > 0.0 ? lb[j] : ub[j];
         } else if (simplex()) {
             Lanes L;
@@ -456,6 +510,17 @@ struct LMO {
 
     bool check_feasible(const double* lb, const double* ub, const uint8_t* flags) const {
         if (l->kind == GBX_LMO_BOX) return true;
+        if (l->kind == GBX_LMO_CARDINALITY) {
+            const int N = n / 2;
+            const int K = (int)std::floor(l->right_side + 1e-9);
+            int nf = 0;
+            bool open = false;
+            for (int j = 0; j < N; ++j) {
+                nf += lb[N + j] > 0.5 ? 1 : 0;
+                open = open || !(ub[N + j] < 0.5);
+            }
+            return nf <= K && (nf >= 1 || (K >= 1 && open));
+        }
         if (simplex()) {
             bool valid = true, cont = false;
             Lanes LM, LC;
@@ -487,6 +552,23 @@ struct LMO {
 
     bool rounded_feasible(const double* x, double tol) const {
         if (l->kind == GBX_LMO_BOX) return true;
+        if (l->kind == GBX_LMO_CARDINALITY) {
+            const int N = n / 2;
+            bool valid = true;
+            Lanes SW, SZ;
+            for (int t = 0; t < kLanes; ++t) {
+                double sw = 0.0, sz = 0.0;
+                for (int j = t; j < N; j += kLanes) {
+                    const double w = x[j], z = x[N + j];
+                    valid = valid && w >= -tol && z >= -tol && z <= 1.0 + tol && w <= z + tol;
+                    sw += w;
+                    sz += z;
+                }
+                SW.v[t] = sw; SZ.v[t] = sz;
+            }
+            const double sum_w = reduce_sum(SW), sum_z = reduce_sum(SZ);
+            return valid && std::fabs(sum_w - 1.0) <= tol && sum_z <= std::floor(l->right_side + 1e-9) + tol;
+        }
         if (simplex()) {
             bool valid = true;
             Lanes L;
@@ -748,7 +830,7 @@ int check_descs(const gbx_objective* o, const gbx_lmo* l, const gbx_algorithm* a
     if (o->kind != GBX_OBJ_GRAPH_MATCHING && o->kind != GBX_OBJ_DENSE_QUADRATIC) {
         g_error = "objective kind"; return GBX_ERR_UNSUPPORTED;
     }
-    if (l->kind < GBX_LMO_BOX || l->kind > GBX_LMO_BIRKHOFF) { g_error = "lmo kind"; return GBX_ERR_UNSUPPORTED; }
+    if (l->kind < GBX_LMO_BOX || l->kind > GBX_LMO_CARDINALITY) { g_error = "lmo kind"; return GBX_ERR_UNSUPPORTED; }
     if (a->line_search < 0 || a->line_search > 4) { g_error = "line search"; return GBX_ERR_INVALID; }
     return GBX_OK;
 }

@@ -122,7 +122,8 @@ def test_learned_branching_gain_on_held_out_pairs(cuda_lib):
         inst = random_pair(7, 200 + k)
         r0 = solve(inst, None)
         r1 = solve(inst, sc)
-        assert r0.reached_tolerance and r1.reached_tolerance
+        for r in (r0, r1):   # finished, and the FW bound certifies the optimum
+            assert not r.reached_time_limit and r.dual_bound >= r.objective - 1e-9
         assert r1.objective == r0.objective
         plain += r0.nodes_processed
         learned += r1.nodes_processed
