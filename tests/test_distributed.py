@@ -1,0 +1,143 @@
+"""Multi-rank branch and bound (gpuboscia_gb300.distributed) with world size 2
+over gloo on the CPU; the relaxation of each rank is the oracle, so only the
+host-side exchange is under test: the incumbent and bound all-reduces, work
+stealing, termination, and the failure of a peer."""
+import datetime
+import os
+import socket
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _instance(kind):
+    from gpuboscia_gb300 import instances
+    if kind == "box":
+        inst = instances.box_qp(n=14, seed=5)
+    else:
+        inst = instances.portfolio(assets=10, months=100, cardinality=3, seed=9)
+    s = inst.settings
+    s.gpu_batch_size = 4
+    s.gpu_max_iters = 3000
+    s.rel_gap_tol = 1e-6
+    s.branch_k = 1
+    return inst
+
+
+def _oracle_relax(inst, flags, fail_on_call=None):
+    sys.path.insert(0, HERE)
+    import _oracle as O
+    calls = [0]
+
+    def relax(lbs, ubs, xs, eps, its, sts):
+        calls[0] += 1
+        if fail_on_call is not None and calls[0] == fail_on_call:
+            raise RuntimeError("injected failure of this rank")
+        s = inst.settings
+        alg = O.algorithm(s.algorithm, s.line_search)
+        return O.relax(inst.objective, inst.lmo, alg, xs.copy(), lbs, ubs, eps, its.copy(), sts.copy(),
+                       s.gpu_max_iters, flags, s.integer_tol)
+    return relax
+
+
+def _worker(rank, world, port, kind, fail_rank, out):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=20))
+    from gpuboscia_gb300 import distributed
+    inst = _instance(kind)
+    flags = np.zeros(inst.problem.n_vars, np.uint8)
+    flags[list(inst.problem.int_vars)] = 1
+    relax = _oracle_relax(inst, flags, fail_on_call=1 if rank == fail_rank else None)
+    try:
+        r = distributed.solve(inst.problem, inst.settings, relax)
+        out.put((rank, "ok", r.objective, r.dual_bound, r.nodes_processed, r.nodes_total, r.stolen,
+                 None if r.x is None else r.x.tolist()))
+    except distributed.RankFailure as e:
+        out.put((rank, "peer-failure", str(e)[:200]))
+    except RuntimeError as e:
+        out.put((rank, "raised", str(e)[:200]))
+    finally:
+        try:
+            dist.destroy_process_group()
+        except Exception:
+            pass
+
+
+def _run(kind, fail_rank=None, world=2):
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    out = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, world, port, kind, fail_rank, out)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = {}
+    for _ in range(world):
+        item = out.get(timeout=240)
+        res[item[0]] = item
+    for p in procs:
+        p.join(timeout=60)
+    return res
+
+
+@pytest.mark.parametrize("kind", ["box", "portfolio"])
+def test_two_ranks_reach_the_single_process_optimum(kind):
+    sys.path.insert(0, HERE)
+    import _oracle as O
+    inst = _instance(kind)
+    s = inst.settings
+    s.num_streams = 1
+    ref = O.solve(inst.problem, inst.objective, inst.lmo, s)
+    res = _run(kind)
+    assert all(res[r][1] == "ok" for r in res), res
+    objs = {res[r][2] for r in res}
+    assert len(objs) == 1                                     # incumbent shared
+    obj = objs.pop()
+    assert abs(obj - ref.objective) <= 1e-9 * max(1.0, abs(ref.objective))
+    for r in res:
+        assert res[r][3] >= obj - 1e-6 * max(1.0, abs(obj))   # certified bound closes the gap
+        assert res[r][4] > 0                                  # both ranks relaxed nodes
+    assert res[1][6] > 0                                      # rank 1 started empty: it stole work
+    assert res[0][5] == res[1][5] == res[0][4] + res[1][4]
+
+
+def test_peer_failure_is_reported_not_awaited():
+    res = _run("box", fail_rank=1)
+    assert res[1][1] == "raised"
+    assert res[0][1] == "peer-failure"
+
+
+@pytest.mark.gpu
+def test_single_rank_on_the_gpu_matches_the_oracle(cuda_lib):
+    """The product relaxation (gbx_relax_batch) under the distributed driver,
+    one rank: the same optimum as the single-process oracle solver."""
+    import torch.distributed as dist
+    from gpuboscia_gb300 import distributed
+    sys.path.insert(0, HERE)
+    import _oracle as O
+    inst = _instance("portfolio")
+    flags = np.zeros(inst.problem.n_vars, np.uint8)
+    flags[list(inst.problem.int_vars)] = 1
+    store = dist.HashStore()
+    dist.init_process_group("gloo", store=store, rank=0, world_size=1)
+    try:
+        r = distributed.solve(inst.problem, inst.settings,
+                              distributed.gpu_relax_fn(inst.objective, inst.lmo, inst.settings, flags))
+    finally:
+        dist.destroy_process_group()
+    s = inst.settings
+    s.num_streams = 1
+    ref = O.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert abs(r.objective - ref.objective) <= 1e-9 * max(1.0, abs(ref.objective))
+    assert r.dual_bound >= r.objective - 1e-6 * max(1.0, abs(r.objective))
