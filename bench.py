@@ -34,6 +34,11 @@ WORKLOADS = {
 }
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of the relaxation kernel per launch,
+# from the committed ncu captures (profiles/); independent of the iteration count
+TRAFFIC = {("birkhoff_gnp36", "mixed"): 8247552, ("birkhoff_regular120", "mixed"): 139682816 + 191056640}
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -329,7 +334,8 @@ def run_gpu(args, rank, world):
     flops = grads * 8.0 * order ** 3
     achieved_tf = flops / (kernel_ms / 1000.0) / 1e12
     roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": bf16_peak, "unit": "TFLOP/s",
-                "frac": achieved_tf / bf16_peak, "traffic": None, "peak_kind": peak_kind,
+                "frac": achieved_tf / bf16_peak, "traffic": TRAFFIC.get((args.workload, args.precision)),
+                "peak_kind": peak_kind,
                 "kernel": "relax_kernel<GRAPH_MATCHING,BIRKHOFF>",
                 "work": f"{grads} gradients x 8*{order}^3 flop per launch"}
     cpu_v, cores, done, dt = cpu_sample(inst, lb, ub, eps, w["alg"], w["ls"], args.iters, budget_s=args.cpu_budget)
@@ -342,7 +348,7 @@ def run_gpu(args, rank, world):
             "cpu_baseline": {"value": cpu_v, "unit": "nodes/s", "cores": cores, "kind": "port",
                              "sample": f"{done} of {N} nodes of the same batch, {args.iters} iterations max, "
                                        f"{dt:.1f} s"},
-            "clocks": clk.summary(), "gpu_launches": args.steps,
+            "clocks": clk.summary(), "gpu_launches": 2 * args.steps,   # sparse_build_kernel + relax_kernel
             "node_iterations_per_step": node_iters,
             "plain_fp64": plain, "time_to_gap": ttg,
             "status_counts": {str(s): int((statuses == s).sum()) for s in np.unique(statuses)}}
