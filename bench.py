@@ -34,9 +34,11 @@ WORKLOADS = {
 }
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of the relaxation kernel per launch,
-# from the committed ncu captures (profiles/); independent of the iteration count
-TRAFFIC = {("birkhoff_gnp36", "mixed"): 8247552, ("birkhoff_regular120", "mixed"): 139682816 + 191056640}
+# dram__bytes_read.sum + dram__bytes_write.sum of the relaxation kernel per node,
+# from the committed ncu captures (profiles/: 256 nodes at order 36, 152 nodes at
+# order 120); independent of the iteration count, scaled by the nodes of a launch
+TRAFFIC_PER_NODE = {("birkhoff_gnp36", "mixed"): 8247552 / 256,
+                    ("birkhoff_regular120", "mixed"): (139682816 + 191056640) / 152}
 
 
 def load_peaks():
@@ -334,7 +336,8 @@ def run_gpu(args, rank, world):
     flops = grads * 8.0 * order ** 3
     achieved_tf = flops / (kernel_ms / 1000.0) / 1e12
     roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": bf16_peak, "unit": "TFLOP/s",
-                "frac": achieved_tf / bf16_peak, "traffic": TRAFFIC.get((args.workload, args.precision)),
+                "frac": achieved_tf / bf16_peak, "traffic": (TRAFFIC_PER_NODE[(args.workload, args.precision)] * N
+                            if (args.workload, args.precision) in TRAFFIC_PER_NODE else None),
                 "peak_kind": peak_kind,
                 "kernel": "relax_kernel<GRAPH_MATCHING,BIRKHOFF>",
                 "work": f"{grads} gradients x 8*{order}^3 flop per launch"}
