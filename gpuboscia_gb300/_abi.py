@@ -117,7 +117,7 @@ class Settings(C.Structure):
         ("time_limit_seconds", C.c_double), ("natural_lower_bound", C.c_double),
         ("root_initial_point", C.c_void_p),
         ("branch_k", C.c_int), ("use_cuda_graph", C.c_int),
-        ("scorer", C.c_void_p),
+        ("scorer", C.c_void_p), ("autotune", C.c_int),
     ]
 
 
@@ -150,6 +150,7 @@ def default_settings() -> Settings:
     s.branch_k = 3
     s.use_cuda_graph = 1
     s.scorer = None
+    s.autotune = 1
     return s
 
 
@@ -159,7 +160,9 @@ STATIC_SCRATCH_BYTES = 32 << 20
 # exported symbols of the CUDA library, as declared in include/gpuboscia_gb300.h
 EXPORTED_SYMBOLS = (
     "gbx_abi_version", "gbx_last_error", "gbx_relax_workspace_bytes",
-    "gbx_relax_batch", "gbx_relax_batch_static", "gbx_lmo_batch", "gbx_objective_gradient_batch",
+    "gbx_relax_batch", "gbx_relax_batch_static", "gbx_relax_autotune", "gbx_relax_set_launch_shape",
+    "gbx_lmo_batch",
+    "gbx_objective_gradient_batch",
     "gbx_node_feasible_batch",
     "gbx_default_settings", "gbx_solve",
     "gbx_scorer_param_count", "gbx_branch_features", "gbx_scorer_forward", "gbx_scorer_workspace_bytes",
@@ -190,6 +193,11 @@ def load(path: os.PathLike | str | None = None) -> C.CDLL:
                                     C.c_void_p, C.c_size_t, C.c_void_p]
     lib.gbx_relax_batch_static.restype = C.c_int
     lib.gbx_relax_batch_static.argtypes = [P(Objective), P(LMO), P(Algorithm), P(NodeBatch), C.c_void_p]
+    lib.gbx_relax_autotune.restype = C.c_int
+    lib.gbx_relax_autotune.argtypes = [P(Objective), P(LMO), P(Algorithm), P(NodeBatch), C.c_void_p, C.c_size_t,
+                                       C.c_void_p, C.c_int, C.c_void_p]
+    lib.gbx_relax_set_launch_shape.restype = C.c_int
+    lib.gbx_relax_set_launch_shape.argtypes = [P(Objective), P(LMO), P(Algorithm), C.c_int, C.c_int]
     lib.gbx_lmo_batch.restype = C.c_int
     lib.gbx_lmo_batch.argtypes = [P(LMO), C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]

@@ -1,6 +1,7 @@
 // capi.cu -- extern "C" entry points of libgpuboscia_gb300 (include/gpuboscia_gb300.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <string>
 
@@ -67,7 +68,7 @@ size_t gbx_relax_workspace_bytes(const gbx_objective* obj, const gbx_lmo* lmo,
         g_err = err;
         return 0;
     }
-    return gbx::workspace_bytes(L, n_nodes);
+    return std::max(gbx::workspace_bytes(L, n_nodes), gbx::workspace_bytes_any_variant(*obj, *lmo, *alg, n_nodes));
 }
 
 int gbx_relax_batch(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
@@ -91,9 +92,12 @@ int gbx_relax_batch(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algo
     rc = gbx::make_layout(*obj, *lmo, *alg, b->n_nodes, &p.L, &err);
     if (rc) return fail(rc, err);
     const size_t need = gbx::workspace_bytes(p.L, b->n_nodes);
-    if (need > 256 && (!workspace || workspace_bytes < need))
+    if ((need > 256 || p.L.persistent) && (!workspace || workspace_bytes < need))
         return fail(GBX_ERR_WORKSPACE, "workspace smaller than gbx_relax_workspace_bytes()");
     p.ws = static_cast<double*>(workspace);
+    p.queue = p.L.persistent && b->n_nodes > 0
+                  ? reinterpret_cast<int*>(static_cast<unsigned char*>(workspace) + gbx::queue_offset(p.L, b->n_nodes))
+                  : nullptr;
     p.mixed = p.L.mixed_node_bytes
                   ? static_cast<unsigned char*>(workspace) + gbx::mixed_region_offset(p.L, b->n_nodes)
                   : nullptr;
@@ -105,6 +109,108 @@ int gbx_relax_batch(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algo
     }
     rc = gbx::launch_relax(p, stream, &err);
     if (rc) return fail(rc, err);
+    return GBX_OK;
+}
+
+int gbx_relax_autotune(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
+                       const gbx_node_batch* b, void* workspace, size_t workspace_bytes, void* stream,
+                       int repeats, int* chosen) {
+    int rc = validate(obj, lmo, alg);
+    if (rc) return rc;
+    if (!b || b->n_nodes <= 0 || !b->x || !b->iterations || !b->status)
+        return fail(GBX_ERR_INVALID, "autotune needs a non-empty batch");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const std::vector<gbx::Variant> cands = gbx::candidate_variants(*obj, *lmo, *alg);
+    const int N = b->n_nodes, n = obj->n;
+    const size_t xb = (size_t)N * n * sizeof(double), ib = (size_t)N * sizeof(int), sb = (size_t)N;
+    unsigned char* save = nullptr;
+    cudaError_t e = cudaMallocAsync(&save, xb + ib + sb, st);
+    if (e != cudaSuccess) return fail(GBX_ERR_CUDA, cudaGetErrorString(e));
+    auto copy_in = [&](bool restore) {
+        const auto k = cudaMemcpyDeviceToDevice;
+        if (!restore) {
+            cudaMemcpyAsync(save, b->x, xb, k, st);
+            cudaMemcpyAsync(save + xb, b->iterations, ib, k, st);
+            cudaMemcpyAsync(save + xb + ib, b->status, sb, k, st);
+        } else {
+            cudaMemcpyAsync(b->x, save, xb, k, st);
+            cudaMemcpyAsync(b->iterations, save + xb, ib, k, st);
+            cudaMemcpyAsync(b->status, save + xb + ib, sb, k, st);
+        }
+    };
+    copy_in(false);
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    float best_ms = 0.f;
+    int best = -1;
+    std::string err;
+    for (int c = 0; c < (int)cands.size() && rc == GBX_OK; ++c) {
+        gbx::Params p{};
+        p.obj = *obj;
+        p.lmo = *lmo;
+        p.alg = *alg;
+        p.b = *b;
+        if (gbx::make_layout(*obj, *lmo, *alg, N, &p.L, &err, &cands[c]) != GBX_OK) continue;
+        if (gbx::workspace_bytes(p.L, N) > workspace_bytes || !workspace) continue;
+        p.ws = static_cast<double*>(workspace);
+        p.mixed = p.L.mixed_node_bytes ? static_cast<unsigned char*>(workspace) + gbx::mixed_region_offset(p.L, N)
+                                       : nullptr;
+        p.queue = p.L.persistent ? reinterpret_cast<int*>(static_cast<unsigned char*>(workspace) +
+                                                          gbx::queue_offset(p.L, N))
+                                 : nullptr;
+        p.sparse = nullptr;
+        if (p.L.sparse_bytes) {
+            p.sparse = static_cast<unsigned char*>(workspace) + gbx::sparse_region_offset(p.L, N);
+            rc = gbx::launch_sparse_build(*obj, p.L, p.sparse, st, &err);
+            if (rc) break;
+        }
+        float ms_min = 0.f;
+        for (int r = 0; r < std::max(1, repeats); ++r) {
+            copy_in(true);
+            cudaEventRecord(t0, st);
+            rc = gbx::launch_relax(p, st, &err);
+            cudaEventRecord(t1, st);
+            if (rc) break;
+            cudaEventSynchronize(t1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, t0, t1);
+            if (r == 0 || ms < ms_min) ms_min = ms;
+        }
+        if (rc == GBX_OK && (best < 0 || ms_min < best_ms)) { best = c; best_ms = ms_min; }
+    }
+    copy_in(true);
+    cudaFreeAsync(save, st);
+    e = cudaStreamSynchronize(st);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (rc) return fail(rc, err);
+    if (e != cudaSuccess) return fail(GBX_ERR_CUDA, cudaGetErrorString(e));
+    if (best < 0) return fail(GBX_ERR_WORKSPACE, "no launch shape fits the workspace");
+    gbx::store_variant(*obj, *lmo, *alg, cands[best]);
+    if (chosen) {
+        gbx::Layout L;
+        gbx::make_layout(*obj, *lmo, *alg, N, &L, &err, &cands[best]);
+        chosen[0] = L.tc;
+        chosen[1] = L.persistent;
+    }
+    return GBX_OK;
+}
+
+int gbx_relax_set_launch_shape(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
+                               int tensor_core, int persistent) {
+    const int rc = validate(obj, lmo, alg);
+    if (rc) return rc;
+    if (tensor_core < -1 || tensor_core > 1 || persistent < 0 || persistent > 1)
+        return fail(GBX_ERR_INVALID, "launch shape: tensor_core in -1..1, persistent in 0..1");
+    gbx::Variant v;
+    v.tc = tensor_core;
+    v.persistent = persistent;
+    gbx::Layout L;
+    std::string err;
+    const int r = gbx::make_layout(*obj, *lmo, *alg, 1, &L, &err, &v);
+    if (r) return fail(r, err);
+    gbx::store_variant(*obj, *lmo, *alg, v);
     return GBX_OK;
 }
 

@@ -6,6 +6,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "../../include/gpuboscia_gb300.h"
 
@@ -40,8 +41,9 @@ struct Layout {
     // and two integer Hungarian workspaces with warm state
     int mixed;
     int mx_global;
-    int tc;                   // gradient on the tensor cores (orders 65..128); the
+    int tc;                   // gradient on the tensor cores (orders 17..128); the
                               // operand images share the cost matrices' memory
+    int persistent;           // persistent grid over an atomic node queue
     size_t sm_mx, sm_cost, sm_code, sm_ihw, ihw_bytes;
     size_t mixed_node_bytes;  // bytes per node of the workspace's mixed region
     // graph matching: nonzero lists of A and B (rows and columns), built once
@@ -59,6 +61,7 @@ struct Params {
     double* ws;             // global workspace (node vectors when not in smem)
     unsigned char* mixed;   // mixed-precision scratch
     unsigned char* sparse;  // nonzero lists of A and B (graph matching), or null
+    int* queue;             // persistent grid: next-node counter (zeroed per launch), or null
 };
 
 #ifdef __CUDACC__
@@ -133,11 +136,24 @@ GBX_HD inline size_t ihw_bytes(int m) {
 void set_last_error(const std::string& msg);
 
 // host helpers (relax.cu)
+// Launch shape chosen by the autotuner (-1: the default rule).
+struct Variant {
+    int tc = -1;          // mixed Birkhoff: 1 tensor-core gradient, 0 FP32 SIMT gradient
+    int persistent = -1;  // 1 persistent grid, 0 one CTA per node
+};
 int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a,
-                int n_nodes, Layout* L, std::string* err);
+                int n_nodes, Layout* L, std::string* err, const Variant* v = nullptr);
+// the autotuner's choice for this shape (or the defaults)
+Variant tuned_variant(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a);
+void store_variant(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a, const Variant& v);
+// candidate launch shapes of this problem (the first is the default)
+std::vector<Variant> candidate_variants(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a);
 size_t workspace_bytes(const Layout& L, int n_nodes);
 size_t mixed_region_offset(const Layout& L, int n_nodes);  // bytes from the workspace start
 size_t sparse_region_offset(const Layout& L, int n_nodes);
+size_t queue_offset(const Layout& L, int n_nodes);   // persistent grid's node counter (int)
+// workspace that fits every candidate launch shape (what the sizing call reports)
+size_t workspace_bytes_any_variant(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a, int n_nodes);
 int launch_sparse_build(const gbx_objective& o, const Layout& L, unsigned char* base, cudaStream_t st,
                         std::string* err);
 int launch_relax(const Params& p, void* stream, std::string* err);

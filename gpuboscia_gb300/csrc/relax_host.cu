@@ -3,7 +3,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 
 #include "relax.cuh"
 
@@ -25,9 +28,11 @@ constexpr size_t kSmemBudget = 220 * 1024;
 }
 
 int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a,
-                int n_nodes, Layout* out, std::string* err) {
+                int n_nodes, Layout* out, std::string* err, const Variant* var) {
     (void)n_nodes;
+    const Variant v = var ? *var : tuned_variant(o, l, a);
     Layout L{};
+    L.persistent = v.persistent == 1 ? 1 : 0;
     const int n = o.n;
     for (int& v : L.off) v = -1;
     const bool dicg = a.kind == GBX_ALG_DICG;
@@ -84,7 +89,11 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
         }
         mx_bytes = mixed_array_bytes(n);
         cost_bytes = align16(2 * (size_t)n * sizeof(int));
-        L.tc = l.order > 64 && l.order <= 128 ? 1 : 0;
+        // the FP32 SIMT gradient keeps its arrays in shared memory up to order ~90;
+        // the tensor-core gradient pads any order up to 128
+        const bool tc_ok = l.order > 16 && l.order <= 128;
+        const bool simt_ok = l.order <= 90;
+        L.tc = tc_ok && (v.tc == 1 || (v.tc < 0 && l.order > 64) || !simt_ok) ? 1 : 0;
         if (L.tc) cost_bytes = std::max(cost_bytes, kTcOperandBytes);
         code_bytes = align16(2 * (size_t)n);
         L.ihw_bytes = ihw_bytes(l.order);
@@ -163,12 +172,68 @@ size_t mixed_region_offset(const Layout& L, int n_nodes) {
     return (L.node_stride * sizeof(double) * (size_t)n_nodes + 255) / 256 * 256;
 }
 
+// ---- autotuned launch shapes, per problem shape, process-wide
+namespace {
+struct Key {
+    int ok, lk, n, order, prec, alg, ls;
+    bool operator<(const Key& o) const {
+        return std::tie(ok, lk, n, order, prec, alg, ls) < std::tie(o.ok, o.lk, o.n, o.order, o.prec, o.alg, o.ls);
+    }
+};
+std::mutex g_tune_mutex;
+std::map<Key, Variant> g_tuned;
+Key key_of(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a) {
+    return {o.kind, l.kind, o.n, l.order, a.precision, a.kind, a.line_search};
+}
+}  // namespace
+
+Variant tuned_variant(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a) {
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    auto it = g_tuned.find(key_of(o, l, a));
+    return it == g_tuned.end() ? Variant{} : it->second;
+}
+
+void store_variant(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a, const Variant& v) {
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    g_tuned[key_of(o, l, a)] = v;
+}
+
+std::vector<Variant> candidate_variants(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a) {
+    std::vector<Variant> out;
+    std::vector<int> tcs = {-1};
+    if (a.precision == GBX_PRECISION_MIXED && o.kind == GBX_OBJ_GRAPH_MATCHING && l.kind == GBX_LMO_BIRKHOFF
+            && l.order > 16 && l.order <= 90)
+        tcs = {l.order > 64 ? 1 : 0, l.order > 64 ? 0 : 1};
+    for (int tc : tcs)
+        for (int pers : {0, 1}) {
+            Variant v;
+            v.tc = tc;
+            v.persistent = pers;
+            out.push_back(v);
+        }
+    return out;
+}
+
 size_t sparse_region_offset(const Layout& L, int n_nodes) {
     return (mixed_region_offset(L, n_nodes) + L.mixed_node_bytes * (size_t)n_nodes + 255) / 256 * 256;
 }
 
 size_t workspace_bytes(const Layout& L, int n_nodes) {
     return sparse_region_offset(L, n_nodes) + L.sparse_bytes + 256;
+}
+
+size_t queue_offset(const Layout& L, int n_nodes) {
+    return (sparse_region_offset(L, n_nodes) + L.sparse_bytes + 15) / 16 * 16;
+}
+
+size_t workspace_bytes_any_variant(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a, int n_nodes) {
+    size_t best = 0;
+    for (const Variant& v : candidate_variants(o, l, a)) {
+        Layout L;
+        std::string err;
+        if (make_layout(o, l, a, n_nodes, &L, &err, &v) == GBX_OK) best = std::max(best, workspace_bytes(L, n_nodes));
+    }
+    return best;
 }
 
 int launch_relax(const Params& p, void* stream, std::string* err) {

@@ -970,6 +970,14 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
     }
     if (tid == 0) { w0.scal[0] = 0; w0.scal[1] = 0; w0.scal[2] = 0; }
     if (tid == 32) { w1.scal[0] = 0; w1.scal[1] = 0; w1.scal[2] = 0; }
+    // warm state of every column: the in-face oracle's free columns change with
+    // the face, so a column may be read before any call has written it
+    for (int j = tid; j < m; j += kThreads) {
+        w0.colpot[j] = 0;
+        w1.colpot[j] = 0;
+        w0.match[j] = -1;
+        w1.match[j] = -1;
+    }
     if (tid == 0) c.flag[4] = 0;  // set when a face-forced bit of x changes
     if (tid == 0) c.flag[5] = 0;  // set when a tensor-core wait timed out
     // small-integer A and B (graph adjacency): permutation residuals are
@@ -1176,11 +1184,7 @@ __device__ inline double* vecp(double* sbase, double* gbase, const Layout& L, in
 // MIX: 0 FP64 iterations, 1 mixed precision with the FP32 SIMT gradient (two
 // nodes per SM), 2 mixed precision with the tensor-core gradient
 template <int OK, int LK, int MIX>
-__global__ void __launch_bounds__(kThreads, MIX == 1 ? 2 : 1) relax_kernel(const __grid_constant__ Params P) {
-    extern __shared__ __align__(16) unsigned char dsm[];
-    __shared__ Scalars sh;
-    const int node = blockIdx.x;
-    if (node >= P.b.n_nodes) return;
+static __device__ __forceinline__ void relax_node(const Params& P, const int node, unsigned char* dsm, Scalars& sh) {
     const int tid = threadIdx.x;
     const int n = P.obj.n;
     const Layout& L = P.L;
@@ -1483,6 +1487,28 @@ __global__ void __launch_bounds__(kThreads, MIX == 1 ? 2 : 1) relax_kernel(const
     }
 }
 
+// One CTA per node (grid = nodes), or a persistent grid whose CTAs take the
+// next node from an atomic queue in the workspace until the batch is done.
+template <int OK, int LK, int MIX>
+__global__ void __launch_bounds__(kThreads, MIX == 1 ? 2 : 1) relax_kernel(const __grid_constant__ Params P) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ Scalars sh;
+    if (!P.queue) {
+        if ((int)blockIdx.x < P.b.n_nodes) relax_node<OK, LK, MIX>(P, blockIdx.x, dsm, sh);
+        return;
+    }
+    __shared__ int next;
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(P.queue, 1);
+        __syncthreads();
+        const int node = next;
+        __syncthreads();
+        if (node >= P.b.n_nodes) return;
+        relax_node<OK, LK, MIX>(P, node, dsm, sh);
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------------ LMO probes
 template <int LK>
 __global__ void __launch_bounds__(kThreads, 1) lmo_probe_kernel(
@@ -1578,7 +1604,20 @@ int launch_one(const Params& p, cudaStream_t st, std::string* err) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::max<size_t>(p.L.sm_total, 1));
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
-    k<<<p.b.n_nodes, kThreads, p.L.sm_total, st>>>(p);
+    int grid = p.b.n_nodes;
+    if (p.queue) {
+        // persistent: as many CTAs as stay resident, each pulling nodes
+        int dev = 0, sms = 0, per_sm = 0;
+        e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, p.L.sm_total);
+        if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+        grid = std::max(1, std::min(grid, sms * std::max(per_sm, 1)));
+        e = cudaMemsetAsync(p.queue, 0, sizeof(int), st);
+        if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    }
+    k<<<grid, kThreads, p.L.sm_total, st>>>(p);
     e = cudaGetLastError();
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
     return GBX_OK;

@@ -172,6 +172,8 @@ void gbx_default_settings(gbx_settings* s) {
     s->root_initial_point = nullptr;
     s->branch_k = 3;
     s->use_cuda_graph = 1;
+    s->scorer = nullptr;
+    s->autotune = 1;
 }
 
 int gbx_solve(const gbx_problem* problem, const gbx_objective* obj, const gbx_lmo* lmo,
@@ -221,6 +223,8 @@ int gbx_solve(const gbx_problem* problem, const gbx_objective* obj, const gbx_lm
         cfg.abs_gap_tol = s->abs_gap_tol;
         cfg.rel_gap_tol = s->rel_gap_tol;
         cfg.precision = s->algorithm.precision;
+        cfg.use_cuda_graph = s->use_cuda_graph != 0;
+        cfg.autotune = s->autotune != 0;
 
         const double tol = s->integer_tol;
         const int k = s->branch_k;

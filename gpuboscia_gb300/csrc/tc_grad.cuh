@@ -113,11 +113,12 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
         :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
 
-// whole warp: allocate kTmemCols columns, base address written to *slot
+// whole warp: allocate kTmemCols columns, base address written to *slot. The
+// CTA keeps its allocation permit: a persistent CTA allocates again for every
+// node it takes (each allocation is released by tmem_dealloc first).
 __device__ __forceinline__ void tmem_alloc(uint32_t* slot) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                  :: "r"(smem_u32(slot)), "r"(kTmemCols) : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 }
 
 __device__ __forceinline__ void tmem_dealloc(uint32_t base) {

@@ -76,6 +76,8 @@ struct DeviceResidentConfig {
     int blocks_per_node = 4;
     // appended GB300 fields
     int precision = GBX_PRECISION_FP64;
+    bool use_cuda_graph = true;  // replay each slot's copy-relax-copy sequence from a CUDA graph
+    bool autotune = true;        // time the launch shapes on the first full batch (gbx_relax_autotune)
 };
 
 enum class DRSSchedulingEventType { Dispatched, CompletionDetached, PostprocessStarted };
@@ -213,6 +215,8 @@ private:
         bool in_use = false;
         std::uint64_t generation = 0;
         std::uint64_t seq = 0;
+        std::vector<std::pair<int, cudaGraphExec_t>> graphs;
+        bool graphs_failed = false;
         std::vector<Node> nodes;
         unsigned char* h = nullptr;
         unsigned char* d = nullptr;
@@ -249,6 +253,37 @@ private:
         s.end = p;
     }
 
+    // Graph of one dispatch of N nodes on this slot (H2D, relaxation, D2H),
+    // captured on first use; a few sizes are kept per slot.
+    cudaGraphExec_t slot_graph(Slot& s, int N, const gbx_node_batch& b) {
+        for (auto& g : s.graphs) if (g.first == N) return g.second;
+        if (s.graphs_failed) return nullptr;
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+            s.graphs_failed = true;
+            cudaGetLastError();
+            return nullptr;
+        }
+        cudaMemcpyAsync(s.d, s.h, s.o_gap, cudaMemcpyHostToDevice, s.stream);
+        const int rc = gbx_relax_batch(&obj_, &lmo_, &alg_, &b, s.ws, ws_bytes_, s.stream);
+        cudaMemcpyAsync(s.h + s.o_x, s.d + s.o_x, s.end - s.o_x, cudaMemcpyDeviceToHost, s.stream);
+        const cudaError_t e = cudaStreamEndCapture(s.stream, &graph);
+        cudaGraphExec_t exec = nullptr;
+        if (rc != GBX_OK || e != cudaSuccess || !graph || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            s.graphs_failed = true;   // fall back to direct launches on this slot
+            cudaGetLastError();
+            return nullptr;
+        }
+        cudaGraphDestroy(graph);
+        if (s.graphs.size() >= 4) {
+            cudaGraphExecDestroy(s.graphs.front().second);
+            s.graphs.erase(s.graphs.begin());
+        }
+        s.graphs.push_back({N, exec});
+        return exec;
+    }
+
     void alloc_slot(Slot& s, int id) {
         s.id = id;
         layout(s, cfg_.gpu_batch_size);
@@ -262,6 +297,7 @@ private:
 
     static void free_slot(Slot& s) {
         if (s.stream) cudaStreamSynchronize(s.stream);
+        for (auto& g : s.graphs) cudaGraphExecDestroy(g.second);
         if (s.done) cudaEventDestroy(s.done);
         if (s.stream) cudaStreamDestroy(s.stream);
         if (s.h) cudaFreeHost(s.h);
@@ -349,7 +385,6 @@ private:
             it[i] = nd.relaxation_iterations;
             st[i] = nd.relaxation_x.empty() ? 0 : GBX_NODE_INITIAL_POINT_SUPPLIED;
         }
-        GBX_CUDA_CHECK(cudaMemcpyAsync(s.d, s.h, s.o_gap, cudaMemcpyHostToDevice, s.stream));
         gbx_node_batch b{};
         b.n_nodes = N;
         b.max_iters = cfg_.gpu_max_iters;
@@ -365,8 +400,23 @@ private:
         b.best_vertex = at<double>(s.d, s.o_best);
         b.best_vertex_val = at<double>(s.d, s.o_bvv);
         b.integer_flags = d_flags_;
-        gbx_check(gbx_relax_batch(&obj_, &lmo_, &alg_, &b, s.ws, ws_bytes_, s.stream), "gbx_relax_batch");
-        GBX_CUDA_CHECK(cudaMemcpyAsync(s.h + s.o_x, s.d + s.o_x, s.end - s.o_x, cudaMemcpyDeviceToHost, s.stream));
+        if (cfg_.autotune && !tuned_ && N == cfg_.gpu_batch_size) {
+            // once, on the first full batch: the tuner relaxes it under every launch
+            // shape and restores it, and later launches (and graphs) use the winner
+            tuned_ = true;
+            GBX_CUDA_CHECK(cudaMemcpyAsync(s.d, s.h, s.o_gap, cudaMemcpyHostToDevice, s.stream));
+            gbx_check(gbx_relax_autotune(&obj_, &lmo_, &alg_, &b, s.ws, ws_bytes_, s.stream, 2, nullptr),
+                      "gbx_relax_autotune");
+        }
+        cudaGraphExec_t exec = cfg_.use_cuda_graph ? slot_graph(s, N, b) : nullptr;
+        if (exec) {
+            GBX_CUDA_CHECK(cudaGraphLaunch(exec, s.stream));
+        } else {
+            GBX_CUDA_CHECK(cudaMemcpyAsync(s.d, s.h, s.o_gap, cudaMemcpyHostToDevice, s.stream));
+            gbx_check(gbx_relax_batch(&obj_, &lmo_, &alg_, &b, s.ws, ws_bytes_, s.stream), "gbx_relax_batch");
+            GBX_CUDA_CHECK(cudaMemcpyAsync(s.h + s.o_x, s.d + s.o_x, s.end - s.o_x, cudaMemcpyDeviceToHost,
+                                           s.stream));
+        }
         GBX_CUDA_CHECK(cudaEventRecord(s.done, s.stream));
         ++batches_launched_;
         nodes_launched_ += N;
@@ -611,6 +661,7 @@ private:
     std::function<void(int, int, double, double, bool)> progress_cb_;
     std::function<void(const DRSSchedulingEvent&)> scheduling_cb_;
     BranchBatchHook branch_hook_;
+    bool tuned_ = false;
 
     std::vector<Slot> slots_;
     size_t ws_bytes_ = 0;

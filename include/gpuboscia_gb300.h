@@ -174,6 +174,25 @@ int gbx_relax_batch_static(const gbx_objective* obj, const gbx_lmo* lmo,
                            const gbx_algorithm* alg, const gbx_node_batch* batch,
                            void* stream);
 
+/* Autotuner (no counterpart in the reference): times each candidate launch
+ * shape of this problem on the caller's batch -- the tensor-core or FP32 SIMT
+ * gradient where both apply (mixed precision, Birkhoff orders 17..90), one CTA
+ * per node or a persistent grid pulling nodes from a queue -- keeping the
+ * fastest of `repeats` runs each, and makes the winner the shape that later
+ * gbx_relax_batch calls of the same problem shape use (process-wide). The
+ * batch's x, iterations and status are restored, so the caller still owns an
+ * unrelaxed batch. workspace: gbx_relax_workspace_bytes (it covers every
+ * shape). chosen (may be NULL) receives {tensor-core gradient, persistent}. */
+int gbx_relax_autotune(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
+                       const gbx_node_batch* batch, void* workspace, size_t workspace_bytes,
+                       void* stream, int repeats, int* chosen);
+
+/* Pins the launch shape of this problem shape by hand (what the autotuner
+ * would store): tensor_core -1/0/1 (default rule / FP32 SIMT / tensor-core
+ * gradient; mixed precision only), persistent 0/1. */
+int gbx_relax_set_launch_shape(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
+                               int tensor_core, int persistent);
+
 /* Batched LMO calls, one case per row (the probes of tests/test_pipeline.cu:
  * 96-163). mode 0: forward v = argmin <direction, v> over the node's set
  * (LMO::compute_v); mode 1: in-face away oracle (LMO::compute_inface_v) on
@@ -279,6 +298,7 @@ typedef struct gbx_settings {
     int branch_k;             /* branch_pow2 k (3) */
     int use_cuda_graph;       /* capture the relax launch (1) */
     const gbx_scorer* scorer; /* learned branching (NULL: most fractional) */
+    int autotune;             /* time the launch shapes on the first full batch (1) */
 } gbx_settings;
 
 typedef struct gbx_result {
