@@ -95,6 +95,7 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
         const bool simt_ok = l.order <= 90;
         L.tc = tc_ok && (v.tc == 1 || (v.tc < 0 && l.order > 64) || !simt_ok) ? 1 : 0;
         if (L.tc) cost_bytes = std::max(cost_bytes, kTcOperandBytes);
+        cost_bytes = std::max(cost_bytes, align16((size_t)n * sizeof(double)));  // the certificate's FP64 costs
         code_bytes = align16(2 * (size_t)n);
         L.ihw_bytes = ihw_bytes(l.order);
         fixed_bytes += cost_bytes + code_bytes + 2 * L.ihw_bytes;

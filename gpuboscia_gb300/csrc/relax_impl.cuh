@@ -282,14 +282,137 @@ static __device__ double perm_value(const Ctx& c, const int* pi, int* pinv) {
 namespace gbx {
 
 // ------------------------------------------------------------------ Hungarian
+// Order-preserving 64-bit key of a double (zeros of both signs map to +0's key,
+// so keys tie exactly when the doubles compare equal); finite values only.
+__device__ __forceinline__ unsigned long long fp64_key(double v) {
+    const long long b = __double_as_longlong(v == 0.0 ? 0.0 : v);
+    return b >= 0 ? (unsigned long long)b ^ 0x8000000000000000ull : ~(unsigned long long)b;
+}
+
+// Solve phase of the FP64 Hungarian with the column state in registers: lane l
+// owns the compacted columns l+1, l+33, ... (CPL per lane; k <= 32*CPL). The
+// arithmetic is the shared-memory loop's, operation for operation (same
+// potentials, slacks and updates), and the step argmin -- lowest slack, lowest
+// column on ties -- takes three warp min-reductions over the slack's key.
+template <int CPL>
+static __device__ bool hung_solve_reg(const HW& w, int m, int k, const double* cost, double sign,
+                                      const double* ub, const double* face, double* out, const uint8_t* code) {
+    const int lane = threadIdx.x & 31;
+    int colE[CPL], way[CPL], pr[CPL];
+    double minv[CPL], pv[CPL];
+    bool valid[CPL], used[CPL];
+#pragma unroll
+    for (int t = 0; t < CPL; ++t) {
+        const int j = lane + 1 + 32 * t;
+        valid[t] = j <= k;
+        colE[t] = valid[t] ? w.cols[j - 1] : 0;
+        pv[t] = 0.0;
+        pr[t] = 0;
+        way[t] = 0;
+    }
+    for (int j = lane; j <= k; j += 32) w.u[j] = 0.0;
+    __syncwarp();
+    for (int i = 1; i <= k; ++i) {
+#pragma unroll
+        for (int t = 0; t < CPL; ++t) { minv[t] = kNone; used[t] = false; }
+        int j0 = 0;
+        bool done = false;
+        for (int step = 0; step <= k; ++step) {
+            // row of column j0 (column 0 holds the row being inserted)
+            int i0 = i;
+            if (j0 != 0) {
+                const int owner = (j0 - 1) & 31, slot = (j0 - 1) >> 5;
+                i0 = __shfl_sync(kFull, lane_slot<CPL>(pr, slot), owner);
+            }
+            const double ui0 = w.u[i0];
+            const int rb = w.rows[i0 - 1] * m;
+            unsigned long long bkey = ~0ull;
+            int bj = 0x7fffffff;
+#pragma unroll
+            for (int t = 0; t < CPL; ++t) {
+                if (!valid[t] || used[t]) continue;
+                const int e = rb + colE[t];
+                double mv = minv[t];
+                const bool allowed = code ? (code[e] & kAllowed) != 0 : ub[e] >= 0.5;
+                if (allowed && (!face || face[e] > 1e-9)) {
+                    const double ce = cost ? sign * cost[e] : 0.0;
+                    const double cur = ce - ui0 - pv[t];
+                    if (cur < mv) { mv = cur; minv[t] = cur; way[t] = j0; }
+                }
+                if (mv < kNone) {
+                    const unsigned long long key = fp64_key(mv);
+                    const int j = lane + 1 + 32 * t;
+                    if (key < bkey) { bkey = key; bj = j; }
+                }
+            }
+            const unsigned hi = __reduce_min_sync(kFull, (unsigned)(bkey >> 32));
+            const unsigned lo = __reduce_min_sync(kFull, (unsigned)(bkey >> 32) == hi ? (unsigned)bkey : ~0u);
+            const unsigned long long best = ((unsigned long long)hi << 32) | lo;
+            const int j1 = (int)__reduce_min_sync(kFull, bkey == best ? (unsigned)bj : 0x7fffffffu);
+            if (j1 == 0x7fffffff) return false;
+            const int owner = (j1 - 1) & 31, slot = (j1 - 1) >> 5;
+            double bvl = 0.0;
+#pragma unroll
+            for (int t = 0; t < CPL; ++t)
+                if (t == slot) bvl = minv[t];
+            const double bv = __shfl_sync(kFull, bvl, owner);
+            if (!isfinite(bv)) return false;
+            // potentials: used columns (and column 0) move with the tree, the others' slacks shrink
+            if (lane == 0) w.u[i] += bv;
+#pragma unroll
+            for (int t = 0; t < CPL; ++t) {
+                if (!valid[t]) continue;
+                if (used[t]) { w.u[pr[t]] += bv; pv[t] -= bv; }
+                else minv[t] -= bv;
+            }
+            __syncwarp();
+            j0 = j1;
+            const int pj = __shfl_sync(kFull, lane_slot<CPL>(pr, slot), owner);
+            if (lane == owner) {
+#pragma unroll
+                for (int t = 0; t < CPL; ++t)
+                    if (t == slot) used[t] = true;
+            }
+            if (pj == 0) { done = true; break; }
+        }
+        if (!done) return false;   // no augmenting path within k+1 steps
+        // flip the path: column jj takes the row of way[jj] (column 0 holds row i)
+        int jj = j0;
+        for (int guard = 0; guard <= k && jj != 0; ++guard) {
+            const int owner = (jj - 1) & 31, slot = (jj - 1) >> 5;
+            const int j1 = __shfl_sync(kFull, lane_slot<CPL>(way, slot), owner);
+            int np = i;
+            if (j1 != 0) np = __shfl_sync(kFull, lane_slot<CPL>(pr, (j1 - 1) >> 5), (j1 - 1) & 31);
+            if (lane == owner) {
+#pragma unroll
+                for (int t = 0; t < CPL; ++t)
+                    if (t == slot) pr[t] = np;
+            }
+            jj = j1;
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int t = 0; t < CPL; ++t) {
+        if (!valid[t]) continue;
+        const int r = w.rows[pr[t] - 1];
+        out[r * m + colE[t]] = 1.0;
+        w.pi[r] = colE[t];
+    }
+    __syncwarp();
+    return true;
+}
+
 // Exact min-cost assignment over the Birkhoff order-m polytope with forced
 // (lb > 1/2), forbidden (ub < 1/2) and face restrictions, ties to the lowest
 // column (lmo.cuh:1239-1417). Executed by ONE warp; `out` must be zeroed and
 // visible. cost may be null (zero costs); the cost of edge e is sign*cost[e].
 // Returns a warp-uniform success flag and leaves the row->column map in w.pi.
-static __device__ bool hungarian_warp(const HW& w, int m, const double* cost, double sign,
-                               const double* lb, const double* ub, const double* face,
-                               double* out) {
+// Pre-pass of the Hungarian (one warp): forced (lb > 1/2 or face-forced) edges,
+// contradictions, and the compacted free rows / columns; writes the forced
+// entries of `out` and w.pi. Returns the number k of free rows, or -1.
+static __device__ int hung_prepass(const HW& w, int m, const double* lb, const double* ub, const double* face,
+                                   double* out) {
     const int lane = threadIdx.x & 31;
     for (int i = lane; i < m; i += 32) { w.fcol[i] = -1; w.frow[i] = -1; }
     __syncwarp();
@@ -308,7 +431,7 @@ static __device__ bool hungarian_warp(const HW& w, int m, const double* cost, do
     }
     ok = __all_sync(kFull, ok);
     __syncwarp();
-    if (!ok) return false;
+    if (!ok) return -1;
     int k = 0, kc = 0;
     const unsigned lt = (1u << lane) - 1u;
     for (int base = 0; base < m; base += 32) {
@@ -321,9 +444,17 @@ static __device__ bool hungarian_warp(const HW& w, int m, const double* cost, do
         k += __popc(mr);
         kc += __popc(mc);
     }
-    if (k != kc) return false;
+    if (k != kc) return -1;
     for (int i = lane; i < m; i += 32)
         if (w.fcol[i] >= 0) { out[i * m + w.fcol[i]] = 1.0; w.pi[i] = w.fcol[i]; }
+    __syncwarp();
+    return k;
+}
+
+// Solve phase with the column state in shared memory (one warp; any k).
+static __device__ bool hung_solve_smem(const HW& w, int m, int k, const double* cost, double sign,
+                                       const double* ub, const double* face, double* out, const uint8_t* code) {
+    const int lane = threadIdx.x & 31;
     for (int j = lane; j <= k; j += 32) { w.u[j] = 0.0; w.pv[j] = 0.0; w.p[j] = 0; w.way[j] = 0; }
     __syncwarp();
     for (int i = 1; i <= k; ++i) {
@@ -343,7 +474,8 @@ static __device__ bool hungarian_warp(const HW& w, int m, const double* cost, do
                 if (w.used[j]) continue;
                 const int e = rb + w.cols[j - 1];
                 double mv = w.minv[j];
-                if (ub[e] >= 0.5 && (!face || face[e] > 1e-9)) {
+                const bool allowed = code ? (code[e] & kAllowed) != 0 : ub[e] >= 0.5;
+                if (allowed && (!face || face[e] > 1e-9)) {
                     const double ce = cost ? sign * cost[e] : 0.0;
                     const double cur = ce - ui0 - w.pv[j];
                     if (cur < mv) { mv = cur; w.minv[j] = cur; w.way[j] = j0; }
@@ -388,12 +520,197 @@ static __device__ bool hungarian_warp(const HW& w, int m, const double* cost, do
     return true;
 }
 
-// Perfect matching by greedy lowest-column choice, for the feasibility test of
-// a Birkhoff node. Executed by ONE warp; `out` must be zeroed and visible.
-// Returns 0 when the bounds are contradictory (the Hungarian's pre-pass fails
-// on exactly these), 1 when every row found a free allowed column (a perfect
-// matching honouring the forced edges, left in out and w.pi), and 2 when the
-// greedy choice got stuck -- only then is the full Hungarian needed to decide.
+template <int MAXCPL = 8>
+static __device__ bool hungarian_warp(const HW& w, int m, const double* cost, double sign,
+                               const double* lb, const double* ub, const double* face,
+                               double* out, const uint8_t* code = nullptr) {
+    const int k = hung_prepass(w, m, lb, ub, face, out);
+    if (k < 0) return false;
+    // register-resident solve up to 32*MAXCPL free columns (MAXCPL bounds the
+    // registers a kernel spends on it), the shared-memory loop beyond
+    if (k <= 64) return hung_solve_reg<2>(w, m, k, cost, sign, ub, face, out, code);
+    if constexpr (MAXCPL >= 4)
+        if (k <= 128) return hung_solve_reg<4>(w, m, k, cost, sign, ub, face, out, code);
+    if constexpr (MAXCPL >= 8)
+        if (k <= 256) return hung_solve_reg<8>(w, m, k, cost, sign, ub, face, out, code);
+    return hung_solve_smem(w, m, k, cost, sign, ub, face, out, code);
+}
+
+// ---- the same Hungarian on a group of four warps (one per SM sub-partition:
+// on GB300 each sub-partition executes its own FP64 instructions, so the
+// per-step slack updates of 128 lanes cost what 32 lanes' did). Groups are
+// threads [0,128) (g = 0, named barrier 1) and [128,256) (g = 1, barrier 2).
+constexpr int kHungWarps = 4;
+constexpr int kHungThreads = kHungWarps * 32;
+
+__device__ __forceinline__ void group_bar(int g) {
+    asm volatile("bar.sync %0, %1;" :: "r"(1 + g), "r"(kHungThreads) : "memory");
+}
+
+__device__ __forceinline__ double key_fp64(unsigned long long key) {
+    const unsigned long long b = (key >> 63) ? key ^ 0x8000000000000000ull : ~key;
+    return __longlong_as_double((long long)b);
+}
+
+// Solve phase: thread gt of the group owns the compacted columns gt+1,
+// gt+1+128, ... (CPL per thread; k <= 128*CPL). Per step every warp reduces its
+// best (slack key, column) with three REDUX, the four warp results meet in
+// shared memory, and every thread derives the step value from the winning key
+// (the key maps back to the slack exactly, up to the sign of a zero, which no
+// comparison sees). Potential updates and the tie rule are those of the
+// single-warp loop, so the assignment is identical.
+template <int CPL>
+static __device__ bool hung_solve_group(const HW& w, int m, int k, const double* cost, double sign,
+                                        const double* ub, const double* face, double* out, const uint8_t* code,
+                                        int g) {
+    __shared__ unsigned long long s_key[2][kHungWarps];
+    __shared__ int s_j[2][kHungWarps];
+    __shared__ int s_row[2];
+    const int gt = threadIdx.x - kHungThreads * g, lane = gt & 31, gw = gt >> 5;
+    int colE[CPL], way[CPL], pr[CPL];
+    double minv[CPL], pv[CPL];
+    bool valid[CPL], used[CPL];
+#pragma unroll
+    for (int t = 0; t < CPL; ++t) {
+        const int j = gt + 1 + kHungThreads * t;
+        valid[t] = j <= k;
+        colE[t] = valid[t] ? w.cols[j - 1] : 0;
+        pv[t] = 0.0;
+        pr[t] = 0;
+        way[t] = 0;
+    }
+    for (int j = gt; j <= k; j += kHungThreads) w.u[j] = 0.0;
+    group_bar(g);
+    for (int i = 1; i <= k; ++i) {
+#pragma unroll
+        for (int t = 0; t < CPL; ++t) { minv[t] = kNone; used[t] = false; }
+        int j0 = 0, i0 = i;
+        bool done = false;
+        for (int step = 0; step <= k; ++step) {
+            const double ui0 = w.u[i0];
+            const int rb = w.rows[i0 - 1] * m;
+            unsigned long long bkey = ~0ull;
+            int bj = 0x7fffffff;
+#pragma unroll
+            for (int t = 0; t < CPL; ++t) {
+                if (!valid[t] || used[t]) continue;
+                const int e = rb + colE[t];
+                double mv = minv[t];
+                const bool allowed = code ? (code[e] & kAllowed) != 0 : ub[e] >= 0.5;
+                if (allowed && (!face || face[e] > 1e-9)) {
+                    const double ce = cost ? sign * cost[e] : 0.0;
+                    const double cur = ce - ui0 - pv[t];
+                    if (cur < mv) { mv = cur; minv[t] = cur; way[t] = j0; }
+                }
+                if (mv < kNone) {
+                    const unsigned long long key = fp64_key(mv);
+                    const int j = gt + 1 + kHungThreads * t;
+                    if (key < bkey) { bkey = key; bj = j; }
+                }
+            }
+            const unsigned hi = __reduce_min_sync(kFull, (unsigned)(bkey >> 32));
+            const unsigned lo = __reduce_min_sync(kFull, (unsigned)(bkey >> 32) == hi ? (unsigned)bkey : ~0u);
+            const unsigned long long wkey = ((unsigned long long)hi << 32) | lo;
+            const int wj = (int)__reduce_min_sync(kFull, bkey == wkey ? (unsigned)bj : 0x7fffffffu);
+            if (lane == 0) { s_key[g][gw] = wkey; s_j[g][gw] = wj; }
+            group_bar(g);
+            unsigned long long best = s_key[g][0];
+            int j1 = s_j[g][0];
+#pragma unroll
+            for (int q = 1; q < kHungWarps; ++q) {
+                const unsigned long long kq = s_key[g][q];
+                const int jq = s_j[g][q];
+                if (kq < best || (kq == best && jq < j1)) { best = kq; j1 = jq; }
+            }
+            if (j1 == 0x7fffffff) return false;
+            const double bv = key_fp64(best);
+            if (!isfinite(bv)) return false;
+            if (gt == 0) w.u[i] += bv;
+#pragma unroll
+            for (int t = 0; t < CPL; ++t) {
+                if (!valid[t]) continue;
+                if (used[t]) { w.u[pr[t]] += bv; pv[t] -= bv; }
+                else minv[t] -= bv;
+            }
+            const int owner = (j1 - 1) % kHungThreads, slot = (j1 - 1) / kHungThreads;
+            if (gt == owner) {
+#pragma unroll
+                for (int t = 0; t < CPL; ++t)
+                    if (t == slot) { used[t] = true; s_row[g] = pr[t]; }
+            }
+            group_bar(g);
+            const int pj = s_row[g];
+            j0 = j1;
+            if (pj == 0) { done = true; break; }
+            i0 = pj;
+        }
+        if (!done) return false;   // no augmenting path within k+1 steps
+        // flip the path in shared memory: column jj takes the row of way[jj]
+#pragma unroll
+        for (int t = 0; t < CPL; ++t)
+            if (valid[t]) {
+                const int j = gt + 1 + kHungThreads * t;
+                w.way[j] = way[t];
+                w.p[j] = pr[t];
+            }
+        group_bar(g);
+        if (gt == 0) {
+            w.p[0] = i;
+            int jj = j0;
+            for (int guard = 0; guard <= k && jj != 0; ++guard) {
+                const int jp = w.way[jj];
+                w.p[jj] = w.p[jp];
+                jj = jp;
+            }
+        }
+        group_bar(g);
+#pragma unroll
+        for (int t = 0; t < CPL; ++t)
+            if (valid[t]) pr[t] = w.p[gt + 1 + kHungThreads * t];
+    }
+#pragma unroll
+    for (int t = 0; t < CPL; ++t) {
+        if (!valid[t]) continue;
+        const int r = w.rows[pr[t] - 1];
+        out[r * m + colE[t]] = 1.0;
+        w.pi[r] = colE[t];
+    }
+    group_bar(g);
+    return true;
+}
+
+// The Hungarian on group g (all 128 of its threads call it): pre-pass on the
+// group's first warp, solve on all four; beyond 256 free columns the first warp
+// runs the shared-memory loop. Same result as hungarian_warp.
+static __device__ bool hungarian_group(const HW& w, int m, const double* cost, double sign, const double* lb,
+                                       const double* ub, const double* face, double* out, const uint8_t* code,
+                                       int g) {
+    __shared__ int s_k[2];
+    const int gt = threadIdx.x - kHungThreads * g;
+    if (gt < 32) {
+        const int k = hung_prepass(w, m, lb, ub, face, out);
+        if (gt == 0) s_k[g] = k;
+    }
+    group_bar(g);
+    const int k = s_k[g];
+    if (k < 0) return false;
+    if (k <= kHungThreads) return hung_solve_group<1>(w, m, k, cost, sign, ub, face, out, code, g);
+    if (k <= 2 * kHungThreads) return hung_solve_group<2>(w, m, k, cost, sign, ub, face, out, code, g);
+    if (gt < 32) {
+        const bool ok = hung_solve_smem(w, m, k, cost, sign, ub, face, out, code);
+        if (gt == 0) s_k[g] = ok ? 1 : 0;
+    }
+    group_bar(g);
+    return s_k[g] != 0;
+}
+
+// Perfect matching of the allowed edges honouring the forced ones, for the
+// feasibility test of a Birkhoff node: greedy lowest-column choice, then
+// augmenting paths for the rows it could not place. Executed by ONE warp;
+// `out` must be zeroed and visible. Returns 0 when no perfect matching exists
+// (contradictory bounds included), 1 with a perfect matching in out and w.pi,
+// and 2 when the masks do not fit the workspace (orders above ~192) -- only
+// then does the caller fall back to the Hungarian.
 static __device__ int greedy_matching_warp(const HW& w, int m, const double* lb, const double* ub,
                                            double* out) {
     const int lane = threadIdx.x & 31;
@@ -427,9 +744,13 @@ static __device__ int greedy_matching_warp(const HW& w, int m, const double* lb,
         kc += __popc(mc);
     }
     if (k != kc) return 0;
-    for (int j = lane; j < k; j += 32) w.used[j] = 0;   // free column position taken
+    // matchR[t] = column position of compacted row t (w.p), matchC[pos] = row (w.way)
+    int* matchR = w.p;
+    int* matchC = w.way;
+    for (int j = lane; j < k; j += 32) { w.used[j] = 0; matchR[j] = -1; matchC[j] = -1; }
     __syncwarp();
     int first = 0;  // lowest position that may still be free
+    int stuck = 0;
     for (int t = 0; t < k; ++t) {
         const int r = w.rows[t];
         int pick = -1;
@@ -439,14 +760,69 @@ static __device__ int greedy_matching_warp(const HW& w, int m, const double* lb,
             const unsigned b = __ballot_sync(kFull, cand);
             if (b) pick = base + __ffs(b) - 1;
         }
-        if (pick < 0) return 2;
-        if (lane == 0) {
-            w.used[pick] = 1;
-            w.pi[r] = w.cols[pick];
-            out[r * m + w.cols[pick]] = 1.0;
-        }
+        if (pick < 0) { ++stuck; continue; }
+        if (lane == 0) { w.used[pick] = 1; matchR[t] = pick; matchC[pick] = t; }
         __syncwarp();
         while (first < k && w.used[first]) ++first;
+    }
+    if (stuck) {
+        // augmenting paths (Kuhn) over allowed-edge bitmasks of the compacted
+        // rows: exact, so a row without an augmenting path means no perfect matching
+        const int W = (k + 31) >> 5;
+        if ((size_t)k * W > 6 * (size_t)(m + 1)) return 2;   // no room for the masks
+        unsigned* mask = reinterpret_cast<unsigned*>(w.u);  // [k][W] over u, pv, minv
+        for (int t = 0; t < k; ++t) {
+            const int r = w.rows[t];
+            for (int base = 0; base < k; base += 32) {
+                const int pos = base + lane;
+                const unsigned b = __ballot_sync(kFull, pos < k && ub[r * m + w.cols[pos]] >= 0.5);
+                if (lane == 0) mask[t * W + (base >> 5)] = b;
+            }
+        }
+        __syncwarp();
+        int ok = 1;
+        if (lane == 0) {
+            int* queue = w.pi;      // BFS queue of compacted rows (pi is written last)
+            int* parent = w.pinv;   // row that reached each column position
+            unsigned vis[32];
+            for (int t0 = 0; t0 < k && ok; ++t0) {
+                if (matchR[t0] >= 0) continue;
+                for (int q = 0; q < W; ++q) vis[q] = 0u;
+                int head = 0, tail = 0, found = -1;
+                queue[tail++] = t0;
+                while (head < tail && found < 0) {
+                    const int t = queue[head++];
+                    for (int q = 0; q < W && found < 0; ++q) {
+                        unsigned cand = mask[t * W + q] & ~vis[q];
+                        while (cand && found < 0) {
+                            const int bit = __ffs(cand) - 1;
+                            cand &= cand - 1;
+                            const int pos = q * 32 + bit;
+                            vis[q] |= 1u << bit;
+                            parent[pos] = t;
+                            if (matchC[pos] < 0) found = pos;
+                            else queue[tail++] = matchC[pos];
+                        }
+                    }
+                }
+                if (found < 0) { ok = 0; break; }
+                for (int pos = found; pos >= 0;) {   // flip the path back to t0
+                    const int t = parent[pos];
+                    const int prev = matchR[t];
+                    matchR[t] = pos;
+                    matchC[pos] = t;
+                    pos = t == t0 ? -1 : prev;
+                }
+            }
+        }
+        ok = __shfl_sync(kFull, ok, 0);
+        __syncwarp();
+        if (!ok) return 0;
+    }
+    for (int t = lane; t < k; t += 32) {
+        const int r = w.rows[t], col = w.cols[matchR[t]];
+        w.pi[r] = col;
+        out[r * m + col] = 1.0;
     }
     for (int i = lane; i < m; i += 32)
         if (w.fcol[i] >= 0) { out[i * m + w.fcol[i]] = 1.0; w.pi[i] = w.fcol[i]; }
@@ -639,9 +1015,9 @@ static __device__ bool lmo_forward(const Ctx& c, const double* g, const double* 
         for (int j = c.tid; j < n; j += kThreads) v[j] = 0.0;
         __syncthreads();
         if (n != c.lorder * c.lorder) return false;
-        if (threadIdx.x < 32) {
+        if (threadIdx.x < kHungThreads) {
             const HW w = hw_at(c.hung[0], c.lorder);
-            const bool ok = hungarian_warp(w, c.lorder, g, 1.0, lb, ub, nullptr, v);
+            const bool ok = hungarian_group(w, c.lorder, g, 1.0, lb, ub, nullptr, v, nullptr, 0);
             if (threadIdx.x == 0) c.flag[0] = ok;
         }
         __syncthreads();
@@ -772,7 +1148,7 @@ static __device__ bool node_feasible(const Ctx& c, const double* lb, const doubl
             if (r == 2) {
                 for (int j = threadIdx.x; j < n; j += 32) scratch[j] = 0.0;
                 __syncwarp();
-                r = hungarian_warp(w, c.lorder, nullptr, 1.0, lb, ub, nullptr, scratch) ? 1 : 0;
+                r = hungarian_warp<2>(w, c.lorder, nullptr, 1.0, lb, ub, nullptr, scratch) ? 1 : 0;
             }
             if (threadIdx.x == 0) c.flag[1] = r;
         }
@@ -1377,12 +1753,12 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
             for (int j = tid; j < n; j += kThreads) { V[j] = 0.0; if (dicg) AW[j] = 0.0; }
             __syncthreads();
             if (n == c.lorder * c.lorder) {
-                if (threadIdx.x < 32) {
-                    const bool ok = hungarian_warp(hw0, c.lorder, G, 1.0, LB, UB, nullptr, V);
+                if (threadIdx.x < kHungThreads) {
+                    const bool ok = hungarian_group(hw0, c.lorder, G, 1.0, LB, UB, nullptr, V, nullptr, 0);
                     if (threadIdx.x == 0) sh.flag[0] = ok;
-                } else if (dicg && threadIdx.x < 64) {
-                    const bool ok = hungarian_warp(hw1, c.lorder, G, -1.0, LB, UB, X, AW);
-                    if (threadIdx.x == 32) sh.flag[2] = ok;
+                } else if (dicg) {
+                    const bool ok = hungarian_group(hw1, c.lorder, G, -1.0, LB, UB, X, AW, nullptr, 1);
+                    if (threadIdx.x == kHungThreads) sh.flag[2] = ok;
                 }
             } else if (tid == 0) {
                 sh.flag[0] = 0;
@@ -1442,7 +1818,23 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
     obj_grad(c, X, G);
     double fval = 0.0;
     if constexpr (OK == GBX_OBJ_GRAPH_MATCHING) fval = value_from_residual(c);
-    const bool fok = lmo_forward<LK>(c, G, LB, UB, V);
+    bool fok;
+    if constexpr (kMixedLoop) {
+        // the integer costs' shared memory is free now: the FP64 Hungarian reads
+        // the gradient from there and edge permissions from the code bytes
+        // (kAllowed is ub >= 1/2), the same arithmetic as lmo_forward
+        double* Gs = reinterpret_cast<double*>(dsm + L.sm_cost);
+        for (int j = tid; j < n; j += kThreads) { Gs[j] = G[j]; V[j] = 0.0; }
+        __syncthreads();
+        if (threadIdx.x < kHungThreads) {
+            const bool ok = hungarian_group(hw0, c.lorder, Gs, 1.0, LB, UB, nullptr, V, dsm + L.sm_code, 0);
+            if (threadIdx.x == 0) sh.flag[0] = ok;
+        }
+        __syncthreads();
+        fok = sh.flag[0] != 0;
+    } else {
+        fok = lmo_forward<LK>(c, G, LB, UB, V);
+    }
     score(V, (graph_perm && fok) ? hw0.pi : nullptr, hw0.pinv);
     double loc = 0.0;
     for (int j = tid; j < n; j += kThreads) loc = fma(G[j], X[j] - V[j], loc);
