@@ -320,9 +320,54 @@ static __device__ float bmax_abs(const float* v, int n, double* red) {
 }
 
 // FP32 gradient g = 2s(A'R - RB') with R = AX - XB; A, B, Bt given in FP32.
+// For m % 4 == 0 every thread computes strips of four consecutive outputs: one
+// scalar and one float4 load per operand pair feed four FMAs (rows of m floats
+// stay 16-byte aligned).
 static __device__ void grad_f32(int m, float two_s, const float* A, const float* B, const float* Bt, const float* X,
                          float* R, float* G) {
     const int n = m * m;
+    if ((m & 3) == 0) {
+        const int strips = n >> 2, sm = m >> 2;
+        for (int s = threadIdx.x; s < strips; s += kThreads) {
+            const int i = s / sm, j = (s - (s / sm) * sm) << 2;
+            float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int k = 0; k < m; ++k) {
+                const float a = A[i * m + k], xi = -X[i * m + k];
+                const float4 xk = *reinterpret_cast<const float4*>(X + k * m + j);
+                const float4 bk = *reinterpret_cast<const float4*>(B + k * m + j);
+                r.x = fmaf(xi, bk.x, fmaf(a, xk.x, r.x));
+                r.y = fmaf(xi, bk.y, fmaf(a, xk.y, r.y));
+                r.z = fmaf(xi, bk.z, fmaf(a, xk.z, r.z));
+                r.w = fmaf(xi, bk.w, fmaf(a, xk.w, r.w));
+            }
+            *reinterpret_cast<float4*>(R + i * m + j) = r;
+        }
+        __syncthreads();
+        for (int s = threadIdx.x; s < strips; s += kThreads) {
+            const int p = s / sm, q = (s - (s / sm) * sm) << 2;
+            float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int r = 0; r < m; ++r) {
+                const float a = A[r * m + p];
+                const float4 rr = *reinterpret_cast<const float4*>(R + r * m + q);
+                g.x = fmaf(a, rr.x, g.x);
+                g.y = fmaf(a, rr.y, g.y);
+                g.z = fmaf(a, rr.z, g.z);
+                g.w = fmaf(a, rr.w, g.w);
+            }
+            for (int c = 0; c < m; ++c) {
+                const float rp = -R[p * m + c];
+                const float4 bt = *reinterpret_cast<const float4*>(Bt + c * m + q);
+                g.x = fmaf(rp, bt.x, g.x);
+                g.y = fmaf(rp, bt.y, g.y);
+                g.z = fmaf(rp, bt.z, g.z);
+                g.w = fmaf(rp, bt.w, g.w);
+            }
+            *reinterpret_cast<float4*>(G + p * m + q) =
+                make_float4(two_s * g.x, two_s * g.y, two_s * g.z, two_s * g.w);
+        }
+        __syncthreads();
+        return;
+    }
     for (int e = threadIdx.x; e < n; e += kThreads) {
         const int i = e / m, j = e - (e / m) * m;
         float r = 0.f;

@@ -1344,6 +1344,16 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
         xf[e] = (float)xe;
         face[e] = (uint8_t)((xe > 1e-9 ? kFaceIn : 0) | (xe >= 1.0 - 1e-9 ? kFaceOne : 0));
     }
+    // Oracle warps: a warp issues on SM sub-partition (hardware slot % 4), and
+    // two of these CTAs share an SM, so the CTA in the upper half of the SM's
+    // warp slots runs its two oracles on warps 2 and 3 -- the four latency-bound
+    // oracle warps of an SM then sit on four different sub-partitions.
+    __shared__ int s_owarp;
+    if (tid == 0) {
+        unsigned slot;
+        asm volatile("mov.u32 %0, %%warpid;" : "=r"(slot));
+        s_owarp = ((slot >> 3) & 1) ? 2 : 0;
+    }
     if (tid == 0) { w0.scal[0] = 0; w0.scal[1] = 0; w0.scal[2] = 0; }
     if (tid == 32) { w1.scal[0] = 0; w1.scal[1] = 0; w1.scal[2] = 0; }
     // warm state of every column: the in-face oracle's free columns change with
@@ -1418,8 +1428,9 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
             if (dicg) costa[e] = (allowed && (face[e] & kFaceIn)) ? -ci : kIntInf;
         }
         __syncthreads();
-        if (threadIdx.x < 64 && (threadIdx.x < 32 || dicg)) {
-            const bool fwd = threadIdx.x < 32;
+        const int owarp = (int)(threadIdx.x >> 5) - s_owarp;
+        if (owarp == 0 || (dicg && owarp == 1)) {
+            const bool fwd = owarp == 0;
             const IHW& w = fwd ? w0 : w1;
             const int* cst = fwd ? costf : costa;
             const uint8_t* fc = fwd ? nullptr : face;
