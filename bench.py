@@ -31,6 +31,8 @@ WORKLOADS = {
     # name: (instance builder, order, nodes per batch, algorithm, line search)
     "birkhoff_gnp36": dict(order=36, nodes=256, alg=1, ls=4, iters=100),
     "birkhoff_regular120": dict(order=120, nodes=256, alg=1, ls=4, iters=20),
+    # config 5 shape (10-regular, B = P A P'); FP64 only: the mixed path stops at order 256
+    "birkhoff_regular400": dict(order=400, nodes=152, alg=1, ls=4, iters=5),
 }
 
 
@@ -56,6 +58,8 @@ def make_workload(name, nodes, rank):
     order = w["order"]
     if name.startswith("birkhoff_gnp"):
         inst = instances.birkhoff_gnp(order=order)
+    elif order == 400:
+        inst = instances.birkhoff_regular_isomorphic(order=order)
     else:
         inst = instances.birkhoff_regular_perturbed(order=order)
     lb, ub = instances.birkhoff_node_batch(order, nodes, seed=4242 + rank)

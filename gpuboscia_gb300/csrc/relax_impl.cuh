@@ -680,7 +680,7 @@ static __device__ bool hung_solve_group(const HW& w, int m, int k, const double*
 }
 
 // The Hungarian on group g (all 128 of its threads call it): pre-pass on the
-// group's first warp, solve on all four; beyond 256 free columns the first warp
+// group's first warp, solve on all four; beyond 512 free columns the first warp
 // runs the shared-memory loop. Same result as hungarian_warp.
 static __device__ bool hungarian_group(const HW& w, int m, const double* cost, double sign, const double* lb,
                                        const double* ub, const double* face, double* out, const uint8_t* code,
@@ -696,6 +696,7 @@ static __device__ bool hungarian_group(const HW& w, int m, const double* cost, d
     if (k < 0) return false;
     if (k <= kHungThreads) return hung_solve_group<1>(w, m, k, cost, sign, ub, face, out, code, g);
     if (k <= 2 * kHungThreads) return hung_solve_group<2>(w, m, k, cost, sign, ub, face, out, code, g);
+    if (k <= 4 * kHungThreads) return hung_solve_group<4>(w, m, k, cost, sign, ub, face, out, code, g);
     if (gt < 32) {
         const bool ok = hung_solve_smem(w, m, k, cost, sign, ub, face, out, code);
         if (gt == 0) s_k[g] = ok ? 1 : 0;

@@ -254,3 +254,14 @@ def test_birkhoff_order64_workspace_path_bitwise(cuda_lib):
     lb, ub = instances.birkhoff_node_batch(64, 4, seed=3)
     g, o_ = run_both(inst.objective, inst.lmo, alg, lb.copy(), lb, ub, 1e-6, 6, np.ones(4096, np.uint8))
     assert_same(g, o_)
+
+
+def test_birkhoff_order400_nodes_bitwise(cuda_lib):
+    """Config-5 shape (10-regular graphs on 400 vertices): the FP64 path with the
+    zero-skipping gradient and the four-warp Hungarian at 400 free columns."""
+    inst = instances.birkhoff_regular_isomorphic(order=400)
+    lb, ub = instances.birkhoff_node_batch(400, 2, seed=5)
+    flags = np.ones(400 * 400, np.uint8)
+    g, o = run_both(inst.objective, inst.lmo, O.algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT), lb.copy(), lb, ub,
+                    1e-6, 2, flags)
+    assert_same(g, o)
