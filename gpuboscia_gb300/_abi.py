@@ -162,7 +162,7 @@ EXPORTED_SYMBOLS = (
     "gbx_abi_version", "gbx_last_error", "gbx_relax_workspace_bytes",
     "gbx_relax_batch", "gbx_relax_batch_static", "gbx_relax_autotune", "gbx_relax_set_launch_shape",
     "gbx_lmo_batch",
-    "gbx_objective_gradient_batch",
+    "gbx_objective_gradient_batch", "gbx_objective_gradient_batch_f32",
     "gbx_node_feasible_batch",
     "gbx_default_settings", "gbx_solve",
     "gbx_scorer_param_count", "gbx_branch_features", "gbx_scorer_forward", "gbx_scorer_workspace_bytes",
@@ -204,6 +204,8 @@ def load(path: os.PathLike | str | None = None) -> C.CDLL:
     lib.gbx_objective_gradient_batch.restype = C.c_int
     lib.gbx_objective_gradient_batch.argtypes = [P(Objective), C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                                  C.c_void_p]
+    lib.gbx_objective_gradient_batch_f32.restype = C.c_int
+    lib.gbx_objective_gradient_batch_f32.argtypes = [P(Objective), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.gbx_node_feasible_batch.restype = C.c_int
     lib.gbx_node_feasible_batch.argtypes = [P(LMO), C.c_int, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.c_void_p]

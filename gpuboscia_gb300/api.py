@@ -342,6 +342,20 @@ def objective_gradient_batch(objective, x, precision: int = A.PRECISION_FP64, st
     return g
 
 
+def objective_gradient_batch_f32(objective, x, stream=None):
+    """Pipelined tensor-core gradients of FP32 points x [cases, n] (orders <= 128)."""
+    import torch
+    lib = A.load()
+    keep = _Keep()
+    X = x.to(dtype=torch.float32).contiguous()
+    cases, n = X.shape
+    o = objective.to_c("cuda", keep)
+    g = torch.empty(cases, n, dtype=torch.float32, device=X.device)
+    rc = lib.gbx_objective_gradient_batch_f32(C.byref(o), cases, X.data_ptr(), g.data_ptr(), _stream_ptr(stream))
+    A.check(lib, rc, "gbx_objective_gradient_batch_f32")
+    return g
+
+
 def node_feasible_batch(lmo, lb, ub, integer_flags=None, stream=None):
     import torch
     lib = A.load()

@@ -286,6 +286,19 @@ int gbx_scorer_adam(gbx_scorer* s, const float* grad, float* m, float* v, int st
     return GBX_OK;
 }
 
+int gbx_objective_gradient_batch_f32(const gbx_objective* obj, int cases, const float* x, float* g,
+                                     void* stream) {
+    if (!obj || cases < 0 || obj->n <= 0) return fail(GBX_ERR_INVALID, "gradient batch arguments");
+    if (cases > 0 && (!x || !g)) return fail(GBX_ERR_INVALID, "null gradient buffer");
+    if (obj->kind != GBX_OBJ_GRAPH_MATCHING || obj->order <= 0 || obj->order > 128
+            || obj->order * obj->order != obj->n || !obj->A || !obj->B)
+        return fail(GBX_ERR_UNSUPPORTED, "the pipelined gradient covers graph matching up to order 128");
+    std::string err;
+    const int rc = gbx::launch_gradient_batch_f32(*obj, cases, x, g, static_cast<cudaStream_t>(stream), &err);
+    if (rc) return fail(rc, err);
+    return GBX_OK;
+}
+
 int gbx_node_feasible_batch(const gbx_lmo* lmo, int cases, const double* lb,
                             const double* ub, const uint8_t* integer_flags, uint8_t* out,
                             void* stream) {

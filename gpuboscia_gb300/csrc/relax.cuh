@@ -170,6 +170,8 @@ int scorer_gradient(const gbx_scorer* s, int rows, const float* X, int groups, c
                     float* grad, float* loss, void* ws, size_t ws_bytes, cudaStream_t st, std::string* err);
 int scorer_adam(gbx_scorer* s, const float* g, float* m, float* v, int step, float lr, cudaStream_t st,
                 std::string* err);
+int launch_gradient_batch_f32(const gbx_objective& o, int cases, const float* x, float* g, cudaStream_t st,
+                              std::string* err);
 int launch_node_feasible(const gbx_lmo& l, int cases, const double* lb, const double* ub,
                          const uint8_t* flags, uint8_t* out, void* stream, std::string* err);
 

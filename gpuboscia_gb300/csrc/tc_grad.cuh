@@ -92,6 +92,16 @@ __device__ __forceinline__ bool bar_try(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
+// non-blocking test of the phase with the given parity
+__device__ __forceinline__ bool bar_test(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+
 // bounded wait for the phase with the given parity to complete
 __device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
     const long long t0 = clock64();

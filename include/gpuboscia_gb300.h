@@ -216,6 +216,15 @@ int gbx_lmo_batch(const gbx_lmo* lmo, int cases, int mode,
 int gbx_objective_gradient_batch(const gbx_objective* obj, int precision, int cases,
                                  const double* x, double* g, void* stream);
 
+/* The mixed-precision graph-matching gradient of FP32 points (device
+ * [cases*n] in and out; orders up to 128), software-pipelined over a
+ * persistent grid so that tensor-core MMAs of one point overlap the loads and
+ * epilogues of the next (the batch form of gbx_objective_gradient_batch for
+ * callers that hold FP32 iterates). Synchronises the stream; GBX_ERR_TIMEOUT
+ * if a tensor-core wait ran out. */
+int gbx_objective_gradient_batch_f32(const gbx_objective* obj, int cases, const float* x, float* g,
+                                     void* stream);
+
 /* Node feasibility before any objective work (drs_node_feasible,
  * device_resident_solver.cuh:206-217): out[case] = 1 feasible, 0 infeasible. */
 int gbx_node_feasible_batch(const gbx_lmo* lmo, int cases, const double* lb,

@@ -72,3 +72,24 @@ def test_mixed_gradient_rejects(cuda_lib):
     with pytest.raises(RuntimeError, match="mixed gradient"):
         api.objective_gradient_batch(inst.objective, torch.zeros(1, 16, dtype=torch.float64).cuda(),
                                      A.PRECISION_MIXED)
+
+
+@pytest.mark.parametrize("order,cases", [(36, 1), (96, 5), (120, 300), (128, 700)])
+def test_pipelined_f32_gradient_error(cuda_lib, order, cases):
+    """gbx_objective_gradient_batch_f32: the persistent pipelined kernel (several
+    points per CTA, both operand buffers reused) against the FP64 oracle."""
+    import torch
+    inst = instances.birkhoff_gnp(order=order, seed=order + 9)
+    X = points(order, cases, order + 2)
+    g = api.objective_gradient_batch_f32(inst.objective, torch.from_numpy(X).cuda()).cpu().numpy()
+    for k in sorted({0, cases // 2, cases - 1}):
+        ref = O.grad(inst.objective, X[k].astype(np.float32).astype(np.float64))
+        err = np.max(np.abs(g[k] - ref)) / np.max(np.abs(ref))
+        assert err <= MIXED_TOL, (order, k, err)
+
+
+def test_pipelined_f32_gradient_rejects(cuda_lib):
+    import torch
+    inst = instances.birkhoff_gnp(order=130, seed=1)
+    with pytest.raises(RuntimeError, match="order 128"):
+        api.objective_gradient_batch_f32(inst.objective, torch.zeros(1, 130 * 130).cuda())
