@@ -158,7 +158,7 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * statistics.mean(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": config_dict(args),
+            "data": "synthetic", "config": dict(config_dict(args), precision="fp64 (CPU oracle)"),
             "cpu_baseline": {"value": value, "unit": "nodes/s", "cores": threads, "kind": "port",
                              "sample": f"{done} of {args.nodes} nodes per step, {args.iters} iterations max"},
             "e2e": {"value": value, "unit": "nodes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -204,31 +204,63 @@ def time_plain(args, inst, lb, x0, d_lb, d_ub, d_eps, d_flags, flush, w, stream)
             "node_iterations_per_step": int(it.sum().item())}
 
 
-def time_to_gap(args, inst):
-    """Wall time of gpuboscia::solve (through gbx_solve) from entry to the certified
-    1e-6 gap, plain FP64 against mixed precision, on the workload's instance."""
+def _solve_timed(inst, prec, scorer_obj, batch, streams, limit):
     from gpuboscia_gb300 import _abi as A
     from gpuboscia_gb300 import api
+    s = inst.settings
+    s.gpu_batch_size = batch
+    s.num_streams = streams
+    s.gpu_max_iters = 1000 if inst.lmo.order <= 16 else 400
+    s.line_search = A.LS_QUADRATIC_EXACT
+    s.abs_gap_tol = 1e-6
+    s.rel_gap_tol = 1e-6
+    s.time_limit_seconds = limit
+    s.precision = prec
+    s.scorer = scorer_obj
+    t0 = time.perf_counter()
+    r = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    wall = time.perf_counter() - t0
+    gap = abs(r.objective - r.dual_bound) if math.isfinite(r.objective) else math.inf
+    certified = bool(not r.reached_time_limit and (gap <= 1e-6 or gap <= 1e-6 * abs(r.objective)))
+    return wall, r, certified
+
+
+def time_to_gap(args, inst):
+    """Wall time of gpuboscia::solve (through gbx_solve) from entry to the certified
+    1e-6 gap. (1) The workload's instance, plain FP64 against mixed precision.
+    (2) Held-out G(9, 1/2) graph pairs (non-isomorphic, the tree branches):
+    plain (FP64 gradients, most-fractional branching) against mixed precision
+    and mixed precision + the learned scorer (trained first on strong-branching
+    labels of four other pairs); same engine settings for all."""
+    from gpuboscia_gb300 import _abi as A
+    from gpuboscia_gb300 import instances, scorer
     out = {}
     for name, prec in (("plain_fp64", A.PRECISION_FP64), ("mixed", A.PRECISION_MIXED)):
-        s = inst.settings
-        s.gpu_batch_size = 256
-        s.num_streams = 2
-        s.gpu_max_iters = 400
-        s.line_search = A.LS_QUADRATIC_EXACT
-        s.abs_gap_tol = 1e-6
-        s.rel_gap_tol = 1e-6
-        s.time_limit_seconds = args.ttg_limit
-        s.precision = prec
-        t0 = time.perf_counter()
-        r = api.solve(inst.problem, inst.objective, inst.lmo, s)
-        wall = time.perf_counter() - t0
-        gap = abs(r.objective - r.dual_bound) if math.isfinite(r.objective) else math.inf
+        wall, r, cert = _solve_timed(inst, prec, None, 256, 2, args.ttg_limit)
         out[name] = {"seconds": wall, "nodes": r.nodes_processed, "objective": r.objective,
-                     "dual_bound": r.dual_bound,
-                     "certified": bool(not r.reached_time_limit
-                                       and (gap <= 1e-6 or gap <= 1e-6 * abs(r.objective))),
-                     "time_limit": bool(r.reached_time_limit)}
+                     "dual_bound": r.dual_bound, "certified": cert, "time_limit": bool(r.reached_time_limit)}
+
+    def pair(seed, order=9):
+        rng = np.random.Generator(np.random.PCG64(seed))
+        return instances.graph_matching(order, instances.gnp_graph(rng, order, 0.5),
+                                        instances.gnp_graph(rng, order, 0.5), f"pair{order}_{seed}")
+    t0 = time.perf_counter()
+    data = scorer.Dataset.concat([scorer.collect_strong_branching(pair(100 + k), max_nodes=30, max_candidates=64)
+                                  for k in range(4)])
+    sc = scorer.Scorer(32, seed=0)
+    sc.train(data, epochs=400, lr=3e-3)
+    train_s = time.perf_counter() - t0
+    pairs = {"instances": "4 held-out G(9,1/2) pairs, batch 64, 1 stream", "scorer_training_seconds": train_s}
+    for name, prec, use in (("plain_fp64", A.PRECISION_FP64, False), ("mixed", A.PRECISION_MIXED, False),
+                            ("mixed_learned", A.PRECISION_MIXED, True)):
+        tot_s, tot_n, cert = 0.0, 0, True
+        for k in range(4):
+            wall, r, c = _solve_timed(pair(200 + k), prec, sc if use else None, 64, 1, args.ttg_limit)
+            tot_s += wall
+            tot_n += r.nodes_processed
+            cert = cert and c
+        pairs[name] = {"seconds": tot_s, "nodes": tot_n, "certified": cert}
+    out["graph_pairs"] = pairs
     return out
 
 
