@@ -163,13 +163,17 @@ __device__ bool int_hungarian_warp(const IHW& w, int m, const int* cost, int shi
     bool rows_ok = true;
     for (int i = lane + 1; i <= k; i += 32) {
         const int rb = w.rowb[i];
-        int best = kIntInf;
+        int best = kIntInf, barg = 0;
         for (int j = 1; j <= k; ++j) {
             const int c = cost[rb + w.cols[j - 1]];
-            if (c < kIntInf) best = min(best, c - w.pvs[j]);
+            if (c < kIntInf) {
+                const int rc = c - w.pvs[j];
+                if (rc < best) { best = rc; barg = j; }
+            }
         }
         if (best >= kIntInf) rows_ok = false;
         w.u[i] = best;
+        w.pinv[i - 1] = barg;   // a tight column of row i (pinv is free during the call)
         w.rmatch[i] = 0;
     }
     if (!__all_sync(kFull, rows_ok)) return false;
@@ -194,6 +198,31 @@ __device__ bool int_hungarian_warp(const IHW& w, int m, const int* cost, int shi
         }
     }
     __syncwarp();
+    // greedy tight matching: every row still free claims its tight column, the
+    // lowest row wins a contested free column (deterministic); the partial
+    // matching is consistent with the potentials, so only the losers need paths
+    {
+        int* claim = w.pi;   // per compacted column; pi is rewritten at the end
+#pragma unroll
+        for (int t = 0; t < CPL; ++t)
+            if (valid[t]) claim[lane + 32 * t] = pj[t] ? 0 : 0x7fffffff;
+        __syncwarp();
+        for (int i = lane + 1; i <= k; i += 32)
+            if (!w.rmatch[i]) atomicMin(&claim[w.pinv[i - 1] - 1], i);
+        __syncwarp();
+#pragma unroll
+        for (int t = 0; t < CPL; ++t) {
+            if (!valid[t] || pj[t]) continue;
+            const int r = claim[lane + 32 * t];
+            if (r != 0x7fffffff) {
+                pj[t] = r;
+                ur[t] = w.u[r];
+                rbr[t] = w.rowb[r];
+                w.rmatch[r] = 1;
+            }
+        }
+        __syncwarp();
+    }
     bool feasible = true;
     for (int i = 1; i <= k && feasible; ++i) {
         if (w.rmatch[i]) continue;
