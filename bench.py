@@ -28,11 +28,15 @@ sys.path.insert(0, ROOT)
 METRIC = "time to certified 1e-6 gap & B&B nodes/s: batched+learned vs plain, 1 GB300"
 
 WORKLOADS = {
-    # name: (instance builder, order, nodes per batch, algorithm, line search)
-    "birkhoff_gnp36": dict(order=36, nodes=256, alg=1, ls=4, iters=100),
-    "birkhoff_regular120": dict(order=120, nodes=256, alg=1, ls=4, iters=20),
+    # name: instance family and size, nodes per batch, algorithm, line search, iterations per launch
+    "birkhoff_gnp36": dict(kind="birkhoff", order=36, nodes=256, alg=1, ls=4, iters=100),
+    "birkhoff_regular120": dict(kind="birkhoff", order=120, nodes=256, alg=1, ls=4, iters=20),
     # config 5 shape (10-regular, B = P A P'); FP64 only: the mixed path stops at order 256
-    "birkhoff_regular400": dict(order=400, nodes=152, alg=1, ls=4, iters=5),
+    "birkhoff_regular400": dict(kind="birkhoff", order=400, nodes=152, alg=1, ls=4, iters=5),
+    # config 1 (box BQP, n = 64, 1024-node batches) and config 3 (cardinality portfolio,
+    # 100 assets, 64 nodes per launch): Frank-Wolfe, FP64
+    "box_qp64": dict(kind="box", n=64, nodes=1024, alg=0, ls=4, iters=200),
+    "portfolio100": dict(kind="portfolio", n=200, nodes=64, alg=0, ls=4, iters=500),
 }
 
 
@@ -52,17 +56,32 @@ def load_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
+def workload_flags(name, n):
+    """Integer flags of the workload's variables (the portfolio's z only)."""
+    flags = np.ones(n, np.uint8)
+    if WORKLOADS[name]["kind"] == "portfolio":
+        flags[: n // 2] = 0
+    return flags
+
+
 def make_workload(name, nodes, rank):
     from gpuboscia_gb300 import instances
     w = WORKLOADS[name]
-    order = w["order"]
-    if name.startswith("birkhoff_gnp"):
-        inst = instances.birkhoff_gnp(order=order)
-    elif order == 400:
-        inst = instances.birkhoff_regular_isomorphic(order=order)
+    if w["kind"] == "box":
+        inst = instances.box_qp(n=w["n"])
+        lb, ub = instances.box_node_batch(w["n"], nodes, seed=4242 + rank)
+    elif w["kind"] == "portfolio":
+        inst = instances.portfolio(assets=w["n"] // 2)
+        lb, ub = instances.portfolio_node_batch(w["n"] // 2, 10, nodes, seed=4242 + rank)
     else:
-        inst = instances.birkhoff_regular_perturbed(order=order)
-    lb, ub = instances.birkhoff_node_batch(order, nodes, seed=4242 + rank)
+        order = w["order"]
+        if name.startswith("birkhoff_gnp"):
+            inst = instances.birkhoff_gnp(order=order)
+        elif order == 400:
+            inst = instances.birkhoff_regular_isomorphic(order=order)
+        else:
+            inst = instances.birkhoff_regular_perturbed(order=order)
+        lb, ub = instances.birkhoff_node_batch(order, nodes, seed=4242 + rank)
     rng = np.random.Generator(np.random.PCG64(77 + rank))
     depth = rng.integers(0, 13, nodes)
     eps = np.maximum(1e-6, 1e-3 * 0.8 ** depth)
@@ -117,13 +136,13 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(inst, lb, ub, eps, alg_kind, ls, iters, budget_s=12.0):
+def cpu_sample(inst, lb, ub, eps, alg_kind, ls, iters, budget_s=12.0, flags=None):
     """The oracle on the machine's host cores over a bounded sample of the batch."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle as O
     threads = os.cpu_count() or 1
     n = lb.shape[1]
-    flags = np.ones(n, np.uint8)
+    flags = np.ones(n, np.uint8) if flags is None else flags
     alg = O.algorithm(alg_kind, ls)
     count = min(len(lb), max(threads, 8))
     t0 = time.perf_counter()
@@ -148,10 +167,12 @@ def run_reference(args, rank, world):
     inst, lb, ub, eps = make_workload(args.workload, args.nodes, 0)
     w = WORKLOADS[args.workload]
     for _ in range(args.warmup):
-        cpu_sample(inst, lb, ub, eps, w["alg"], w["ls"], args.iters, budget_s=0.0)
+        cpu_sample(inst, lb, ub, eps, w["alg"], w["ls"], args.iters, budget_s=0.0,
+                   flags=workload_flags(args.workload, lb.shape[1]))
     vals, times = [], []
     for _ in range(args.steps):
-        v, threads, done, dt = cpu_sample(inst, lb, ub, eps, w["alg"], w["ls"], args.iters, budget_s=args.ref_budget)
+        v, threads, done, dt = cpu_sample(inst, lb, ub, eps, w["alg"], w["ls"], args.iters, budget_s=args.ref_budget,
+                                          flags=workload_flags(args.workload, lb.shape[1]))
         vals.append(v)
         times.append(dt)
     value = statistics.mean(vals)
@@ -167,10 +188,15 @@ def run_reference(args, rank, world):
 
 def config_dict(args):
     w = WORKLOADS[args.workload]
-    return {"workload": args.workload, "order": w["order"], "variables": w["order"] ** 2,
-            "nodes_per_batch": args.nodes, "max_iters_per_dispatch": args.iters,
-            "algorithm": "DICG", "line_search": "quadratic_exact",
-            "precision": args.precision, "l2": "flushed between timed steps (256 MiB write)"}
+    d = {"workload": args.workload}
+    if w["kind"] == "birkhoff":
+        d.update(order=w["order"], variables=w["order"] ** 2)
+    else:
+        d.update(variables=w["n"])
+    d.update({"nodes_per_batch": args.nodes, "max_iters_per_dispatch": args.iters,
+              "algorithm": "DICG" if w["alg"] == 1 else "Frank-Wolfe", "line_search": "quadratic_exact",
+              "precision": args.precision, "l2": "flushed between timed steps (256 MiB write)"})
+    return d
 
 
 def time_plain(args, inst, lb, x0, d_lb, d_ub, d_eps, d_flags, flush, w, stream):
@@ -250,12 +276,15 @@ def time_to_gap(args, inst):
     sc = scorer.Scorer(32, seed=0)
     sc.train(data, epochs=400, lr=3e-3)
     train_s = time.perf_counter() - t0
-    pairs = {"instances": "4 held-out G(9,1/2) pairs, batch 64, 1 stream", "scorer_training_seconds": train_s}
-    for name, prec, use in (("plain_fp64", A.PRECISION_FP64, False), ("mixed", A.PRECISION_MIXED, False),
-                            ("mixed_learned", A.PRECISION_MIXED, True)):
+    pairs = {"instances": "4 held-out G(9,1/2) pairs; batch 64 x 1 stream unless named",
+             "scorer_training_seconds": train_s}
+    for name, prec, use, batch, streams in (("plain_fp64", A.PRECISION_FP64, False, 64, 1),
+                                            ("mixed", A.PRECISION_MIXED, False, 64, 1),
+                                            ("mixed_learned", A.PRECISION_MIXED, True, 64, 1),
+                                            ("full_stack_256x4", A.PRECISION_MIXED, True, 256, 4)):
         tot_s, tot_n, cert = 0.0, 0, True
         for k in range(4):
-            wall, r, c = _solve_timed(pair(200 + k), prec, sc if use else None, 64, 1, args.ttg_limit)
+            wall, r, c = _solve_timed(pair(200 + k), prec, sc if use else None, batch, streams, args.ttg_limit)
             tot_s += wall
             tot_n += r.nodes_processed
             cert = cert and c
@@ -273,13 +302,14 @@ def run_gpu(args, rank, world):
     dev = torch.device("cuda")
     inst, lb, ub, eps = make_workload(args.workload, args.nodes, rank)
     w = WORKLOADS[args.workload]
-    order = w["order"]
+    birkhoff = w["kind"] == "birkhoff"
+    order = w.get("order", 0)
     N, n = lb.shape
     prec = A.PRECISION_MIXED if args.precision == "mixed" else A.PRECISION_FP64
     alg = A.Algorithm(w["alg"], w["ls"], 4, 1e-10, 1e-14, prec)
     T = lambda a, t=None: torch.from_numpy(np.ascontiguousarray(a if t is None else np.asarray(a, t))).to(dev)
     d_lb, d_ub, d_eps = T(lb), T(ub), T(eps)
-    d_flags = T(np.ones(n), np.uint8)
+    d_flags = T(workload_flags(args.workload, n), np.uint8)
     x0 = d_lb.clone()
     x = torch.empty_like(x0)
     it = torch.zeros(N, dtype=torch.int32, device=dev)
@@ -365,22 +395,33 @@ def run_gpu(args, rank, world):
     e2e_value = N * args.steps * world / float(e2e_local.item())
 
     plain = None
-    if args.plain_steps > 0 and prec != A.PRECISION_FP64:
+    if args.plain_steps > 0 and prec != A.PRECISION_FP64 and birkhoff:
         plain = time_plain(args, inst, lb, x0, d_lb, d_ub, d_eps, d_flags, flush, w, stream)
-    ttg = time_to_gap(args, inst) if rank == 0 and args.ttg_limit > 0 else None
+    ttg = time_to_gap(args, inst) if rank == 0 and args.ttg_limit > 0 and birkhoff else None
     if rank != 0:
         return
     hbm_peak, bf16_peak, peak_kind = load_peaks()
     grads = node_iters + N  # iterations plus the final certificate gradient of each node
-    flops = grads * 8.0 * order ** 3
-    achieved_tf = flops / (kernel_ms / 1000.0) / 1e12
-    roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": bf16_peak, "unit": "TFLOP/s",
-                "frac": achieved_tf / bf16_peak, "traffic": (TRAFFIC_PER_NODE[(args.workload, args.precision)] * N
-                            if (args.workload, args.precision) in TRAFFIC_PER_NODE else None),
-                "peak_kind": peak_kind,
-                "kernel": "relax_kernel<GRAPH_MATCHING,BIRKHOFF>",
-                "work": f"{grads} gradients x 8*{order}^3 flop per launch"}
-    cpu_v, cores, done, dt = cpu_sample(inst, lb, ub, eps, w["alg"], w["ls"], args.iters, budget_s=args.cpu_budget)
+    if birkhoff:
+        flops = grads * 8.0 * order ** 3
+        achieved_tf = flops / (kernel_ms / 1000.0) / 1e12
+        roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": bf16_peak, "unit": "TFLOP/s",
+                    "frac": achieved_tf / bf16_peak,
+                    "traffic": (TRAFFIC_PER_NODE[(args.workload, args.precision)] * N
+                                if (args.workload, args.precision) in TRAFFIC_PER_NODE else None),
+                    "peak_kind": peak_kind,
+                    "kernel": "relax_kernel<GRAPH_MATCHING,BIRKHOFF>",
+                    "work": f"{grads} gradients x 8*{order}^3 flop per launch"}
+    else:
+        # the box / simplex LMO phase: g, lb, ub in and v out, 32 bytes per variable per call
+        lmo_bytes = grads * 32.0 * n
+        achieved_gbs = lmo_bytes / (kernel_ms / 1000.0) / 1e9
+        roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": achieved_gbs / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                    "kernel": "relax_kernel<DENSE_QUADRATIC,%s>" % ("BOX" if w["kind"] == "box" else "CARDINALITY"),
+                    "work": f"{grads} LMO calls x 32*{n} bytes per launch"}
+    cpu_v, cores, done, dt = cpu_sample(inst, lb, ub, eps, w["alg"], w["ls"], args.iters, budget_s=args.cpu_budget,
+                                        flags=workload_flags(args.workload, n))
     line = {"metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == A.PRECISION_FP64 else "bf16+f64",
@@ -390,7 +431,8 @@ def run_gpu(args, rank, world):
             "cpu_baseline": {"value": cpu_v, "unit": "nodes/s", "cores": cores, "kind": "port",
                              "sample": f"{done} of {N} nodes of the same batch, {args.iters} iterations max, "
                                        f"{dt:.1f} s"},
-            "clocks": clk.summary(), "gpu_launches": 2 * args.steps,   # sparse_build_kernel + relax_kernel
+            # relax_kernel, plus sparse_build_kernel for graph matching
+            "clocks": clk.summary(), "gpu_launches": (2 if birkhoff else 1) * args.steps,
             "node_iterations_per_step": node_iters,
             "plain_fp64": plain, "time_to_gap": ttg,
             "status_counts": {str(s): int((statuses == s).sum()) for s in np.unique(statuses)}}
@@ -415,6 +457,8 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=8.0)
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
+    if w["kind"] != "birkhoff":
+        args.precision = "fp64"   # mixed precision covers graph matching over Birkhoff only
     args.nodes = args.nodes or w["nodes"]
     args.iters = args.iters or w["iters"]
     world = int(os.environ.get("WORLD_SIZE", "1"))
