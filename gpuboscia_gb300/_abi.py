@@ -118,6 +118,7 @@ class Settings(C.Structure):
         ("root_initial_point", C.c_void_p),
         ("branch_k", C.c_int), ("use_cuda_graph", C.c_int),
         ("scorer", C.c_void_p), ("autotune", C.c_int),
+        ("device_frontier", C.c_int), ("frontier_capacity", C.c_int),
     ]
 
 
@@ -151,6 +152,8 @@ def default_settings() -> Settings:
     s.use_cuda_graph = 1
     s.scorer = None
     s.autotune = 1
+    s.device_frontier = 0
+    s.frontier_capacity = 0
     return s
 
 

@@ -198,6 +198,8 @@ class Settings:
     use_cuda_graph: int = 1
     scorer: Optional[object] = None   # gpuboscia_gb300.scorer.Scorer: learned branching
     autotune: int = 1
+    device_frontier: int = 0        # open nodes stay in HBM; each search round runs on the device
+    frontier_capacity: int = 0      # pool size in nodes (0: automatic)
 
     def algorithm_c(self) -> A.Algorithm:
         return A.Algorithm(self.algorithm, self.line_search, self.secant_iters, self.secant_tol,
@@ -207,7 +209,7 @@ class Settings:
         s = A.Settings()
         for f in ("gpu_batch_size", "num_streams", "gpu_max_iters", "gpu_eps", "gpu_eps_decay", "gpu_eps_min",
                   "integer_tol", "abs_gap_tol", "rel_gap_tol", "time_limit_seconds", "natural_lower_bound",
-                  "branch_k", "use_cuda_graph", "autotune"):
+                  "branch_k", "use_cuda_graph", "autotune", "device_frontier", "frontier_capacity"):
             setattr(s, f, getattr(self, f))
         s.algorithm = self.algorithm_c()
         s.root_initial_point = keep.ptr(_f64(self.root_initial_point) if self.root_initial_point is not None

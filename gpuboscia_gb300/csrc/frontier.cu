@@ -1,0 +1,763 @@
+// frontier.cu -- branch and bound with the frontier in device memory.
+//
+// The host engine (device_resident_solver.h; reference loop
+// device_resident_solver.cuh:1570-2067) copies every batch of node vectors
+// host -> device and every result back, and branches on the host. Here the
+// open nodes live in HBM and a round of the search is a fixed sequence of
+// kernels on one stream:
+//
+//   select   pop the best min(B, live) nodes (the frontier is kept sorted by
+//            (bound, id), so this is its head)
+//   gather   copy their bounds / start points into the relaxation batch
+//   relax    the node-relaxation kernel, batch size read from device memory
+//   vars     branch_pow2's variables per node: the k most fractional
+//            (branching.h:24-65), ties to the lowest variable index
+//   decide   in batch order: incumbent (prefix minimum of the candidates'
+//            values, strict improvement as AtomicIncumbent::try_update),
+//            certified bound, pruning, continuation of unconverged integral
+//            nodes, child ids and sorted frontier keys
+//            (process_completed_batch, device_resident_solver.cuh:1865-2007)
+//   expand   write the children (2^k' per branched node: bit b of the child
+//            index sets lb = ceil(x) or ub = floor(x), branching.h:80-118)
+//   merge    merge the sorted children into the rest of the frontier, drop
+//            what the incumbent prunes and recycle its pool slots
+//   status   live bound, termination (frontier empty, or the certified gap
+//            within tolerance, gap_utils.h:44-52)
+//
+// The sequence is captured once into a CUDA graph of R rounds and replayed;
+// the host reads a 64-byte control block after every replay (time limit,
+// completion). Kernels of a finished search return at once. Nothing waits on
+// another CTA: every round is ordered by the stream alone.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/gpuboscia/gap_utils.h"
+#include "relax.cuh"
+
+namespace gbx {
+namespace {
+
+constexpr int kMaxBatch = 1024;    // nodes per round: one decide CTA
+constexpr int kMaxK = 8;           // branch_pow2 variables per node on this path
+constexpr int kEpsDepths = 4096;   // node tolerance by depth (deeper nodes use the last)
+constexpr int kRoundsPerReplay = 4;
+
+enum Why { RUNNING = 0, EXHAUSTED = 1, TOLERANCE = 2, CAPACITY = 3 };
+
+// device control block (read by the host after every replay)
+struct FState {
+    double incumbent;
+    double bound;          // live bound after the last round
+    long long nodes_done;
+    int done;
+    int why;
+    int cur;               // frontier buffer holding the live entries
+    int n_front;           // live entries (sorted by bound, id)
+    int n_batch;           // nodes popped this round
+    int n_new;             // entries pushed this round
+    int free_top;          // free pool slots on the stack
+    int next_id;
+    int inc_src;           // batch index whose best vertex is the new incumbent (-1)
+    int has_inc;
+    int rounds;
+    int pad;
+};
+
+struct Tree {
+    int n, cap, B, k, n_int, id_stride;
+    double abs_tol, rel_tol, int_tol;
+    // pool of open nodes [cap * n] and their records [cap]
+    double* plb;
+    double* pub;
+    double* px;
+    double* mbound;
+    int* mdepth;
+    int* mid;
+    int* miters;
+    unsigned char* mhasx;
+    // frontier, sorted by (bound, id), double-buffered for the merge
+    double* fkey[2];
+    int* fid[2];
+    int* fslot[2];
+    int* free_stack;       // [cap]
+    // relaxation batch [B * n] / [B]
+    double* x;
+    double* lb;
+    double* ub;
+    double* eps;
+    double* gap;
+    double* value;
+    double* best;
+    double* bvv;
+    int* it;
+    unsigned char* st;
+    double* bbound;
+    int* bdepth;
+    int* bid;
+    int* bvars;            // [B * kMaxK]
+    int* bnv;              // [B]
+    // entries pushed this round, sorted by (bound, id) [B << k]
+    double* ekey;
+    int* eid;
+    int* eslot;
+    int* esrc;
+    int* emask;            // child index, -1: continuation of the node itself
+    const int* int_vars;   // [n_int]
+    const double* eps_tab; // [kEpsDepths]
+    double* inc_x;         // [n]
+    FState* S;
+};
+
+__device__ inline bool key_less(double ka, int ia, double kb, int ib) {
+    return ka < kb || (ka == kb && ia < ib);
+}
+
+// number of entries of the sorted (key, id) list strictly before (k, i)
+__device__ inline int count_before(const double* key, const int* id, int len, double k, int i) {
+    int lo = 0, hi = len;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (key_less(key[mid], id[mid], k, i)) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// first index whose key is >= v
+__device__ inline int first_at_least(const double* key, int len, double v) {
+    int lo = 0, hi = len;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (key[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ inline double certified_lower(double inherited, double value, double gap) {
+    if (!isfinite(value) || !isfinite(gap) || gap < 0.0) return inherited;
+    return fmax(inherited, value - gap);
+}
+
+__device__ inline bool within_tolerance(double bound, double inc, double abs_tol, double rel_tol) {
+    if (!isfinite(bound) || !isfinite(inc)) return false;
+    const double a = fabs(inc - bound);
+    if (a <= abs_tol) return true;
+    const double scale = fmin(fabs(bound), fabs(inc));
+    if (scale == 0.0) return false;
+    return (inc - bound) / scale <= rel_tol;
+}
+
+__global__ void select_kernel(Tree T) {
+    FState* S = T.S;
+    S->n_new = 0;
+    S->n_batch = S->done ? 0 : min(T.B, S->n_front);
+}
+
+// one CTA per batch node
+__global__ void __launch_bounds__(256) gather_kernel(Tree T) {
+    const FState* S = T.S;
+    const int i = blockIdx.x;
+    if (i >= S->n_batch) return;
+    const int slot = T.fslot[S->cur][i];
+    const size_t n = T.n, src = (size_t)slot * n, dst = (size_t)i * n;
+    const bool hx = T.mhasx[slot] != 0;
+    for (size_t j = threadIdx.x; j < n; j += blockDim.x) {
+        const double l = T.plb[src + j];
+        T.lb[dst + j] = l;
+        T.ub[dst + j] = T.pub[src + j];
+        T.x[dst + j] = hx ? T.px[src + j] : l;
+    }
+    if (threadIdx.x == 0) {
+        const int d = T.mdepth[slot];
+        T.eps[i] = T.eps_tab[min(d, kEpsDepths - 1)];
+        T.it[i] = T.miters[slot];
+        T.st[i] = hx ? GBX_NODE_INITIAL_POINT_SUPPLIED : 0;
+        T.bbound[i] = T.mbound[slot];
+        T.bdepth[i] = d;
+        T.bid[i] = T.mid[slot];
+        // the node now lives in the batch; its slot goes back to the pool
+        T.free_stack[S->free_top + i] = slot;
+    }
+}
+
+// branch_pow2's variables: up to k integer variables with fractional distance
+// above the tolerance, most fractional first, ties to the lower index
+__global__ void __launch_bounds__(256) vars_kernel(Tree T) {
+    const FState* S = T.S;
+    const int i = blockIdx.x;
+    if (i >= S->n_batch) return;
+    __shared__ double s_d[8];
+    __shared__ int s_j[8];
+    __shared__ int s_pick[kMaxK];
+    __shared__ int s_count;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (T.st[i] >= GBX_NODE_INTEGRAL_UNCONVERGED) {
+        if (tid == 0) T.bnv[i] = 0;
+        return;
+    }
+    const double* x = T.x + (size_t)i * T.n;
+    if (tid == 0) s_count = 0;
+    __syncthreads();
+    for (int r = 0; r < T.k; ++r) {
+        double bd = -1.0;
+        int bj = INT_MAX;
+        for (int q = tid; q < T.n_int; q += blockDim.x) {
+            const int j = T.int_vars[q];
+            bool taken = false;
+            for (int t = 0; t < r; ++t) taken = taken || s_pick[t] == j;
+            if (taken) continue;
+            const double v = x[j];
+            const double fr = v - floor(v);
+            const double d = fmin(fr, 1.0 - fr);
+            if (!(d > T.int_tol)) continue;
+            if (d > bd || (d == bd && j < bj)) { bd = d; bj = j; }
+        }
+        for (int o = 16; o; o >>= 1) {
+            const double od = __shfl_xor_sync(0xffffffffu, bd, o);
+            const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+            if (od > bd || (od == bd && oj < bj)) { bd = od; bj = oj; }
+        }
+        if (lane == 0) { s_d[w] = bd; s_j[w] = bj; }
+        __syncthreads();
+        if (tid == 0) {
+            double d = s_d[0];
+            int j = s_j[0];
+            for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
+                if (s_d[q] > d || (s_d[q] == d && s_j[q] < j)) { d = s_d[q]; j = s_j[q]; }
+            if (j != INT_MAX && d > T.int_tol) s_pick[s_count++] = j;
+        }
+        __syncthreads();
+        if (s_count <= r) break;   // no further fractional variable
+    }
+    if (tid < s_count) T.bvars[i * kMaxK + tid] = s_pick[tid];
+    if (tid == 0) T.bnv[i] = s_count;
+}
+
+// block-wide inclusive scans over kMaxBatch threads
+__device__ double block_scan_min(double v, double* wbuf) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        const double u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v = fmin(v, u);
+    }
+    if (lane == 31) wbuf[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        double t = wbuf[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const double u = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t = fmin(t, u);
+        }
+        wbuf[lane] = t;
+    }
+    __syncthreads();
+    if (w > 0) v = fmin(v, wbuf[w - 1]);
+    __syncthreads();
+    return v;
+}
+
+__device__ int block_scan_sum(int v, int* wbuf, int* total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    if (lane == 31) wbuf[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int t = wbuf[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += u;
+        }
+        wbuf[lane] = t;
+    }
+    __syncthreads();
+    if (w > 0) v += wbuf[w - 1];
+    *total = wbuf[31];
+    __syncthreads();
+    return v;   // inclusive
+}
+
+// one CTA of kMaxBatch threads; thread i owns batch node i
+__global__ void __launch_bounds__(kMaxBatch) decide_kernel(Tree T) {
+    FState* S = T.S;
+    const int N = S->n_batch;
+    if (N == 0) return;
+    __shared__ double s_key[kMaxBatch];
+    __shared__ int s_first[kMaxBatch];
+    __shared__ int s_node[kMaxBatch];
+    __shared__ int s_cnt[kMaxBatch];
+    __shared__ double s_lower[kMaxBatch];
+    __shared__ double wd[32];
+    __shared__ int wi[32];
+    __shared__ int s_src;
+    const int i = threadIdx.x;
+    const bool real = i < N;
+    const double inc0 = S->incumbent;
+    const double kInfD = __longlong_as_double(0x7ff0000000000000ll);
+
+    // incumbent after node i (AtomicIncumbent::try_update in batch order)
+    double cand = kInfD;
+    if (real) {
+        const double v = T.bvv[i];
+        if (v < 1e299 && isfinite(v)) cand = v;
+    }
+    const double inc_i = fmin(inc0, block_scan_min(cand, wd));
+    if (i == kMaxBatch - 1) wd[0] = inc_i;   // reuse: final incumbent
+    if (i == 0) s_src = INT_MAX;
+    __syncthreads();
+    const double inc_final = wd[0];
+    if (real && inc_final < inc0 && cand == inc_final) atomicMin(&s_src, i);
+
+    // per-node decision
+    int cnt = 0, branched = 0, first = INT_MAX;
+    double lower = kInfD;
+    int status = 0, nv = 0;
+    bool cont = false;
+    if (real) {
+        status = T.st[i];
+        const double gap = T.gap[i];
+        if (status != GBX_NODE_INFEASIBLE) {
+            lower = certified_lower(T.bbound[i], T.value[i], gap);
+            const bool certified = isfinite(gap) && gap >= 0.0 && gap < T.eps[i];
+            if (lower < inc_i) {
+                if (status >= GBX_NODE_INTEGRAL_UNCONVERGED) {
+                    cont = !certified;
+                } else {
+                    nv = T.bnv[i];
+                }
+            }
+        }
+        cnt = cont ? 1 : (nv > 0 ? 1 << nv : 0);
+        branched = nv > 0 ? 1 : 0;
+    }
+    int n_branched = 0;
+    const int b_incl = block_scan_sum(branched, wi, &n_branched);
+    const int id_base = S->next_id + (b_incl - branched) * T.id_stride;
+    int n_cont = 0;
+    block_scan_sum(cont ? 1 : 0, wi, &n_cont);
+    if (real) first = cont ? T.bid[i] : id_base;
+    // groups sorted by (bound, first id); a group's ids are consecutive, so the
+    // concatenation is sorted by (bound, id)
+    s_key[i] = cnt ? lower : kInfD;
+    s_first[i] = cnt ? first : INT_MAX;
+    s_node[i] = i;
+    s_cnt[i] = cnt;
+    s_lower[i] = lower;
+    __syncthreads();
+    for (int size = 2; size <= kMaxBatch; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            const int j = i ^ stride;
+            if (j > i) {
+                const bool up = (i & size) == 0;
+                const bool gt = key_less(s_key[j], s_first[j], s_key[i], s_first[i]);
+                if (gt == up) {
+                    const double tk = s_key[i]; s_key[i] = s_key[j]; s_key[j] = tk;
+                    const int tf = s_first[i]; s_first[i] = s_first[j]; s_first[j] = tf;
+                    const int tn = s_node[i]; s_node[i] = s_node[j]; s_node[j] = tn;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    const int node = s_node[i];
+    const int gcnt = (node < N) ? s_cnt[node] : 0;
+    int E = 0;
+    const int off = block_scan_sum(gcnt, wi, &E) - gcnt;
+    const int top = S->free_top + N;   // the batch's slots were returned by gather
+    if (E > top) {
+        if (i == 0) { S->done = 1; S->why = CAPACITY; }
+        return;
+    }
+    if (gcnt) {
+        const int g = node;
+        const bool gc = T.st[g] >= GBX_NODE_INTEGRAL_UNCONVERGED;   // continuation
+        const double lo = s_lower[g];
+        const int depth = T.bdepth[g];
+        for (int c = 0; c < gcnt; ++c) {
+            const int p = off + c;
+            const int slot = T.free_stack[top - 1 - p];
+            const int id = s_first[i] + (gc ? 0 : c);
+            T.ekey[p] = lo;
+            T.eid[p] = id;
+            T.eslot[p] = slot;
+            T.esrc[p] = g;
+            T.emask[p] = gc ? -1 : c;
+            T.mbound[slot] = lo;
+            T.mdepth[slot] = gc ? depth : depth + 1;
+            T.mid[slot] = id;
+            T.miters[slot] = gc ? T.it[g] : 0;
+            T.mhasx[slot] = gc ? 1 : 0;
+        }
+    }
+    if (i == 0) {
+        S->free_top = top - E;
+        S->n_new = E;
+        S->next_id += n_branched * T.id_stride;
+        S->nodes_done += N - n_cont;
+        if (s_src != INT_MAX) {
+            S->incumbent = inc_final;
+            S->inc_src = s_src;
+            S->has_inc = 1;
+        } else {
+            S->inc_src = -1;
+        }
+    }
+}
+
+// children / continuations into their pool slots, and the incumbent's x
+__global__ void __launch_bounds__(256) expand_kernel(Tree T) {
+    const FState* S = T.S;
+    if (S->done) return;
+    const int E = S->n_new;
+    const size_t n = T.n;
+    __shared__ int s_vars[kMaxK];
+    for (int p = blockIdx.x; p <= E; p += gridDim.x) {
+        if (p == E) {
+            const int src = S->inc_src;
+            if (src < 0) break;
+            for (size_t j = threadIdx.x; j < n; j += blockDim.x) T.inc_x[j] = T.best[(size_t)src * n + j];
+            break;
+        }
+        const int slot = T.eslot[p], g = T.esrc[p], mask = T.emask[p];
+        const int nv = mask < 0 ? 0 : T.bnv[g];
+        __syncthreads();
+        if ((int)threadIdx.x < nv) s_vars[threadIdx.x] = T.bvars[g * kMaxK + threadIdx.x];
+        __syncthreads();
+        const size_t src = (size_t)g * n, dst = (size_t)slot * n;
+        for (size_t j = threadIdx.x; j < n; j += blockDim.x) {
+            double l = T.lb[src + j], u = T.ub[src + j];
+            for (int b = 0; b < nv; ++b) {
+                if (s_vars[b] == (int)j) {
+                    const double xv = T.x[src + j];
+                    if (mask >> b & 1) l = ceil(xv);
+                    else u = floor(xv);
+                }
+            }
+            T.plb[dst + j] = l;
+            T.pub[dst + j] = u;
+            if (mask < 0) T.px[dst + j] = T.x[src + j];
+        }
+    }
+}
+
+// merge the rest of the frontier with the sorted new entries into the other
+// buffer; entries the incumbent prunes form the tail and free their slots
+__global__ void __launch_bounds__(256) merge_kernel(Tree T) {
+    FState* S = T.S;
+    if (S->done) return;
+    const int cur = S->cur, N = S->n_batch, E = S->n_new;
+    const int R = S->n_front - N;
+    const double inc = S->incumbent;
+    const double* rk = T.fkey[cur] + N;
+    const int* ri = T.fid[cur] + N;
+    const int* rs = T.fslot[cur] + N;
+    double* ok = T.fkey[cur ^ 1];
+    int* oi = T.fid[cur ^ 1];
+    int* os = T.fslot[cur ^ 1];
+    const int total = R + E;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        double k;
+        int id, slot, pos;
+        if (t < R) {
+            k = rk[t]; id = ri[t]; slot = rs[t];
+            pos = t + count_before(T.ekey, T.eid, E, k, id);
+        } else {
+            const int e = t - R;
+            k = T.ekey[e]; id = T.eid[e]; slot = T.eslot[e];
+            pos = e + count_before(rk, ri, R, k, id);
+        }
+        if (k < inc) {
+            ok[pos] = k; oi[pos] = id; os[pos] = slot;
+        } else {
+            T.free_stack[atomicAdd(&S->free_top, 1)] = slot;
+        }
+    }
+}
+
+__global__ void status_kernel(Tree T) {
+    FState* S = T.S;
+    if (S->done) return;
+    const int cur = S->cur, N = S->n_batch, E = S->n_new;
+    const int R = S->n_front - N;
+    const double inc = S->incumbent;
+    const int live = first_at_least(T.fkey[cur] + N, R, inc) + first_at_least(T.ekey, E, inc);
+    S->cur = cur ^ 1;
+    S->n_front = live;
+    S->rounds += 1;
+    S->inc_src = -1;
+    const double bound = live > 0 ? fmin(T.fkey[cur ^ 1][0], inc) : inc;
+    S->bound = bound;
+    if (live == 0) { S->done = 1; S->why = EXHAUSTED; }
+    else if (within_tolerance(bound, inc, T.abs_tol, T.rel_tol)) { S->done = 1; S->why = TOLERANCE; }
+}
+
+struct DeviceBuffers {
+    std::vector<void*> ptrs;
+    ~DeviceBuffers() { for (void* p : ptrs) cudaFree(p); }
+    template <class T>
+    T* get(size_t count, cudaError_t* e) {
+        void* p = nullptr;
+        if (*e == cudaSuccess) *e = cudaMalloc(&p, std::max<size_t>(count * sizeof(T), 16));
+        if (*e != cudaSuccess) return nullptr;
+        ptrs.push_back(p);
+        return static_cast<T*>(p);
+    }
+};
+
+}  // namespace
+
+size_t frontier_slot_bytes(int n) {
+    return 3 * (size_t)n * sizeof(double) + sizeof(double) + 3 * sizeof(int) + 1  // pool
+           + 2 * (sizeof(double) + 2 * sizeof(int)) + sizeof(int);                 // frontier, free stack
+}
+
+int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const gbx_lmo& lmo,
+                          const gbx_settings& s, const double* root_x, gbx_result* res, std::string* err) {
+    const int n = pr.n_vars, B = s.gpu_batch_size, k = s.branch_k;
+    if (B < 1 || B > kMaxBatch) { *err = "device frontier: gpu_batch_size must be in [1, 1024]"; return GBX_ERR_INVALID; }
+    if (k < 1 || k > kMaxK) { *err = "device frontier: branch_k must be in [1, 8]"; return GBX_ERR_INVALID; }
+    if (s.scorer) { *err = "device frontier: the learned scorer runs with the host frontier only"; return GBX_ERR_UNSUPPORTED; }
+    // the host engine's argument checks (its constructor)
+    if (s.gpu_max_iters <= 0) { *err = "GPU iterations, batch size and streams must be positive"; return GBX_ERR_INVALID; }
+    if (!std::isfinite(s.gpu_eps) || s.gpu_eps <= 0.0 || !std::isfinite(s.gpu_eps_min) || s.gpu_eps_min <= 0.0
+            || !std::isfinite(s.gpu_eps_decay) || s.gpu_eps_decay <= 0.0 || s.gpu_eps_decay > 1.0
+            || !std::isfinite(s.abs_gap_tol) || s.abs_gap_tol < 0.0 || !std::isfinite(s.rel_gap_tol)
+            || s.rel_gap_tol < 0.0) {
+        *err = "invalid tolerance configuration";
+        return GBX_ERR_INVALID;
+    }
+    if (std::isnan(s.time_limit_seconds) || s.time_limit_seconds <= 0.0) {
+        *err = "time limit must be positive";
+        return GBX_ERR_INVALID;
+    }
+    for (int q = 0; q < pr.n_int; ++q)
+        if (pr.int_vars[q] < 0 || pr.int_vars[q] >= n) { *err = "integer variable index out of range"; return GBX_ERR_INVALID; }
+    if (gbx_relax_workspace_bytes(&obj, &lmo, &s.algorithm, B) == 0) {
+        *err = gbx_last_error();
+        return GBX_ERR_INVALID;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t st = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{st};
+
+    // pool capacity: the caller's, else a quarter of free memory up to 2^18 nodes
+    long long cap = s.frontier_capacity;
+    const int E_max = B << k;
+    if (cap <= 0) {
+        size_t fr = 0, tot = 0;
+        e = cudaMemGetInfo(&fr, &tot);
+        if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+        cap = std::min<long long>(1 << 18, (long long)(fr / 4 / frontier_slot_bytes(n)));
+        cap = std::max<long long>(cap, (long long)E_max + B + 1);
+    }
+    if (cap < (long long)E_max + 1 || cap > (1ll << 30)) {
+        *err = "device frontier: frontier_capacity must hold at least one round's children (batch * 2^branch_k + 1)";
+        return GBX_ERR_INVALID;
+    }
+
+    DeviceBuffers D;
+    Tree T{};
+    T.n = n; T.cap = (int)cap; T.B = B; T.k = k; T.n_int = pr.n_int;
+    T.id_stride = std::max(8, 1 << k);
+    T.abs_tol = s.abs_gap_tol; T.rel_tol = s.rel_gap_tol; T.int_tol = s.integer_tol;
+    const size_t C = (size_t)cap, Nn = (size_t)n;
+    T.plb = D.get<double>(C * Nn, &e);
+    T.pub = D.get<double>(C * Nn, &e);
+    T.px = D.get<double>(C * Nn, &e);
+    T.mbound = D.get<double>(C, &e);
+    T.mdepth = D.get<int>(C, &e);
+    T.mid = D.get<int>(C, &e);
+    T.miters = D.get<int>(C, &e);
+    T.mhasx = D.get<unsigned char>(C, &e);
+    for (int b = 0; b < 2; ++b) {
+        T.fkey[b] = D.get<double>(C, &e);
+        T.fid[b] = D.get<int>(C, &e);
+        T.fslot[b] = D.get<int>(C, &e);
+    }
+    T.free_stack = D.get<int>(C, &e);
+    const size_t BN = (size_t)B * Nn;
+    T.x = D.get<double>(BN, &e);
+    T.lb = D.get<double>(BN, &e);
+    T.ub = D.get<double>(BN, &e);
+    T.best = D.get<double>(BN, &e);
+    T.eps = D.get<double>(B, &e);
+    T.gap = D.get<double>(B, &e);
+    T.value = D.get<double>(B, &e);
+    T.bvv = D.get<double>(B, &e);
+    T.it = D.get<int>(B, &e);
+    T.st = D.get<unsigned char>(B, &e);
+    T.bbound = D.get<double>(B, &e);
+    T.bdepth = D.get<int>(B, &e);
+    T.bid = D.get<int>(B, &e);
+    T.bvars = D.get<int>((size_t)B * kMaxK, &e);
+    T.bnv = D.get<int>(B, &e);
+    T.ekey = D.get<double>(E_max, &e);
+    T.eid = D.get<int>(E_max, &e);
+    T.eslot = D.get<int>(E_max, &e);
+    T.esrc = D.get<int>(E_max, &e);
+    T.emask = D.get<int>(E_max, &e);
+    int* d_int_vars = D.get<int>(std::max(pr.n_int, 1), &e);
+    double* d_eps = D.get<double>(kEpsDepths, &e);
+    T.inc_x = D.get<double>(Nn, &e);
+    T.S = D.get<FState>(1, &e);
+    unsigned char* d_flags = D.get<unsigned char>(Nn, &e);
+    if (e != cudaSuccess) { *err = std::string("device frontier allocation: ") + cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    T.int_vars = d_int_vars;
+    T.eps_tab = d_eps;
+
+    // host-side initial state: the root in slot 0, every other slot free
+    std::vector<unsigned char> flags(n, 0);
+    for (int q = 0; q < pr.n_int; ++q) flags[pr.int_vars[q]] = 1;
+    std::vector<double> eps(kEpsDepths);
+    for (int d = 0; d < kEpsDepths; ++d)
+        eps[d] = gpuboscia::depth_dependent_tolerance(s.gpu_eps, s.gpu_eps_decay, s.gpu_eps_min, d);
+    std::vector<int> stack(C - 1);
+    for (size_t q = 0; q + 1 < C; ++q) stack[q] = (int)(C - 1 - q);   // slot 1 on top
+    FState S0{};
+    S0.incumbent = std::numeric_limits<double>::infinity();
+    S0.bound = s.natural_lower_bound;
+    S0.n_front = 1;
+    S0.free_top = (int)C - 1;
+    S0.next_id = 1;
+    S0.inc_src = -1;
+    const double root_bound = s.natural_lower_bound;
+    const int zero = 0;
+    const unsigned char hx = root_x ? 1 : 0;
+    auto up = [&](void* dst, const void* src, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+    };
+    up(d_flags, flags.data(), Nn);
+    up(d_int_vars, pr.int_vars, sizeof(int) * pr.n_int);
+    up(d_eps, eps.data(), sizeof(double) * kEpsDepths);
+    up(T.free_stack, stack.data(), sizeof(int) * stack.size());
+    up(T.plb, pr.lb, sizeof(double) * Nn);
+    up(T.pub, pr.ub, sizeof(double) * Nn);
+    if (root_x) up(T.px, root_x, sizeof(double) * Nn);
+    up(T.mbound, &root_bound, sizeof(double));
+    up(T.mdepth, &zero, sizeof(int));
+    up(T.mid, &zero, sizeof(int));
+    up(T.miters, &zero, sizeof(int));
+    up(T.mhasx, &hx, 1);
+    up(T.fkey[0], &root_bound, sizeof(double));
+    up(T.fid[0], &zero, sizeof(int));
+    up(T.fslot[0], &zero, sizeof(int));
+    up(T.S, &S0, sizeof(FState));
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+
+    // the relaxation launch over the batch buffers
+    Params p{};
+    p.obj = obj;
+    p.lmo = lmo;
+    p.alg = s.algorithm;
+    p.b.n_nodes = B;
+    p.b.max_iters = s.gpu_max_iters;
+    p.b.candidate_tol = s.integer_tol;
+    p.b.x = T.x; p.b.lb = T.lb; p.b.ub = T.ub; p.b.eps = T.eps;
+    p.b.iterations = T.it; p.b.status = T.st; p.b.gap = T.gap; p.b.value = T.value;
+    p.b.best_vertex = T.best; p.b.best_vertex_val = T.bvv; p.b.integer_flags = d_flags;
+    int rc = make_layout(obj, lmo, s.algorithm, B, &p.L, err);
+    if (rc) return rc;
+    const size_t wsb = workspace_bytes(p.L, B);
+    unsigned char* ws = D.get<unsigned char>(wsb, &e);
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    p.ws = reinterpret_cast<double*>(ws);
+    p.queue = p.L.persistent ? reinterpret_cast<int*>(ws + queue_offset(p.L, B)) : nullptr;
+    p.mixed = p.L.mixed_node_bytes ? ws + mixed_region_offset(p.L, B) : nullptr;
+    p.sparse = nullptr;
+    p.live_count = &T.S->n_batch;
+    if (p.L.sparse_bytes) {
+        p.sparse = ws + sparse_region_offset(p.L, B);
+        rc = launch_sparse_build(obj, p.L, p.sparse, st, err);
+        if (rc) return rc;
+    }
+
+    int dev = 0, sms = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    const int expand_grid = std::min(E_max + 1, 4 * sms);
+    const int merge_grid = 4 * sms;
+    auto round = [&]() -> int {
+        select_kernel<<<1, 1, 0, st>>>(T);
+        gather_kernel<<<B, 256, 0, st>>>(T);
+        int r = launch_relax(p, st, err);
+        if (r) return r;
+        vars_kernel<<<B, 256, 0, st>>>(T);
+        decide_kernel<<<1, kMaxBatch, 0, st>>>(T);
+        expand_kernel<<<expand_grid, 256, 0, st>>>(T);
+        merge_kernel<<<merge_grid, 256, 0, st>>>(T);
+        status_kernel<<<1, 1, 0, st>>>(T);
+        const cudaError_t le = cudaGetLastError();
+        if (le != cudaSuccess) { *err = cudaGetErrorString(le); return GBX_ERR_CUDA; }
+        return GBX_OK;
+    };
+
+    cudaGraphExec_t exec = nullptr;
+    struct ExecGuard { cudaGraphExec_t* g; ~ExecGuard() { if (*g) cudaGraphExecDestroy(*g); } } eg{&exec};
+    if (s.use_cuda_graph) {
+        cudaGraph_t g = nullptr;
+        e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
+        int crc = e == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+        for (int r = 0; r < kRoundsPerReplay && crc == GBX_OK; ++r) crc = round();
+        const cudaError_t ee = cudaStreamEndCapture(st, &g);
+        if (crc == GBX_OK && ee == cudaSuccess && g) {
+            if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) exec = nullptr;
+        }
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();   // a failed capture falls back to direct launches
+        if (!exec) err->clear();
+    }
+
+    FState* hS = nullptr;
+    e = cudaMallocHost(&hS, sizeof(FState));
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    struct HostGuard { FState* p; ~HostGuard() { cudaFreeHost(p); } } hg{hS};
+    bool timed_out = false;
+    const auto t_search = std::chrono::steady_clock::now();   // the time limit counts from here
+    for (;;) {
+        if (exec) {
+            e = cudaGraphLaunch(exec, st);
+            if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+        } else {
+            for (int r = 0; r < kRoundsPerReplay; ++r) {
+                rc = round();
+                if (rc) return rc;
+            }
+        }
+        e = cudaMemcpyAsync(hS, T.S, sizeof(FState), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+        if (hS->done) break;
+        const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_search).count();
+        if (std::isfinite(s.time_limit_seconds) && el >= s.time_limit_seconds) { timed_out = true; break; }
+    }
+    if (hS->why == CAPACITY) {
+        *err = "device frontier: pool capacity exceeded (raise frontier_capacity)";
+        return GBX_ERR_WORKSPACE;
+    }
+    res->objective = hS->incumbent;
+    res->dual_bound = hS->why == EXHAUSTED ? hS->incumbent : hS->bound;
+    res->nodes_processed = (int)hS->nodes_done;
+    res->reached_tolerance = hS->why == TOLERANCE ? 1 : 0;
+    res->reached_time_limit = timed_out ? 1 : 0;
+    res->has_incumbent = hS->has_inc;
+    if (res->x && hS->has_inc) {
+        e = cudaMemcpy(res->x, T.inc_x, sizeof(double) * Nn, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    }
+    res->elapsed_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return GBX_OK;
+}
+
+}  // namespace gbx

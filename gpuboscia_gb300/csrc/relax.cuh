@@ -62,6 +62,7 @@ struct Params {
     unsigned char* mixed;   // mixed-precision scratch
     unsigned char* sparse;  // nonzero lists of A and B (graph matching), or null
     int* queue;             // persistent grid: next-node counter (zeroed per launch), or null
+    const int* live_count;  // device-side node count (<= b.n_nodes) read at launch, or null
 };
 
 #ifdef __CUDACC__
@@ -172,6 +173,11 @@ int scorer_adam(gbx_scorer* s, const float* g, float* m, float* v, int step, flo
                 std::string* err);
 int launch_gradient_batch_f32(const gbx_objective& o, int cases, const float* x, float* g, cudaStream_t st,
                               std::string* err);
+// branch and bound with the frontier in device memory (frontier.cu); root_x
+// is the validated root start point or null
+int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const gbx_lmo& lmo,
+                          const gbx_settings& s, const double* root_x, gbx_result* res, std::string* err);
+size_t frontier_slot_bytes(int n);
 int launch_node_feasible(const gbx_lmo& l, int cases, const double* lb, const double* ub,
                          const uint8_t* flags, uint8_t* out, void* stream, std::string* err);
 

@@ -1897,8 +1897,11 @@ template <int OK, int LK, int MIX>
 __global__ void __launch_bounds__(kThreads, MIX == 1 ? 2 : 1) relax_kernel(const __grid_constant__ Params P) {
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ Scalars sh;
+    // a batch assembled on the device (frontier rounds) carries its size in
+    // device memory; the grid is sized for the largest batch
+    const int n_nodes = P.live_count ? min(*P.live_count, P.b.n_nodes) : P.b.n_nodes;
     if (!P.queue) {
-        if ((int)blockIdx.x < P.b.n_nodes) relax_node<OK, LK, MIX>(P, blockIdx.x, dsm, sh);
+        if ((int)blockIdx.x < n_nodes) relax_node<OK, LK, MIX>(P, blockIdx.x, dsm, sh);
         return;
     }
     __shared__ int next;
@@ -1907,7 +1910,7 @@ __global__ void __launch_bounds__(kThreads, MIX == 1 ? 2 : 1) relax_kernel(const
         __syncthreads();
         const int node = next;
         __syncthreads();
-        if (node >= P.b.n_nodes) return;
+        if (node >= n_nodes) return;
         relax_node<OK, LK, MIX>(P, node, dsm, sh);
         __syncthreads();
     }

@@ -174,6 +174,8 @@ void gbx_default_settings(gbx_settings* s) {
     s->use_cuda_graph = 1;
     s->scorer = nullptr;
     s->autotune = 1;
+    s->device_frontier = 0;
+    s->frontier_capacity = 0;
 }
 
 int gbx_solve(const gbx_problem* problem, const gbx_objective* obj, const gbx_lmo* lmo,
@@ -211,6 +213,14 @@ int gbx_solve(const gbx_problem* problem, const gbx_objective* obj, const gbx_lm
         }
         if (std::isnan(s->natural_lower_bound) || s->natural_lower_bound == std::numeric_limits<double>::infinity())
             throw std::invalid_argument("natural lower bound must be finite or negative infinity");
+
+        if (s->device_frontier) {
+            std::string err;
+            const int rc = gbx::solve_device_frontier(*problem, *obj, *lmo, *s, root_x.empty() ? nullptr : root_x.data(),
+                                                      res, &err);
+            if (rc) gbx::set_last_error(err);
+            return rc;
+        }
 
         DeviceResidentConfig cfg;
         cfg.gpu_batch_size = s->gpu_batch_size;

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GBX_ABI_VERSION 2
+#define GBX_ABI_VERSION 3
 
 /* ---- status codes ------------------------------------------------------ */
 enum {
@@ -308,6 +308,13 @@ typedef struct gbx_settings {
     int use_cuda_graph;       /* capture the relax launch (1) */
     const gbx_scorer* scorer; /* learned branching (NULL: most fractional) */
     int autotune;             /* time the launch shapes on the first full batch (1) */
+    /* frontier in device memory (no counterpart in the reference): open nodes
+     * stay in HBM and each round of the search (pop the best batch, relax,
+     * branch_pow2, merge the children) runs as kernels replayed from a CUDA
+     * graph; batch <= 1024, branch_k <= 8, no learned scorer, num_streams and
+     * autotune unused (a stored launch shape still applies) */
+    int device_frontier;      /* 0 */
+    int frontier_capacity;    /* open nodes the pool holds (0: a quarter of free memory, <= 2^18) */
 } gbx_settings;
 
 typedef struct gbx_result {

@@ -40,7 +40,7 @@ def test_library_exports_every_declared_symbol(lib):
     assert not missing, missing
     for f in declared_functions():
         assert hasattr(lib, f)
-    assert lib.gbx_abi_version() == 2
+    assert lib.gbx_abi_version() == 3
 
 
 _LAYOUT_C = r"""
@@ -56,7 +56,8 @@ int main(void) {
   S(gbx_node_batch) O(gbx_node_batch, x) O(gbx_node_batch, integer_flags)
   S(gbx_problem) O(gbx_problem, n_int)
   S(gbx_settings) O(gbx_settings, algorithm) O(gbx_settings, time_limit_seconds) O(gbx_settings, use_cuda_graph)
-  O(gbx_settings, scorer) O(gbx_settings, autotune)
+  O(gbx_settings, scorer) O(gbx_settings, autotune) O(gbx_settings, device_frontier)
+  O(gbx_settings, frontier_capacity)
   S(gbx_scorer) O(gbx_scorer, params) O(gbx_scorer, params_bf16)
   S(gbx_result) O(gbx_result, x)
   return 0;

@@ -1,0 +1,207 @@
+"""Branch and bound with the frontier in device memory (settings.device_frontier):
+same optima and valid certified bounds as the host-frontier solver and the
+oracle's B&B. The trees may differ where the host heap and the device's
+(bound, id) order break ties differently, so node counts are not compared
+across the two frontiers; a device run is compared with itself for
+determinism."""
+import math
+
+import numpy as np
+import pytest
+
+import _oracle as O
+from gpuboscia_gb300 import _abi as A
+from gpuboscia_gb300 import api, instances
+
+pytestmark = pytest.mark.gpu
+
+
+def _proved(r, tol=1e-6):
+    return (not r.reached_time_limit) and math.isfinite(r.objective) and r.dual_bound <= r.objective + 1e-12 \
+        and (r.objective - r.dual_bound <= tol or r.objective - r.dual_bound <= tol * abs(r.objective))
+
+
+def test_minimal_example(cuda_lib):
+    """examples/minimal.cu: min (x0-.3)^2 + (x1-.7)^2 over binaries -> x = [0, 1], f = .18."""
+    obj = api.DenseQuadraticObjective(2 * np.eye(2), np.array([-.6, -1.4]), 1.0, 1.0, .58)
+    prob = api.Problem(2, np.zeros(2), np.ones(2), [0, 1])
+    s = api.Settings(line_search=A.LS_QUADRATIC_EXACT, natural_lower_bound=0, time_limit_seconds=10,
+                     device_frontier=1)
+    r = api.solve(prob, obj, api.BoxLMO(), s)
+    assert r.x.tolist() == [0.0, 1.0]
+    assert abs(r.objective - .18) < 1e-8
+
+
+@pytest.mark.parametrize("c,lo,hi,alg,ls", [
+    ([1.3, 1.6], 0, 3, A.ALG_FRANK_WOLFE, A.LS_OPEN_LOOP),
+    ([0.7, 1.6, -0.3, 2.8], -1, 4, A.ALG_FRANK_WOLFE, A.LS_OPEN_LOOP),
+    ([0.7, 1.6, -0.3, 2.8], -1, 4, A.ALG_DICG, A.LS_SECANT),
+])
+def test_separable_ils_optimum(cuda_lib, c, lo, hi, alg, ls):
+    """tests/test_pipeline.cu:647-893: incumbent within 0.02 of the separable optimum."""
+    c = np.array(c)
+    n = len(c)
+    obj = api.ILSObjective(np.eye(n), c, float(c @ c))
+    prob = api.Problem(n, np.full(n, float(lo)), np.full(n, float(hi)), list(range(n)))
+    s = api.Settings(algorithm=alg, line_search=ls, gpu_batch_size=16, num_streams=1, gpu_max_iters=50000,
+                     gpu_eps=1e-6, device_frontier=1)
+    g = api.solve(prob, obj, api.BoxLMO(), s)
+    true = sum(min((k - ci) ** 2 for k in range(lo, hi + 1)) for ci in c)
+    assert abs(g.objective - true) < 0.02
+    assert g.dual_bound <= g.objective + 1e-12
+    assert np.array_equal(g.x, np.round(g.x)) and np.all(g.x >= lo) and np.all(g.x <= hi)
+
+
+@pytest.mark.parametrize("batch,k", [(32, 3), (7, 1), (64, 2)])
+def test_box_qp_proves_the_oracle_optimum(cuda_lib, batch, k):
+    inst = instances.box_qp(n=16, seed=21)
+    s = inst.settings
+    s.num_streams = 1
+    s.gpu_batch_size = batch
+    s.branch_k = k
+    s.gpu_max_iters = 2000
+    s.rel_gap_tol = 0.0
+    o = O.solve(inst.problem, inst.objective, inst.lmo, s)
+    s.device_frontier = 1
+    g = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert _proved(g) and _proved(o)
+    assert abs(g.objective - o.objective) <= 1e-6
+    assert g.dual_bound <= o.objective + 1e-6
+    # the incumbent is integral, in bounds, and its value is the objective
+    x = g.x
+    assert np.array_equal(x, np.round(x)) and x.min() >= 0 and x.max() <= 1
+    Q, c = inst.objective.Q, inst.objective.c
+    assert abs(0.5 * x @ Q @ x + c @ x - g.objective) <= 1e-9 * max(1.0, abs(g.objective))
+
+
+def test_deterministic(cuda_lib):
+    inst = instances.box_qp(n=16, seed=5)
+    s = inst.settings
+    s.gpu_batch_size = 16
+    s.gpu_max_iters = 2000
+    s.rel_gap_tol = 0.0
+    s.device_frontier = 1
+    a = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    b = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert a.nodes_processed == b.nodes_processed
+    assert a.objective == b.objective and a.dual_bound == b.dual_bound
+    assert np.array_equal(a.x, b.x)
+
+
+def test_graph_without_cuda_graph_replay_is_identical(cuda_lib):
+    inst = instances.box_qp(n=12, seed=9)
+    s = inst.settings
+    s.gpu_batch_size = 8
+    s.gpu_max_iters = 2000
+    s.rel_gap_tol = 0.0
+    s.device_frontier = 1
+    a = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    s.use_cuda_graph = 0
+    b = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert (a.nodes_processed, a.objective, a.dual_bound) == (b.nodes_processed, b.objective, b.dual_bound)
+    assert np.array_equal(a.x, b.x)
+
+
+def _pair(seed, order):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return instances.graph_matching(order, instances.gnp_graph(rng, order, 0.5),
+                                    instances.gnp_graph(rng, order, 0.5), f"pair{order}_{seed}")
+
+
+@pytest.mark.parametrize("precision", [A.PRECISION_FP64, A.PRECISION_MIXED])
+def test_graph_pair_same_optimum_as_host_frontier(cuda_lib, precision):
+    inst = _pair(203, 7)
+    s = inst.settings
+    s.algorithm = A.ALG_DICG
+    s.line_search = A.LS_QUADRATIC_EXACT
+    s.gpu_batch_size = 64
+    s.num_streams = 1
+    s.abs_gap_tol = 1e-6
+    s.rel_gap_tol = 1e-6
+    s.precision = precision
+    s.time_limit_seconds = 60
+    h = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    s.device_frontier = 1
+    g = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert _proved(h) and _proved(g)
+    assert abs(g.objective - h.objective) <= 1e-6
+    m = inst.lmo.order
+    P = g.x.reshape(m, m)
+    assert np.array_equal(P.sum(0), np.ones(m)) and np.array_equal(P.sum(1), np.ones(m))
+
+
+def test_isomorphic_graph_reaches_zero(cuda_lib):
+    inst = instances.birkhoff_gnp(order=8, seed=3)
+    s = inst.settings
+    s.gpu_batch_size = 16
+    s.gpu_max_iters = 200
+    s.device_frontier = 1
+    g = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert g.objective <= 1e-9
+
+
+def test_cardinality_portfolio_same_optimum(cuda_lib):
+    inst = instances.portfolio(assets=8, months=120, cardinality=3, seed=11)
+    s = inst.settings
+    s.gpu_batch_size = 32
+    s.num_streams = 1
+    s.gpu_max_iters = 3000
+    s.rel_gap_tol = 0.0
+    s.time_limit_seconds = 60
+    h = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    s.device_frontier = 1
+    g = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert _proved(h) and _proved(g)
+    assert abs(g.objective - h.objective) <= 1e-6
+
+
+def test_root_initial_point(cuda_lib):
+    obj = api.DenseQuadraticObjective(2 * np.eye(2), np.array([-.6, -1.4]), 1.0, 1.0, .58)
+    prob = api.Problem(2, np.zeros(2), np.ones(2), [0, 1])
+    s = api.Settings(line_search=A.LS_QUADRATIC_EXACT, natural_lower_bound=0, time_limit_seconds=10,
+                     device_frontier=1, root_initial_point=np.array([0.5, 0.5]))
+    r = api.solve(prob, obj, api.BoxLMO(), s)
+    assert r.x.tolist() == [0.0, 1.0]
+
+
+def test_time_limit_returns_a_valid_bound(cuda_lib):
+    inst = _pair(301, 10)
+    s = inst.settings
+    s.algorithm = A.ALG_DICG
+    s.line_search = A.LS_QUADRATIC_EXACT
+    s.gpu_batch_size = 2
+    s.abs_gap_tol = 1e-9
+    s.rel_gap_tol = 0.0
+    s.time_limit_seconds = 0.01
+    s.device_frontier = 1
+    r = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert r.reached_time_limit
+    assert r.dual_bound <= r.objective
+
+
+def test_capacity_exceeded_is_reported(cuda_lib):
+    inst = _pair(302, 9)
+    s = inst.settings
+    s.algorithm = A.ALG_DICG
+    s.line_search = A.LS_QUADRATIC_EXACT
+    s.gpu_batch_size = 4
+    s.abs_gap_tol = 1e-9
+    s.rel_gap_tol = 0.0
+    s.time_limit_seconds = 30
+    s.device_frontier = 1
+    s.frontier_capacity = 33           # one round's children (4 * 2^3) + 1
+    with pytest.raises(RuntimeError, match="capacity"):
+        api.solve(inst.problem, inst.objective, inst.lmo, s)
+
+
+def test_rejects_unsupported_settings(cuda_lib):
+    inst = instances.box_qp(n=8, seed=1)
+    s = inst.settings
+    s.device_frontier = 1
+    s.gpu_batch_size = 2048
+    with pytest.raises(ValueError, match="gpu_batch_size"):
+        api.solve(inst.problem, inst.objective, inst.lmo, s)
+    s.gpu_batch_size = 16
+    s.branch_k = 9
+    with pytest.raises(ValueError, match="branch_k"):
+        api.solve(inst.problem, inst.objective, inst.lmo, s)
