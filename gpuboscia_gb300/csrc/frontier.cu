@@ -38,7 +38,9 @@
 #include <vector>
 
 #include "../../include/gpuboscia/gap_utils.h"
+#include "features.h"
 #include "relax.cuh"
+#include "scorer_mlp.cuh"
 
 namespace gbx {
 namespace {
@@ -187,22 +189,15 @@ __global__ void __launch_bounds__(256) gather_kernel(Tree T) {
     }
 }
 
-// branch_pow2's variables: up to k integer variables with fractional distance
-// above the tolerance, most fractional first, ties to the lower index
-__global__ void __launch_bounds__(256) vars_kernel(Tree T) {
-    const FState* S = T.S;
-    const int i = blockIdx.x;
-    if (i >= S->n_batch) return;
+// branch_pow2's variables of batch node i: up to k integer variables with
+// fractional distance above the tolerance, most fractional first, ties to the
+// lower index (top_k_infeasible). Called by all threads of the CTA.
+__device__ void pick_most_fractional(const Tree& T, int i, const double* x) {
     __shared__ double s_d[8];
     __shared__ int s_j[8];
     __shared__ int s_pick[kMaxK];
     __shared__ int s_count;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    if (T.st[i] >= GBX_NODE_INTEGRAL_UNCONVERGED) {
-        if (tid == 0) T.bnv[i] = 0;
-        return;
-    }
-    const double* x = T.x + (size_t)i * T.n;
     if (tid == 0) s_count = 0;
     __syncthreads();
     for (int r = 0; r < T.k; ++r) {
@@ -238,6 +233,153 @@ __global__ void __launch_bounds__(256) vars_kernel(Tree T) {
     }
     if (tid < s_count) T.bvars[i * kMaxK + tid] = s_pick[tid];
     if (tid == 0) T.bnv[i] = s_count;
+}
+
+__global__ void __launch_bounds__(256) vars_kernel(Tree T) {
+    const FState* S = T.S;
+    const int i = blockIdx.x;
+    if (i >= S->n_batch) return;
+    if (T.st[i] >= GBX_NODE_INTEGRAL_UNCONVERGED) {
+        if (threadIdx.x == 0) T.bnv[i] = 0;
+        return;
+    }
+    pick_most_fractional(T, i, T.x + (size_t)i * T.n);
+}
+
+// Learned branching (the host's LearnedBrancher): every fractional candidate
+// of the node is scored by the MLP (BF16 weights widened to FP32 when a BF16
+// copy exists, as gbx_scorer_forward); branch_pow2 splits on the k highest
+// scores, ties to the earlier candidate. A non-finite score sends the node
+// to the most-fractional rule. Shared memory: the parameters, then the
+// permutation row / column statistics of a Birkhoff iterate.
+template <int H>
+__global__ void __launch_bounds__(256) learned_vars_kernel(Tree T, gbx_scorer sc, int order) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    __shared__ float s_z[8];
+    __shared__ int s_q[8];
+    __shared__ int s_win;
+    const FState* S = T.S;
+    const int i = blockIdx.x;
+    if (i >= S->n_batch) return;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (T.st[i] >= GBX_NODE_INTEGRAL_UNCONVERGED) {
+        if (tid == 0) T.bnv[i] = 0;
+        return;
+    }
+    const int cnt = mlp::param_count(mlp::kF, H);
+    float* prm = reinterpret_cast<float*>(dyn);
+    const bool perm = order > 0 && order * order == T.n;
+    const int m = perm ? order : 0;
+    double* rmax = reinterpret_cast<double*>(dyn + align16((size_t)cnt * sizeof(float)));
+    double* cmax = rmax + m;
+    int* rfrac = reinterpret_cast<int*>(cmax + m);
+    int* cfrac = rfrac + m;
+    int* rfree = cfrac + m;
+    for (int q = tid; q < cnt; q += blockDim.x)
+        prm[q] = sc.params_bf16 ? mlp::bf16_to_f(sc.params_bf16[q]) : sc.params[q];
+    const size_t base = (size_t)i * T.n;
+    const double* x = T.x + base;
+    const double* lb = T.lb + base;
+    const double* ub = T.ub + base;
+    for (int r = tid; r < m; r += blockDim.x) {
+        double rm = 0.0, cm = 0.0;
+        int rf = 0, cf = 0, rfr = 0;
+        for (int j = 0; j < m; ++j) {
+            const int e = r * m + j;
+            const double v = x[e];
+            rm = (rm < v) ? v : rm;
+            const double fr = v - floor(v);
+            if (((1.0 - fr) < fr ? 1.0 - fr : fr) > 1e-6) ++rf;
+            if (lb[e] < 0.5 && ub[e] >= 0.5) ++rfr;
+            const double u = x[j * m + r];
+            cm = (cm < u) ? u : cm;
+            const double fu = u - floor(u);
+            if (((1.0 - fu) < fu ? 1.0 - fu : fu) > 1e-6) ++cf;
+        }
+        rmax[r] = rm;
+        cmax[r] = cm;
+        rfrac[r] = rf;
+        cfrac[r] = cf;
+        rfree[r] = rfr;
+    }
+    __syncthreads();
+    const double rel = feature_rel_gap(T.gap[i], T.value[i]);
+    const int depth = T.bdepth[i];
+    const mlp::Off o = mlp::offsets(mlp::kF, H);
+    // this thread's k best candidates, score descending (earlier first on ties)
+    float ks[kMaxK];
+    int kq[kMaxK];
+    int kc = 0;
+    bool bad = false;
+    for (int q = tid; q < T.n_int; q += blockDim.x) {
+        const int v = T.int_vars[q];
+        const double xv = x[v];
+        if (!isfinite(xv)) continue;
+        const double fr = xv - floor(xv);
+        if (!(((1.0 - fr) < fr ? 1.0 - fr : fr) > T.int_tol)) continue;
+        PermStats p{};
+        if (perm) {
+            const int r = v / m, c = v - (v / m) * m;
+            p.rfrac = rfrac[r];
+            p.cfrac = cfrac[c];
+            p.rfree = rfree[r];
+            p.rmax = rmax[r];
+            p.cmax = cmax[c];
+        }
+        float f[mlp::kF], a1[H], a2[H];
+        candidate_features(xv, depth, rel, perm, m, p, f);
+        const float z = mlp::forward_row<H>(prm, o, f, a1, a2);
+        if (!isfinite(z)) { bad = true; continue; }
+        int pos = kc;
+        while (pos > 0 && ks[pos - 1] < z) --pos;
+        if (pos >= T.k) continue;
+        const int last = kc < T.k ? kc : T.k - 1;
+        for (int t = last; t > pos; --t) { ks[t] = ks[t - 1]; kq[t] = kq[t - 1]; }
+        ks[pos] = z;
+        kq[pos] = q;
+        if (kc < T.k) ++kc;
+    }
+    if (__syncthreads_or(bad)) {
+        pick_most_fractional(T, i, x);
+        return;
+    }
+    // k rounds over the threads' heads: highest score, then earliest candidate
+    int h = 0, picked = 0;
+    for (int r = 0; r < T.k; ++r) {
+        float bz = 0.f;
+        int bq = INT_MAX;
+        if (h < kc) { bz = ks[h]; bq = kq[h]; }
+        for (int off = 16; off; off >>= 1) {
+            const float oz = __shfl_xor_sync(0xffffffffu, bz, off);
+            const int oq = __shfl_xor_sync(0xffffffffu, bq, off);
+            if (oq != INT_MAX && (bq == INT_MAX || oz > bz || (oz == bz && oq < bq))) { bz = oz; bq = oq; }
+        }
+        if (lane == 0) { s_z[w] = bz; s_q[w] = bq; }
+        __syncthreads();
+        if (tid == 0) {
+            float z = s_z[0];
+            int q = s_q[0];
+            for (int t = 1; t < (int)(blockDim.x >> 5); ++t)
+                if (s_q[t] != INT_MAX && (q == INT_MAX || s_z[t] > z || (s_z[t] == z && s_q[t] < q))) {
+                    z = s_z[t];
+                    q = s_q[t];
+                }
+            s_win = q;
+            if (q != INT_MAX) T.bvars[i * kMaxK + r] = T.int_vars[q];
+        }
+        __syncthreads();
+        const int win = s_win;
+        __syncthreads();
+        if (win == INT_MAX) break;
+        if (h < kc && kq[h] == win) ++h;
+        ++picked;
+    }
+    if (tid == 0) T.bnv[i] = picked;
+}
+
+size_t learned_smem_bytes(int H, int order) {
+    return align16((size_t)mlp::param_count(mlp::kF, H) * sizeof(float))
+           + (size_t)std::max(order, 0) * (2 * sizeof(double) + 3 * sizeof(int));
 }
 
 // block-wide inclusive scans over kMaxBatch threads
@@ -525,7 +667,11 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     const int n = pr.n_vars, B = s.gpu_batch_size, k = s.branch_k;
     if (B < 1 || B > kMaxBatch) { *err = "device frontier: gpu_batch_size must be in [1, 1024]"; return GBX_ERR_INVALID; }
     if (k < 1 || k > kMaxK) { *err = "device frontier: branch_k must be in [1, 8]"; return GBX_ERR_INVALID; }
-    if (s.scorer) { *err = "device frontier: the learned scorer runs with the host frontier only"; return GBX_ERR_UNSUPPORTED; }
+    if (s.scorer && (!s.scorer->params || s.scorer->n_features != GBX_SCORER_FEATURES
+                     || (s.scorer->hidden != 16 && s.scorer->hidden != 32 && s.scorer->hidden != 64))) {
+        *err = "scorer: invalid descriptor (hidden must be 16, 32 or 64)";
+        return GBX_ERR_INVALID;
+    }
     // the host engine's argument checks (its constructor)
     if (s.gpu_max_iters <= 0) { *err = "GPU iterations, batch size and streams must be positive"; return GBX_ERR_INVALID; }
     if (!std::isfinite(s.gpu_eps) || s.gpu_eps <= 0.0 || !std::isfinite(s.gpu_eps_min) || s.gpu_eps_min <= 0.0
@@ -686,6 +832,16 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    // branching kernel: most fractional, or the learned scorer
+    const gbx_scorer sc = s.scorer ? *s.scorer : gbx_scorer{};
+    const int sc_order = lmo.kind == GBX_LMO_BIRKHOFF ? lmo.order : 0;
+    const size_t sc_smem = s.scorer ? learned_smem_bytes(sc.hidden, sc_order) : 0;
+    if (s.scorer) {
+        auto kfn = sc.hidden == 16 ? learned_vars_kernel<16> : sc.hidden == 32 ? learned_vars_kernel<32>
+                                                                                 : learned_vars_kernel<64>;
+        e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc_smem);
+        if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    }
     const int expand_grid = std::min(E_max + 1, 4 * sms);
     const int merge_grid = 4 * sms;
     auto round = [&]() -> int {
@@ -693,7 +849,10 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
         gather_kernel<<<B, 256, 0, st>>>(T);
         int r = launch_relax(p, st, err);
         if (r) return r;
-        vars_kernel<<<B, 256, 0, st>>>(T);
+        if (!s.scorer) vars_kernel<<<B, 256, 0, st>>>(T);
+        else if (sc.hidden == 16) learned_vars_kernel<16><<<B, 256, sc_smem, st>>>(T, sc, sc_order);
+        else if (sc.hidden == 32) learned_vars_kernel<32><<<B, 256, sc_smem, st>>>(T, sc, sc_order);
+        else learned_vars_kernel<64><<<B, 256, sc_smem, st>>>(T, sc, sc_order);
         decide_kernel<<<1, kMaxBatch, 0, st>>>(T);
         expand_kernel<<<expand_grid, 256, 0, st>>>(T);
         merge_kernel<<<merge_grid, 256, 0, st>>>(T);

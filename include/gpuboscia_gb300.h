@@ -311,8 +311,9 @@ typedef struct gbx_settings {
     /* frontier in device memory (no counterpart in the reference): open nodes
      * stay in HBM and each round of the search (pop the best batch, relax,
      * branch_pow2, merge the children) runs as kernels replayed from a CUDA
-     * graph; batch <= 1024, branch_k <= 8, no learned scorer, num_streams and
-     * autotune unused (a stored launch shape still applies) */
+     * graph; batch <= 1024, branch_k <= 8; the learned scorer runs inside the
+     * branching kernel; num_streams and autotune unused (a stored launch
+     * shape still applies) */
     int device_frontier;      /* 0 */
     int frontier_capacity;    /* open nodes the pool holds (0: a quarter of free memory, <= 2^18) */
 } gbx_settings;

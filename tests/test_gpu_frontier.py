@@ -205,3 +205,44 @@ def test_rejects_unsupported_settings(cuda_lib):
     s.branch_k = 9
     with pytest.raises(ValueError, match="branch_k"):
         api.solve(inst.problem, inst.objective, inst.lmo, s)
+
+
+@pytest.mark.parametrize("hidden", [16, 32, 64])
+def test_learned_branching_same_optimum_as_host_frontier(cuda_lib, hidden):
+    """The scorer inside the device branching kernel: same certified optimum as
+    the host engine with the same scorer, and the same node count (a node's
+    relaxation, features and scores depend on its bounds alone)."""
+    from gpuboscia_gb300 import scorer
+    sc = scorer.Scorer(hidden, seed=3)
+    inst = _pair(204, 7)
+    s = inst.settings
+    s.algorithm = A.ALG_DICG
+    s.line_search = A.LS_QUADRATIC_EXACT
+    s.gpu_batch_size = 32
+    s.num_streams = 1
+    s.gpu_max_iters = 1000
+    s.abs_gap_tol = 1e-6
+    s.rel_gap_tol = 1e-6
+    s.precision = A.PRECISION_MIXED
+    s.time_limit_seconds = 60
+    s.scorer = sc
+    h = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    s.device_frontier = 1
+    g = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    g2 = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert _proved(h) and _proved(g)
+    assert abs(g.objective - h.objective) <= 1e-6
+    assert g.nodes_processed == h.nodes_processed
+    assert (g2.nodes_processed, g2.objective) == (g.nodes_processed, g.objective)
+
+
+def test_learned_scorer_bad_descriptor(cuda_lib):
+    from gpuboscia_gb300 import scorer
+    sc = scorer.Scorer(32, seed=1)
+    sc.hidden = 48
+    inst = instances.box_qp(n=8, seed=1)
+    s = inst.settings
+    s.device_frontier = 1
+    s.scorer = sc
+    with pytest.raises(ValueError, match="scorer"):
+        api.solve(inst.problem, inst.objective, inst.lmo, s)
