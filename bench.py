@@ -230,7 +230,7 @@ def time_plain(args, inst, lb, x0, d_lb, d_ub, d_eps, d_flags, flush, w, stream)
             "node_iterations_per_step": int(it.sum().item())}
 
 
-def _solve_timed(inst, prec, scorer_obj, batch, streams, limit, device_frontier=0):
+def _solve_timed(inst, prec, scorer_obj, batch, streams, limit, device_frontier=0, cutoff=0):
     from gpuboscia_gb300 import _abi as A
     from gpuboscia_gb300 import api
     s = inst.settings
@@ -244,6 +244,7 @@ def _solve_timed(inst, prec, scorer_obj, batch, streams, limit, device_frontier=
     s.precision = prec
     s.scorer = scorer_obj
     s.device_frontier = device_frontier
+    s.incumbent_cutoff = cutoff
     t0 = time.perf_counter()
     r = api.solve(inst.problem, inst.objective, inst.lmo, s)
     wall = time.perf_counter() - t0
@@ -277,19 +278,21 @@ def time_to_gap(args, inst):
     sc = scorer.Scorer(32, seed=0)
     sc.train(data, epochs=400, lr=3e-3)
     train_s = time.perf_counter() - t0
-    pairs = {"instances": "4 held-out G(9,1/2) pairs; batch 64 x 1 stream, host frontier, unless named",
+    pairs = {"instances": "4 held-out G(9,1/2) pairs; batch 64 x 1 stream, host frontier, unless named; "
+                          "full_stack = mixed + learned + device frontier (1024-node rounds) + incumbent cutoff",
              "scorer_training_seconds": train_s}
-    for name, prec, use, batch, streams, dev in (
-            ("plain_fp64", A.PRECISION_FP64, False, 64, 1, 0),
-            ("mixed", A.PRECISION_MIXED, False, 64, 1, 0),
-            ("mixed_learned", A.PRECISION_MIXED, True, 64, 1, 0),
-            ("mixed_learned_256x4", A.PRECISION_MIXED, True, 256, 4, 0),
-            ("device_frontier_mixed_1024", A.PRECISION_MIXED, False, 1024, 1, 1),
-            ("full_stack_device_frontier_1024", A.PRECISION_MIXED, True, 1024, 1, 1)):
+    for name, prec, use, batch, streams, dev, cut in (
+            ("plain_fp64", A.PRECISION_FP64, False, 64, 1, 0, 0),
+            ("mixed", A.PRECISION_MIXED, False, 64, 1, 0, 0),
+            ("mixed_learned", A.PRECISION_MIXED, True, 64, 1, 0, 0),
+            ("mixed_learned_256x4", A.PRECISION_MIXED, True, 256, 4, 0, 0),
+            ("device_frontier_mixed_1024", A.PRECISION_MIXED, False, 1024, 1, 1, 0),
+            ("device_frontier_mixed_learned_1024", A.PRECISION_MIXED, True, 1024, 1, 1, 0),
+            ("full_stack", A.PRECISION_MIXED, True, 1024, 1, 1, 1)):
         tot_s, tot_n, cert = 0.0, 0, True
         for k in range(4):
             wall, r, c = _solve_timed(pair(200 + k), prec, sc if use else None, batch, streams, args.ttg_limit,
-                                      dev)
+                                      dev, cut)
             tot_s += wall
             tot_n += r.nodes_processed
             cert = cert and c

@@ -87,7 +87,7 @@ class NodeBatch(C.Structure):
         ("x", C.c_void_p), ("lb", C.c_void_p), ("ub", C.c_void_p), ("eps", C.c_void_p),
         ("iterations", C.c_void_p), ("status", C.c_void_p), ("gap", C.c_void_p),
         ("value", C.c_void_p), ("best_vertex", C.c_void_p), ("best_vertex_val", C.c_void_p),
-        ("integer_flags", C.c_void_p),
+        ("integer_flags", C.c_void_p), ("cutoff", C.c_void_p),
     ]
 
 
@@ -118,7 +118,7 @@ class Settings(C.Structure):
         ("root_initial_point", C.c_void_p),
         ("branch_k", C.c_int), ("use_cuda_graph", C.c_int),
         ("scorer", C.c_void_p), ("autotune", C.c_int),
-        ("device_frontier", C.c_int), ("frontier_capacity", C.c_int),
+        ("device_frontier", C.c_int), ("incumbent_cutoff", C.c_int), ("frontier_capacity", C.c_int),
     ]
 
 
@@ -153,6 +153,7 @@ def default_settings() -> Settings:
     s.scorer = None
     s.autotune = 1
     s.device_frontier = 0
+    s.incumbent_cutoff = 0
     s.frontier_capacity = 0
     return s
 

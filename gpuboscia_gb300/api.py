@@ -199,6 +199,7 @@ class Settings:
     scorer: Optional[object] = None   # gpuboscia_gb300.scorer.Scorer: learned branching
     autotune: int = 1
     device_frontier: int = 0        # open nodes stay in HBM; each search round runs on the device
+    incumbent_cutoff: int = 0       # stop node relaxations whose FW bound clears the incumbent
     frontier_capacity: int = 0      # pool size in nodes (0: automatic)
 
     def algorithm_c(self) -> A.Algorithm:
@@ -209,7 +210,8 @@ class Settings:
         s = A.Settings()
         for f in ("gpu_batch_size", "num_streams", "gpu_max_iters", "gpu_eps", "gpu_eps_decay", "gpu_eps_min",
                   "integer_tol", "abs_gap_tol", "rel_gap_tol", "time_limit_seconds", "natural_lower_bound",
-                  "branch_k", "use_cuda_graph", "autotune", "device_frontier", "frontier_capacity"):
+                  "branch_k", "use_cuda_graph", "autotune", "device_frontier", "incumbent_cutoff",
+                  "frontier_capacity"):
             setattr(s, f, getattr(self, f))
         s.algorithm = self.algorithm_c()
         s.root_initial_point = keep.ptr(_f64(self.root_initial_point) if self.root_initial_point is not None
@@ -281,9 +283,11 @@ def _stream_ptr(stream) -> int:
 
 def relax_batch(objective, lmo, algorithm: A.Algorithm, x, lb, ub, eps, iterations, status,
                 max_iters: int, integer_flags=None, candidate_tol: float = 1e-6,
-                workspace: Optional[RelaxWorkspace] = None, stream=None, keep: Optional[_Keep] = None):
+                workspace: Optional[RelaxWorkspace] = None, stream=None, keep: Optional[_Keep] = None,
+                cutoff: Optional[float] = None):
     """Run gbx_relax_batch over device tensors (x, iterations, status updated in place).
 
+    cutoff: incumbent value at which a node may stop iterating (gbx_node_batch.cutoff).
     Returns dict(gap, value, best_vertex, best_vertex_val) of new device tensors.
     """
     import torch
@@ -301,6 +305,10 @@ def relax_batch(objective, lmo, algorithm: A.Algorithm, x, lb, ub, eps, iteratio
                     iterations.data_ptr(), status.data_ptr(), out["gap"].data_ptr(), out["value"].data_ptr(),
                     out["best_vertex"].data_ptr(), out["best_vertex_val"].data_ptr(),
                     integer_flags.data_ptr() if integer_flags is not None else None)
+    if cutoff is not None:
+        cut = torch.full((1,), float(cutoff), dtype=torch.float64, device=dev)
+        out["cutoff"] = cut   # returned with the outputs: alive while the launch runs
+        b.cutoff = cut.data_ptr()
     need = lib.gbx_relax_workspace_bytes(C.byref(o), C.byref(lm), C.byref(algorithm), N)
     if need == 0:
         A.check(lib, A.ERR_INVALID, "gbx_relax_workspace_bytes")

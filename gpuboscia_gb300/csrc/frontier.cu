@@ -812,6 +812,7 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     p.b.x = T.x; p.b.lb = T.lb; p.b.ub = T.ub; p.b.eps = T.eps;
     p.b.iterations = T.it; p.b.status = T.st; p.b.gap = T.gap; p.b.value = T.value;
     p.b.best_vertex = T.best; p.b.best_vertex_val = T.bvv; p.b.integer_flags = d_flags;
+    p.b.cutoff = s.incumbent_cutoff ? &T.S->incumbent : nullptr;
     int rc = make_layout(obj, lmo, s.algorithm, B, &p.L, err);
     if (rc) return rc;
     const size_t wsb = workspace_bytes(p.L, B);

@@ -29,6 +29,7 @@
 namespace gbx {
 
 constexpr unsigned kFull = 0xffffffffu;
+constexpr double kInfD = __builtin_huge_val();   // +infinity
 
 // ------------------------------------------------------------------ layout
 
@@ -219,6 +220,20 @@ static __device__ double value_from_residual(const Ctx& c) {
     double loc = 0.0;
     for (int e = c.tid; e < c.n; e += kThreads) loc = fma(c.R[e], c.R[e], loc);
     return c.s * bsum(loc, c.red);
+}
+
+// f(x) from the gradient g just evaluated at x (graph matching: from the
+// residual obj_grad left in c.R; dense quadratic: f = x'g/2 + s l c'x/2 + k),
+// for the incumbent cutoff. Lane order as bsum.
+static __device__ double value_at_grad(const Ctx& c, const double* x, const double* g) {
+    if (c.ok == GBX_OBJ_GRAPH_MATCHING) return value_from_residual(c);
+    const double hb = 0.5 * c.s * c.ls;
+    double loc = 0.0;
+    for (int j = c.tid; j < c.n; j += kThreads) {
+        loc = fma(0.5 * x[j], g[j], loc);
+        if (c.c) loc = fma(hb * c.c[j], x[j], loc);
+    }
+    return bsum(loc, c.red) + c.k0;
 }
 
 static __device__ double obj_value(const Ctx& c, const double* x) {
@@ -1272,7 +1287,7 @@ static __device__ double perm_score(const Ctx& c, const uint8_t* code, const int
 template <bool TC>
 static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, int node, double* X,
                           const double* LB, const double* UB, double* best, double& best_val,
-                          double eps, int it0, bool dicg, int ls) {
+                          double eps, int it0, bool dicg, int ls, double cutv) {
     const Layout& L = P.L;
     const int n = c.n, m = c.m, tid = c.tid;
     unsigned char* mx = L.mx_global ? P.mixed + (size_t)node * L.mixed_node_bytes : dsm + L.sm_mx;
@@ -1406,7 +1421,7 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
     for (int iter = 0; iter < P.b.max_iters; ++iter) {
         iters = it0 + iter + 1;
         if constexpr (tcg) {
-            if (!tc::gradient(tg, m, xf, two_s, gf, dicg ? nullptr : Rf)) {
+            if (!tc::gradient(tg, m, xf, two_s, gf, (dicg && !(cutv < kInfD)) ? nullptr : Rf)) {
                 iters = it0 + iter;  // the iteration did not happen
                 if (tid == 0) c.flag[5] = 1;
                 __syncthreads();
@@ -1453,6 +1468,14 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
         }
         const double gap = bsum(loc, c.red);
         if (gap >= 0.0 && gap < eps) break;
+        if (cutv < kInfD && iter > 0) {
+            // the FP32 residual's bound clears the incumbent by a margin that
+            // covers its rounding; the certificate is recomputed exactly
+            double l2 = 0.0;
+            for (int e = tid; e < n; e += kThreads) l2 = fma((double)Rf[e], (double)Rf[e], l2);
+            const double fv = c.s * bsum(l2, c.red);
+            if (fv - gap >= cutv + 1e-5 * (1.0 + fabs(cutv))) break;
+        }
 
         if (!dicg) {
             double gm;
@@ -1654,6 +1677,7 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
         c.A = c.B = nullptr;
     }
     const double eps = P.b.eps[node];
+    const double cutv = P.b.cutoff ? *P.b.cutoff : kInfD;   // incumbent cutoff (+inf: none)
     const int it0 = P.b.iterations[node];
     const bool supplied = (P.b.status[node] & GBX_NODE_INITIAL_POINT_SUPPLIED) != 0;
     __syncthreads();
@@ -1755,10 +1779,12 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
     int iters = it0;
     constexpr bool kMixedLoop = MIX != 0 && OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF;
     if constexpr (kMixedLoop)
-        iters = mixed_loop<MIX == 2>(c, P, dsm, node, X, LB, UB, best, best_val, eps, it0, dicg, ls);
+        iters = mixed_loop<MIX == 2>(c, P, dsm, node, X, LB, UB, best, best_val, eps, it0, dicg, ls, cutv);
     for (int iter = 0; !kMixedLoop && iter < P.b.max_iters; ++iter) {
         iters = it0 + iter + 1;
         obj_grad(c, X, G);
+        // f(x) for the incumbent cutoff, before vertex scoring reuses the residual
+        const double fcut = (cutv < kInfD && iter > 0) ? value_at_grad(c, X, G) : 0.0;
         bool fwd_perm = false, away_perm = false;
         if constexpr (LK == GBX_LMO_BIRKHOFF) {
             // forward oracle on warp 0, DICG away oracle on warp 1
@@ -1787,6 +1813,7 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
         for (int j = tid; j < n; j += kThreads) loc = fma(G[j], X[j] - V[j], loc);
         const double gap = bsum(loc, c.red);
         if (gap >= 0.0 && gap < eps) break;
+        if (cutv < kInfD && iter > 0 && fcut - gap >= cutv) break;
 
         if (!dicg) {
             if (search) {

@@ -175,6 +175,7 @@ void gbx_default_settings(gbx_settings* s) {
     s->scorer = nullptr;
     s->autotune = 1;
     s->device_frontier = 0;
+    s->incumbent_cutoff = 0;
     s->frontier_capacity = 0;
 }
 
@@ -235,6 +236,7 @@ int gbx_solve(const gbx_problem* problem, const gbx_objective* obj, const gbx_lm
         cfg.precision = s->algorithm.precision;
         cfg.use_cuda_graph = s->use_cuda_graph != 0;
         cfg.autotune = s->autotune != 0;
+        cfg.incumbent_cutoff = s->incumbent_cutoff != 0;
 
         const double tol = s->integer_tol;
         const int k = s->branch_k;

@@ -78,6 +78,15 @@ struct DeviceResidentConfig {
     int precision = GBX_PRECISION_FP64;
     bool use_cuda_graph = true;  // replay each slot's copy-relax-copy sequence from a CUDA graph
     bool autotune = true;        // time the launch shapes on the first full batch (gbx_relax_autotune)
+    // frontier in device memory: every round of the search runs as kernels
+    // (gbx_solve with gbx_settings.device_frontier); branching is branch_pow2
+    // over branch_k variables and the BranchStrategy callback is not called
+    bool device_frontier = false;
+    int frontier_capacity = 0;   // open nodes in the device pool (0: automatic)
+    int branch_k = 3;
+    // stop a node's relaxation once its FW bound clears the incumbent
+    // (gbx_node_batch.cutoff): the node is pruned at any bound above it
+    bool incumbent_cutoff = false;
 };
 
 enum class DRSSchedulingEventType { Dispatched, CompletionDetached, PostprocessStarted };
@@ -182,6 +191,10 @@ public:
 
     void solve() {
         solve_started_ = Clock::now();
+        if (cfg_.device_frontier) {
+            solve_device_frontier();
+            return;
+        }
         gpu_worker();
         for (auto& s : slots_) if (s.stream) GBX_CUDA_CHECK(cudaStreamSynchronize(s.stream));
         if (final_dual_bound_ == -std::numeric_limits<double>::infinity())
@@ -222,8 +235,8 @@ private:
         unsigned char* d = nullptr;
         void* ws = nullptr;
         // byte offsets of the current batch
-        size_t o_lb = 0, o_ub = 0, o_eps = 0, o_x = 0, o_it = 0, o_st = 0, o_gap = 0, o_val = 0, o_bvv = 0,
-               o_best = 0, end = 0;
+        size_t o_lb = 0, o_ub = 0, o_eps = 0, o_cut = 0, o_x = 0, o_it = 0, o_st = 0, o_gap = 0, o_val = 0,
+               o_bvv = 0, o_best = 0, end = 0;
     };
 
     struct Completed {
@@ -243,6 +256,7 @@ private:
         s.o_lb = p; p += vb;
         s.o_ub = p; p += vb;
         s.o_eps = p; p += sb;
+        s.o_cut = p; p += sizeof(double);   // incumbent at dispatch (the cutoff)
         s.o_x = p; p += vb;
         s.o_it = p; p += a8(N * sizeof(int));
         s.o_st = p; p += a8((size_t)N);
@@ -385,6 +399,7 @@ private:
             it[i] = nd.relaxation_iterations;
             st[i] = nd.relaxation_x.empty() ? 0 : GBX_NODE_INITIAL_POINT_SUPPLIED;
         }
+        *at<double>(s.h, s.o_cut) = incumbent_.get();
         gbx_node_batch b{};
         b.n_nodes = N;
         b.max_iters = cfg_.gpu_max_iters;
@@ -400,6 +415,7 @@ private:
         b.best_vertex = at<double>(s.d, s.o_best);
         b.best_vertex_val = at<double>(s.d, s.o_bvv);
         b.integer_flags = d_flags_;
+        b.cutoff = cfg_.incumbent_cutoff ? at<double>(s.d, s.o_cut) : nullptr;
         if (cfg_.autotune && !tuned_ && N == cfg_.gpu_batch_size) {
             // once, on the first full batch: the tuner relaxes it under every launch
             // shape and restores it, and later launches (and graphs) use the winner
@@ -582,6 +598,52 @@ private:
             retire(active_bound, fresh);
         }
         if (active_tasks_.load(std::memory_order_acquire) == 0) finish_if_search_complete();
+    }
+
+    // the whole search on the device, from the single root node pushed
+    void solve_device_frontier() {
+        if (queue_.size() != 1) throw std::invalid_argument("the device frontier starts from exactly one root node");
+        const Node root = queue_.pop_batch(1, std::numeric_limits<double>::infinity()).front();
+        if (root.relaxation_iterations > 0)
+            throw std::invalid_argument("the device frontier cannot resume an interrupted root relaxation");
+        gbx_problem pr{};
+        pr.n_vars = prob_.n_vars;
+        pr.lb = root.lb.data();
+        pr.ub = root.ub.data();
+        pr.int_vars = prob_.int_vars.data();
+        pr.n_int = (int)prob_.int_vars.size();
+        gbx_settings s;
+        gbx_default_settings(&s);
+        s.gpu_batch_size = cfg_.gpu_batch_size;
+        s.num_streams = cfg_.num_streams;
+        s.gpu_max_iters = cfg_.gpu_max_iters;
+        s.gpu_eps = cfg_.gpu_eps;
+        s.gpu_eps_decay = cfg_.gpu_eps_decay;
+        s.gpu_eps_min = cfg_.gpu_eps_min;
+        s.integer_tol = cfg_.integer_tol;
+        s.abs_gap_tol = cfg_.abs_gap_tol;
+        s.rel_gap_tol = cfg_.rel_gap_tol;
+        s.algorithm = alg_;
+        s.time_limit_seconds = time_limit_seconds_;
+        s.natural_lower_bound = root.dual_bound;
+        s.root_initial_point = root.relaxation_x.empty() ? nullptr : root.relaxation_x.data();
+        s.branch_k = cfg_.branch_k;
+        s.use_cuda_graph = cfg_.use_cuda_graph ? 1 : 0;
+        s.device_frontier = 1;
+        s.incumbent_cutoff = cfg_.incumbent_cutoff ? 1 : 0;
+        s.frontier_capacity = cfg_.frontier_capacity;
+        std::vector<double> x(prob_.n_vars);
+        gbx_result r{};
+        r.x = x.data();
+        const int rc = gbx_solve(&pr, &obj_, &lmo_, &s, &r);
+        if (rc == GBX_ERR_INVALID) throw std::invalid_argument(gbx_last_error());
+        gbx_check(rc, "gbx_solve");
+        if (r.has_incumbent) incumbent_.try_update(r.objective, x);
+        final_dual_bound_ = r.dual_bound;
+        nodes_done_.store(r.nodes_processed);
+        reached_tolerance_ = r.reached_tolerance != 0;
+        reached_time_limit_ = r.reached_time_limit != 0;
+        signal_done();
     }
 
     void retire(double active_bound, bool fresh) {

@@ -60,6 +60,8 @@ Result solve_with_algorithm(const Problem& problem, DeviceObjective objective, L
                             Algorithm algorithm, Heuristic heuristic = {}) {
     validate_root_initial_point(problem, lmo, settings.root_initial_point, settings.root_initial_point_feasible);
     BranchStrategy branch = settings.branch;
+    if (settings.device.device_frontier && branch)
+        throw std::invalid_argument("the device frontier branches with branch_pow2; leave Settings::branch empty");
     if (!branch) {
         const double integer_tol = settings.device.integer_tol;
         branch = [integer_tol](const Node& parent, int& next_id, const std::vector<double>& x,

@@ -139,6 +139,13 @@ typedef struct gbx_node_batch {
     double* best_vertex;      /* device [n_nodes*n] out: best integral point  */
     double* best_vertex_val;  /* device [n_nodes] out: its value (1e300 none) */
     const uint8_t* integer_flags; /* device [n] problem integer flags         */
+    /* device pointer to the incumbent value, or NULL (the reference's
+     * behaviour). When set, a node stops iterating once its FW bound
+     * f(x) - gap clears the incumbent (after at least one step of this
+     * dispatch), since branch and bound prunes it at any bound above; the
+     * returned gap, value and status are the usual exact certificate at the
+     * returned iterate. No counterpart in the reference. */
+    const double* cutoff;
 } gbx_node_batch;
 
 /* Library identity. */
@@ -315,6 +322,7 @@ typedef struct gbx_settings {
      * branching kernel; num_streams and autotune unused (a stored launch
      * shape still applies) */
     int device_frontier;      /* 0 */
+    int incumbent_cutoff;     /* stop node relaxations at the incumbent (gbx_node_batch.cutoff); 0 */
     int frontier_capacity;    /* open nodes the pool holds (0: a quarter of free memory, <= 2^18) */
 } gbx_settings;
 

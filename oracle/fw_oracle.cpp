@@ -185,6 +185,24 @@ struct Objective {
         return reduce_sum(L);
     }
 
+    // f(x) from the gradient g just evaluated at x, for the incumbent cutoff
+    // (the kernel's value_at_grad: graph matching from the residual, dense
+    // quadratic as x'g/2 + s l c'x/2 + k, lane order of the reductions)
+    double value_at_grad(const double* x, const double* g) const {
+        if (graph()) return value_from_residual();
+        const double hb = 0.5 * o->scale * o->linear_scale;
+        Lanes L;
+        for (int l = 0; l < kLanes; ++l) {
+            double loc = 0.0;
+            for (int j = l; j < n; j += kLanes) {
+                loc = std::fma(0.5 * x[j], g[j], loc);
+                if (o->c) loc = std::fma(hb * o->c[j], x[j], loc);
+            }
+            L.v[l] = loc;
+        }
+        return reduce_sum(L) + o->constant;
+    }
+
     // value at the point whose gradient was just evaluated
     double value_after_grad(const double* x) const {
         return graph() ? value_from_residual() : value(x);
@@ -746,9 +764,13 @@ struct Relaxer {
                 for (int j = 0; j < n; ++j) best[j] = vert[j];
         };
         const int ls = alg->line_search;
+        // incumbent cutoff (gbx_node_batch.cutoff): stop once the FW bound
+        // f - gap clears it, after at least one step of this dispatch
+        const double cutv = b->cutoff ? *b->cutoff : kInf;
         for (int iter = 0; iter < b->max_iters; ++iter) {
             b->iterations[node] = it0 + iter + 1;
             obj.grad(x, g.data());
+            const double fcut = (cutv < kInf && iter > 0) ? obj.value_at_grad(x, g.data()) : 0.0;
             lmo.forward(g.data(), lb, ub, v.data());
             score(v.data());
             const double gap = dot_gap(g.data(), x, v.data());
@@ -756,6 +778,7 @@ struct Relaxer {
             b->gap[node] = gap;
             b->status[node] = done ? 1 : 0;
             if (done) break;
+            if (cutv < kInf && iter > 0 && fcut - gap >= cutv) break;
             if (!dicg()) {
                 if (uses_search()) {
                     for (int j = 0; j < n; ++j) v[j] -= x[j];
@@ -1029,6 +1052,8 @@ struct BnB {
         b.gap = bt.gap.data(); b.value = bt.value.data();
         b.best_vertex = bt.best_vertex.data(); b.best_vertex_val = bt.best_vertex_val.data();
         b.integer_flags = flags.data();
+        const double cut = inc;   // the incumbent at dispatch
+        b.cutoff = s->incumbent_cutoff ? &cut : nullptr;
         Relaxer r(obj, lmo, &s->algorithm);
         for (int i = 0; i < N; ++i) r.relax(i, &b);
         bt.nodes = std::move(nodes);

@@ -80,7 +80,7 @@ def algorithm(kind=A.ALG_DICG, ls=A.LS_OPEN_LOOP, secant_iters=4, secant_tol=1e-
 
 
 def relax(objective, lmo, alg: A.Algorithm, x, lb, ub, eps, iterations=None, status=None, max_iters=100,
-          flags=None, tol=1e-6, threads=1):
+          flags=None, tol=1e-6, threads=1, cutoff=None):
     """oracle_relax_batch over host arrays; returns a dict of outputs (x, iterations, status, gap, value,
     best_vertex, best_vertex_val)."""
     L = lib()
@@ -99,6 +99,10 @@ def relax(objective, lmo, alg: A.Algorithm, x, lb, ub, eps, iterations=None, sta
     lm = lmo.to_c(n, "host", keep)
     b = A.NodeBatch(N, max_iters, tol, _p(x), _p(lb), _p(ub), _p(eps), _p(it), _p(st), _p(out["gap"]),
                     _p(out["value"]), _p(out["best_vertex"]), _p(out["best_vertex_val"]), _p(fl))
+    if cutoff is not None:
+        cut = np.array([float(cutoff)])
+        keep.items.append(cut)
+        b.cutoff = _p(cut)
     rc = L.oracle_relax_batch(C.byref(o), C.byref(lm), C.byref(alg), C.byref(b), threads)
     if rc != 0:
         raise RuntimeError(L.oracle_last_error().decode())

@@ -1,0 +1,36 @@
+"""The C++ drop-in headers (gpuboscia::solve over the built-in objective / LMO
+types, as a reference program would call them) compiled with the host
+compiler and linked against the in-tree library: the reference's
+examples/minimal.cu answer and a graph pair, on the host and the device
+frontier (tests/cpp/minimal_gpu.cpp)."""
+import pathlib
+import subprocess
+
+import pytest
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def exe(tmp_path_factory):
+    from gpuboscia_gb300 import build
+    lib = build.build()
+    cuda = build._cuda_home()
+    out = tmp_path_factory.mktemp("cppgpu") / "minimal_gpu"
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-I", str(cuda / "include"),
+           str(ROOT / "tests" / "cpp" / "minimal_gpu.cpp"), "-o", str(out),
+           "-L", str(lib.parent), "-lgpuboscia_gb300", "-Wl,-rpath," + str(lib.parent),
+           "-L", str(cuda / "lib64"), "-lcudart", "-Wl,-rpath," + str(cuda / "lib64"), "-lpthread"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return out
+
+
+def test_dropin_program_compiles_and_links(exe):
+    assert exe.exists()
+
+
+@pytest.mark.gpu
+def test_dropin_program_runs(cuda_lib, exe):
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "0 failed" in r.stdout

@@ -246,3 +246,25 @@ def test_learned_scorer_bad_descriptor(cuda_lib):
     s.scorer = sc
     with pytest.raises(ValueError, match="scorer"):
         api.solve(inst.problem, inst.objective, inst.lmo, s)
+
+
+@pytest.mark.parametrize("precision", [A.PRECISION_FP64, A.PRECISION_MIXED])
+def test_incumbent_cutoff_same_optimum(cuda_lib, precision):
+    inst = _pair(205, 7)
+    s = inst.settings
+    s.algorithm = A.ALG_DICG
+    s.line_search = A.LS_QUADRATIC_EXACT
+    s.gpu_batch_size = 64
+    s.gpu_max_iters = 1000
+    s.abs_gap_tol = 1e-6
+    s.rel_gap_tol = 1e-6
+    s.precision = precision
+    s.time_limit_seconds = 60
+    s.device_frontier = 1
+    a = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    s.incumbent_cutoff = 1
+    b = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    s.device_frontier = 0
+    h = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert _proved(a) and _proved(b) and _proved(h)
+    assert abs(a.objective - b.objective) <= 1e-6 and abs(h.objective - b.objective) <= 1e-6

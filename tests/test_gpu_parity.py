@@ -265,3 +265,49 @@ def test_birkhoff_order400_nodes_bitwise(cuda_lib):
     g, o = run_both(inst.objective, inst.lmo, O.algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT), lb.copy(), lb, ub,
                     1e-6, 2, flags)
     assert_same(g, o)
+
+
+@pytest.mark.parametrize("kind,ls", [(A.ALG_FRANK_WOLFE, A.LS_QUADRATIC_EXACT), (A.ALG_DICG, A.LS_QUADRATIC_EXACT),
+                                     (A.ALG_FRANK_WOLFE, A.LS_OPEN_LOOP)])
+@pytest.mark.parametrize("problem", ["box", "graph"])
+def test_incumbent_cutoff_nodes_bitwise(cuda_lib, problem, kind, ls):
+    """gbx_node_batch.cutoff: nodes whose FW bound clears the incumbent stop
+    early; the FP64 kernel and the oracle stop at the same iteration with the
+    same certificate."""
+    if problem == "box":
+        inst = instances.box_qp(n=48)
+        lb, ub = instances.box_node_batch(48, 32, seed=11)
+        flags = np.ones(48, np.uint8)
+        x0 = lb.copy()
+    else:
+        inst = instances.birkhoff_gnp(order=8, seed=5)
+        lb, ub = instances.birkhoff_node_batch(8, 32, seed=4)
+        flags = np.ones(64, np.uint8)
+        x0 = lb.copy()
+    alg = O.algorithm(kind, ls)
+    free = O.relax(inst.objective, inst.lmo, alg, x0, lb, ub, 1e-9, max_iters=200, flags=flags)
+    bounds = np.where(free["status"] != A.NODE_INFEASIBLE, free["value"] - free["gap"], np.nan)
+    cut = float(np.nanpercentile(bounds, 40))
+    g = gpu_relax_cut(inst.objective, inst.lmo, alg, x0, lb, ub, 1e-9, 200, flags, cut)
+    o = O.relax(inst.objective, inst.lmo, alg, x0, lb, ub, 1e-9, max_iters=200, flags=flags, cutoff=cut)
+    assert_same(g, o)
+    stopped = o["iterations"] < free["iterations"]
+    assert stopped.any()
+    # a stopped node's certified bound reaches the cutoff (up to the rounding
+    # between the loop's value and the certificate's)
+    lo = o["value"] - o["gap"]
+    assert np.all(lo[stopped] >= cut - 1e-9 * max(1.0, abs(cut)))
+
+
+def gpu_relax_cut(obj, lmo, alg, x, lb, ub, eps, max_iters, flags, cutoff):
+    import torch
+    X = _t(x)
+    N = x.shape[0]
+    it = _t(np.zeros(N), np.int32)
+    st = _t(np.zeros(N), np.uint8)
+    out = api.relax_batch(obj, lmo, alg, X, _t(lb), _t(ub), _t(np.full(N, eps), np.float64), it, st, max_iters,
+                          _t(flags, np.uint8), 1e-6, cutoff=cutoff)
+    torch.cuda.synchronize()
+    return dict(x=X.cpu().numpy(), iterations=it.cpu().numpy(), status=st.cpu().numpy(),
+                gap=out["gap"].cpu().numpy(), value=out["value"].cpu().numpy(),
+                best_vertex=out["best_vertex"].cpu().numpy(), best_vertex_val=out["best_vertex_val"].cpu().numpy())

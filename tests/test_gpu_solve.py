@@ -83,3 +83,22 @@ def test_multistream_same_optimum(cuda_lib):
     many = api.solve(inst.problem, inst.objective, inst.lmo, s)
     assert abs(one.objective - many.objective) <= 1e-9 * max(1.0, abs(one.objective))
     assert many.dual_bound <= many.objective + 1e-9
+
+
+@pytest.mark.parametrize("seed", [21, 5])
+def test_incumbent_cutoff_matches_oracle(cuda_lib, seed):
+    """Relaxations stopped at the incumbent (settings.incumbent_cutoff): the
+    host-frontier solver and the oracle's B&B stay identical, and reach the
+    optimum of the search without the cutoff."""
+    inst = instances.box_qp(n=16, seed=seed)
+    s = inst.settings
+    s.num_streams = 1
+    s.gpu_batch_size = 8
+    s.gpu_max_iters = 2000
+    s.rel_gap_tol = 0.0
+    ref = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    s.incumbent_cutoff = 1
+    g = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    o = O.solve(inst.problem, inst.objective, inst.lmo, s)
+    _same(g, o)
+    assert abs(g.objective - ref.objective) <= 1e-6
