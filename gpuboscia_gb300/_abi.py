@@ -169,6 +169,7 @@ EXPORTED_SYMBOLS = (
     "gbx_objective_gradient_batch", "gbx_objective_gradient_batch_f32",
     "gbx_node_feasible_batch",
     "gbx_default_settings", "gbx_solve",
+    "gbx_read_mat", "gbx_read_dimacs",
     "gbx_scorer_param_count", "gbx_branch_features", "gbx_scorer_forward", "gbx_scorer_workspace_bytes",
     "gbx_scorer_gradient", "gbx_scorer_adam",
 )
@@ -218,6 +219,11 @@ def load(path: os.PathLike | str | None = None) -> C.CDLL:
     lib.gbx_branch_features.restype = None
     lib.gbx_branch_features.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                         C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p]
+    lib.gbx_read_mat.restype = C.c_int
+    lib.gbx_read_mat.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p,
+                                 C.c_size_t]
+    lib.gbx_read_dimacs.restype = C.c_int
+    lib.gbx_read_dimacs.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.c_void_p, C.c_size_t]
     lib.gbx_scorer_forward.restype = C.c_int
     lib.gbx_scorer_forward.argtypes = [P(Scorer), C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
     lib.gbx_scorer_workspace_bytes.restype = C.c_size_t

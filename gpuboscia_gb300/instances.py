@@ -229,3 +229,52 @@ def box_node_batch(n: int, nodes: int, seed: int, max_fixed: int | None = None):
         lb[i, idx] = val
         ub[i, idx] = val
     return lb, ub
+
+
+# ---------------------------------------------------------------- instance files
+def load_mat(path, name: str = "A") -> np.ndarray:
+    """The real matrix `name` of a MATLAB v5 file (gbx_read_mat), row-major float64."""
+    import ctypes as C
+    from . import _abi as A
+    lib = A.load()
+    r, c = C.c_int(0), C.c_int(0)
+    p = str(path).encode()
+    rc = lib.gbx_read_mat(p, name.encode(), C.byref(r), C.byref(c), None, 0)
+    if rc != A.OK:
+        raise (ValueError if rc == A.ERR_INVALID else RuntimeError)(lib.gbx_last_error().decode())
+    out = np.zeros((r.value, c.value))
+    rc = lib.gbx_read_mat(p, name.encode(), C.byref(r), C.byref(c), out.ctypes.data, out.size)
+    A.check(lib, rc, "gbx_read_mat")
+    return out
+
+
+def load_dimacs(path) -> np.ndarray:
+    """The symmetric 0/1 adjacency of a DIMACS edge list (gbx_read_dimacs)."""
+    import ctypes as C
+    from . import _abi as A
+    lib = A.load()
+    n = C.c_int(0)
+    p = str(path).encode()
+    rc = lib.gbx_read_dimacs(p, C.byref(n), None, 0)
+    if rc != A.OK:
+        raise (ValueError if rc == A.ERR_INVALID else RuntimeError)(lib.gbx_last_error().decode())
+    out = np.zeros((n.value, n.value))
+    rc = lib.gbx_read_dimacs(p, C.byref(n), out.ctypes.data, out.size)
+    A.check(lib, rc, "gbx_read_dimacs")
+    return out
+
+
+def graph_matching_from_file(path, seed: int = 0) -> Instance:
+    """examples/main.cu:183-226: A from an instance file (.mat variable A, or a
+    DIMACS edge list), B = A with rows and columns permuted by a seeded random
+    permutation (B[r, c] = A[p[r], p[c]]), so the optimum is 0 at X = P'."""
+    import os
+    A = load_dimacs(path) if str(path).endswith(".dimacs") else load_mat(path, "A")
+    if A.shape[0] != A.shape[1]:
+        raise ValueError(f"{path}: adjacency is {A.shape[0]}x{A.shape[1]}, not square")
+    m = A.shape[0]
+    p = permutation(_rng(seed), m)
+    B = A[np.ix_(p, p)]
+    X = np.zeros((m, m))
+    X[p, np.arange(m)] = 1.0   # A X = X B
+    return graph_matching(m, A, B, os.path.basename(str(path)), 0.0, X.ravel())

@@ -337,6 +337,17 @@ typedef struct gbx_result {
     double* x;                /* host [n_vars], caller-owned, filled when has_incumbent */
 } gbx_result;
 
+/* ---- graph-matching instance files (examples/main.cu:41-129 reads the
+ * reference's test_instances MAT files this way). Host arrays, row-major.
+ * gbx_read_mat: the real matrix `name` ("A" when NULL) of a MATLAB v5 file,
+ * plain or zlib-compressed, any numeric storage type; with out == NULL only
+ * rows / cols are returned. gbx_read_dimacs: the 0/1 symmetric adjacency of a
+ * DIMACS edge list ("p edge n m", "e u v", 1-based). GBX_ERR_INVALID for a
+ * missing file or variable or a short buffer, GBX_ERR_UNSUPPORTED for a
+ * malformed or unsupported file. */
+int gbx_read_mat(const char* path, const char* name, int* rows, int* cols, double* out, size_t capacity);
+int gbx_read_dimacs(const char* path, int* n_vertices, double* out, size_t capacity);
+
 /* Fill *s with the reference defaults (create_default_settings). */
 void gbx_default_settings(gbx_settings* s);
 
