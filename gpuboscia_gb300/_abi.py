@@ -39,6 +39,7 @@ LMO_SIMPLEX = 2
 LMO_EQUALITY_SIMPLEX = 3
 LMO_BIRKHOFF = 4
 LMO_CARDINALITY = 5
+LMO_LINKED_CARDINALITY = 6
 
 ALG_FRANK_WOLFE = 0
 ALG_DICG = 1
@@ -69,7 +70,7 @@ class Objective(C.Structure):
 class LMO(C.Structure):
     _fields_ = [
         ("kind", C.c_int), ("n", C.c_int), ("right_side", C.c_double),
-        ("is_int", C.c_void_p), ("order", C.c_int),
+        ("is_int", C.c_void_p), ("order", C.c_int), ("upper", C.c_void_p),
     ]
 
 

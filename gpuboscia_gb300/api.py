@@ -164,6 +164,29 @@ class CardinalityLMO:
         return A.LMO(A.LMO_CARDINALITY, n, float(self.cardinality), None, 0)
 
 
+@dataclasses.dataclass
+class LinkedCardinalityLMO:
+    """The sparse-Sharpe set {(v, y): 0 <= v_i <= upper_i y_i, sum y <= cardinality,
+    y in [0, 1]} (GBX_LMO_LINKED_CARDINALITY, examples/sparse_sharpe.cu:266-546):
+    v_i at i, y_i at n/2 + i for the len(upper) active assets, the rest of each
+    half padding. Frank-Wolfe and DICG; branching fixes y."""
+    upper: np.ndarray
+    cardinality: int
+    supports_dicg = True
+
+    def to_c(self, n: int, where: str, keep: _Keep) -> A.LMO:
+        U = _f64(self.upper)
+        assert n % 2 == 0 and len(U) <= n // 2
+        return A.LMO(A.LMO_LINKED_CARDINALITY, n, float(self.cardinality), None, len(U), keep.ptr(U, where))
+
+    def relaxation_feasible(self, x, lb, ub, tol) -> bool:
+        x = np.asarray(x, dtype=np.float64)
+        h, k = len(x) // 2, len(self.upper)
+        v, y = x[:k], x[h:h + k]
+        return bool((v >= -tol).all() and (v <= np.asarray(self.upper) * y + tol).all()
+                    and (y >= -tol).all() and (y <= 1 + tol).all() and y.sum() <= self.cardinality + tol)
+
+
 # ---------------------------------------------------------------- problem / settings
 @dataclasses.dataclass
 class Problem:

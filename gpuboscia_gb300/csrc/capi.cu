@@ -29,8 +29,15 @@ int validate(const gbx_objective* o, const gbx_lmo* l, const gbx_algorithm* a) {
     }
     if (l->kind == GBX_LMO_BIRKHOFF && l->order * l->order != l->n)
         return fail(GBX_ERR_INVALID, "Birkhoff LMO needs order*order == n");
-    if (l->kind < GBX_LMO_BOX || l->kind > GBX_LMO_CARDINALITY)
+    if (l->kind < GBX_LMO_BOX || l->kind > GBX_LMO_LINKED_CARDINALITY)
         return fail(GBX_ERR_UNSUPPORTED, "unknown LMO kind");
+    if (l->kind == GBX_LMO_LINKED_CARDINALITY) {
+        if (l->n % 2 || l->order < 0 || l->order > l->n / 2 || !(l->right_side >= 0.0) || !l->upper)
+            return fail(GBX_ERR_INVALID,
+                        "linked cardinality LMO needs n = 2 * assets, 0 <= order <= n / 2, a cardinality and upper");
+        if (o->kind != GBX_OBJ_DENSE_QUADRATIC)
+            return fail(GBX_ERR_UNSUPPORTED, "the linked cardinality LMO needs a dense quadratic objective");
+    }
     if (l->kind == GBX_LMO_CARDINALITY) {
         if (l->n % 2 || !(l->right_side >= 1.0))
             return fail(GBX_ERR_INVALID, "cardinality LMO needs n = 2 * assets and a cardinality >= 1");
@@ -223,6 +230,8 @@ int gbx_lmo_batch(const gbx_lmo* lmo, int cases, int mode, const double* directi
         return fail(GBX_ERR_INVALID, "null LMO buffer");
     if (lmo->kind == GBX_LMO_BIRKHOFF && lmo->order * lmo->order != lmo->n)
         return fail(GBX_ERR_INVALID, "Birkhoff LMO needs order*order == n");
+    if (lmo->kind == GBX_LMO_LINKED_CARDINALITY && !lmo->upper)
+        return fail(GBX_ERR_INVALID, "linked cardinality LMO needs upper");
     std::string err;
     const int rc = gbx::launch_lmo_batch(*lmo, cases, mode, direction, x, lb, ub, out,
                                          out_step, stream, &err);
@@ -304,6 +313,8 @@ int gbx_node_feasible_batch(const gbx_lmo* lmo, int cases, const double* lb,
                             void* stream) {
     if (!lmo || cases < 0 || lmo->n <= 0) return fail(GBX_ERR_INVALID, "feasibility arguments");
     if (cases > 0 && (!lb || !ub || !out)) return fail(GBX_ERR_INVALID, "null buffer");
+    if (lmo->kind == GBX_LMO_LINKED_CARDINALITY && !lmo->upper)
+        return fail(GBX_ERR_INVALID, "linked cardinality LMO needs upper");
     std::string err;
     const int rc = gbx::launch_node_feasible(*lmo, cases, lb, ub, integer_flags, out, stream, &err);
     if (rc) return fail(rc, err);

@@ -7,4 +7,5 @@ template int launch_one<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_SIMPLEX>(const Params&,
 template int launch_one<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_EQUALITY_SIMPLEX>(const Params&, cudaStream_t, std::string*);
 template int launch_one<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_BIRKHOFF>(const Params&, cudaStream_t, std::string*);
 template int launch_one<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_CARDINALITY>(const Params&, cudaStream_t, std::string*);
+template int launch_one<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_LINKED_CARDINALITY>(const Params&, cudaStream_t, std::string*);
 }  // namespace gbx

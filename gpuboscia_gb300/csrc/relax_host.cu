@@ -73,6 +73,12 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
         fixed_bytes += align16((size_t)L.sort_size * 8) * 2 + align16((size_t)L.sort_size * 4)
                        + align16((size_t)n);
     }
+    if (l.kind == GBX_LMO_LINKED_CARDINALITY) {
+        if (n % 2 || l.order < 0 || l.order > n / 2) {
+            *err = "linked cardinality LMO needs n = 2 * (padded) assets and 0 <= order <= n / 2";
+            return GBX_ERR_UNSUPPORTED;
+        }
+    }
     if (l.kind == GBX_LMO_BIRKHOFF) {
         if (l.order <= 0 || l.order > 1024) { *err = "Birkhoff order out of range"; return GBX_ERR_UNSUPPORTED; }
         L.hung_order = l.order;
@@ -247,6 +253,7 @@ int launch_relax(const Params& p, void* stream, std::string* err) {
     GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_EQUALITY_SIMPLEX)
     GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_BIRKHOFF)
     GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_CARDINALITY)
+    GBX_CASE(GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_LINKED_CARDINALITY)
     GBX_CASE(GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BIRKHOFF)
     GBX_CASE(GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BOX)
 #undef GBX_CASE
@@ -293,6 +300,8 @@ int launch_lmo_batch(const gbx_lmo& l, int cases, int mode, const double* dir,
     case GBX_LMO_CARDINALITY:
         if (mode != 0) { *err = "the cardinality LMO has no in-face oracle (Frank-Wolfe only)"; return GBX_ERR_UNSUPPORTED; }
         return probe_one<GBX_LMO_CARDINALITY>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
+    case GBX_LMO_LINKED_CARDINALITY:
+        return probe_one<GBX_LMO_LINKED_CARDINALITY>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
     default: *err = "lmo kind"; return GBX_ERR_UNSUPPORTED;
     }
 }
@@ -310,6 +319,8 @@ int launch_node_feasible(const gbx_lmo& l, int cases, const double* lb, const do
     case GBX_LMO_EQUALITY_SIMPLEX: return feas_one<GBX_LMO_EQUALITY_SIMPLEX>(l, L, cases, lb, ub, flags, out, st, err);
     case GBX_LMO_BIRKHOFF: return feas_one<GBX_LMO_BIRKHOFF>(l, L, cases, lb, ub, flags, out, st, err);
     case GBX_LMO_CARDINALITY: return feas_one<GBX_LMO_CARDINALITY>(l, L, cases, lb, ub, flags, out, st, err);
+    case GBX_LMO_LINKED_CARDINALITY:
+        return feas_one<GBX_LMO_LINKED_CARDINALITY>(l, L, cases, lb, ub, flags, out, st, err);
     default: *err = "lmo kind"; return GBX_ERR_UNSUPPORTED;
     }
 }

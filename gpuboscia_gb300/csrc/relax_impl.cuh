@@ -126,6 +126,7 @@ struct Ctx {
     double rhs;
     const uint8_t* is_int;
     int lorder;
+    const double* U;      // linked cardinality: per-asset bounds U_i
     int S;
     double* keys;
     double* prefix;
@@ -1018,6 +1019,174 @@ static __device__ bool card_forward(const Ctx& c, const double* g, const double*
     return true;
 }
 
+// Linked cardinality {(v, y): 0 <= v_i <= U_i y_i, sum y <= m, 0 <= y <= 1}
+// (the sparse-Sharpe LinkedCardinalityLMO, examples/sparse_sharpe.cu:266-546):
+// v_i at i, y_i at n/2 + i for the first `order` assets (the rest of each half
+// is padding and stays 0); branching fixes y. Ranks by (cost, asset) are
+// counted directly instead of sorted: rank(i) = #{k eligible : (c_k, k) < (c_i, i)}.
+struct Linked {
+    int half, assets, m;
+};
+static __device__ inline Linked linked_of(const Ctx& c) {
+    Linked L;
+    L.half = c.n / 2;
+    L.assets = c.lorder > 0 ? min(c.lorder, L.half) : L.half;
+    L.m = (int)floor(c.rhs + 1e-9);
+    return L;
+}
+
+// compute_v: the mandatory assets (lb_y > 1/2), then up to m - mandatory
+// optional assets of negative joint cost g_y + min(0, U g_v), cheapest first;
+// a selected asset takes v = U when g_v < 0
+static __device__ void linked_forward(const Ctx& c, const double* g, const double* lb, const double* ub,
+                                      double* v) {
+    const Linked L = linked_of(c);
+    const int h = L.half;
+    int mand = 0;
+    for (int j = c.tid; j < c.n; j += kThreads) v[j] = 0.0;
+    for (int i = c.tid; i < L.assets; i += kThreads) mand += lb[h + i] > 0.5 ? 1 : 0;
+    const int nm = (int)bsum((double)mand, c.red);
+    if (nm > L.m) return;   // node_feasible rejects such nodes first
+    const int slots = L.m - nm;
+    auto cost = [&](int i) { return g[h + i] + fmin(0.0, c.U[i] * g[i]); };
+    auto eligible = [&](int i, double ci) { return ci < 0.0 && lb[h + i] <= 0.5 && ub[h + i] > 0.5; };
+    for (int i = c.tid; i < L.assets; i += kThreads) {
+        bool take = lb[h + i] > 0.5;
+        if (!take && slots > 0) {
+            const double ci = cost(i);
+            if (eligible(i, ci)) {
+                int rank = 0;
+                for (int k = 0; k < L.assets && rank < slots; ++k) {
+                    if (k == i) continue;
+                    const double ck = cost(k);
+                    if (eligible(k, ck) && (ck < ci || (ck == ci && k < i))) ++rank;
+                }
+                take = rank < slots;
+            }
+        }
+        if (take) {
+            v[h + i] = 1.0;
+            v[i] = g[i] < 0.0 ? c.U[i] : 0.0;
+        }
+    }
+    __syncthreads();
+}
+
+// compute_inface_v on the direction sign*g: y entries at a bound stay there,
+// v keeps its zero / linked (v = U y) state, and the free y take the cheapest
+// costs (all of them, cheapest first, when sum y = m is active)
+static __device__ void linked_inface(const Ctx& c, const double* g, double sign, const double* x,
+                                     const double* lb, const double* ub, double* a) {
+    const double atol = 1e-6, rtol = 1e-4;
+    const Linked L = linked_of(c);
+    const int h = L.half;
+    struct Face { bool yf, vz, la; double fy; };
+    auto face = [&](int i) {
+        Face f;
+        const double U = c.U[i], vi = x[i], yi = x[h + i];
+        const bool lo = fabs(yi - lb[h + i]) <= atol + rtol * fmax(fabs(yi), fabs(lb[h + i]));
+        const bool up = fabs(yi - ub[h + i]) <= atol + rtol * fmax(fabs(yi), fabs(ub[h + i]));
+        f.yf = lo || up;
+        f.fy = lo ? lb[h + i] : ub[h + i];
+        f.vz = fabs(vi) <= atol + rtol * fabs(vi);
+        f.la = fabs(vi - U * yi) <= atol + rtol * fmax(fabs(vi), fabs(U * yi));
+        return f;
+    };
+    auto cost = [&](int i, const Face& f) {
+        const double gv = sign * g[i];
+        double ci = sign * g[h + i];
+        if (f.la) ci += c.U[i] * gv;
+        else if (!f.vz) ci += fmin(0.0, c.U[i] * gv);
+        return ci;
+    };
+    for (int j = c.tid; j < c.n; j += kThreads) a[j] = 0.0;
+    int fsel = 0;
+    double sy = 0.0;
+    for (int i = c.tid; i < L.assets; i += kThreads) {
+        const Face f = face(i);
+        if (f.yf) {
+            a[h + i] = f.fy;
+            if (f.fy > 0.5) ++fsel;
+            if (!f.vz) a[i] = f.la ? c.U[i] * f.fy : (sign * g[i] < 0.0 ? c.U[i] * f.fy : 0.0);
+        }
+        sy += x[h + i];
+    }
+    const int fixed_sel = (int)bsum((double)fsel, c.red);
+    const double sum_y = bsum(sy, c.red);
+    const bool full = fabs(sum_y - L.m) <= atol + rtol * fmax(fabs(sum_y), (double)L.m);
+    const int slots = L.m - fixed_sel;
+    for (int i = c.tid; i < L.assets; i += kThreads) {
+        const Face f = face(i);
+        if (f.yf || slots <= 0) continue;
+        const double ci = cost(i, f);
+        if (!(full || ci < 0.0)) continue;
+        int rank = 0;
+        for (int k = 0; k < L.assets && rank < slots; ++k) {
+            if (k == i) continue;
+            const Face fk = face(k);
+            if (fk.yf) continue;
+            const double ck = cost(k, fk);
+            if ((full || ck < 0.0) && (ck < ci || (ck == ci && k < i))) ++rank;
+        }
+        if (rank < slots) {
+            a[h + i] = 1.0;
+            a[i] = f.la ? c.U[i] : (!f.vz ? (sign * g[i] < 0.0 ? c.U[i] : 0.0) : 0.0);
+        }
+    }
+    __syncthreads();
+}
+
+// integer_candidate_device: the mandatory assets plus the largest positive v
+// of x up to m, v taken from x (or the asset of largest mu = -ls c when x has
+// no positive v), scaled to the objective's minimum along that direction,
+// t = -ls c'd / d'Qd, capped by U_i / d_i. Thread 0, assets in order.
+static __device__ void linked_candidate(const Ctx& c, const double* x, const double* lb, const double* ub,
+                                        double* cand) {
+    const Linked L = linked_of(c);
+    const int h = L.half, n = c.n;
+    for (int j = c.tid; j < n; j += kThreads) cand[j] = 0.0;
+    __syncthreads();
+    if (c.tid == 0) {
+        auto mu = [&](int i) { return c.c ? -c.ls * c.c[i] : 0.0; };
+        int selected = 0;
+        for (int i = 0; i < L.assets; ++i)
+            if (lb[h + i] > 0.5) { cand[h + i] = 1.0; ++selected; }
+        while (selected < L.m) {
+            int best = -1;
+            for (int i = 0; i < L.assets; ++i)
+                if (cand[h + i] == 0.0 && ub[h + i] > 0.5 && x[i] > 1e-12 && (best < 0 || x[i] > x[best])) best = i;
+            if (best < 0) break;
+            cand[h + best] = 1.0;
+            ++selected;
+        }
+        bool direction = false;
+        for (int i = 0; i < L.assets; ++i)
+            if (cand[h + i] == 1.0) {
+                cand[i] = fmax(0.0, x[i]);
+                direction = direction || cand[i] > 0.0;
+            }
+        if (!direction) {
+            int best = -1;
+            for (int i = 0; i < L.assets; ++i)
+                if ((cand[h + i] == 1.0 || (selected < L.m && ub[h + i] > 0.5)) && (best < 0 || mu(i) > mu(best)))
+                    best = i;
+            if (best >= 0 && mu(best) > 0.0) {
+                cand[h + best] = 1.0;
+                cand[best] = 1.0;
+            }
+        }
+        double lin = 0.0, quad = 0.0, cap = CUDART_INF;
+        for (int i = 0; i < L.assets; ++i) {
+            lin += mu(i) * cand[i];
+            if (cand[i] > 0.0) cap = fmin(cap, c.U[i] / cand[i]);
+            for (int j = 0; j < L.assets; ++j) quad += cand[i] * c.Q[(size_t)i * n + j] * cand[j];
+        }
+        const double t = lin > 0.0 && quad > 0.0 ? fmin(lin / quad, cap) : 0.0;
+        for (int i = 0; i < L.assets; ++i) cand[i] *= t;
+    }
+    __syncthreads();
+}
+
 // ------------------------------------------------------------------ LMOs
 template <int LK>
 static __device__ bool lmo_forward(const Ctx& c, const double* g, const double* lb,
@@ -1040,6 +1209,9 @@ static __device__ bool lmo_forward(const Ctx& c, const double* g, const double* 
         return c.flag[0] != 0;
     } else if constexpr (LK == GBX_LMO_CARDINALITY) {
         card_forward(c, g, lb, ub, v);
+        return false;
+    } else if constexpr (LK == GBX_LMO_LINKED_CARDINALITY) {
+        linked_forward(c, g, lb, ub, v);
         return false;
     } else {
         double loc = 0.0;
@@ -1079,6 +1251,9 @@ static __device__ bool lmo_inface(const Ctx& c, const double* g, double sign, co
         for (int j = c.tid; j < n; j += kThreads) a[j] = x[j];
         __syncthreads();
         return false;
+    } else if constexpr (LK == GBX_LMO_LINKED_CARDINALITY) {
+        linked_inface(c, g, sign, x, lb, ub, a);
+        return false;
     } else {
         double lm = 0.0, lx = 0.0;
         for (int j = c.tid; j < n; j += kThreads) {
@@ -1112,6 +1287,29 @@ static __device__ double lmo_max_step(const Ctx& c, const double* d, const doubl
                                const double* lb, const double* ub) {
     const int n = c.n;
     double res = 1.0;
+    if constexpr (LK == GBX_LMO_LINKED_CARDINALITY) {
+        // dicg_maximum_step_local and dicg_sum_maximum_step
+        const Linked L = linked_of(c);
+        const int h = L.half;
+        const double tol = 1e-9;
+        double sx = 0.0, sd = 0.0;
+        for (int i = c.tid; i < L.assets; i += kThreads) {
+            const double dv = d[i], dy = d[h + i];
+            if (dv > tol) res = fmin(res, x[i] / dv);
+            const double link_d = dv - c.U[i] * dy;
+            const double link_x = x[i] - c.U[i] * x[h + i];
+            if (link_d < -tol) res = fmin(res, link_x / link_d);
+            if (dy > tol) res = fmin(res, (x[h + i] - lb[h + i]) / dy);
+            else if (dy < -tol) res = fmin(res, (ub[h + i] - x[h + i]) / -dy);
+            sx += x[h + i];
+            sd += dy;
+        }
+        const double coord = bmin(res, c.red);
+        const double sum_x = bsum(sx, c.red);
+        const double sum_d = bsum(sd, c.red);
+        const double agg = sum_d < -1e-9 ? fmax(0.0, fmin(1.0, (sum_x - L.m) / sum_d)) : 1.0;
+        return fmax(0.0, fmin(coord, agg));
+    }
     for (int j = c.tid; j < n; j += kThreads) {
         const double dj = d[j];
         if constexpr (LK == GBX_LMO_BOX) {
@@ -1182,6 +1380,11 @@ static __device__ bool node_feasible(const Ctx& c, const double* lb, const doubl
         const int nf = (int)bsum((double)forced, c.red);
         const bool any_open = __syncthreads_or(open) != 0;
         return nf <= K && (nf >= 1 || (K >= 1 && any_open));
+    } else if constexpr (LK == GBX_LMO_LINKED_CARDINALITY) {
+        const Linked L = linked_of(c);
+        int mand = 0;
+        for (int i = c.tid; i < L.assets; i += kThreads) mand += lb[L.half + i] > 0.5 ? 1 : 0;
+        return (int)bsum((double)mand, c.red) <= L.m;
     } else {
         bool v2 = true, cont = false;
         double mand = 0.0, cap = 0.0;
@@ -1241,6 +1444,19 @@ static __device__ bool rounded_feasible(const Ctx& c, const double* x) {
         const double SW = bsum(sw, c.red);
         const double SZ = bsum(sz, c.red);
         return nn && fabs(SW - 1.0) <= tol && SZ <= floor(c.rhs + 1e-9) + tol;
+    } else if constexpr (LK == GBX_LMO_LINKED_CARDINALITY) {
+        // candidate_feasible_device: 0 <= v <= U y, sum y <= m
+        const Linked L = linked_of(c);
+        bool valid = true;
+        double sy = 0.0;
+        for (int i = c.tid; i < L.assets; i += kThreads) {
+            const double y = x[L.half + i];
+            valid = valid && x[i] >= -tol && x[i] <= c.U[i] * y + tol;
+            sy += y;
+        }
+        const bool ok = __syncthreads_and(valid);
+        const double SY = bsum(sy, c.red);
+        return ok && SY <= L.m + tol;
     } else {
         bool valid = true;
         double s = 0.0;
@@ -1637,6 +1853,7 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
     c.rhs = P.lmo.right_side;
     c.is_int = P.lmo.is_int;
     c.lorder = P.lmo.order;
+    c.U = P.lmo.upper;
     c.S = L.sort_size;
     c.keys = reinterpret_cast<double*>(dsm + L.sm_keys);
     c.prefix = reinterpret_cast<double*>(dsm + L.sm_prefix);
@@ -1882,12 +2099,17 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
     int st = (fgap >= 0.0 && fgap < eps) ? 1 : 0;
     if (c.flags) {
         bool zero_one = true;
-        for (int j = tid; j < n; j += kThreads) {
-            const double r = c.flags[j] ? round(X[j]) : X[j];
-            CAND[j] = r;
-            if (r != 0.0 && r != 1.0) zero_one = false;
+        if constexpr (LK == GBX_LMO_LINKED_CARDINALITY) {
+            linked_candidate(c, X, LB, UB, CAND);
+            zero_one = false;
+        } else {
+            for (int j = tid; j < n; j += kThreads) {
+                const double r = c.flags[j] ? round(X[j]) : X[j];
+                CAND[j] = r;
+                if (r != 0.0 && r != 1.0) zero_one = false;
+            }
+            __syncthreads();
         }
-        __syncthreads();
         if (rounded_feasible<LK>(c, CAND)) {
             // a 0/1 point with unit row and column sums is a permutation: its
             // value in O(m^2) is bit-identical to the generic one
@@ -1964,6 +2186,7 @@ __global__ void __launch_bounds__(kThreads, 1) lmo_probe_kernel(
     c.rhs = lmo.right_side;
     c.is_int = lmo.is_int;
     c.lorder = lmo.order;
+    c.U = lmo.upper;
     c.S = L.sort_size;
     c.keys = reinterpret_cast<double*>(dsm + L.sm_keys);
     c.prefix = reinterpret_cast<double*>(dsm + L.sm_prefix);
@@ -2019,6 +2242,7 @@ __global__ void __launch_bounds__(kThreads, 1) feasible_kernel(
     c.rhs = lmo.right_side;
     c.is_int = lmo.is_int;
     c.lorder = lmo.order;
+    c.U = lmo.upper;
     c.S = L.sort_size;
     c.hung[0] = dsm + L.sm_hung;
     c.hung[1] = dsm + L.sm_hung + L.hung_bytes;

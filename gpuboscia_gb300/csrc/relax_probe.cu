@@ -13,5 +13,6 @@ GBX_PROBE(GBX_LMO_SIMPLEX)
 GBX_PROBE(GBX_LMO_EQUALITY_SIMPLEX)
 GBX_PROBE(GBX_LMO_BIRKHOFF)
 GBX_PROBE(GBX_LMO_CARDINALITY)
+GBX_PROBE(GBX_LMO_LINKED_CARDINALITY)
 #undef GBX_PROBE
 }  // namespace gbx

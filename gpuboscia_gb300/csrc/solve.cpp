@@ -41,6 +41,19 @@ bool relaxation_feasible(const gbx_lmo& l, const std::vector<double>& x, double 
         }
         return std::abs(sw - 1.0) <= tol && sz <= std::floor(l.right_side + 1e-9) + tol;
     }
+    if (l.kind == GBX_LMO_LINKED_CARDINALITY) {
+        // candidate_feasible_device of the sparse-Sharpe LMO on the host
+        const int half = (int)x.size() / 2, assets = l.order > 0 ? l.order : half;
+        std::vector<double> U(assets);
+        GBX_CUDA_CHECK(cudaMemcpy(U.data(), l.upper, assets * sizeof(double), cudaMemcpyDeviceToHost));
+        double sy = 0.0;
+        for (int i = 0; i < assets; ++i) {
+            const double v = x[i], y = x[half + i];
+            if (v < -tol || v > U[i] * y + tol || y < -tol || y > 1 + tol) return false;
+            sy += y;
+        }
+        return sy <= std::floor(l.right_side + 1e-9) + tol;
+    }
     const int m = l.order;
     if ((int)x.size() != m * m) return false;
     for (double v : x) if (v < -tol || v > 1 + tol) return false;
@@ -201,6 +214,7 @@ int gbx_solve(const gbx_problem* problem, const gbx_objective* obj, const gbx_lm
         spec.kind = lmo->kind;
         spec.right_side = lmo->right_side;
         spec.order = lmo->order;
+        spec.upper = lmo->upper;
         if (lmo->is_int) {
             spec.is_int.resize(n);
             GBX_CUDA_CHECK(cudaMemcpy(spec.is_int.data(), lmo->is_int, n, cudaMemcpyDeviceToHost));

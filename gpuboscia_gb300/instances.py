@@ -278,3 +278,60 @@ def graph_matching_from_file(path, seed: int = 0) -> Instance:
     X = np.zeros((m, m))
     X[p, np.arange(m)] = 1.0   # A X = X B
     return graph_matching(m, A, B, os.path.basename(str(path)), 0.0, X.ravel())
+
+
+# ---------------------------------------------------------------- sparse Sharpe
+def sparse_sharpe(prices: np.ndarray, assets: int = 125, cardinality: int = 10, observations: int = 60,
+                  epsilon: float = 1e-3, padded: int | None = None) -> Instance:
+    """examples/sparse_sharpe.cu:550-799: discrete sparse Sharpe-ratio portfolio.
+
+    prices: T x N gross returns (the MAT variable `data`); the first `assets`
+    columns over the last `observations` rows. minimize 0.5 v'(Sigma + eps I)v
+    - mu'v over 0 <= v_i <= U_i y_i, sum y <= cardinality, y binary; the
+    portfolio is w = v / sum v. U_i = max(c_i + sqrt(max((H^-1)_ii r^2, 0)), 0)
+    with c = H^-1 mu and r^2 = max(mu'c, 0) bounds every v on the level set
+    below f = 0, and -r^2 / 2 (the unconstrained minimum) is the natural lower
+    bound. x = (v, y) with y at `padded` (default: assets)."""
+    prices = np.asarray(prices, np.float64)
+    T, N = prices.shape
+    if not 1 <= cardinality <= assets <= N:
+        raise ValueError("need 1 <= cardinality <= assets <= available columns")
+    half = assets if padded is None else int(padded)
+    if half < assets:
+        raise ValueError("padded must be >= assets")
+    obs = T if observations <= 0 else min(observations, T)
+    R = prices[T - obs:, :assets] - 1.0
+    mu = R.sum(0) / obs
+    D = R - mu
+    H = D.T @ D * (1.0 / (obs - 1) if obs > 1 else 1.0) + epsilon * np.eye(assets)
+    L = np.linalg.cholesky(H)
+    center = np.linalg.solve(L.T, np.linalg.solve(L, mu))
+    r2 = max(float(mu @ center), 0.0)
+    Hinv_diag = np.diag(np.linalg.solve(L.T, np.linalg.solve(L, np.eye(assets))))
+    U = np.maximum(center + np.sqrt(np.maximum(Hinv_diag * r2, 0.0)), 0.0)
+    n = 2 * half
+    Q = np.zeros((n, n))
+    Q[:assets, :assets] = H
+    c = np.zeros(n)
+    c[:assets] = -mu
+    lb = np.zeros(n)
+    ub = np.zeros(n)
+    ub[:assets] = U
+    ub[half:half + assets] = 1.0
+    prob = api.Problem(n, lb, ub, list(range(half, half + assets)))
+    s = api.Settings(algorithm=1, line_search=3, secant_iters=16, secant_tol=1e-10, secant_denom_eps=1e-14,
+                     gpu_max_iters=10000, integer_tol=1e-5, abs_gap_tol=1e-6, rel_gap_tol=1e-2,
+                     natural_lower_bound=-0.5 * r2)
+    return Instance(f"sparse_sharpe_n{assets}_m{cardinality}", prob, api.DenseQuadraticObjective(Q, c),
+                    api.LinkedCardinalityLMO(U, cardinality), s)
+
+
+def synthetic_gross_returns(months: int, assets: int, seed: int = SEEDS[3]) -> np.ndarray:
+    """Monthly gross returns (1 + r) of a 3-factor model, the shape of the
+    sparse-Sharpe example's `data` matrix."""
+    rng = _rng(seed)
+    f = normal(rng, (months, 3), 0.006, 0.04)
+    beta = normal(rng, (assets, 3), 1.0, 0.3)
+    vol = 0.03 + 0.08 * rng.random(assets)
+    alpha = normal(rng, assets, 0.0, 0.004)
+    return 1.0 + f @ beta.T + alpha[None, :] + normal(rng, (months, assets)) * vol[None, :]

@@ -142,6 +142,7 @@ public:
         lmo_.n = n;
         lmo_.right_side = lmo_spec_.right_side;
         lmo_.order = lmo_spec_.order;
+        lmo_.upper = lmo_spec_.upper;
         std::vector<uint8_t> flags(n, 0);
         for (int j : prob_.int_vars) flags[j] = 1;
         GBX_CUDA_CHECK(cudaMalloc(&d_flags_, std::max<size_t>(n, 1)));

@@ -19,6 +19,7 @@ struct LMOSpec {
     double right_side = 1.0;
     std::vector<uint8_t> is_int;  // simplex integer flags, empty = none
     int order = 0;
+    const double* upper = nullptr;  // linked cardinality: device per-asset bounds U_i
 };
 }  // namespace gpuboscia
 
@@ -94,12 +95,12 @@ struct BirkhoffLMO {
     gpuboscia::LMOSpec spec(int) const { return {GBX_LMO_BIRKHOFF, 1.0, {}, Order}; }
 };
 
-// Cardinality-linked simplex over x = (w, z), n = 2*Assets:
+// Cardinality-constrained simplex over x = (w, z), n = 2*Assets:
 // sum w = 1, 0 <= w <= z, sum z <= cardinality, 0 <= z <= 1. Branching fixes z;
 // Frank-Wolfe only (no in-face oracle). No counterpart in the reference (its
-// LinkedCardinalityLMO, examples/sparse_sharpe.cu:266-546, lacks sum w = 1).
+// LinkedCardinalityLMO, below, lacks sum w = 1).
 template <int Assets>
-struct LinkedCardinalityLMO {
+struct SimplexCardinalityLMO {
     static_assert(Assets > 0, "asset count must be positive");
     static constexpr bool supports_dicg = false;
     static constexpr int variable_count = 2 * Assets;
@@ -117,4 +118,26 @@ struct LinkedCardinalityLMO {
         return std::abs(sw - 1) <= tol && sz <= cardinality + tol;
     }
     gpuboscia::LMOSpec spec(int) const { return {GBX_LMO_CARDINALITY, double(cardinality), {}, 0}; }
+};
+
+// The reference's sparse-Sharpe oracle (examples/sparse_sharpe.cu:266-546),
+// same members in the same order so `LinkedCardinalityLMO lmo{assets, m, d_U,
+// d_H, d_mu}` compiles unchanged: D = {(v, y): 0 <= v_i <= U_i y_i, 1'y <= m}
+// with x = (v, y), y at offset n_vars / 2 (the example's MaxAssets), the first
+// `assets` coordinates of each half active. Frank-Wolfe and DICG. The rounding
+// candidate scales along the objective (a dense quadratic whose v-block is H
+// and whose linear term is -mu), so device_H / device_mu are not read.
+struct LinkedCardinalityLMO {
+    static constexpr bool supports_dicg = true;
+    int assets = 0;
+    int cardinality = 1;
+    const double* device_upper_bounds = nullptr;
+    const double* device_H = nullptr;
+    const double* device_mu = nullptr;
+    gpuboscia::LMOSpec spec(int n) const {
+        gpuboscia::LMOSpec s{GBX_LMO_LINKED_CARDINALITY, double(cardinality), {}, assets};
+        (void)n;
+        s.upper = device_upper_bounds;
+        return s;
+    }
 };

@@ -84,11 +84,17 @@ enum {
     GBX_LMO_SIMPLEX = 2,            /* UnitSimplexLMO<n,false>, lmo.cuh:335-907       */
     GBX_LMO_EQUALITY_SIMPLEX = 3,   /* EqualitySimplexLMO<n>, lmo.cuh:911-912         */
     GBX_LMO_BIRKHOFF = 4,           /* BirkhoffLMO<order>, lmo.cuh:918-1419           */
-    GBX_LMO_CARDINALITY = 5         /* x = (w, z), n = 2N: sum w = 1, 0 <= w <= z,
+    GBX_LMO_CARDINALITY = 5,        /* x = (w, z), n = 2N: sum w = 1, 0 <= w <= z,
                                        sum z <= right_side, 0 <= z <= 1; node bounds on z
                                        (lb > 1/2 forced, ub < 1/2 forbidden); Frank-Wolfe
                                        only (no counterpart in the reference; the pattern
                                        of examples/sparse_sharpe.cu:266-546 plus sum w = 1) */
+    GBX_LMO_LINKED_CARDINALITY = 6  /* LinkedCardinalityLMO, examples/sparse_sharpe.cu:266-546:
+                                       x = (v, y), y at offset n/2; the first `order`
+                                       assets are active (0: n/2), the rest padding;
+                                       0 <= v_i <= upper[i] * y_i, sum y <= right_side,
+                                       0 <= y <= 1; node bounds on y; FW and DICG;
+                                       needs a dense quadratic objective */
 };
 
 typedef struct gbx_lmo {
@@ -96,7 +102,8 @@ typedef struct gbx_lmo {
     int n;                    /* number of variables                          */
     double right_side;        /* simplex mass                                 */
     const uint8_t* is_int;    /* device, n: the simplex LMO's integer flags   */
-    int order;                /* Birkhoff order                               */
+    int order;                /* Birkhoff order; linked cardinality: active assets */
+    const double* upper;      /* device [order]: linked cardinality bounds U_i */
 } gbx_lmo;
 
 /* ---- algorithm policy (algorithms.cuh, line_search_options.h) ---------- */

@@ -415,8 +415,86 @@ struct LMO {
         return true;
     }
 
+    // ---- linked cardinality (LinkedCardinalityLMO, examples/sparse_sharpe.cu:266-546):
+    // x = (v, y), y at n/2, the first `order` assets active, 0 <= v <= U y, sum y <= m
+    bool linked() const { return l->kind == GBX_LMO_LINKED_CARDINALITY; }
+    int lhalf() const { return n / 2; }
+    int lassets() const { return l->order > 0 ? std::min(l->order, n / 2) : n / 2; }
+    int lm() const { return (int)std::floor(l->right_side + 1e-9); }
+
+    // compute_v: mandatory y, then the cheapest negative joint costs
+    // g_y + min(0, U g_v) by (cost, asset) while slots remain
+    void linked_forward(const double* g, const double* lb, const double* ub, double* v) const {
+        const int h = lhalf(), A = lassets(), m = lm();
+        for (int j = 0; j < n; ++j) v[j] = 0.0;
+        int mand = 0;
+        for (int i = 0; i < A; ++i) mand += lb[h + i] > 0.5 ? 1 : 0;
+        if (mand > m) return;
+        std::vector<std::pair<double, int>> opt;
+        for (int i = 0; i < A; ++i) {
+            const double ci = g[h + i] + std::fmin(0.0, l->upper[i] * g[i]);
+            if (ci < 0.0 && lb[h + i] <= 0.5 && ub[h + i] > 0.5) opt.push_back({ci, i});
+        }
+        std::sort(opt.begin(), opt.end());
+        for (int i = 0; i < A; ++i)
+            if (lb[h + i] > 0.5) { v[h + i] = 1.0; v[i] = g[i] < 0.0 ? l->upper[i] : 0.0; }
+        for (int r = 0; r < (int)opt.size() && r < m - mand; ++r) {
+            const int i = opt[r].second;
+            v[h + i] = 1.0;
+            v[i] = g[i] < 0.0 ? l->upper[i] : 0.0;
+        }
+    }
+
+    // compute_inface_v on the direction gd (the away step passes -g)
+    void linked_inface(const double* gd, const double* x, const double* lb, const double* ub, double* a) const {
+        const double atol = 1e-6, rtol = 1e-4;
+        const int h = lhalf(), A = lassets(), m = lm();
+        const double* U = l->upper;
+        for (int j = 0; j < n; ++j) a[j] = 0.0;
+        std::vector<unsigned char> yf(A), vz(A), la(A);
+        int fixed_sel = 0;
+        Lanes SY;
+        for (int t = 0; t < kLanes; ++t) {
+            double sy = 0.0;
+            for (int i = t; i < A; i += kLanes) sy += x[h + i];
+            SY.v[t] = sy;
+        }
+        for (int i = 0; i < A; ++i) {
+            const double vi = x[i], yi = x[h + i];
+            const bool lo = std::fabs(yi - lb[h + i]) <= atol + rtol * std::fmax(std::fabs(yi), std::fabs(lb[h + i]));
+            const bool up = std::fabs(yi - ub[h + i]) <= atol + rtol * std::fmax(std::fabs(yi), std::fabs(ub[h + i]));
+            yf[i] = lo || up;
+            vz[i] = std::fabs(vi) <= atol + rtol * std::fabs(vi);
+            la[i] = std::fabs(vi - U[i] * yi) <= atol + rtol * std::fmax(std::fabs(vi), std::fabs(U[i] * yi));
+            if (yf[i]) {
+                const double fy = lo ? lb[h + i] : ub[h + i];
+                a[h + i] = fy;
+                if (fy > 0.5) ++fixed_sel;
+                if (!vz[i]) a[i] = la[i] ? U[i] * fy : (gd[i] < 0.0 ? U[i] * fy : 0.0);
+            }
+        }
+        const double sum_y = reduce_sum(SY);
+        const bool full = std::fabs(sum_y - m) <= atol + rtol * std::fmax(std::fabs(sum_y), (double)m);
+        std::vector<std::pair<double, int>> opt;
+        for (int i = 0; i < A; ++i) {
+            if (yf[i]) continue;
+            double ci = gd[h + i];
+            if (la[i]) ci += U[i] * gd[i];
+            else if (!vz[i]) ci += std::fmin(0.0, U[i] * gd[i]);
+            if (full || ci < 0.0) opt.push_back({ci, i});
+        }
+        std::sort(opt.begin(), opt.end());
+        for (int r = 0; r < (int)opt.size() && r < m - fixed_sel; ++r) {
+            const int i = opt[r].second;
+            a[h + i] = 1.0;
+            a[i] = la[i] ? U[i] : (!vz[i] ? (gd[i] < 0.0 ? U[i] : 0.0) : 0.0);
+        }
+    }
+
     void forward(const double* g, const double* lb, const double* ub, double* v) const {
-        if (l->kind == GBX_LMO_CARDINALITY) {
+        if (linked()) {
+            linked_forward(g, lb, ub, v);
+        } else if (l->kind == GBX_LMO_CARDINALITY) {
             card_forward(g, lb, ub, v);
         } else if (l->kind == GBX_LMO_BOX) {
             for (int j = 0; j < n; ++j) v[j] = g[j] > 0.0 ? lb[j] : ub[j];
@@ -443,7 +521,9 @@ struct LMO {
     void inface(const double* g, const double* x, const double* lb,
                 const double* ub, double* a) const {
         const double atol = 1e-6, rtol = 1e-4;
-        if (l->kind == GBX_LMO_BOX) {
+        if (linked()) {
+            linked_inface(g, x, lb, ub, a);
+        } else if (l->kind == GBX_LMO_BOX) {
             for (int j = 0; j < n; ++j) {
                 const double ut = atol + rtol * std::fabs(ub[j]);
                 const double lt = atol + rtol * std::fabs(lb[j]);
@@ -489,6 +569,30 @@ struct LMO {
     // the aggregate constraint, clipped at 0 (device_resident_solver.cuh:533-545)
     double max_step(const double* d, const double* x, const double* lb,
                     const double* ub) const {
+        if (linked()) {
+            // dicg_maximum_step_local and dicg_sum_maximum_step
+            const int h = lhalf(), A = lassets(), m = lm();
+            const double tol = 1e-9;
+            Lanes R, SX, SD;
+            for (int t = 0; t < kLanes; ++t) {
+                double res = 1.0, sx = 0.0, sd = 0.0;
+                for (int i = t; i < A; i += kLanes) {
+                    const double dv = d[i], dy = d[h + i], U = l->upper[i];
+                    if (dv > tol) res = std::fmin(res, x[i] / dv);
+                    const double link_d = dv - U * dy, link_x = x[i] - U * x[h + i];
+                    if (link_d < -tol) res = std::fmin(res, link_x / link_d);
+                    if (dy > tol) res = std::fmin(res, (x[h + i] - lb[h + i]) / dy);
+                    else if (dy < -tol) res = std::fmin(res, (ub[h + i] - x[h + i]) / -dy);
+                    sx += x[h + i];
+                    sd += dy;
+                }
+                R.v[t] = res; SX.v[t] = sx; SD.v[t] = sd;
+            }
+            const double coord = reduce_min(R);
+            const double sum_x = reduce_sum(SX), sum_d = reduce_sum(SD);
+            const double agg = sum_d < -1e-9 ? std::fmax(0.0, std::fmin(1.0, (sum_x - m) / sum_d)) : 1.0;
+            return std::fmax(0.0, std::fmin(coord, agg));
+        }
         Lanes L;
         for (int t = 0; t < kLanes; ++t) {
             double res = 1.0;
@@ -528,6 +632,11 @@ struct LMO {
 
     bool check_feasible(const double* lb, const double* ub, const uint8_t* flags) const {
         if (l->kind == GBX_LMO_BOX) return true;
+        if (linked()) {
+            int mand = 0;
+            for (int i = 0; i < lassets(); ++i) mand += lb[lhalf() + i] > 0.5 ? 1 : 0;
+            return mand <= lm();
+        }
         if (l->kind == GBX_LMO_CARDINALITY) {
             const int N = n / 2;
             const int K = (int)std::floor(l->right_side + 1e-9);
@@ -570,6 +679,21 @@ struct LMO {
 
     bool rounded_feasible(const double* x, double tol) const {
         if (l->kind == GBX_LMO_BOX) return true;
+        if (linked()) {
+            // candidate_feasible_device: 0 <= v <= U y, sum y <= m
+            const int h = lhalf(), A = lassets();
+            bool valid = true;
+            Lanes SY;
+            for (int t = 0; t < kLanes; ++t) {
+                double sy = 0.0;
+                for (int i = t; i < A; i += kLanes) {
+                    valid = valid && x[i] >= -tol && x[i] <= l->upper[i] * x[h + i] + tol;
+                    sy += x[h + i];
+                }
+                SY.v[t] = sy;
+            }
+            return valid && reduce_sum(SY) <= lm() + tol;
+        }
         if (l->kind == GBX_LMO_CARDINALITY) {
             const int N = n / 2;
             bool valid = true;
@@ -636,6 +760,53 @@ struct Relaxer {
             L.v[t] = loc;
         }
         return reduce_sum(L);
+    }
+
+    // integer_candidate_device of the linked cardinality LMO: mandatory assets,
+    // then the largest positive v of x up to m (or the asset of largest
+    // mu = -ls c), scaled to the objective's minimum along the direction,
+    // t = -ls c'd / d'Qd, capped by U_i / d_i; assets in order
+    void linked_candidate(const double* x, const double* lb, const double* ub, double* cand) const {
+        const int h = lmo.lhalf(), A = lmo.lassets(), m = lmo.lm();
+        const gbx_objective* o = obj.o;
+        const double* U = lmo.l->upper;
+        for (int j = 0; j < n; ++j) cand[j] = 0.0;
+        auto mu = [&](int i) { return o->c ? -o->linear_scale * o->c[i] : 0.0; };
+        int selected = 0;
+        for (int i = 0; i < A; ++i)
+            if (lb[h + i] > 0.5) { cand[h + i] = 1.0; ++selected; }
+        while (selected < m) {
+            int best = -1;
+            for (int i = 0; i < A; ++i)
+                if (cand[h + i] == 0.0 && ub[h + i] > 0.5 && x[i] > 1e-12 && (best < 0 || x[i] > x[best])) best = i;
+            if (best < 0) break;
+            cand[h + best] = 1.0;
+            ++selected;
+        }
+        bool direction = false;
+        for (int i = 0; i < A; ++i)
+            if (cand[h + i] == 1.0) {
+                cand[i] = std::fmax(0.0, x[i]);
+                direction = direction || cand[i] > 0.0;
+            }
+        if (!direction) {
+            int best = -1;
+            for (int i = 0; i < A; ++i)
+                if ((cand[h + i] == 1.0 || (selected < m && ub[h + i] > 0.5)) && (best < 0 || mu(i) > mu(best)))
+                    best = i;
+            if (best >= 0 && mu(best) > 0.0) {
+                cand[h + best] = 1.0;
+                cand[best] = 1.0;
+            }
+        }
+        double lin = 0.0, quad = 0.0, cap = kInf;
+        for (int i = 0; i < A; ++i) {
+            lin += mu(i) * cand[i];
+            if (cand[i] > 0.0) cap = std::fmin(cap, U[i] / cand[i]);
+            for (int j = 0; j < A; ++j) quad += cand[i] * o->Q[(size_t)i * n + j] * cand[j];
+        }
+        const double t = lin > 0.0 && quad > 0.0 ? std::fmin(lin / quad, cap) : 0.0;
+        for (int i = 0; i < A; ++i) cand[i] *= t;
     }
 
     double integer_value(const double* x, const double* lb, const double* ub,
@@ -824,9 +995,11 @@ struct Relaxer {
         b->value[node] = fval;
         b->gap[node] = fgap;
         uint8_t st = (fgap >= 0.0 && fgap < eps) ? 1 : 0;
-        // rounding heuristic
+        // rounding heuristic (the linked cardinality LMO's own candidate)
         if (flags) {
-            for (int j = 0; j < n; ++j) cand[j] = flags[j] ? std::round(x[j]) : x[j];
+            if (lmo.linked()) linked_candidate(x, lb, ub, cand.data());
+            else
+                for (int j = 0; j < n; ++j) cand[j] = flags[j] ? std::round(x[j]) : x[j];
             if (lmo.rounded_feasible(cand.data(), tol)) {
                 const double cv = integer_value(cand.data(), lb, ub, flags, tol);
                 if (cv < b->best_vertex_val[node]) {
@@ -853,7 +1026,7 @@ int check_descs(const gbx_objective* o, const gbx_lmo* l, const gbx_algorithm* a
     if (o->kind != GBX_OBJ_GRAPH_MATCHING && o->kind != GBX_OBJ_DENSE_QUADRATIC) {
         g_error = "objective kind"; return GBX_ERR_UNSUPPORTED;
     }
-    if (l->kind < GBX_LMO_BOX || l->kind > GBX_LMO_CARDINALITY) { g_error = "lmo kind"; return GBX_ERR_UNSUPPORTED; }
+    if (l->kind < GBX_LMO_BOX || l->kind > GBX_LMO_LINKED_CARDINALITY) { g_error = "lmo kind"; return GBX_ERR_UNSUPPORTED; }
     if (a->line_search < 0 || a->line_search > 4) { g_error = "line search"; return GBX_ERR_INVALID; }
     return GBX_OK;
 }

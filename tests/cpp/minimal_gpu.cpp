@@ -1,7 +1,8 @@
 // The reference's examples/minimal.cu (min (x0-.3)^2 + (x1-.7)^2 over binaries:
 // x = [0, 1], f = .18) through the C++ drop-in headers, once with the host
 // frontier and once with the device frontier; and a graph-matching pair of
-// order 5 solved both ways to the same certified optimum.
+// order 5 solved both ways to the same certified optimum; and a small
+// sparse-Sharpe portfolio through the reference's LinkedCardinalityLMO.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -92,6 +93,46 @@ int main() {
         obj_val[dev] = r.objective;
     }
     CHECK(std::fabs(obj_val[0] - obj_val[1]) <= 1e-9);
+
+    // sparse Sharpe (examples/sparse_sharpe.cu): 3 assets padded to 4, at most
+    // one; min 0.5 v'Hv - mu'v with H = I, mu = (.5, .3, .1): v = (.5, 0, 0),
+    // f = -0.125, y = (1, 0, 0)
+    constexpr int MaxAssets = 4, Vars = 2 * MaxAssets;
+    std::vector<double> Q(Vars * Vars, 0.0), lin(Vars, 0.0);
+    for (int i = 0; i < 3; ++i) Q[i * Vars + i] = 1.0;
+    lin[0] = -.5; lin[1] = -.3; lin[2] = -.1;
+    double* dQs = upload(Q);
+    double* dls = upload(lin);
+    double* dU = upload<double>({10.0, 10.0, 10.0});
+    GlobalCachedDenseQuadraticObjective<Vars> sharpe(dQs, dls);
+    LinkedCardinalityLMO linked{3, 1, dU, nullptr, nullptr};
+    Problem sp;
+    sp.n_vars = Vars;
+    sp.lb.assign(Vars, 0.0);
+    sp.ub.assign(Vars, 0.0);
+    for (int i = 0; i < 3; ++i) {
+        sp.ub[i] = 10.0;
+        sp.ub[MaxAssets + i] = 1.0;
+        sp.int_vars.push_back(MaxAssets + i);
+    }
+    for (int dev = 0; dev < 2; ++dev) {
+        auto s = gpuboscia::create_default_settings();
+        s.line_search.kind = LineSearchKind::QuadraticExact;
+        s.natural_lower_bound = -0.5 * (.25 + .09 + .01);
+        s.time_limit_seconds = 30;
+        s.device.gpu_batch_size = 16;
+        s.device.rel_gap_tol = 1e-9;
+        s.device.device_frontier = dev != 0;
+        const auto r = gpuboscia::solve(sp, sharpe, linked, s);
+        std::printf("sparse sharpe device_frontier=%d: f=%.12f y=[%g %g %g] nodes=%d\n", dev, r.objective,
+                    r.x.size() == Vars ? r.x[MaxAssets] : -1.0, r.x.size() == Vars ? r.x[MaxAssets + 1] : -1.0,
+                    r.x.size() == Vars ? r.x[MaxAssets + 2] : -1.0, r.nodes_processed);
+        CHECK(std::fabs(r.objective + 0.125) <= 1e-6);
+        CHECK(r.x.size() == Vars && r.x[MaxAssets] == 1.0 && r.x[MaxAssets + 1] == 0.0 && r.x[MaxAssets + 2] == 0.0);
+    }
+    cudaFree(dQs);
+    cudaFree(dls);
+    cudaFree(dU);
     cudaFree(dQ);
     cudaFree(dc);
     cudaFree(dA);
