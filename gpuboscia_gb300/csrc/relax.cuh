@@ -46,6 +46,11 @@ struct Layout {
     int persistent;           // persistent grid over an atomic node queue
     size_t sm_mx, sm_cost, sm_code, sm_ihw, ihw_bytes;
     size_t mixed_node_bytes;  // bytes per node of the workspace's mixed region
+    // orders whose oracle costs do not fit in shared memory (above ~128):
+    // the costs and edge codes live in the node's mixed region at these
+    // offsets, the gradient runs over the nonzero lists in FP32
+    int cost_global;
+    size_t mx_cost_off, mx_code_off;
     // graph matching: nonzero lists of A and B (rows and columns), built once
     // per launch at the end of the workspace; up to sparse_cap entries each
     int sparse_cap;

@@ -89,8 +89,8 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
     L.mixed = mixed ? 1 : 0;
     size_t mx_bytes = 0, cost_bytes = 0, code_bytes = 0;
     if (mixed) {
-        if (l.order > 256) {
-            *err = "mixed precision supports Birkhoff orders up to 256";
+        if (l.order > 512) {
+            *err = "mixed precision supports Birkhoff orders up to 512";
             return GBX_ERR_UNSUPPORTED;
         }
         mx_bytes = mixed_array_bytes(n);
@@ -104,7 +104,9 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
         cost_bytes = std::max(cost_bytes, align16((size_t)n * sizeof(double)));  // the certificate's FP64 costs
         code_bytes = align16(2 * (size_t)n);
         L.ihw_bytes = ihw_bytes(l.order);
-        fixed_bytes += cost_bytes + code_bytes + 2 * L.ihw_bytes;
+        // large orders: the oracle costs and edge codes move to the node's workspace
+        L.cost_global = !L.tc && fixed_bytes + cost_bytes + code_bytes + 2 * L.ihw_bytes > kSmemBudget ? 1 : 0;
+        fixed_bytes += (L.cost_global ? 0 : cost_bytes + code_bytes) + 2 * L.ihw_bytes;
     }
     size_t obj_doubles = o.kind == GBX_OBJ_GRAPH_MATCHING ? 2 * (size_t)o.order * o.order
                                                           : (size_t)n * n;
@@ -121,7 +123,7 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
         // the FP32 arrays go to the workspace when they do not fit beside
         // the oracle costs (orders above ~90); x and the bounds follow them
         L.obj_smem = 0;
-        L.mx_global = (L.tc || mx_bytes + fixed_bytes > kSmemBudget) ? 1 : 0;
+        L.mx_global = (L.tc || L.cost_global || mx_bytes + fixed_bytes > kSmemBudget) ? 1 : 0;
         if (!L.mx_global) fixed_bytes += mx_bytes;
         const bool xs = align16(3 * (size_t)n * sizeof(double)) + fixed_bytes <= kSmemBudget;
         smem[B_X] = smem[B_LB] = smem[B_UB] = xs;
@@ -157,12 +159,19 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
     }
     L.sm_hung = p; p += 2 * L.hung_bytes;
     L.sm_mx = p; if (mixed && !L.mx_global) p += mx_bytes;
-    L.sm_cost = p; p += cost_bytes;
-    L.sm_code = p; p += code_bytes;
+    L.sm_cost = p; if (!L.cost_global) p += cost_bytes;
+    L.sm_code = p; if (!L.cost_global) p += code_bytes;
     L.sm_ihw = p; p += mixed ? 2 * L.ihw_bytes : 0;
     L.sm_total = p;
     L.mixed_node_bytes = L.mx_global ? (mx_bytes + 255) / 256 * 256 : 0;
     if (L.tc) L.mixed_node_bytes += kTcImageBytes;
+    L.mx_cost_off = L.mx_code_off = 0;
+    if (L.cost_global) {
+        L.mx_cost_off = L.mixed_node_bytes;
+        L.mixed_node_bytes += (cost_bytes + 255) / 256 * 256;
+        L.mx_code_off = L.mixed_node_bytes;
+        L.mixed_node_bytes += (code_bytes + 255) / 256 * 256;
+    }
     L.sparse_cap = 0;
     L.sparse_bytes = 0;
     if (o.kind == GBX_OBJ_GRAPH_MATCHING && o.order >= 16) {

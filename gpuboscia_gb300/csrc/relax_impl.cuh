@@ -726,8 +726,8 @@ static __device__ bool hungarian_group(const HW& w, int m, const double* cost, d
 // augmenting paths for the rows it could not place. Executed by ONE warp;
 // `out` must be zeroed and visible. Returns 0 when no perfect matching exists
 // (contradictory bounds included), 1 with a perfect matching in out and w.pi,
-// and 2 when the masks do not fit the workspace (orders above ~192) -- only
-// then does the caller fall back to the Hungarian.
+// and 2 only above order 1024 (the augmenting-path search's visited set) --
+// then the caller falls back to the Hungarian.
 static __device__ int greedy_matching_warp(const HW& w, int m, const double* lb, const double* ub,
                                            double* out) {
     const int lane = threadIdx.x & 31;
@@ -786,8 +786,12 @@ static __device__ int greedy_matching_warp(const HW& w, int m, const double* lb,
         // augmenting paths (Kuhn) over allowed-edge bitmasks of the compacted
         // rows: exact, so a row without an augmenting path means no perfect matching
         const int W = (k + 31) >> 5;
-        if ((size_t)k * W > 6 * (size_t)(m + 1)) return 2;   // no room for the masks
-        unsigned* mask = reinterpret_cast<unsigned*>(w.u);  // [k][W] over u, pv, minv
+        if (W > 32) return 2;   // beyond the visited set below (orders above 1024)
+        // [k][W] words over u, pv, minv, or over the caller's m*m doubles when
+        // larger (k W <= m ceil(m/32) <= 2 m^2 words); the latter are cleared
+        // before the matching is written
+        const bool in_out = (size_t)k * W > 6 * (size_t)(m + 1);
+        unsigned* mask = reinterpret_cast<unsigned*>(in_out ? out : w.u);
         for (int t = 0; t < k; ++t) {
             const int r = w.rows[t];
             for (int base = 0; base < k; base += 32) {
@@ -834,6 +838,10 @@ static __device__ int greedy_matching_warp(const HW& w, int m, const double* lb,
         }
         ok = __shfl_sync(kFull, ok, 0);
         __syncwarp();
+        if (in_out) {
+            for (int e = lane; e < nn; e += 32) out[e] = 0.0;
+            __syncwarp();
+        }
         if (!ok) return 0;
     }
     for (int t = lane; t < k; t += 32) {
@@ -1497,13 +1505,49 @@ static __device__ double perm_score(const Ctx& c, const uint8_t* code, const int
     return isfinite(val) ? val : kNone;
 }
 
+// R = A X - X B and G = 2s (A'R - R B') in FP32 over the nonzero lists of A
+// and B (rows of A, columns of B for R; columns of A, rows of B for G): for
+// d-regular graphs 4 m^2 d multiply-adds instead of 4 m^3.
+static __device__ void grad_f32_sparse(const SparseAB& S, int m, float two_s, const float* X, float* R, float* G) {
+    const int n = m * m;
+    for (int e = threadIdx.x; e < n; e += kThreads) {
+        const int i = e / m, j = e - (e / m) * m;
+        float r = 0.f;
+        for (int t = S.ptr[0][i]; t < S.ptr[0][i + 1]; ++t) r = fmaf((float)S.val[0][t], X[S.idx[0][t] * m + j], r);
+        for (int t = S.ptr[1][j]; t < S.ptr[1][j + 1]; ++t) r = fmaf(-X[i * m + S.idx[1][t]], (float)S.val[1][t], r);
+        R[e] = r;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n; e += kThreads) {
+        const int p = e / m, q = e - (e / m) * m;
+        float acc = 0.f;
+        for (int t = S.ptr[2][p]; t < S.ptr[2][p + 1]; ++t) acc = fmaf((float)S.val[2][t], R[S.idx[2][t] * m + q], acc);
+        for (int t = S.ptr[3][q]; t < S.ptr[3][q + 1]; ++t) acc = fmaf(-R[p * m + S.idx[3][t]], (float)S.val[3][t], acc);
+        G[e] = two_s * acc;
+    }
+    __syncthreads();
+}
+
+// Oracle costs and edge codes of a mixed-precision node: shared memory, or the
+// node's workspace for large orders.
+static __device__ inline unsigned char* mixed_costs(const Params& P, unsigned char* dsm, int node) {
+    return P.L.cost_global ? P.mixed + (size_t)node * P.L.mixed_node_bytes + P.L.mx_cost_off : dsm + P.L.sm_cost;
+}
+static __device__ inline uint8_t* mixed_codes(const Params& P, unsigned char* dsm, int node) {
+    return P.L.cost_global ? P.mixed + (size_t)node * P.L.mixed_node_bytes + P.L.mx_code_off : dsm + P.L.sm_code;
+}
+
 // Mixed-precision DICG / FW iterations (see mixed.cuh). Works on the FP64
 // iterate X in place and returns the cumulative iteration count; the caller
-// then computes the FP64 certificate at the returned iterate.
-template <bool TC>
+// then computes the FP64 certificate at the returned iterate. MODE 1: FP32
+// SIMT gradient; 2: tensor-core gradient; 3: large orders (costs in the
+// workspace, FP32 gradient over the nonzero lists, 16 columns per lane).
+template <int MODE>
 static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, int node, double* X,
                           const double* LB, const double* UB, double* best, double& best_val,
                           double eps, int it0, bool dicg, int ls, double cutv) {
+    constexpr bool TC = MODE == 2;
+    constexpr bool BIG = MODE == 3;
     const Layout& L = P.L;
     const int n = c.n, m = c.m, tid = c.tid;
     unsigned char* mx = L.mx_global ? P.mixed + (size_t)node * L.mixed_node_bytes : dsm + L.sm_mx;
@@ -1515,9 +1559,9 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
     float* Btf = Bf + n;
     int8_t* Ai = reinterpret_cast<int8_t*>(mx + align16(6 * (size_t)n * sizeof(float)));  // A, B as small
     int8_t* Bi = Ai + align16((size_t)n);      // integers when they are (exact integer scores, curvature)
-    int* costf = reinterpret_cast<int*>(dsm + L.sm_cost);   // forward oracle costs
+    int* costf = reinterpret_cast<int*>(mixed_costs(P, dsm, node));   // forward oracle costs
     int* costa = costf + n;                                  // in-face oracle costs (negated, face only)
-    uint8_t* code = dsm + L.sm_code;
+    uint8_t* code = mixed_codes(P, dsm, node);
     uint8_t* face = code + n;
     const IHW w0 = ihw_at(dsm + L.sm_ihw, m);
     const IHW w1 = ihw_at(dsm + L.sm_ihw + L.ihw_bytes, m);
@@ -1643,6 +1687,8 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
                 __syncthreads();
                 break;
             }
+        } else if (BIG && c.use_sp) {
+            grad_f32_sparse(c.sp, m, two_s, xf, Rf, gf);
         } else {
             grad_f32(m, two_s, Af, Bf, Btf, xf, Rf, gf);
         }
@@ -1668,9 +1714,14 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
             const uint8_t* fc = fwd ? nullptr : face;
             const bool same = fwd || c.flag[4] == 0;
             bool ok;
-            if (m <= 64) ok = int_hungarian_warp<2>(w, m, cst, shift, code, fc, same);
-            else if (m <= 128) ok = int_hungarian_warp<4>(w, m, cst, shift, code, fc, same);
-            else ok = int_hungarian_warp<8>(w, m, cst, shift, code, fc, same);
+            if constexpr (BIG) {
+                if (m <= 256) ok = int_hungarian_warp<8>(w, m, cst, shift, code, fc, same);
+                else ok = int_hungarian_warp<16>(w, m, cst, shift, code, fc, same);
+            } else {
+                if (m <= 64) ok = int_hungarian_warp<2>(w, m, cst, shift, code, fc, same);
+                else if (m <= 128) ok = int_hungarian_warp<4>(w, m, cst, shift, code, fc, same);
+                else ok = int_hungarian_warp<8>(w, m, cst, shift, code, fc, same);
+            }
             if ((threadIdx.x & 31) == 0) c.flag[fwd ? 0 : 2] = ok;
         }
         __syncthreads();
@@ -1996,7 +2047,7 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
     int iters = it0;
     constexpr bool kMixedLoop = MIX != 0 && OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF;
     if constexpr (kMixedLoop)
-        iters = mixed_loop<MIX == 2>(c, P, dsm, node, X, LB, UB, best, best_val, eps, it0, dicg, ls, cutv);
+        iters = mixed_loop<MIX>(c, P, dsm, node, X, LB, UB, best, best_val, eps, it0, dicg, ls, cutv);
     for (int iter = 0; !kMixedLoop && iter < P.b.max_iters; ++iter) {
         iters = it0 + iter + 1;
         obj_grad(c, X, G);
@@ -2079,11 +2130,11 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
         // the integer costs' shared memory is free now: the FP64 Hungarian reads
         // the gradient from there and edge permissions from the code bytes
         // (kAllowed is ub >= 1/2), the same arithmetic as lmo_forward
-        double* Gs = reinterpret_cast<double*>(dsm + L.sm_cost);
+        double* Gs = reinterpret_cast<double*>(mixed_costs(P, dsm, node));
         for (int j = tid; j < n; j += kThreads) { Gs[j] = G[j]; V[j] = 0.0; }
         __syncthreads();
         if (threadIdx.x < kHungThreads) {
-            const bool ok = hungarian_group(hw0, c.lorder, Gs, 1.0, LB, UB, nullptr, V, dsm + L.sm_code, 0);
+            const bool ok = hungarian_group(hw0, c.lorder, Gs, 1.0, LB, UB, nullptr, V, mixed_codes(P, dsm, node), 0);
             if (threadIdx.x == 0) sh.flag[0] = ok;
         }
         __syncthreads();
@@ -2258,7 +2309,7 @@ template <int OK, int LK>
 int launch_one(const Params& p, cudaStream_t st, std::string* err) {
     auto k = relax_kernel<OK, LK, 0>;
     if constexpr (OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF)
-        if (p.L.mixed) k = p.L.tc ? relax_kernel<OK, LK, 2> : relax_kernel<OK, LK, 1>;
+        if (p.L.mixed) k = p.L.tc ? relax_kernel<OK, LK, 2> : p.L.cost_global ? relax_kernel<OK, LK, 3> : relax_kernel<OK, LK, 1>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::max<size_t>(p.L.sm_total, 1));
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }

@@ -168,3 +168,27 @@ def test_mixed_rejects_other_kinds(cuda_lib):
     alg = O.algorithm(A.ALG_DICG, A.LS_SECANT, precision=A.PRECISION_MIXED)
     assert cuda_lib.gbx_relax_workspace_bytes(C.byref(o), C.byref(lm), C.byref(alg), 4) == 0
     assert b"secant" in cuda_lib.gbx_last_error()
+
+
+@pytest.mark.parametrize("order,degree,N,iters", [(180, 8, 4, 10), (400, 10, 3, 4)])
+def test_mixed_large_order_costs_in_workspace(cuda_lib, order, degree, N, iters):
+    """Orders whose oracle costs exceed shared memory (config 5 shape at 400):
+    costs and edge codes in the workspace, FP32 gradient over the nonzero
+    lists, 16 columns per lane in the integer Hungarian above 256; the
+    certificate is still the exact FP64 one at the returned iterate."""
+    inst = instances.birkhoff_regular_isomorphic(order=order, degree=degree, seed=order)
+    n = order * order
+    lb, ub = instances.birkhoff_node_batch(order, N, seed=9)
+    flags = np.ones(n, np.uint8)
+    g = gpu_relax(inst.objective, inst.lmo, mixed(), lb.copy(), lb, ub, 1e-6, np.zeros(N, np.int32),
+                  np.zeros(N, np.uint8), iters, flags)
+    assert (g["iterations"] > 0).all()
+    o = O.relax(inst.objective, inst.lmo, O.algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT), g["x"], lb, ub, 1e-6,
+                g["iterations"], np.full(N, A.NODE_INITIAL_POINT_SUPPLIED, np.uint8), 0, flags)
+    assert np.array_equal(g["gap"], o["gap"])
+    assert np.array_equal(g["value"], o["value"])
+    assert np.array_equal(g["status"], o["status"])
+    assert (g["gap"] >= 0).all()
+    X = g["x"].reshape(N, order, order)
+    assert np.allclose(X.sum(1), 1.0, atol=1e-9) and np.allclose(X.sum(2), 1.0, atol=1e-9)
+    assert (g["x"] >= lb - 1e-12).all() and (g["x"] <= ub + 1e-12).all()
