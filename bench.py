@@ -262,44 +262,64 @@ def time_to_gap(args, inst):
     and mixed precision + the learned scorer (trained first on strong-branching
     labels of four other pairs); same engine settings for all."""
     from gpuboscia_gb300 import _abi as A
-    from gpuboscia_gb300 import instances, scorer
     out = {}
     for name, prec in (("plain_fp64", A.PRECISION_FP64), ("mixed", A.PRECISION_MIXED)):
         wall, r, cert = _solve_timed(inst, prec, None, 256, 2, args.ttg_limit)
         out[name] = {"seconds": wall, "nodes": r.nodes_processed, "objective": r.objective,
                      "dual_bound": r.dual_bound, "certified": cert, "time_limit": bool(r.reached_time_limit)}
 
-    def pair(seed, order=9):
-        rng = np.random.Generator(np.random.PCG64(seed))
-        return instances.graph_matching(order, instances.gnp_graph(rng, order, 0.5),
-                                        instances.gnp_graph(rng, order, 0.5), f"pair{order}_{seed}")
     t0 = time.perf_counter()
-    data = scorer.Dataset.concat([scorer.collect_strong_branching(pair(100 + k), max_nodes=30, max_candidates=64)
-                                  for k in range(4)])
-    sc = scorer.Scorer(32, seed=0)
-    sc.train(data, epochs=400, lr=3e-3)
+    sc = _trained_scorer()
     train_s = time.perf_counter() - t0
     pairs = {"instances": "4 held-out G(9,1/2) pairs; batch 64 x 1 stream, host frontier, unless named; "
                           "full_stack = mixed + learned + device frontier (1024-node rounds) + incumbent cutoff",
              "scorer_training_seconds": train_s}
-    for name, prec, use, batch, streams, dev, cut in (
-            ("plain_fp64", A.PRECISION_FP64, False, 64, 1, 0, 0),
-            ("mixed", A.PRECISION_MIXED, False, 64, 1, 0, 0),
-            ("mixed_learned", A.PRECISION_MIXED, True, 64, 1, 0, 0),
-            ("mixed_learned_256x4", A.PRECISION_MIXED, True, 256, 4, 0, 0),
-            ("device_frontier_mixed_1024", A.PRECISION_MIXED, False, 1024, 1, 1, 0),
-            ("device_frontier_mixed_learned_1024", A.PRECISION_MIXED, True, 1024, 1, 1, 0),
-            ("full_stack", A.PRECISION_MIXED, True, 1024, 1, 1, 1)):
-        tot_s, tot_n, cert = 0.0, 0, True
-        for k in range(4):
-            wall, r, c = _solve_timed(pair(200 + k), prec, sc if use else None, batch, streams, args.ttg_limit,
-                                      dev, cut)
-            tot_s += wall
-            tot_n += r.nodes_processed
-            cert = cert and c
-        pairs[name] = {"seconds": tot_s, "nodes": tot_n, "certified": cert}
+    for name in PAIR_CONFIGS:
+        pairs[name] = _solve_pairs(name, sc, args.ttg_limit)
     out["graph_pairs"] = pairs
     return out
+
+
+def _pair(seed, order=9):
+    from gpuboscia_gb300 import instances
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return instances.graph_matching(order, instances.gnp_graph(rng, order, 0.5),
+                                    instances.gnp_graph(rng, order, 0.5), f"pair{order}_{seed}")
+
+
+def _trained_scorer():
+    """The learned scorer: strong-branching labels of four G(9, 1/2) pairs (seeds
+    100-103, disjoint from the held-out pairs 200-203), 400 Adam epochs."""
+    from gpuboscia_gb300 import scorer
+    data = scorer.Dataset.concat([scorer.collect_strong_branching(_pair(100 + k), max_nodes=30, max_candidates=64)
+                                  for k in range(4)])
+    sc = scorer.Scorer(32, seed=0)
+    sc.train(data, epochs=400, lr=3e-3)
+    return sc
+
+
+# time-to-gap configurations over the held-out pairs:
+# precision, learned scorer, batch, streams, device frontier, incumbent cutoff
+PAIR_CONFIGS = {
+    "plain_fp64": (0, False, 64, 1, 0, 0),
+    "mixed": (1, False, 64, 1, 0, 0),
+    "mixed_learned": (1, True, 64, 1, 0, 0),
+    "mixed_learned_256x4": (1, True, 256, 4, 0, 0),
+    "device_frontier_mixed_1024": (1, False, 1024, 1, 1, 0),
+    "device_frontier_mixed_learned_1024": (1, True, 1024, 1, 1, 0),
+    "full_stack": (1, True, 1024, 1, 1, 1),
+}
+
+
+def _solve_pairs(name, sc, limit):
+    prec, use, batch, streams, dev, cut = PAIR_CONFIGS[name]
+    tot_s, tot_n, cert = 0.0, 0, True
+    for k in range(4):
+        wall, r, c = _solve_timed(_pair(200 + k), prec, sc if use else None, batch, streams, limit, dev, cut)
+        tot_s += wall
+        tot_n += r.nodes_processed
+        cert = cert and c
+    return {"seconds": tot_s, "nodes": tot_n, "certified": cert}
 
 
 def run_gpu(args, rank, world):
@@ -464,7 +484,16 @@ def main():
                     help="time limit of each time-to-gap solve in seconds (0 skips them)")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-budget", type=float, default=8.0)
+    ap.add_argument("--solve", default=None, choices=sorted(PAIR_CONFIGS),
+                    help="only solve the held-out graph pairs with this time-to-gap configuration "
+                         "(one JSON line; for profiling the search)")
     args = ap.parse_args()
+    if args.solve:
+        from gpuboscia_gb300 import build
+        build.build()
+        sc = _trained_scorer() if PAIR_CONFIGS[args.solve][1] else None
+        print(json.dumps({"solve": args.solve, **_solve_pairs(args.solve, sc, args.ttg_limit or 60.0)}))
+        return
     w = WORKLOADS[args.workload]
     if w["kind"] != "birkhoff":
         args.precision = "fp64"   # mixed precision covers graph matching over Birkhoff only
