@@ -104,7 +104,10 @@ void inflate_block(BitReader& br, const Huffman& lit, const Huffman& dist, std::
         const size_t d = (size_t)kDistBase[di] + br.bits(kDistExtra[di]);
         if (d > out.size()) throw std::runtime_error("deflate distance before the start of the output");
         const size_t from = out.size() - d;
-        for (int k = 0; k < len; ++k) out.push_back(out[from + k]);
+        for (int k = 0; k < len; ++k) {
+            const uint8_t b = out[from + k];   // copied before the vector may grow
+            out.push_back(b);
+        }
     }
 }
 
