@@ -237,7 +237,7 @@ def _solve_timed(inst, prec, scorer_obj, batch, streams, limit, device_frontier=
     s = inst.settings
     s.gpu_batch_size = batch
     s.num_streams = streams
-    s.gpu_max_iters = 1000 if inst.lmo.order <= 16 else 400
+    s.gpu_max_iters = 500   # the reference's graph-matching example (examples/main.cu:218)
     s.line_search = A.LS_QUADRATIC_EXACT
     s.abs_gap_tol = 1e-6
     s.rel_gap_tol = 1e-6
