@@ -197,6 +197,8 @@ def config_dict(args):
     d.update({"nodes_per_batch": args.nodes, "max_iters_per_dispatch": args.iters,
               "algorithm": "DICG" if w["alg"] == 1 else "Frank-Wolfe", "line_search": "quadratic_exact",
               "precision": args.precision, "l2": "flushed between timed steps (256 MiB write)"})
+    if getattr(args, "launch_shape", "auto") != "auto":
+        d["launch_shape"] = args.launch_shape
     return d
 
 
@@ -344,6 +346,8 @@ def run_gpu(args, rank, world):
     it = torch.zeros(N, dtype=torch.int32, device=dev)
     st = torch.zeros(N, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
+    if args.launch_shape != "auto":
+        api.set_launch_shape(inst.objective, inst.lmo, alg, n, 1 if args.launch_shape == "tc" else 0, 0)
     relaxer = api.BatchRelaxer(inst.objective, inst.lmo, alg, x, d_lb, d_ub, d_eps, it, st, args.iters, d_flags,
                                1e-6, stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -484,6 +488,9 @@ def main():
                     help="time limit of each time-to-gap solve in seconds (0 skips them)")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-budget", type=float, default=8.0)
+    ap.add_argument("--launch-shape", default="auto", choices=["auto", "tc", "simt"],
+                    help="mixed Birkhoff gradient: the default rule, tensor cores, or FP32 SIMT "
+                         "(over the nonzero lists for sparse graphs above order 64)")
     ap.add_argument("--solve", default=None, choices=sorted(PAIR_CONFIGS),
                     help="only solve the held-out graph pairs with this time-to-gap configuration "
                          "(one JSON line; for profiling the search)")

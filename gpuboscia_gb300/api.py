@@ -360,6 +360,19 @@ def lmo_batch(lmo, mode: int, direction, lb, ub, x=None, want_step: bool = False
     return out, step
 
 
+def set_launch_shape(objective, lmo, algorithm: A.Algorithm, n: int, tensor_core: int = -1, persistent: int = 0):
+    """gbx_relax_set_launch_shape: pin this problem shape's launch shape (tensor_core -1 default rule,
+    0 FP32 SIMT gradient -- over the nonzero lists for sparse graphs above order 64 --, 1 tensor cores)."""
+    lib = A.load()
+    keep = _Keep()
+    o = objective.to_c("cuda", keep)
+    lm = lmo.to_c(n, "cuda", keep)
+    rc = lib.gbx_relax_set_launch_shape(C.byref(o), C.byref(lm), C.byref(algorithm), tensor_core, persistent)
+    if rc == A.ERR_INVALID:
+        raise ValueError(lib.gbx_last_error().decode())
+    A.check(lib, rc, "gbx_relax_set_launch_shape")
+
+
 def objective_gradient_batch(objective, x, precision: int = A.PRECISION_FP64, stream=None):
     """Gradients of the objective at the rows of the device tensor x [cases, n]."""
     import torch

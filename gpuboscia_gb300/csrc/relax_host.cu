@@ -95,11 +95,12 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
         }
         mx_bytes = mixed_array_bytes(n);
         cost_bytes = align16(2 * (size_t)n * sizeof(int));
-        // the FP32 SIMT gradient keeps its arrays in shared memory up to order ~90;
-        // the tensor-core gradient pads any order up to 128
+        // the FP32 SIMT gradient keeps its arrays in shared memory up to order ~90
+        // (above, in the workspace, over the nonzero lists of sparse graphs); the
+        // tensor-core gradient pads any order up to 128
         const bool tc_ok = l.order > 16 && l.order <= 128;
-        const bool simt_ok = l.order <= 90;
-        L.tc = tc_ok && (v.tc == 1 || (v.tc < 0 && l.order > 64) || !simt_ok) ? 1 : 0;
+        const bool simt_ok = l.order <= 128;
+        L.tc = tc_ok && (v.tc == 1 || (v.tc < 0 && l.order > 64)) ? 1 : 0;
         if (L.tc) cost_bytes = std::max(cost_bytes, kTcOperandBytes);
         cost_bytes = std::max(cost_bytes, align16((size_t)n * sizeof(double)));  // the certificate's FP64 costs
         code_bytes = align16(2 * (size_t)n);
@@ -218,7 +219,7 @@ std::vector<Variant> candidate_variants(const gbx_objective& o, const gbx_lmo& l
     std::vector<Variant> out;
     std::vector<int> tcs = {-1};
     if (a.precision == GBX_PRECISION_MIXED && o.kind == GBX_OBJ_GRAPH_MATCHING && l.kind == GBX_LMO_BIRKHOFF
-            && l.order > 16 && l.order <= 90)
+            && l.order > 16 && l.order <= 128)
         tcs = {l.order > 64 ? 1 : 0, l.order > 64 ? 0 : 1};
     for (int tc : tcs)
         for (int pers : {0, 1}) {

@@ -1687,7 +1687,8 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
                 __syncthreads();
                 break;
             }
-        } else if (BIG && c.use_sp) {
+        } else if (c.use_sp && (BIG || m > 64)) {
+            // sparse graphs above order 64: products over the nonzero lists
             grad_f32_sparse(c.sp, m, two_s, xf, Rf, gf);
         } else {
             grad_f32(m, two_s, Af, Bf, Btf, xf, Rf, gf);
