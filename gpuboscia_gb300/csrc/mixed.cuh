@@ -164,12 +164,19 @@ __device__ bool int_hungarian_warp(const IHW& w, int m, const int* cost, int shi
     for (int i = lane + 1; i <= k; i += 32) {
         const int rb = w.rowb[i];
         int best = kIntInf, barg = 0;
-        for (int j = 1; j <= k; ++j) {
+        int j = 1;
+        // eight columns' costs in flight at a time, compared in column order
+        for (; j + 7 <= k; j += 8) {
+            int cc[8], pp[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) { cc[q] = cost[rb + w.cols[j - 1 + q]]; pp[q] = w.pvs[j + q]; }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (cc[q] < kIntInf && cc[q] - pp[q] < best) { best = cc[q] - pp[q]; barg = j + q; }
+        }
+        for (; j <= k; ++j) {
             const int c = cost[rb + w.cols[j - 1]];
-            if (c < kIntInf) {
-                const int rc = c - w.pvs[j];
-                if (rc < best) { best = rc; barg = j; }
-            }
+            if (c < kIntInf && c - w.pvs[j] < best) { best = c - w.pvs[j]; barg = j; }
         }
         if (best >= kIntInf) rows_ok = false;
         w.u[i] = best;
@@ -237,15 +244,32 @@ __device__ bool int_hungarian_warp(const IHW& w, int m, const int* cost, int shi
         bool augmented = false;
         for (int step = 0; step <= k; ++step) {
             int bv = kIntInf, bj = 0x7fffffff;
+            if constexpr (CPL >= 8) {
+                // large orders read their costs from L2: all of this lane's costs
+                // of the row at once (invalid slots read column 0 of the same row),
+                // then the scan -- one memory latency per step instead of CPL
+                int cv[CPL];
 #pragma unroll
-            for (int t = 0; t < CPL; ++t) {
-                if (!valid[t] || usedAt[t] >= 0) continue;
-                const int c = cost[rb + colE[t]];
-                if (c < kIntInf) {
-                    const int cur = c - ui0 - pv[t] + D;
-                    if (cur < mraw[t]) { mraw[t] = cur; way[t] = j0; }
+                for (int t = 0; t < CPL; ++t) cv[t] = cost[rb + colE[t]];
+#pragma unroll
+                for (int t = 0; t < CPL; ++t) {
+                    const bool live = valid[t] && usedAt[t] < 0;
+                    const int c = cv[t];
+                    const int cur = c < kIntInf ? c - ui0 - pv[t] + D : kIntInf;
+                    if (live && c < kIntInf && cur < mraw[t]) { mraw[t] = cur; way[t] = j0; }
+                    if (live && mraw[t] < bv) { bv = mraw[t]; bj = lane + 1 + 32 * t; }
                 }
-                if (mraw[t] < bv) { bv = mraw[t]; bj = lane + 1 + 32 * t; }
+            } else {
+#pragma unroll
+                for (int t = 0; t < CPL; ++t) {
+                    if (!valid[t] || usedAt[t] >= 0) continue;
+                    const int c = cost[rb + colE[t]];
+                    if (c < kIntInf) {
+                        const int cur = c - ui0 - pv[t] + D;
+                        if (cur < mraw[t]) { mraw[t] = cur; way[t] = j0; }
+                    }
+                    if (mraw[t] < bv) { bv = mraw[t]; bj = lane + 1 + 32 * t; }
+                }
             }
             int gmin, j1;
             const int key = bv < kPackLimit ? (bv << 10) | bj : 0x7fffffff;

@@ -106,7 +106,10 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
         code_bytes = align16(2 * (size_t)n);
         L.ihw_bytes = ihw_bytes(l.order);
         // large orders: the oracle costs and edge codes move to the node's workspace
-        L.cost_global = !L.tc && fixed_bytes + cost_bytes + code_bytes + 2 * L.ihw_bytes > kSmemBudget ? 1 : 0;
+        // (every order above 128: the large-order kernel then holds the only
+        // 8- and 16-column integer Hungarians)
+        L.cost_global = !L.tc && (l.order > 128 || fixed_bytes + cost_bytes + code_bytes + 2 * L.ihw_bytes > kSmemBudget)
+                            ? 1 : 0;
         fixed_bytes += (L.cost_global ? 0 : cost_bytes + code_bytes) + 2 * L.ihw_bytes;
     }
     size_t obj_doubles = o.kind == GBX_OBJ_GRAPH_MATCHING ? 2 * (size_t)o.order * o.order

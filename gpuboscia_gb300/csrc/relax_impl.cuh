@@ -344,14 +344,24 @@ static __device__ bool hung_solve_reg(const HW& w, int m, int k, const double* c
             const int rb = w.rows[i0 - 1] * m;
             unsigned long long bkey = ~0ull;
             int bj = 0x7fffffff;
+            // every column's permission and cost of the row first (invalid slots
+            // read column 0 of the same row), then the scan in column order
+            double cc[CPL];
+            bool al[CPL];
+#pragma unroll
+            for (int t = 0; t < CPL; ++t) {
+                const int e = rb + colE[t];
+                const bool a1 = code ? (code[e] & kAllowed) != 0 : ub[e] >= 0.5;
+                const bool a2 = !face || face[e] > 1e-9;
+                al[t] = a1 && a2;
+                cc[t] = cost ? cost[e] : 0.0;
+            }
 #pragma unroll
             for (int t = 0; t < CPL; ++t) {
                 if (!valid[t] || used[t]) continue;
-                const int e = rb + colE[t];
                 double mv = minv[t];
-                const bool allowed = code ? (code[e] & kAllowed) != 0 : ub[e] >= 0.5;
-                if (allowed && (!face || face[e] > 1e-9)) {
-                    const double ce = cost ? sign * cost[e] : 0.0;
+                if (al[t]) {
+                    const double ce = cost ? sign * cc[t] : 0.0;
                     const double cur = ce - ui0 - pv[t];
                     if (cur < mv) { mv = cur; minv[t] = cur; way[t] = j0; }
                 }
@@ -607,14 +617,24 @@ static __device__ bool hung_solve_group(const HW& w, int m, int k, const double*
             const int rb = w.rows[i0 - 1] * m;
             unsigned long long bkey = ~0ull;
             int bj = 0x7fffffff;
+            // every column's permission and cost of the row first (invalid slots
+            // read column 0 of the same row), then the scan in column order
+            double cc[CPL];
+            bool al[CPL];
+#pragma unroll
+            for (int t = 0; t < CPL; ++t) {
+                const int e = rb + colE[t];
+                const bool a1 = code ? (code[e] & kAllowed) != 0 : ub[e] >= 0.5;
+                const bool a2 = !face || face[e] > 1e-9;
+                al[t] = a1 && a2;
+                cc[t] = cost ? cost[e] : 0.0;
+            }
 #pragma unroll
             for (int t = 0; t < CPL; ++t) {
                 if (!valid[t] || used[t]) continue;
-                const int e = rb + colE[t];
                 double mv = minv[t];
-                const bool allowed = code ? (code[e] & kAllowed) != 0 : ub[e] >= 0.5;
-                if (allowed && (!face || face[e] > 1e-9)) {
-                    const double ce = cost ? sign * cost[e] : 0.0;
+                if (al[t]) {
+                    const double ce = cost ? sign * cc[t] : 0.0;
                     const double cur = ce - ui0 - pv[t];
                     if (cur < mv) { mv = cur; minv[t] = cur; way[t] = j0; }
                 }
@@ -1718,10 +1738,9 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
             if constexpr (BIG) {
                 if (m <= 256) ok = int_hungarian_warp<8>(w, m, cst, shift, code, fc, same);
                 else ok = int_hungarian_warp<16>(w, m, cst, shift, code, fc, same);
-            } else {
+            } else {   // orders up to 128
                 if (m <= 64) ok = int_hungarian_warp<2>(w, m, cst, shift, code, fc, same);
-                else if (m <= 128) ok = int_hungarian_warp<4>(w, m, cst, shift, code, fc, same);
-                else ok = int_hungarian_warp<8>(w, m, cst, shift, code, fc, same);
+                else ok = int_hungarian_warp<4>(w, m, cst, shift, code, fc, same);
             }
             if ((threadIdx.x & 31) == 0) c.flag[fwd ? 0 : 2] = ok;
         }
