@@ -120,6 +120,7 @@ class Settings(C.Structure):
         ("branch_k", C.c_int), ("use_cuda_graph", C.c_int),
         ("scorer", C.c_void_p), ("autotune", C.c_int),
         ("device_frontier", C.c_int), ("incumbent_cutoff", C.c_int), ("frontier_capacity", C.c_int),
+        ("frontier_slots", C.c_int),
     ]
 
 
@@ -156,6 +157,7 @@ def default_settings() -> Settings:
     s.device_frontier = 0
     s.incumbent_cutoff = 0
     s.frontier_capacity = 0
+    s.frontier_slots = 2
     return s
 
 

@@ -224,6 +224,7 @@ class Settings:
     device_frontier: int = 0        # open nodes stay in HBM; each search round runs on the device
     incumbent_cutoff: int = 0       # stop node relaxations whose FW bound clears the incumbent
     frontier_capacity: int = 0      # pool size in nodes (0: automatic)
+    frontier_slots: int = 2         # device frontier: batches in flight (1 or 2)
 
     def algorithm_c(self) -> A.Algorithm:
         return A.Algorithm(self.algorithm, self.line_search, self.secant_iters, self.secant_tol,
@@ -234,7 +235,7 @@ class Settings:
         for f in ("gpu_batch_size", "num_streams", "gpu_max_iters", "gpu_eps", "gpu_eps_decay", "gpu_eps_min",
                   "integer_tol", "abs_gap_tol", "rel_gap_tol", "time_limit_seconds", "natural_lower_bound",
                   "branch_k", "use_cuda_graph", "autotune", "device_frontier", "incumbent_cutoff",
-                  "frontier_capacity"):
+                  "frontier_capacity", "frontier_slots"):
             setattr(s, f, getattr(self, f))
         s.algorithm = self.algorithm_c()
         s.root_initial_point = keep.ptr(_f64(self.root_initial_point) if self.root_initial_point is not None

@@ -25,9 +25,16 @@
 //            within tolerance, gap_utils.h:44-52)
 //
 // The sequence is captured once into a CUDA graph of R rounds and replayed;
-// the host reads a 64-byte control block after every replay (time limit,
+// the host reads a small control block after every replay (time limit,
 // completion). Kernels of a finished search return at once. Nothing waits on
-// another CTA: every round is ordered by the stream alone.
+// another CTA: every round is ordered by streams and events alone.
+//
+// Two batch slots (default): round r pops slot r % 2 and relaxes it on that
+// slot's stream while the control stream branches, decides and merges the
+// other slot, so the GPU is not idle behind a batch's slowest node. The
+// frontier keeps a head pointer for the popped-but-unmerged entries; the live
+// bound includes the slot still relaxing; each slot's cutoff is the incumbent
+// at its pop, so results do not depend on timing.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -52,7 +59,8 @@ constexpr int kRoundsPerReplay = 4;
 
 enum Why { RUNNING = 0, EXHAUSTED = 1, TOLERANCE = 2, CAPACITY = 3 };
 
-// device control block (read by the host after every replay)
+// device control block (read by the host after every replay). Two batch
+// slots can be in flight: one relaxing while the other is decided and merged.
 struct FState {
     double incumbent;
     double bound;          // live bound after the last round
@@ -60,15 +68,44 @@ struct FState {
     int done;
     int why;
     int cur;               // frontier buffer holding the live entries
-    int n_front;           // live entries (sorted by bound, id)
-    int n_batch;           // nodes popped this round
-    int n_new;             // entries pushed this round
+    int n_front;           // entries of that buffer; [head, n_front) are open
+    int head;              // entries before head were popped into a slot
     int free_top;          // free pool slots on the stack
     int next_id;
     int inc_src;           // batch index whose best vertex is the new incumbent (-1)
     int has_inc;
     int rounds;
-    int pad;
+    int n_batch[2];        // nodes popped into each slot
+    int n_new[2];          // entries each slot pushes
+    int pop_at[2];         // frontier position the slot's nodes were popped from
+    int pop_base[2];       // free-stack position their pool slots went to
+    double slot_bound[2];  // smallest bound among a slot's nodes (+inf: empty)
+    double slot_cut[2];    // the incumbent when the slot was popped (its relaxation cutoff)
+};
+
+// one relaxation batch and the entries it pushes
+struct Slot {
+    double* x;             // [B * n]
+    double* lb;
+    double* ub;
+    double* best;
+    double* eps;           // [B]
+    double* gap;
+    double* value;
+    double* bvv;
+    int* it;
+    unsigned char* st;
+    double* bbound;
+    int* bdepth;
+    int* bid;
+    int* bvars;            // [B * kMaxK]
+    int* bnv;              // [B]
+    // entries pushed by the slot's decision, sorted by (bound, id) [B << k]
+    double* ekey;
+    int* eid;
+    int* eslot;
+    int* esrc;
+    int* emask;            // child index, -1: continuation of the node itself
 };
 
 struct Tree {
@@ -88,28 +125,7 @@ struct Tree {
     int* fid[2];
     int* fslot[2];
     int* free_stack;       // [cap]
-    // relaxation batch [B * n] / [B]
-    double* x;
-    double* lb;
-    double* ub;
-    double* eps;
-    double* gap;
-    double* value;
-    double* best;
-    double* bvv;
-    int* it;
-    unsigned char* st;
-    double* bbound;
-    int* bdepth;
-    int* bid;
-    int* bvars;            // [B * kMaxK]
-    int* bnv;              // [B]
-    // entries pushed this round, sorted by (bound, id) [B << k]
-    double* ekey;
-    int* eid;
-    int* eslot;
-    int* esrc;
-    int* emask;            // child index, -1: continuation of the node itself
+    Slot sl[2];
     const int* int_vars;   // [n_int]
     const double* eps_tab; // [kEpsDepths]
     double* inc_x;         // [n]
@@ -156,43 +172,53 @@ __device__ inline bool within_tolerance(double bound, double inc, double abs_tol
     return (inc - bound) / scale <= rel_tol;
 }
 
-__global__ void select_kernel(Tree T) {
+// pop the best min(B, open) nodes into slot s; their pool slots are reserved
+// on the free stack (gather writes them there once their data is copied)
+__global__ void select_kernel(Tree T, int s) {
     FState* S = T.S;
-    S->n_new = 0;
-    S->n_batch = S->done ? 0 : min(T.B, S->n_front);
+    const int N = S->done ? 0 : min(T.B, S->n_front - S->head);
+    S->n_new[s] = 0;
+    S->n_batch[s] = N;
+    S->pop_at[s] = S->head;
+    S->pop_base[s] = S->free_top;
+    S->slot_bound[s] = N > 0 ? T.fkey[S->cur][S->head] : __longlong_as_double(0x7ff0000000000000ll);
+    S->slot_cut[s] = S->incumbent;   // fixed for the slot's relaxation: the result is timing-independent
+    S->head += N;
+    S->free_top += N;
 }
 
 // one CTA per batch node
-__global__ void __launch_bounds__(256) gather_kernel(Tree T) {
+__global__ void __launch_bounds__(256) gather_kernel(Tree T, int s) {
     const FState* S = T.S;
+    const Slot& B = T.sl[s];
     const int i = blockIdx.x;
-    if (i >= S->n_batch) return;
-    const int slot = T.fslot[S->cur][i];
+    if (i >= S->n_batch[s]) return;
+    const int slot = T.fslot[S->cur][S->pop_at[s] + i];
     const size_t n = T.n, src = (size_t)slot * n, dst = (size_t)i * n;
     const bool hx = T.mhasx[slot] != 0;
     for (size_t j = threadIdx.x; j < n; j += blockDim.x) {
         const double l = T.plb[src + j];
-        T.lb[dst + j] = l;
-        T.ub[dst + j] = T.pub[src + j];
-        T.x[dst + j] = hx ? T.px[src + j] : l;
+        B.lb[dst + j] = l;
+        B.ub[dst + j] = T.pub[src + j];
+        B.x[dst + j] = hx ? T.px[src + j] : l;
     }
     if (threadIdx.x == 0) {
         const int d = T.mdepth[slot];
-        T.eps[i] = T.eps_tab[min(d, kEpsDepths - 1)];
-        T.it[i] = T.miters[slot];
-        T.st[i] = hx ? GBX_NODE_INITIAL_POINT_SUPPLIED : 0;
-        T.bbound[i] = T.mbound[slot];
-        T.bdepth[i] = d;
-        T.bid[i] = T.mid[slot];
-        // the node now lives in the batch; its slot goes back to the pool
-        T.free_stack[S->free_top + i] = slot;
+        B.eps[i] = T.eps_tab[min(d, kEpsDepths - 1)];
+        B.it[i] = T.miters[slot];
+        B.st[i] = hx ? GBX_NODE_INITIAL_POINT_SUPPLIED : 0;
+        B.bbound[i] = T.mbound[slot];
+        B.bdepth[i] = d;
+        B.bid[i] = T.mid[slot];
+        // the node now lives in the batch; its pool slot goes back to the stack
+        T.free_stack[S->pop_base[s] + i] = slot;
     }
 }
 
 // branch_pow2's variables of batch node i: up to k integer variables with
 // fractional distance above the tolerance, most fractional first, ties to the
 // lower index (top_k_infeasible). Called by all threads of the CTA.
-__device__ void pick_most_fractional(const Tree& T, int i, const double* x) {
+__device__ void pick_most_fractional(const Tree& T, const Slot& B, int i, const double* x) {
     __shared__ double s_d[8];
     __shared__ int s_j[8];
     __shared__ int s_pick[kMaxK];
@@ -231,19 +257,20 @@ __device__ void pick_most_fractional(const Tree& T, int i, const double* x) {
         __syncthreads();
         if (s_count <= r) break;   // no further fractional variable
     }
-    if (tid < s_count) T.bvars[i * kMaxK + tid] = s_pick[tid];
-    if (tid == 0) T.bnv[i] = s_count;
+    if (tid < s_count) B.bvars[i * kMaxK + tid] = s_pick[tid];
+    if (tid == 0) B.bnv[i] = s_count;
 }
 
-__global__ void __launch_bounds__(256) vars_kernel(Tree T) {
+__global__ void __launch_bounds__(256) vars_kernel(Tree T, int s) {
     const FState* S = T.S;
+    const Slot& B = T.sl[s];
     const int i = blockIdx.x;
-    if (i >= S->n_batch) return;
-    if (T.st[i] >= GBX_NODE_INTEGRAL_UNCONVERGED) {
-        if (threadIdx.x == 0) T.bnv[i] = 0;
+    if (i >= S->n_batch[s]) return;
+    if (B.st[i] >= GBX_NODE_INTEGRAL_UNCONVERGED) {
+        if (threadIdx.x == 0) B.bnv[i] = 0;
         return;
     }
-    pick_most_fractional(T, i, T.x + (size_t)i * T.n);
+    pick_most_fractional(T, B, i, B.x + (size_t)i * T.n);
 }
 
 // Learned branching (the host's LearnedBrancher): every fractional candidate
@@ -253,17 +280,18 @@ __global__ void __launch_bounds__(256) vars_kernel(Tree T) {
 // to the most-fractional rule. Shared memory: the parameters, then the
 // permutation row / column statistics of a Birkhoff iterate.
 template <int H>
-__global__ void __launch_bounds__(256) learned_vars_kernel(Tree T, gbx_scorer sc, int order) {
+__global__ void __launch_bounds__(256) learned_vars_kernel(Tree T, int s, gbx_scorer sc, int order) {
     extern __shared__ __align__(16) unsigned char dyn[];
     __shared__ float s_z[8];
     __shared__ int s_q[8];
     __shared__ int s_win;
     const FState* S = T.S;
+    const Slot& B = T.sl[s];
     const int i = blockIdx.x;
-    if (i >= S->n_batch) return;
+    if (i >= S->n_batch[s]) return;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    if (T.st[i] >= GBX_NODE_INTEGRAL_UNCONVERGED) {
-        if (tid == 0) T.bnv[i] = 0;
+    if (B.st[i] >= GBX_NODE_INTEGRAL_UNCONVERGED) {
+        if (tid == 0) B.bnv[i] = 0;
         return;
     }
     const int cnt = mlp::param_count(mlp::kF, H);
@@ -278,9 +306,9 @@ __global__ void __launch_bounds__(256) learned_vars_kernel(Tree T, gbx_scorer sc
     for (int q = tid; q < cnt; q += blockDim.x)
         prm[q] = sc.params_bf16 ? mlp::bf16_to_f(sc.params_bf16[q]) : sc.params[q];
     const size_t base = (size_t)i * T.n;
-    const double* x = T.x + base;
-    const double* lb = T.lb + base;
-    const double* ub = T.ub + base;
+    const double* x = B.x + base;
+    const double* lb = B.lb + base;
+    const double* ub = B.ub + base;
     for (int r = tid; r < m; r += blockDim.x) {
         double rm = 0.0, cm = 0.0;
         int rf = 0, cf = 0, rfr = 0;
@@ -303,8 +331,8 @@ __global__ void __launch_bounds__(256) learned_vars_kernel(Tree T, gbx_scorer sc
         rfree[r] = rfr;
     }
     __syncthreads();
-    const double rel = feature_rel_gap(T.gap[i], T.value[i]);
-    const int depth = T.bdepth[i];
+    const double rel = feature_rel_gap(B.gap[i], B.value[i]);
+    const int depth = B.bdepth[i];
     const mlp::Off o = mlp::offsets(mlp::kF, H);
     // this thread's k best candidates, score descending (earlier first on ties)
     float ks[kMaxK];
@@ -340,7 +368,7 @@ __global__ void __launch_bounds__(256) learned_vars_kernel(Tree T, gbx_scorer sc
         if (kc < T.k) ++kc;
     }
     if (__syncthreads_or(bad)) {
-        pick_most_fractional(T, i, x);
+        pick_most_fractional(T, B, i, x);
         return;
     }
     // k rounds over the threads' heads: highest score, then earliest candidate
@@ -365,7 +393,7 @@ __global__ void __launch_bounds__(256) learned_vars_kernel(Tree T, gbx_scorer sc
                     q = s_q[t];
                 }
             s_win = q;
-            if (q != INT_MAX) T.bvars[i * kMaxK + r] = T.int_vars[q];
+            if (q != INT_MAX) B.bvars[i * kMaxK + r] = T.int_vars[q];
         }
         __syncthreads();
         const int win = s_win;
@@ -374,7 +402,7 @@ __global__ void __launch_bounds__(256) learned_vars_kernel(Tree T, gbx_scorer sc
         if (h < kc && kq[h] == win) ++h;
         ++picked;
     }
-    if (tid == 0) T.bnv[i] = picked;
+    if (tid == 0) B.bnv[i] = picked;
 }
 
 size_t learned_smem_bytes(int H, int order) {
@@ -429,9 +457,10 @@ __device__ int block_scan_sum(int v, int* wbuf, int* total) {
 }
 
 // one CTA of kMaxBatch threads; thread i owns batch node i
-__global__ void __launch_bounds__(kMaxBatch) decide_kernel(Tree T) {
+__global__ void __launch_bounds__(kMaxBatch) decide_kernel(Tree T, int s) {
     FState* S = T.S;
-    const int N = S->n_batch;
+    const Slot& B = T.sl[s];
+    const int N = S->n_batch[s];
     if (N == 0) return;
     __shared__ double s_key[kMaxBatch];
     __shared__ int s_first[kMaxBatch];
@@ -449,7 +478,7 @@ __global__ void __launch_bounds__(kMaxBatch) decide_kernel(Tree T) {
     // incumbent after node i (AtomicIncumbent::try_update in batch order)
     double cand = kInfD;
     if (real) {
-        const double v = T.bvv[i];
+        const double v = B.bvv[i];
         if (v < 1e299 && isfinite(v)) cand = v;
     }
     const double inc_i = fmin(inc0, block_scan_min(cand, wd));
@@ -465,16 +494,16 @@ __global__ void __launch_bounds__(kMaxBatch) decide_kernel(Tree T) {
     int status = 0, nv = 0;
     bool cont = false;
     if (real) {
-        status = T.st[i];
-        const double gap = T.gap[i];
+        status = B.st[i];
+        const double gap = B.gap[i];
         if (status != GBX_NODE_INFEASIBLE) {
-            lower = certified_lower(T.bbound[i], T.value[i], gap);
-            const bool certified = isfinite(gap) && gap >= 0.0 && gap < T.eps[i];
+            lower = certified_lower(B.bbound[i], B.value[i], gap);
+            const bool certified = isfinite(gap) && gap >= 0.0 && gap < B.eps[i];
             if (lower < inc_i) {
                 if (status >= GBX_NODE_INTEGRAL_UNCONVERGED) {
                     cont = !certified;
                 } else {
-                    nv = T.bnv[i];
+                    nv = B.bnv[i];
                 }
             }
         }
@@ -486,7 +515,7 @@ __global__ void __launch_bounds__(kMaxBatch) decide_kernel(Tree T) {
     const int id_base = S->next_id + (b_incl - branched) * T.id_stride;
     int n_cont = 0;
     block_scan_sum(cont ? 1 : 0, wi, &n_cont);
-    if (real) first = cont ? T.bid[i] : id_base;
+    if (real) first = cont ? B.bid[i] : id_base;
     // groups sorted by (bound, first id); a group's ids are consecutive, so the
     // concatenation is sorted by (bound, id)
     s_key[i] = cnt ? lower : kInfD;
@@ -514,35 +543,35 @@ __global__ void __launch_bounds__(kMaxBatch) decide_kernel(Tree T) {
     const int gcnt = (node < N) ? s_cnt[node] : 0;
     int E = 0;
     const int off = block_scan_sum(gcnt, wi, &E) - gcnt;
-    const int top = S->free_top + N;   // the batch's slots were returned by gather
+    const int top = S->free_top;   // the batch's pool slots were returned by gather
     if (E > top) {
         if (i == 0) { S->done = 1; S->why = CAPACITY; }
         return;
     }
     if (gcnt) {
         const int g = node;
-        const bool gc = T.st[g] >= GBX_NODE_INTEGRAL_UNCONVERGED;   // continuation
+        const bool gc = B.st[g] >= GBX_NODE_INTEGRAL_UNCONVERGED;   // continuation
         const double lo = s_lower[g];
-        const int depth = T.bdepth[g];
+        const int depth = B.bdepth[g];
         for (int c = 0; c < gcnt; ++c) {
             const int p = off + c;
             const int slot = T.free_stack[top - 1 - p];
             const int id = s_first[i] + (gc ? 0 : c);
-            T.ekey[p] = lo;
-            T.eid[p] = id;
-            T.eslot[p] = slot;
-            T.esrc[p] = g;
-            T.emask[p] = gc ? -1 : c;
+            B.ekey[p] = lo;
+            B.eid[p] = id;
+            B.eslot[p] = slot;
+            B.esrc[p] = g;
+            B.emask[p] = gc ? -1 : c;
             T.mbound[slot] = lo;
             T.mdepth[slot] = gc ? depth : depth + 1;
             T.mid[slot] = id;
-            T.miters[slot] = gc ? T.it[g] : 0;
+            T.miters[slot] = gc ? B.it[g] : 0;
             T.mhasx[slot] = gc ? 1 : 0;
         }
     }
     if (i == 0) {
         S->free_top = top - E;
-        S->n_new = E;
+        S->n_new[s] = E;
         S->next_id += n_branched * T.id_stride;
         S->nodes_done += N - n_cont;
         if (s_src != INT_MAX) {
@@ -556,52 +585,54 @@ __global__ void __launch_bounds__(kMaxBatch) decide_kernel(Tree T) {
 }
 
 // children / continuations into their pool slots, and the incumbent's x
-__global__ void __launch_bounds__(256) expand_kernel(Tree T) {
+__global__ void __launch_bounds__(256) expand_kernel(Tree T, int s) {
     const FState* S = T.S;
     if (S->done) return;
-    const int E = S->n_new;
+    const Slot& B = T.sl[s];
+    const int E = S->n_new[s];
     const size_t n = T.n;
     __shared__ int s_vars[kMaxK];
     for (int p = blockIdx.x; p <= E; p += gridDim.x) {
         if (p == E) {
             const int src = S->inc_src;
             if (src < 0) break;
-            for (size_t j = threadIdx.x; j < n; j += blockDim.x) T.inc_x[j] = T.best[(size_t)src * n + j];
+            for (size_t j = threadIdx.x; j < n; j += blockDim.x) T.inc_x[j] = B.best[(size_t)src * n + j];
             break;
         }
-        const int slot = T.eslot[p], g = T.esrc[p], mask = T.emask[p];
-        const int nv = mask < 0 ? 0 : T.bnv[g];
+        const int slot = B.eslot[p], g = B.esrc[p], mask = B.emask[p];
+        const int nv = mask < 0 ? 0 : B.bnv[g];
         __syncthreads();
-        if ((int)threadIdx.x < nv) s_vars[threadIdx.x] = T.bvars[g * kMaxK + threadIdx.x];
+        if ((int)threadIdx.x < nv) s_vars[threadIdx.x] = B.bvars[g * kMaxK + threadIdx.x];
         __syncthreads();
         const size_t src = (size_t)g * n, dst = (size_t)slot * n;
         for (size_t j = threadIdx.x; j < n; j += blockDim.x) {
-            double l = T.lb[src + j], u = T.ub[src + j];
+            double l = B.lb[src + j], u = B.ub[src + j];
             for (int b = 0; b < nv; ++b) {
                 if (s_vars[b] == (int)j) {
-                    const double xv = T.x[src + j];
+                    const double xv = B.x[src + j];
                     if (mask >> b & 1) l = ceil(xv);
                     else u = floor(xv);
                 }
             }
             T.plb[dst + j] = l;
             T.pub[dst + j] = u;
-            if (mask < 0) T.px[dst + j] = T.x[src + j];
+            if (mask < 0) T.px[dst + j] = B.x[src + j];
         }
     }
 }
 
-// merge the rest of the frontier with the sorted new entries into the other
-// buffer; entries the incumbent prunes form the tail and free their slots
-__global__ void __launch_bounds__(256) merge_kernel(Tree T) {
+// merge the open part of the frontier with slot s's sorted new entries into
+// the other buffer; entries the incumbent prunes form the tail and free their slots
+__global__ void __launch_bounds__(256) merge_kernel(Tree T, int s) {
     FState* S = T.S;
     if (S->done) return;
-    const int cur = S->cur, N = S->n_batch, E = S->n_new;
-    const int R = S->n_front - N;
+    const Slot& B = T.sl[s];
+    const int cur = S->cur, h = S->head, E = S->n_new[s];
+    const int R = S->n_front - h;
     const double inc = S->incumbent;
-    const double* rk = T.fkey[cur] + N;
-    const int* ri = T.fid[cur] + N;
-    const int* rs = T.fslot[cur] + N;
+    const double* rk = T.fkey[cur] + h;
+    const int* ri = T.fid[cur] + h;
+    const int* rs = T.fslot[cur] + h;
     double* ok = T.fkey[cur ^ 1];
     int* oi = T.fid[cur ^ 1];
     int* os = T.fslot[cur ^ 1];
@@ -611,10 +642,10 @@ __global__ void __launch_bounds__(256) merge_kernel(Tree T) {
         int id, slot, pos;
         if (t < R) {
             k = rk[t]; id = ri[t]; slot = rs[t];
-            pos = t + count_before(T.ekey, T.eid, E, k, id);
+            pos = t + count_before(B.ekey, B.eid, E, k, id);
         } else {
             const int e = t - R;
-            k = T.ekey[e]; id = T.eid[e]; slot = T.eslot[e];
+            k = B.ekey[e]; id = B.eid[e]; slot = B.eslot[e];
             pos = e + count_before(rk, ri, R, k, id);
         }
         if (k < inc) {
@@ -625,20 +656,29 @@ __global__ void __launch_bounds__(256) merge_kernel(Tree T) {
     }
 }
 
-__global__ void status_kernel(Tree T) {
+// after slot s's merge: the open frontier, the live bound (the frontier's head,
+// the other slot's nodes still relaxing, the incumbent) and termination
+__global__ void status_kernel(Tree T, int s) {
     FState* S = T.S;
     if (S->done) return;
-    const int cur = S->cur, N = S->n_batch, E = S->n_new;
-    const int R = S->n_front - N;
+    const Slot& B = T.sl[s];
+    const int cur = S->cur, h = S->head, E = S->n_new[s];
+    const int R = S->n_front - h;
     const double inc = S->incumbent;
-    const int live = first_at_least(T.fkey[cur] + N, R, inc) + first_at_least(T.ekey, E, inc);
+    const int live = first_at_least(T.fkey[cur] + h, R, inc) + first_at_least(B.ekey, E, inc);
     S->cur = cur ^ 1;
     S->n_front = live;
+    S->head = 0;
     S->rounds += 1;
     S->inc_src = -1;
-    const double bound = live > 0 ? fmin(T.fkey[cur ^ 1][0], inc) : inc;
+    S->n_batch[s] = 0;
+    S->n_new[s] = 0;
+    S->slot_bound[s] = __longlong_as_double(0x7ff0000000000000ll);
+    const bool other = S->n_batch[s ^ 1] > 0;
+    double bound = live > 0 ? fmin(T.fkey[cur ^ 1][0], inc) : inc;
+    if (other) bound = fmin(bound, S->slot_bound[s ^ 1]);
     S->bound = bound;
-    if (live == 0) { S->done = 1; S->why = EXHAUSTED; }
+    if (live == 0 && !other) { S->done = 1; S->why = EXHAUSTED; }
     else if (within_tolerance(bound, inc, T.abs_tol, T.rel_tol)) { S->done = 1; S->why = TOLERANCE; }
 }
 
@@ -667,6 +707,10 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     const int n = pr.n_vars, B = s.gpu_batch_size, k = s.branch_k;
     if (B < 1 || B > kMaxBatch) { *err = "device frontier: gpu_batch_size must be in [1, 1024]"; return GBX_ERR_INVALID; }
     if (k < 1 || k > kMaxK) { *err = "device frontier: branch_k must be in [1, 8]"; return GBX_ERR_INVALID; }
+    if (s.frontier_slots != 1 && s.frontier_slots != 2) {
+        *err = "device frontier: frontier_slots must be 1 or 2";
+        return GBX_ERR_INVALID;
+    }
     if (s.scorer && (!s.scorer->params || s.scorer->n_features != GBX_SCORER_FEATURES
                      || (s.scorer->hidden != 16 && s.scorer->hidden != 32 && s.scorer->hidden != 64))) {
         *err = "scorer: invalid descriptor (hidden must be 16, 32 or 64)";
@@ -733,26 +777,31 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     }
     T.free_stack = D.get<int>(C, &e);
     const size_t BN = (size_t)B * Nn;
-    T.x = D.get<double>(BN, &e);
-    T.lb = D.get<double>(BN, &e);
-    T.ub = D.get<double>(BN, &e);
-    T.best = D.get<double>(BN, &e);
-    T.eps = D.get<double>(B, &e);
-    T.gap = D.get<double>(B, &e);
-    T.value = D.get<double>(B, &e);
-    T.bvv = D.get<double>(B, &e);
-    T.it = D.get<int>(B, &e);
-    T.st = D.get<unsigned char>(B, &e);
-    T.bbound = D.get<double>(B, &e);
-    T.bdepth = D.get<int>(B, &e);
-    T.bid = D.get<int>(B, &e);
-    T.bvars = D.get<int>((size_t)B * kMaxK, &e);
-    T.bnv = D.get<int>(B, &e);
-    T.ekey = D.get<double>(E_max, &e);
-    T.eid = D.get<int>(E_max, &e);
-    T.eslot = D.get<int>(E_max, &e);
-    T.esrc = D.get<int>(E_max, &e);
-    T.emask = D.get<int>(E_max, &e);
+    const int NS = s.frontier_slots == 1 ? 1 : 2;
+    for (int q = 0; q < NS; ++q) {
+        Slot& L = T.sl[q];
+        L.x = D.get<double>(BN, &e);
+        L.lb = D.get<double>(BN, &e);
+        L.ub = D.get<double>(BN, &e);
+        L.best = D.get<double>(BN, &e);
+        L.eps = D.get<double>(B, &e);
+        L.gap = D.get<double>(B, &e);
+        L.value = D.get<double>(B, &e);
+        L.bvv = D.get<double>(B, &e);
+        L.it = D.get<int>(B, &e);
+        L.st = D.get<unsigned char>(B, &e);
+        L.bbound = D.get<double>(B, &e);
+        L.bdepth = D.get<int>(B, &e);
+        L.bid = D.get<int>(B, &e);
+        L.bvars = D.get<int>((size_t)B * kMaxK, &e);
+        L.bnv = D.get<int>(B, &e);
+        L.ekey = D.get<double>(E_max, &e);
+        L.eid = D.get<int>(E_max, &e);
+        L.eslot = D.get<int>(E_max, &e);
+        L.esrc = D.get<int>(E_max, &e);
+        L.emask = D.get<int>(E_max, &e);
+    }
+    if (NS == 1) T.sl[1] = T.sl[0];
     int* d_int_vars = D.get<int>(std::max(pr.n_int, 1), &e);
     double* d_eps = D.get<double>(kEpsDepths, &e);
     T.inc_x = D.get<double>(Nn, &e);
@@ -777,6 +826,7 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     S0.free_top = (int)C - 1;
     S0.next_id = 1;
     S0.inc_src = -1;
+    S0.slot_bound[0] = S0.slot_bound[1] = std::numeric_limits<double>::infinity();
     const double root_bound = s.natural_lower_bound;
     const int zero = 0;
     const unsigned char hx = root_x ? 1 : 0;
@@ -801,33 +851,59 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     up(T.S, &S0, sizeof(FState));
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
 
-    // the relaxation launch over the batch buffers
-    Params p{};
-    p.obj = obj;
-    p.lmo = lmo;
-    p.alg = s.algorithm;
-    p.b.n_nodes = B;
-    p.b.max_iters = s.gpu_max_iters;
-    p.b.candidate_tol = s.integer_tol;
-    p.b.x = T.x; p.b.lb = T.lb; p.b.ub = T.ub; p.b.eps = T.eps;
-    p.b.iterations = T.it; p.b.status = T.st; p.b.gap = T.gap; p.b.value = T.value;
-    p.b.best_vertex = T.best; p.b.best_vertex_val = T.bvv; p.b.integer_flags = d_flags;
-    p.b.cutoff = s.incumbent_cutoff ? &T.S->incumbent : nullptr;
-    int rc = make_layout(obj, lmo, s.algorithm, B, &p.L, err);
-    if (rc) return rc;
-    const size_t wsb = workspace_bytes(p.L, B);
-    unsigned char* ws = D.get<unsigned char>(wsb, &e);
-    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
-    p.ws = reinterpret_cast<double*>(ws);
-    p.queue = p.L.persistent ? reinterpret_cast<int*>(ws + queue_offset(p.L, B)) : nullptr;
-    p.mixed = p.L.mixed_node_bytes ? ws + mixed_region_offset(p.L, B) : nullptr;
-    p.sparse = nullptr;
-    p.live_count = &T.S->n_batch;
-    if (p.L.sparse_bytes) {
-        p.sparse = ws + sparse_region_offset(p.L, B);
-        rc = launch_sparse_build(obj, p.L, p.sparse, st, err);
+    // the relaxation launch of each slot over its batch buffers, with its own
+    // workspace (nonzero lists, persistent-grid counter)
+    Params P[2] = {};
+    for (int q = 0; q < NS; ++q) {
+        Params& p = P[q];
+        const Slot& L = T.sl[q];
+        p.obj = obj;
+        p.lmo = lmo;
+        p.alg = s.algorithm;
+        p.b.n_nodes = B;
+        p.b.max_iters = s.gpu_max_iters;
+        p.b.candidate_tol = s.integer_tol;
+        p.b.x = L.x; p.b.lb = L.lb; p.b.ub = L.ub; p.b.eps = L.eps;
+        p.b.iterations = L.it; p.b.status = L.st; p.b.gap = L.gap; p.b.value = L.value;
+        p.b.best_vertex = L.best; p.b.best_vertex_val = L.bvv; p.b.integer_flags = d_flags;
+        p.b.cutoff = s.incumbent_cutoff ? &T.S->slot_cut[q] : nullptr;
+        int rc = make_layout(obj, lmo, s.algorithm, B, &p.L, err);
         if (rc) return rc;
+        const size_t wsb = workspace_bytes(p.L, B);
+        unsigned char* ws = D.get<unsigned char>(wsb, &e);
+        if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+        p.ws = reinterpret_cast<double*>(ws);
+        p.queue = p.L.persistent ? reinterpret_cast<int*>(ws + queue_offset(p.L, B)) : nullptr;
+        p.mixed = p.L.mixed_node_bytes ? ws + mixed_region_offset(p.L, B) : nullptr;
+        p.sparse = nullptr;
+        p.live_count = &T.S->n_batch[q];
+        if (p.L.sparse_bytes) {
+            p.sparse = ws + sparse_region_offset(p.L, B);
+            rc = launch_sparse_build(obj, p.L, p.sparse, st, err);
+            if (rc) return rc;
+        }
     }
+    // one stream per slot for its relaxation; the frontier work stays on `st`
+    cudaStream_t rs[2] = {nullptr, nullptr};
+    cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join[2] = {nullptr, nullptr};
+    struct SlotStreams {
+        cudaStream_t* s; cudaEvent_t* a; cudaEvent_t* b;
+        ~SlotStreams() {
+            for (int q = 0; q < 2; ++q) {
+                if (s[q]) cudaStreamDestroy(s[q]);
+                if (a[q]) cudaEventDestroy(a[q]);
+                if (b[q]) cudaEventDestroy(b[q]);
+            }
+        }
+    } ssg{rs, ev_fork, ev_join};
+    if (NS == 2)
+        for (int q = 0; q < 2; ++q) {
+            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&rs[q], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_fork[q], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_join[q], cudaEventDisableTiming);
+        }
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+    int rc = GBX_OK;
 
     int dev = 0, sms = 0;
     e = cudaGetDevice(&dev);
@@ -845,19 +921,45 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     }
     const int expand_grid = std::min(E_max + 1, 4 * sms);
     const int merge_grid = 4 * sms;
-    auto round = [&]() -> int {
-        select_kernel<<<1, 1, 0, st>>>(T);
-        gather_kernel<<<B, 256, 0, st>>>(T);
-        int r = launch_relax(p, st, err);
-        if (r) return r;
-        if (!s.scorer) vars_kernel<<<B, 256, 0, st>>>(T);
-        else if (sc.hidden == 16) learned_vars_kernel<16><<<B, 256, sc_smem, st>>>(T, sc, sc_order);
-        else if (sc.hidden == 32) learned_vars_kernel<32><<<B, 256, sc_smem, st>>>(T, sc, sc_order);
-        else learned_vars_kernel<64><<<B, 256, sc_smem, st>>>(T, sc, sc_order);
-        decide_kernel<<<1, kMaxBatch, 0, st>>>(T);
-        expand_kernel<<<expand_grid, 256, 0, st>>>(T);
-        merge_kernel<<<merge_grid, 256, 0, st>>>(T);
-        status_kernel<<<1, 1, 0, st>>>(T);
+    // the other half of a round: branch, decide, expand, merge, status of slot q
+    auto finish = [&](int q) {
+        if (!s.scorer) vars_kernel<<<B, 256, 0, st>>>(T, q);
+        else if (sc.hidden == 16) learned_vars_kernel<16><<<B, 256, sc_smem, st>>>(T, q, sc, sc_order);
+        else if (sc.hidden == 32) learned_vars_kernel<32><<<B, 256, sc_smem, st>>>(T, q, sc, sc_order);
+        else learned_vars_kernel<64><<<B, 256, sc_smem, st>>>(T, q, sc, sc_order);
+        decide_kernel<<<1, kMaxBatch, 0, st>>>(T, q);
+        expand_kernel<<<expand_grid, 256, 0, st>>>(T, q);
+        merge_kernel<<<merge_grid, 256, 0, st>>>(T, q);
+        status_kernel<<<1, 1, 0, st>>>(T, q);
+    };
+    // Round r pops into slot r % 2 and relaxes it on that slot's stream, then
+    // finishes the other slot, whose relaxation the previous round started.
+    // A replay holds an even number of rounds and ends by joining its last
+    // relaxation, so the next replay's first round finishes it in stream order.
+    // With one slot a round is pop, relax, finish on one stream.
+    auto round = [&](int r) -> int {
+        const int q = NS == 1 ? 0 : (r & 1);
+        select_kernel<<<1, 1, 0, st>>>(T, q);
+        gather_kernel<<<B, 256, 0, st>>>(T, q);
+        if (NS == 1) {
+            int rr = launch_relax(P[0], st, err);
+            if (rr) return rr;
+            finish(0);
+        } else {
+            cudaError_t ee = cudaEventRecord(ev_fork[q], st);
+            if (ee == cudaSuccess) ee = cudaStreamWaitEvent(rs[q], ev_fork[q], 0);
+            if (ee != cudaSuccess) { *err = cudaGetErrorString(ee); return GBX_ERR_CUDA; }
+            int rr = launch_relax(P[q], rs[q], err);
+            if (rr) return rr;
+            ee = cudaEventRecord(ev_join[q], rs[q]);
+            if (ee == cudaSuccess && r % kRoundsPerReplay != 0) ee = cudaStreamWaitEvent(st, ev_join[q ^ 1], 0);
+            if (ee != cudaSuccess) { *err = cudaGetErrorString(ee); return GBX_ERR_CUDA; }
+            finish(q ^ 1);
+            if (r % kRoundsPerReplay == kRoundsPerReplay - 1) {   // join the last relaxation of the replay
+                ee = cudaStreamWaitEvent(st, ev_join[q], 0);
+                if (ee != cudaSuccess) { *err = cudaGetErrorString(ee); return GBX_ERR_CUDA; }
+            }
+        }
         const cudaError_t le = cudaGetLastError();
         if (le != cudaSuccess) { *err = cudaGetErrorString(le); return GBX_ERR_CUDA; }
         return GBX_OK;
@@ -869,7 +971,7 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
         cudaGraph_t g = nullptr;
         e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
         int crc = e == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
-        for (int r = 0; r < kRoundsPerReplay && crc == GBX_OK; ++r) crc = round();
+        for (int r = 0; r < kRoundsPerReplay && crc == GBX_OK; ++r) crc = round(r);
         const cudaError_t ee = cudaStreamEndCapture(st, &g);
         if (crc == GBX_OK && ee == cudaSuccess && g) {
             if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) exec = nullptr;
@@ -891,7 +993,7 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
             if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
         } else {
             for (int r = 0; r < kRoundsPerReplay; ++r) {
-                rc = round();
+                rc = round(r);
                 if (rc) return rc;
             }
         }

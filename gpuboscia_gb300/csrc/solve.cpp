@@ -190,6 +190,7 @@ void gbx_default_settings(gbx_settings* s) {
     s->device_frontier = 0;
     s->incumbent_cutoff = 0;
     s->frontier_capacity = 0;
+    s->frontier_slots = 2;
 }
 
 int gbx_solve(const gbx_problem* problem, const gbx_objective* obj, const gbx_lmo* lmo,

@@ -83,6 +83,7 @@ struct DeviceResidentConfig {
     // over branch_k variables and the BranchStrategy callback is not called
     bool device_frontier = false;
     int frontier_capacity = 0;   // open nodes in the device pool (0: automatic)
+    int frontier_slots = 2;      // batches in flight on the device frontier (1 or 2)
     int branch_k = 3;
     // stop a node's relaxation once its FW bound clears the incumbent
     // (gbx_node_batch.cutoff): the node is pruned at any bound above it
@@ -633,6 +634,7 @@ private:
         s.device_frontier = 1;
         s.incumbent_cutoff = cfg_.incumbent_cutoff ? 1 : 0;
         s.frontier_capacity = cfg_.frontier_capacity;
+        s.frontier_slots = cfg_.frontier_slots;
         std::vector<double> x(prob_.n_vars);
         gbx_result r{};
         r.x = x.data();

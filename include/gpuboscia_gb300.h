@@ -331,6 +331,8 @@ typedef struct gbx_settings {
     int device_frontier;      /* 0 */
     int incumbent_cutoff;     /* stop node relaxations at the incumbent (gbx_node_batch.cutoff); 0 */
     int frontier_capacity;    /* open nodes the pool holds (0: a quarter of free memory, <= 2^18) */
+    int frontier_slots;       /* device frontier: batches in flight, 1 or 2 (2: one relaxes while
+                                 the other is branched and merged); 2 */
 } gbx_settings;
 
 typedef struct gbx_result {

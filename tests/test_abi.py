@@ -58,6 +58,7 @@ int main(void) {
   S(gbx_settings) O(gbx_settings, algorithm) O(gbx_settings, time_limit_seconds) O(gbx_settings, use_cuda_graph)
   O(gbx_settings, scorer) O(gbx_settings, autotune) O(gbx_settings, device_frontier)
   O(gbx_settings, frontier_capacity) O(gbx_settings, incumbent_cutoff) O(gbx_node_batch, cutoff)
+  O(gbx_settings, frontier_slots)
   S(gbx_scorer) O(gbx_scorer, params) O(gbx_scorer, params_bf16)
   S(gbx_result) O(gbx_result, x)
   return 0;

@@ -268,3 +268,36 @@ def test_incumbent_cutoff_same_optimum(cuda_lib, precision):
     h = api.solve(inst.problem, inst.objective, inst.lmo, s)
     assert _proved(a) and _proved(b) and _proved(h)
     assert abs(a.objective - b.objective) <= 1e-6 and abs(h.objective - b.objective) <= 1e-6
+
+
+@pytest.mark.parametrize("precision,learned,cutoff", [(A.PRECISION_FP64, False, 0), (A.PRECISION_MIXED, True, 1)])
+def test_two_slots_same_optimum_and_deterministic(cuda_lib, precision, learned, cutoff):
+    """frontier_slots = 2 (one batch relaxing while the other is merged) reaches
+    the optimum of the one-slot search and repeats itself exactly."""
+    from gpuboscia_gb300 import scorer
+    inst = _pair(206, 8)
+    s = inst.settings
+    s.algorithm = A.ALG_DICG
+    s.line_search = A.LS_QUADRATIC_EXACT
+    s.gpu_batch_size = 32
+    s.gpu_max_iters = 500
+    s.abs_gap_tol = 1e-6
+    s.rel_gap_tol = 1e-6
+    s.precision = precision
+    s.scorer = scorer.Scorer(32, seed=2) if learned else None
+    s.incumbent_cutoff = cutoff
+    s.time_limit_seconds = 60
+    s.device_frontier = 1
+    s.frontier_slots = 1
+    one = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    s.frontier_slots = 2
+    two = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    again = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert _proved(one) and _proved(two)
+    assert abs(one.objective - two.objective) <= 1e-6
+    assert (two.nodes_processed, two.objective, two.dual_bound) == (again.nodes_processed, again.objective,
+                                                                    again.dual_bound)
+    assert np.array_equal(two.x, again.x)
+    s.use_cuda_graph = 0
+    direct = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert (direct.nodes_processed, direct.objective) == (two.nodes_processed, two.objective)
