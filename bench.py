@@ -100,10 +100,15 @@ class ClockSampler:
         self.proc = None
 
     def __enter__(self):
+        import select
+        self.first = ""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            # the timed region starts once sampling runs (the first sample is the state entering it)
+            if select.select([self.proc.stdout], [], [], 5.0)[0]:
+                self.first = self.proc.stdout.readline()
         except OSError:
             self.proc = None
         return self
@@ -117,6 +122,7 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
                 self.text, _ = self.proc.communicate()
+            self.text = self.first + self.text
 
     def summary(self):
         sm, mx, reasons = [], None, set()
@@ -475,7 +481,7 @@ def run_gpu(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="birkhoff_gnp36", choices=sorted(WORKLOADS))
