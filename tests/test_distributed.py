@@ -120,7 +120,7 @@ def test_peer_failure_is_reported_not_awaited():
 
 @pytest.mark.gpu
 def test_single_rank_on_the_gpu_matches_the_oracle(cuda_lib):
-    """The product relaxation (gbx_relax_batch) under the distributed driver,
+    """The product relaxation (gbx_relax_batch) under the distributed search,
     one rank: the same optimum as the single-process oracle solver."""
     import torch.distributed as dist
     from gpuboscia_gb300 import distributed

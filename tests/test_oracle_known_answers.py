@@ -188,7 +188,7 @@ def secant_probe(iters, tol, deps):
 
 
 def test_secant_tolerance_stall_regression():
-    # converged as the host judges it: 0 <= gap < node tolerance (device_resident_solver.cuh:1936-1939)
+    # converged as the host decides it: 0 <= gap < node tolerance (device_resident_solver.cuh:1936-1939)
     loose = secant_probe(8, 1e-3, 1e-4)
     assert loose["iterations"][0] >= 64 and loose["gap"][0] > 1e-6
     tight = secant_probe(16, 1e-10, 1e-14)
