@@ -205,6 +205,8 @@ def config_dict(args):
               "precision": args.precision, "l2": "flushed between timed steps (256 MiB write)"})
     if getattr(args, "launch_shape", "auto") != "auto":
         d["launch_shape"] = args.launch_shape
+        if getattr(args, "tuned_shape", None):
+            d["tuned_shape"] = {"tensor_core": args.tuned_shape[0], "persistent": args.tuned_shape[1]}
     return d
 
 
@@ -352,10 +354,15 @@ def run_gpu(args, rank, world):
     it = torch.zeros(N, dtype=torch.int32, device=dev)
     st = torch.zeros(N, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
-    if args.launch_shape != "auto":
+    if args.launch_shape in ("tc", "simt"):
         api.set_launch_shape(inst.objective, inst.lmo, alg, n, 1 if args.launch_shape == "tc" else 0, 0)
     relaxer = api.BatchRelaxer(inst.objective, inst.lmo, alg, x, d_lb, d_ub, d_eps, it, st, args.iters, d_flags,
                                1e-6, stream)
+    if args.launch_shape == "tuned":
+        x.copy_(x0)
+        it.zero_()
+        st.zero_()
+        args.tuned_shape = relaxer.autotune()   # before the warm-up, on this batch
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def step():
@@ -494,9 +501,10 @@ def main():
                     help="time limit of each time-to-gap solve in seconds (0 skips them)")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-budget", type=float, default=8.0)
-    ap.add_argument("--launch-shape", default="auto", choices=["auto", "tc", "simt"],
-                    help="mixed Birkhoff gradient: the default rule, tensor cores, or FP32 SIMT "
-                         "(over the nonzero lists for sparse graphs above order 64)")
+    ap.add_argument("--launch-shape", default="auto", choices=["auto", "tc", "simt", "tuned"],
+                    help="mixed Birkhoff gradient: the default rule, tensor cores, FP32 SIMT "
+                         "(over the nonzero lists for sparse graphs above order 64), or the "
+                         "autotuner's choice on the batch (gbx_relax_autotune)")
     ap.add_argument("--solve", default=None, choices=sorted(PAIR_CONFIGS),
                     help="only solve the held-out graph pairs with this time-to-gap configuration "
                          "(one JSON line; for profiling the search)")

@@ -453,3 +453,11 @@ class BatchRelaxer:
         rc = self.lib.gbx_relax_batch(*self._args)
         if rc != A.OK:
             A.check(self.lib, rc, "gbx_relax_batch")
+
+    def autotune(self, repeats: int = 2):
+        """gbx_relax_autotune on this batch (inputs restored): keeps the fastest launch
+        shape for the problem shape; returns (tensor-core gradient, persistent grid)."""
+        chosen = (C.c_int * 2)()
+        rc = self.lib.gbx_relax_autotune(*self._args, repeats, C.cast(chosen, C.c_void_p))
+        A.check(self.lib, rc, "gbx_relax_autotune")
+        return int(chosen[0]), int(chosen[1])

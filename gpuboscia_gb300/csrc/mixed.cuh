@@ -30,9 +30,10 @@ constexpr uint8_t kAllowed = 2;    // ub >= 1/2
 constexpr uint8_t kBad = 4;        // lb > ub + 1e-9
 constexpr uint8_t kZeroOk = 8;     // 0 lies in [lb - tol, ub + tol]
 constexpr uint8_t kOneOk = 16;     // 1 lies in [lb - tol, ub + tol]
-// face bytes (DICG in-face oracle)
-constexpr uint8_t kFaceIn = 1;     // x > 1e-9
-constexpr uint8_t kFaceOne = 2;    // x >= 1 - 1e-9
+// the iterate's face, in the same byte (DICG in-face oracle)
+constexpr uint8_t kFaceIn = 32;    // x > 1e-9
+constexpr uint8_t kFaceOne = 64;   // x >= 1 - 1e-9
+constexpr uint8_t kFaceBits = kFaceIn | kFaceOne;
 
 struct IHW {
     int *u, *rowb, *pvs;                         // [m+1] row potentials, row offsets r*m, column potentials
@@ -77,8 +78,12 @@ __device__ __forceinline__ int lane_slot(const int (&a)[CPL], int slot) {
 // through a single warp min-reduction; larger ones take the two-reduction path.
 constexpr int kPackLimit = 1 << 21;
 
-// Exact assignment on integer costs over the Birkhoff polytope. `cost` holds
-// round(sign*g*2^shift) for allowed edges and kIntInf for excluded ones; the
+// Exact assignment on integer costs over the Birkhoff polytope. `costs` holds
+// round(g*2^shift) for allowed edges and kIntInf for excluded ones; the
+// in-face oracle (FACE 1: `costs` already holds its negated face costs; FACE
+// 2: it negates the forward costs on the iterate's face -- edge code bit
+// kFaceIn -- and excludes every other edge) also forces the face's unit
+// entries (kFaceOne). The
 // forced / face-forced pre-pass reads the edge codes and is skipped when
 // `restrict_same` says the restrictions equal those of the previous call. One
 // warp; lane l owns the compacted columns l+1, l+33, ... and keeps, per column,
@@ -91,10 +96,15 @@ constexpr int kPackLimit = 1 << 21;
 // relaxed, so the integer arithmetic equals the eager update exactly. Column
 // potentials and the matching persist in `w`. Ties go to the lowest column.
 // Returns a warp-uniform success flag; the row->column map is left in w.pi.
-template <int CPL>
-__device__ bool int_hungarian_warp(const IHW& w, int m, const int* cost, int shift, const uint8_t* code,
-                                   const uint8_t* face, bool restrict_same) {
+template <int CPL, int FACE>
+__device__ bool int_hungarian_warp(const IHW& w, int m, const int* costs, int shift, const uint8_t* code,
+                                   bool restrict_same) {
     const int lane = threadIdx.x & 31;
+    auto cost_at = [&](int e) -> int {
+        const int c0 = costs[e];
+        if constexpr (FACE == 2) return (c0 < kIntInf && (code[e] & kFaceIn)) ? -c0 : kIntInf;
+        else return c0;
+    };
     const unsigned lt = (1u << lane) - 1u;
     int k;
     if (restrict_same && w.scal[2] > 0) {
@@ -107,7 +117,7 @@ __device__ bool int_hungarian_warp(const IHW& w, int m, const int* cost, int shi
         for (int e = lane; e < nn; e += 32) {
             const uint8_t c = code[e];
             if (c & kBad) ok = false;
-            const bool forced = (c & kForced) || (face && (face[e] & kFaceOne));
+            const bool forced = (c & kForced) || (FACE != 0 && (c & kFaceOne));
             if (forced) {
                 const int r = e / m, col = e - r * m;
                 if (!(c & kAllowed)) ok = false;
@@ -169,13 +179,13 @@ __device__ bool int_hungarian_warp(const IHW& w, int m, const int* cost, int shi
         for (; j + 7 <= k; j += 8) {
             int cc[8], pp[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) { cc[q] = cost[rb + w.cols[j - 1 + q]]; pp[q] = w.pvs[j + q]; }
+            for (int q = 0; q < 8; ++q) { cc[q] = cost_at(rb + w.cols[j - 1 + q]); pp[q] = w.pvs[j + q]; }
 #pragma unroll
             for (int q = 0; q < 8; ++q)
                 if (cc[q] < kIntInf && cc[q] - pp[q] < best) { best = cc[q] - pp[q]; barg = j + q; }
         }
         for (; j <= k; ++j) {
-            const int c = cost[rb + w.cols[j - 1]];
+            const int c = cost_at(rb + w.cols[j - 1]);
             if (c < kIntInf && c - w.pvs[j] < best) { best = c - w.pvs[j]; barg = j; }
         }
         if (best >= kIntInf) rows_ok = false;
@@ -194,7 +204,7 @@ __device__ bool int_hungarian_warp(const IHW& w, int m, const int* cost, int shi
             if (r < 0 || r >= m) continue;
             const int i = w.rowpos[r];
             if (i <= 0) continue;
-            const int c = cost[r * m + colE[t]];
+            const int c = cost_at(r * m + colE[t]);
             const int ui = w.u[i];
             if (c < kIntInf && c - ui - pv[t] == 0) {
                 pj[t] = i;
@@ -250,7 +260,7 @@ __device__ bool int_hungarian_warp(const IHW& w, int m, const int* cost, int shi
                 // then the scan -- one memory latency per step instead of CPL
                 int cv[CPL];
 #pragma unroll
-                for (int t = 0; t < CPL; ++t) cv[t] = cost[rb + colE[t]];
+                for (int t = 0; t < CPL; ++t) cv[t] = cost_at(rb + colE[t]);
 #pragma unroll
                 for (int t = 0; t < CPL; ++t) {
                     const bool live = valid[t] && usedAt[t] < 0;
@@ -263,7 +273,7 @@ __device__ bool int_hungarian_warp(const IHW& w, int m, const int* cost, int shi
 #pragma unroll
                 for (int t = 0; t < CPL; ++t) {
                     if (!valid[t] || usedAt[t] >= 0) continue;
-                    const int c = cost[rb + colE[t]];
+                    const int c = cost_at(rb + colE[t]);
                     if (c < kIntInf) {
                         const int cur = c - ui0 - pv[t] + D;
                         if (cur < mraw[t]) { mraw[t] = cur; way[t] = j0; }

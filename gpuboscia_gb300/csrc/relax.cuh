@@ -51,6 +51,13 @@ struct Layout {
     // offsets, the gradient runs over the nonzero lists in FP32
     int cost_global;
     size_t mx_cost_off, mx_code_off;
+    // the certificate's FP64 Hungarian reads the gradient staged in the cost
+    // region (1), or straight from the node's gradient vector (0) when staging
+    // would cost a resident node per SM
+    int cert_stage;
+    // the in-face oracle derives its costs from the forward ones (no second
+    // cost array) -- only where that fits two nodes per SM
+    int derive_inface;
     // graph matching: nonzero lists of A and B (rows and columns), built once
     // per launch at the end of the workspace; up to sparse_cap entries each
     int sparse_cap;

@@ -25,6 +25,8 @@ int feas_one(const gbx_lmo& l, const Layout& L, int cases, const double* lb, con
 namespace {
 int next_pow2(int v) { int r = 1; while (r < v) r <<= 1; return r; }
 constexpr size_t kSmemBudget = 220 * 1024;
+constexpr size_t kSmemPerSm = 228 * 1024;        // shared memory of an SM
+constexpr size_t kSmemPerCtaReserve = 2 * 1024;  // per-CTA reserve and the kernels' static shared memory
 }
 
 int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a,
@@ -94,6 +96,7 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
             return GBX_ERR_UNSUPPORTED;
         }
         mx_bytes = mixed_array_bytes(n);
+        // forward and in-face integer costs
         cost_bytes = align16(2 * (size_t)n * sizeof(int));
         // the FP32 SIMT gradient keeps its arrays in shared memory up to order ~90
         // (above, in the workspace, over the nonzero lists of sparse graphs); the
@@ -102,14 +105,45 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
         const bool simt_ok = l.order <= 128;
         L.tc = tc_ok && (v.tc == 1 || (v.tc < 0 && l.order > 64)) ? 1 : 0;
         if (L.tc) cost_bytes = std::max(cost_bytes, kTcOperandBytes);
-        cost_bytes = std::max(cost_bytes, align16((size_t)n * sizeof(double)));  // the certificate's FP64 costs
-        code_bytes = align16(2 * (size_t)n);
+        const size_t staged = std::max(cost_bytes, align16((size_t)n * sizeof(double)));  // + certificate costs
+        code_bytes = align16((size_t)n);   // edge codes and the iterate's face bits
         L.ihw_bytes = ihw_bytes(l.order);
         // large orders: the oracle costs and edge codes move to the node's workspace
         // (every order above 128: the large-order kernel then holds the only
         // 8- and 16-column integer Hungarians)
-        L.cost_global = !L.tc && (l.order > 128 || fixed_bytes + cost_bytes + code_bytes + 2 * L.ihw_bytes > kSmemBudget)
+        L.cost_global = !L.tc && (l.order > 128 || fixed_bytes + staged + code_bytes + 2 * L.ihw_bytes > kSmemBudget)
                             ? 1 : 0;
+        // The SIMT kernel holds up to two nodes per SM (its register limit). Of
+        // the cost-region layouts -- both oracles' costs with the certificate's
+        // gradient staged beside them, without staging, the in-face costs
+        // derived from the forward ones (staged or not) -- take the first that
+        // reaches the most nodes per SM (order 120: derived, not staged).
+        L.cert_stage = 1;
+        L.derive_inface = 0;
+        if (!L.tc && !L.cost_global && l.order > 64) {
+            auto per_sm = [&](size_t bytes) {
+                return std::min<int>(2, (int)(kSmemPerSm / (bytes + kSmemPerCtaReserve)));
+            };
+            const size_t base = fixed_bytes + code_bytes + 2 * L.ihw_bytes;
+            const size_t one = align16((size_t)n * sizeof(int)), dbl = align16((size_t)n * sizeof(double));
+            const size_t opts[4][3] = {{std::max(cost_bytes, dbl), 1, 0}, {cost_bytes, 0, 0},
+                                       {std::max(one, dbl), 1, 1}, {one, 0, 1}};
+            // the FP32 arrays join shared memory whenever they fit (placement below)
+            auto total = [&](size_t costs) {
+                return base + costs + (mx_bytes + base + costs > kSmemBudget ? 0 : mx_bytes);
+            };
+            int best = 0;
+            for (int q = 0; q < 4; ++q) best = std::max(best, per_sm(total(opts[q][0])));
+            for (int q = 0; q < 4; ++q)
+                if (per_sm(total(opts[q][0])) == best) {
+                    cost_bytes = opts[q][0];
+                    L.cert_stage = (int)opts[q][1];
+                    L.derive_inface = (int)opts[q][2];
+                    break;
+                }
+        } else {
+            cost_bytes = staged;
+        }
         fixed_bytes += (L.cost_global ? 0 : cost_bytes + code_bytes) + 2 * L.ihw_bytes;
     }
     size_t obj_doubles = o.kind == GBX_OBJ_GRAPH_MATCHING ? 2 * (size_t)o.order * o.order

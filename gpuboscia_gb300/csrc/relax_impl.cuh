@@ -1580,9 +1580,9 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
     int8_t* Ai = reinterpret_cast<int8_t*>(mx + align16(6 * (size_t)n * sizeof(float)));  // A, B as small
     int8_t* Bi = Ai + align16((size_t)n);      // integers when they are (exact integer scores, curvature)
     int* costf = reinterpret_cast<int*>(mixed_costs(P, dsm, node));   // forward oracle costs
-    int* costa = costf + n;                                  // in-face oracle costs (negated, face only)
-    uint8_t* code = mixed_codes(P, dsm, node);
-    uint8_t* face = code + n;
+    int* costa = costf + n;   // in-face oracle costs (negated, face only), unless derived on the fly
+    uint8_t* code = mixed_codes(P, dsm, node);   // edge codes, with the iterate's face bits
+    const bool derive = L.derive_inface != 0;
     const IHW w0 = ihw_at(dsm + L.sm_ihw, m);
     const IHW w1 = ihw_at(dsm + L.sm_ihw + L.ihw_bytes, m);
     const double tol = c.tol;
@@ -1635,10 +1635,9 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
         if (lo > up + 1e-9) cd |= kBad;
         if (!(0.0 < lo - tol) && !(0.0 > up + tol)) cd |= kZeroOk;
         if (!(1.0 < lo - tol) && !(1.0 > up + tol)) cd |= kOneOk;
-        code[e] = cd;
         const double xe = X[e];
         xf[e] = (float)xe;
-        face[e] = (uint8_t)((xe > 1e-9 ? kFaceIn : 0) | (xe >= 1.0 - 1e-9 ? kFaceOne : 0));
+        code[e] = (uint8_t)(cd | (xe > 1e-9 ? kFaceIn : 0) | (xe >= 1.0 - 1e-9 ? kFaceOne : 0));
     }
     // Oracle warps: a warp issues on SM sub-partition (hardware slot % 4), and
     // two of these CTAs share an SM, so the CTA in the upper half of the SM's
@@ -1724,23 +1723,31 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
             const int ci = __float2int_rn(scalbnf(gf[e], shift));
             const bool allowed = (code[e] & kAllowed) != 0;
             costf[e] = allowed ? ci : kIntInf;
-            if (dicg) costa[e] = (allowed && (face[e] & kFaceIn)) ? -ci : kIntInf;
+            if (dicg && !derive) costa[e] = (allowed && (code[e] & kFaceIn)) ? -ci : kIntInf;
         }
         __syncthreads();
         const int owarp = (int)(threadIdx.x >> 5) - s_owarp;
         if (owarp == 0 || (dicg && owarp == 1)) {
             const bool fwd = owarp == 0;
             const IHW& w = fwd ? w0 : w1;
-            const int* cst = fwd ? costf : costa;
-            const uint8_t* fc = fwd ? nullptr : face;
             const bool same = fwd || c.flag[4] == 0;
             bool ok;
             if constexpr (BIG) {
-                if (m <= 256) ok = int_hungarian_warp<8>(w, m, cst, shift, code, fc, same);
-                else ok = int_hungarian_warp<16>(w, m, cst, shift, code, fc, same);
-            } else {   // orders up to 128
-                if (m <= 64) ok = int_hungarian_warp<2>(w, m, cst, shift, code, fc, same);
-                else ok = int_hungarian_warp<4>(w, m, cst, shift, code, fc, same);
+                if (m <= 256) ok = fwd ? int_hungarian_warp<8, 0>(w, m, costf, shift, code, same)
+                                       : int_hungarian_warp<8, 1>(w, m, costa, shift, code, same);
+                else ok = fwd ? int_hungarian_warp<16, 0>(w, m, costf, shift, code, same)
+                              : int_hungarian_warp<16, 1>(w, m, costa, shift, code, same);
+            } else if constexpr (TC) {   // orders 17..128, costs beside the operand images
+                if (m <= 64) ok = fwd ? int_hungarian_warp<2, 0>(w, m, costf, shift, code, same)
+                                      : int_hungarian_warp<2, 1>(w, m, costa, shift, code, same);
+                else ok = fwd ? int_hungarian_warp<4, 0>(w, m, costf, shift, code, same)
+                              : int_hungarian_warp<4, 1>(w, m, costa, shift, code, same);
+            } else {   // orders up to 128; in-face costs derived where that fits two nodes per SM
+                if (m <= 64) ok = fwd ? int_hungarian_warp<2, 0>(w, m, costf, shift, code, same)
+                                      : int_hungarian_warp<2, 1>(w, m, costa, shift, code, same);
+                else if (fwd) ok = int_hungarian_warp<4, 0>(w, m, costf, shift, code, same);
+                else ok = derive ? int_hungarian_warp<4, 2>(w, m, costf, shift, code, same)
+                                 : int_hungarian_warp<4, 1>(w, m, costa, shift, code, same);
             }
             if ((threadIdx.x & 31) == 0) c.flag[fwd ? 0 : 2] = ok;
         }
@@ -1850,9 +1857,9 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
             xf[ev] = (float)X[ev];
             const uint8_t fa = (uint8_t)((X[ea] > 1e-9 ? kFaceIn : 0) | (X[ea] >= 1.0 - 1e-9 ? kFaceOne : 0));
             const uint8_t fv = (uint8_t)((X[ev] > 1e-9 ? kFaceIn : 0) | (X[ev] >= 1.0 - 1e-9 ? kFaceOne : 0));
-            if (((fa ^ face[ea]) | (fv ^ face[ev])) & kFaceOne) c.flag[4] = 1;
-            face[ea] = fa;
-            face[ev] = fv;
+            if (((fa ^ code[ea]) | (fv ^ code[ev])) & kFaceOne) c.flag[4] = 1;
+            code[ea] = (uint8_t)((code[ea] & ~kFaceBits) | fa);
+            code[ev] = (uint8_t)((code[ev] & ~kFaceBits) | fv);
         }
         __syncthreads();
     }
@@ -2150,8 +2157,11 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
         // the integer costs' shared memory is free now: the FP64 Hungarian reads
         // the gradient from there and edge permissions from the code bytes
         // (kAllowed is ub >= 1/2), the same arithmetic as lmo_forward
-        double* Gs = reinterpret_cast<double*>(mixed_costs(P, dsm, node));
-        for (int j = tid; j < n; j += kThreads) { Gs[j] = G[j]; V[j] = 0.0; }
+        double* Gs = L.cert_stage ? reinterpret_cast<double*>(mixed_costs(P, dsm, node)) : G;
+        for (int j = tid; j < n; j += kThreads) {
+            if (L.cert_stage) Gs[j] = G[j];
+            V[j] = 0.0;
+        }
         __syncthreads();
         if (threadIdx.x < kHungThreads) {
             const bool ok = hungarian_group(hw0, c.lorder, Gs, 1.0, LB, UB, nullptr, V, mixed_codes(P, dsm, node), 0);
