@@ -301,3 +301,45 @@ def test_two_slots_same_optimum_and_deterministic(cuda_lib, precision, learned, 
     s.use_cuda_graph = 0
     direct = api.solve(inst.problem, inst.objective, inst.lmo, s)
     assert (direct.nodes_processed, direct.objective) == (two.nodes_processed, two.objective)
+
+
+@pytest.mark.parametrize("problem,slots,cutoff", [("box", 1, 0), ("box", 2, 0), ("box", 2, 1),
+                                                  ("graph", 1, 0), ("graph", 2, 1), ("portfolio", 1, 0)])
+def test_fp64_search_matches_the_restated_frontier(cuda_lib, problem, slots, cutoff):
+    """FP64 node relaxations are bit-identical to the oracle's, and the device
+    frontier's rules are deterministic, so the whole device search equals its
+    CPU restatement (tests/_frontier_oracle.py): node count, objective,
+    certified bound and incumbent."""
+    import _frontier_oracle as F
+    if problem == "box":
+        inst = instances.box_qp(n=12, seed=9)
+        s = inst.settings
+        s.gpu_batch_size = 8
+        s.gpu_max_iters = 2000
+        s.rel_gap_tol = 0.0
+    elif problem == "graph":
+        inst = _pair(207, 6)
+        s = inst.settings
+        s.algorithm = A.ALG_DICG
+        s.line_search = A.LS_QUADRATIC_EXACT
+        s.gpu_batch_size = 16
+        s.gpu_max_iters = 500
+        s.abs_gap_tol = 1e-6
+        s.rel_gap_tol = 1e-6
+    else:
+        inst = instances.portfolio(assets=8, months=120, cardinality=3, seed=11)
+        s = inst.settings
+        s.gpu_batch_size = 16
+        s.gpu_max_iters = 3000
+        s.rel_gap_tol = 0.0
+    s.incumbent_cutoff = cutoff
+    s.time_limit_seconds = 60
+    ref = F.solve(inst.problem, inst.objective, inst.lmo, s, slots)
+    s.device_frontier = 1
+    s.frontier_slots = slots
+    g = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert g.nodes_processed == ref["nodes"]
+    assert g.objective == ref["objective"]
+    assert g.dual_bound == ref["dual_bound"]
+    assert g.reached_tolerance == ref["tolerance"]
+    assert np.array_equal(g.x, ref["x"])
