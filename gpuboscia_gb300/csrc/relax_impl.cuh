@@ -2335,11 +2335,11 @@ __global__ void __launch_bounds__(kThreads, 1) feasible_kernel(
 
 
 // ------------------------------------------------------------------ launchers
-template <int OK, int LK>
-int launch_one(const Params& p, cudaStream_t st, std::string* err) {
-    auto k = relax_kernel<OK, LK, 0>;
-    if constexpr (OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF)
-        if (p.L.mixed) k = p.L.tc ? relax_kernel<OK, LK, 2> : p.L.cost_global ? relax_kernel<OK, LK, 3> : relax_kernel<OK, LK, 1>;
+// One kernel variant (MIX) of a kind; each variant of the graph-matching
+// Birkhoff kernel is instantiated in its own translation unit.
+template <int OK, int LK, int MIX>
+int launch_mix(const Params& p, cudaStream_t st, std::string* err) {
+    auto k = relax_kernel<OK, LK, MIX>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::max<size_t>(p.L.sm_total, 1));
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
@@ -2360,6 +2360,18 @@ int launch_one(const Params& p, cudaStream_t st, std::string* err) {
     e = cudaGetLastError();
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
     return GBX_OK;
+}
+
+template <int OK, int LK>
+int launch_one(const Params& p, cudaStream_t st, std::string* err) {
+    if constexpr (OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF) {
+        if (p.L.mixed) {
+            if (p.L.tc) return launch_mix<OK, LK, 2>(p, st, err);
+            if (p.L.cost_global) return launch_mix<OK, LK, 3>(p, st, err);
+            return launch_mix<OK, LK, 1>(p, st, err);
+        }
+    }
+    return launch_mix<OK, LK, 0>(p, st, err);
 }
 
 template <int LK>
