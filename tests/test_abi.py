@@ -126,3 +126,55 @@ def test_relax_rejects_bad_arguments_without_launching(lib):
     b.n_nodes = 2
     assert lib.gbx_relax_batch(C.byref(obj), C.byref(lmo), C.byref(alg), C.byref(b), None, 0, None) == A.ERR_INVALID
     assert b"null" in lib.gbx_last_error()
+
+
+def test_device_frontier_rejects_bad_settings_without_launching(lib):
+    """gbx_solve with device_frontier checks its arguments on the host before any
+    CUDA call (frontier.cu, solve_device_frontier), so every rejection below is
+    reachable without a GPU and names the offending setting."""
+    keep = api._Keep()
+    n = 4
+    obj = api.DenseQuadraticObjective(np.eye(n)).to_c("host", keep)
+    lmo = api.BoxLMO().to_c(n, "host", keep)
+    lb, ub = np.zeros(n), np.ones(n)
+    iv = np.arange(n, dtype=np.int32)
+    prob = A.Problem(n, lb.ctypes.data, ub.ctypes.data, iv.ctypes.data, n)
+    res = A.Result()
+
+    def solve(**kw):
+        s = A.default_settings()
+        s.device_frontier = 1
+        for k, v in kw.items():
+            setattr(s, k, v)
+        rc = lib.gbx_solve(C.byref(prob), C.byref(obj), C.byref(lmo), C.byref(s), C.byref(res))
+        return rc, lib.gbx_last_error().decode()
+
+    for kw, word in [(dict(gpu_batch_size=0), "gpu_batch_size"),
+                     (dict(gpu_batch_size=1025), "gpu_batch_size"),
+                     (dict(branch_k=9), "branch_k"),
+                     (dict(branch_k=0), "branch_k"),
+                     (dict(frontier_slots=3), "frontier_slots"),
+                     (dict(gpu_max_iters=0), "positive"),
+                     (dict(gpu_eps_decay=1.5), "tolerance"),
+                     (dict(abs_gap_tol=-1.0), "tolerance"),
+                     (dict(time_limit_seconds=0.0), "time limit"),
+                     (dict(natural_lower_bound=float("nan")), "natural lower bound")]:
+        rc, msg = solve(**kw)
+        assert rc == A.ERR_INVALID, (kw, rc, msg)
+        assert word in msg, (kw, msg)
+
+    sc = A.Scorer(A.SCORER_FEATURES, 7, C.c_void_p(16), None)   # hidden must be 16, 32 or 64
+    rc, msg = solve(scorer=C.cast(C.pointer(sc), C.c_void_p))
+    assert rc == A.ERR_INVALID and "scorer" in msg
+
+    bad_iv = np.array([n + 3], dtype=np.int32)
+    prob_bad = A.Problem(n, lb.ctypes.data, ub.ctypes.data, bad_iv.ctypes.data, 1)
+    s = A.default_settings()
+    s.device_frontier = 1
+    rc = lib.gbx_solve(C.byref(prob_bad), C.byref(obj), C.byref(lmo), C.byref(s), C.byref(res))
+    assert rc == A.ERR_INVALID and b"out of range" in lib.gbx_last_error()
+
+    # an LMO the relaxation kernel cannot size (Birkhoff order not matching n)
+    blmo = A.LMO(A.LMO_BIRKHOFF, n, 1.0, None, 3)
+    rc = lib.gbx_solve(C.byref(prob), C.byref(obj), C.byref(blmo), C.byref(s), C.byref(res))
+    assert rc == A.ERR_INVALID
