@@ -17,7 +17,8 @@ A rank that fails (raises, dies, never joins) makes the next collective of its
 peers fail within the process group's timeout; they raise
 ``RankFailure`` instead of waiting. Only the certified FW bound (value - gap of
 a node whose gap is finite and non-negative) prunes, as in the single-GPU
-solver; branching is branch_pow2 over the most fractional variables, or over
+solver (with ``settings.incumbent_cutoff`` each relaxation stops once that
+bound reaches the shared incumbent); branching is branch_pow2 over the most fractional variables, or over
 the learned scorer's choice when one is given.
 """
 from __future__ import annotations
@@ -61,8 +62,9 @@ class DistributedResult:
     stolen: int                   # nodes this rank received from others
 
 
-# relax(lbs, ubs, xs, eps, iterations, status) -> dict(x, gap, value, status, iterations,
-#                                                     best_vertex, best_vertex_val)
+# relax(lbs, ubs, xs, eps, iterations, status[, cutoff=incumbent]) -> dict(x, gap, value, status,
+#                                                     iterations, best_vertex, best_vertex_val)
+# (cutoff is passed only when settings.incumbent_cutoff is set)
 RelaxFn = Callable[..., dict]
 
 
@@ -73,13 +75,13 @@ def gpu_relax_fn(objective, lmo, settings, integer_flags):
     alg = settings.algorithm_c()
     flags = torch.from_numpy(np.ascontiguousarray(integer_flags, np.uint8)).cuda()
 
-    def relax(lbs, ubs, xs, eps, iterations, status):
+    def relax(lbs, ubs, xs, eps, iterations, status, cutoff=None):
         T = lambda a, dt=None: torch.from_numpy(np.ascontiguousarray(a if dt is None else np.asarray(a, dt))).cuda()
         x = T(xs)
         it = T(iterations, np.int32)
         st = T(status, np.uint8)
         out = api.relax_batch(objective, lmo, alg, x, T(lbs), T(ubs), T(eps), it, st, settings.gpu_max_iters, flags,
-                              settings.integer_tol)
+                              settings.integer_tol, cutoff=cutoff)
         torch.cuda.synchronize()
         return dict(x=x.cpu().numpy(), gap=out["gap"].cpu().numpy(), value=out["value"].cpu().numpy(),
                     status=st.cpu().numpy(), iterations=it.cpu().numpy(),
@@ -156,7 +158,10 @@ def solve(problem, settings, relax: RelaxFn, group=None, branch_vars: Optional[C
             sts = np.array([A.NODE_INITIAL_POINT_SUPPLIED if b.x is not None else 0 for b in batch], np.uint8)
             eps = np.array([max(settings.gpu_eps_min, settings.gpu_eps * settings.gpu_eps_decay ** b.depth)
                             for b in batch])
-            r = relax(lbs, ubs, xs, eps, its, sts)
+            # with the incumbent cutoff a node stops iterating once its FW bound
+            # reaches the shared incumbent: it is pruned below all the same
+            cut = {"cutoff": inc_val} if getattr(settings, "incumbent_cutoff", 0) and math.isfinite(inc_val) else {}
+            r = relax(lbs, ubs, xs, eps, its, sts, **cut)
             processed += N
             for i, nd in enumerate(batch):
                 bv = r["best_vertex_val"][i]

@@ -38,31 +38,36 @@ def _oracle_relax(inst, flags, fail_on_call=None):
     import _oracle as O
     calls = [0]
 
-    def relax(lbs, ubs, xs, eps, its, sts):
+    def relax(lbs, ubs, xs, eps, its, sts, cutoff=None):
         calls[0] += 1
         if fail_on_call is not None and calls[0] == fail_on_call:
             raise RuntimeError("injected failure of this rank")
+        if cutoff is not None:
+            cutoffs.append(cutoff)
         s = inst.settings
         alg = O.algorithm(s.algorithm, s.line_search)
         return O.relax(inst.objective, inst.lmo, alg, xs.copy(), lbs, ubs, eps, its.copy(), sts.copy(),
-                       s.gpu_max_iters, flags, s.integer_tol)
+                       s.gpu_max_iters, flags, s.integer_tol, cutoff=cutoff)
+    cutoffs = []
+    relax.cutoffs = cutoffs
     return relax
 
 
-def _worker(rank, world, port, kind, fail_rank, out):
+def _worker(rank, world, port, kind, fail_rank, out, cutoff=0):
     import torch.distributed as dist
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=20))
     from gpuboscia_gb300 import distributed
     inst = _instance(kind)
+    inst.settings.incumbent_cutoff = cutoff
     flags = np.zeros(inst.problem.n_vars, np.uint8)
     flags[list(inst.problem.int_vars)] = 1
     relax = _oracle_relax(inst, flags, fail_on_call=1 if rank == fail_rank else None)
     try:
         r = distributed.solve(inst.problem, inst.settings, relax)
         out.put((rank, "ok", r.objective, r.dual_bound, r.nodes_processed, r.nodes_total, r.stolen,
-                 None if r.x is None else r.x.tolist()))
+                 None if r.x is None else r.x.tolist(), len(relax.cutoffs)))
     except distributed.RankFailure as e:
         out.put((rank, "peer-failure", str(e)[:200]))
     except RuntimeError as e:
@@ -74,12 +79,12 @@ def _worker(rank, world, port, kind, fail_rank, out):
             pass
 
 
-def _run(kind, fail_rank=None, world=2):
+def _run(kind, fail_rank=None, world=2, cutoff=0):
     import torch.multiprocessing as mp
     ctx = mp.get_context("spawn")
     out = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_worker, args=(r, world, port, kind, fail_rank, out)) for r in range(world)]
+    procs = [ctx.Process(target=_worker, args=(r, world, port, kind, fail_rank, out, cutoff)) for r in range(world)]
     for p in procs:
         p.start()
     res = {}
@@ -91,15 +96,15 @@ def _run(kind, fail_rank=None, world=2):
     return res
 
 
-@pytest.mark.parametrize("kind", ["box", "portfolio"])
-def test_two_ranks_reach_the_single_process_optimum(kind):
+@pytest.mark.parametrize("kind,cutoff", [("box", 0), ("portfolio", 0), ("box", 1)])
+def test_two_ranks_reach_the_single_process_optimum(kind, cutoff):
     sys.path.insert(0, HERE)
     import _oracle as O
     inst = _instance(kind)
     s = inst.settings
     s.num_streams = 1
     ref = O.solve(inst.problem, inst.objective, inst.lmo, s)
-    res = _run(kind)
+    res = _run(kind, cutoff=cutoff)
     assert all(res[r][1] == "ok" for r in res), res
     objs = {res[r][2] for r in res}
     assert len(objs) == 1                                     # incumbent shared
@@ -110,6 +115,8 @@ def test_two_ranks_reach_the_single_process_optimum(kind):
         assert res[r][4] > 0                                  # both ranks relaxed nodes
     assert res[1][6] > 0                                      # rank 1 started empty: it stole work
     assert res[0][5] == res[1][5] == res[0][4] + res[1][4]
+    # the shared incumbent reached the relaxations as their cutoff (only when enabled)
+    assert (sum(res[r][8] for r in res) > 0) == bool(cutoff)
 
 
 def test_peer_failure_is_reported_not_awaited():
