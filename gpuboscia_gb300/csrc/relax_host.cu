@@ -102,7 +102,6 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
         // (above, in the workspace, over the nonzero lists of sparse graphs); the
         // tensor-core gradient pads any order up to 128
         const bool tc_ok = l.order > 16 && l.order <= 128;
-        const bool simt_ok = l.order <= 128;
         L.tc = tc_ok && (v.tc == 1 || (v.tc < 0 && l.order > 64)) ? 1 : 0;
         if (L.tc) cost_bytes = std::max(cost_bytes, kTcOperandBytes);
         const size_t staged = std::max(cost_bytes, align16((size_t)n * sizeof(double)));  // + certificate costs

@@ -1337,32 +1337,33 @@ static __device__ double lmo_max_step(const Ctx& c, const double* d, const doubl
         const double sum_d = bsum(sd, c.red);
         const double agg = sum_d < -1e-9 ? fmax(0.0, fmin(1.0, (sum_x - L.m) / sum_d)) : 1.0;
         return fmax(0.0, fmin(coord, agg));
-    }
-    for (int j = c.tid; j < n; j += kThreads) {
-        const double dj = d[j];
-        if constexpr (LK == GBX_LMO_BOX) {
-            if (dj < 0.0) res = fmin(res, (ub[j] - x[j]) / -dj);
-            else if (dj > 0.0) res = fmin(res, (x[j] - lb[j]) / dj);
-        } else if constexpr (LK == GBX_LMO_BIRKHOFF || LK == GBX_LMO_CARDINALITY) {
-            if (dj > 0.0) res = fmin(res, (x[j] - lb[j]) / dj);
-            else if (dj < 0.0) res = fmin(res, (ub[j] - x[j]) / -dj);
-        } else {
-            const bool ij = c.is_int && c.is_int[j];
-            if (dj > 1e-6) res = fmin(res, (x[j] - (ij ? lb[j] : 0.0)) / dj);
-            else if (dj < -1e-6) res = fmin(res, ((ij ? ub[j] : c.rhs) - x[j]) / -dj);
+    } else {
+        for (int j = c.tid; j < n; j += kThreads) {
+            const double dj = d[j];
+            if constexpr (LK == GBX_LMO_BOX) {
+                if (dj < 0.0) res = fmin(res, (ub[j] - x[j]) / -dj);
+                else if (dj > 0.0) res = fmin(res, (x[j] - lb[j]) / dj);
+            } else if constexpr (LK == GBX_LMO_BIRKHOFF || LK == GBX_LMO_CARDINALITY) {
+                if (dj > 0.0) res = fmin(res, (x[j] - lb[j]) / dj);
+                else if (dj < 0.0) res = fmin(res, (ub[j] - x[j]) / -dj);
+            } else {
+                const bool ij = c.is_int && c.is_int[j];
+                if (dj > 1e-6) res = fmin(res, (x[j] - (ij ? lb[j] : 0.0)) / dj);
+                else if (dj < -1e-6) res = fmin(res, ((ij ? ub[j] : c.rhs) - x[j]) / -dj);
+            }
         }
+        const double coord = bmin(res, c.red);
+        double agg = 1.0;
+        if constexpr (LK == GBX_LMO_SIMPLEX || LK == GBX_LMO_EQUALITY_SIMPLEX) {
+            double sx = 0.0, sd = 0.0;
+            for (int j = c.tid; j < n; j += kThreads) { sx += x[j]; sd += d[j]; }
+            const double sum_x = bsum(sx, c.red);
+            const double sum_d = bsum(sd, c.red);
+            if (LK == GBX_LMO_EQUALITY_SIMPLEX && fabs(sum_d) > 1e-9) agg = 0.0;
+            else agg = sum_d < 0.0 ? fmin(1.0, (sum_x - c.rhs) / sum_d) : 1.0;
+        }
+        return fmax(0.0, fmin(coord, agg));
     }
-    const double coord = bmin(res, c.red);
-    double agg = 1.0;
-    if constexpr (LK == GBX_LMO_SIMPLEX || LK == GBX_LMO_EQUALITY_SIMPLEX) {
-        double sx = 0.0, sd = 0.0;
-        for (int j = c.tid; j < n; j += kThreads) { sx += x[j]; sd += d[j]; }
-        const double sum_x = bsum(sx, c.red);
-        const double sum_d = bsum(sd, c.red);
-        if (LK == GBX_LMO_EQUALITY_SIMPLEX && fabs(sum_d) > 1e-9) agg = 0.0;
-        else agg = sum_d < 0.0 ? fmin(1.0, (sum_x - c.rhs) / sum_d) : 1.0;
-    }
-    return fmax(0.0, fmin(coord, agg));
 }
 
 // drs_node_feasible (device_resident_solver.cuh:206-217) + LMO check.
