@@ -70,7 +70,9 @@ def test_struct_layouts_match_ctypes(tmp_path):
     src = tmp_path / "layout.c"
     src.write_text(_LAYOUT_C)
     exe = tmp_path / "layout"
-    subprocess.run(["gcc", "-std=c99", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    # the header is plain C: it compiles warning-free under strict C99
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", str(ROOT / "include"),
+                    str(src), "-o", str(exe)], check=True)
     got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
                                                        check=True).stdout.splitlines())
     M = {"gbx_objective": A.Objective, "gbx_lmo": A.LMO, "gbx_algorithm": A.Algorithm,
