@@ -132,3 +132,19 @@ def test_reference_instance_files():
         A = instances.load_dimacs(f)
         m = int(next(line for line in f.read_text().splitlines() if line.startswith("p")).split()[3])
         assert np.array_equal(A, A.T) and int(A.sum()) == 2 * m, f.name
+
+
+DATASETS = REF.parent / "DataSets"
+
+
+@pytest.mark.skipif(not DATASETS.is_dir(), reason="reference data sets not present")
+def test_reference_datasets():
+    """The return matrices the sparse-Sharpe example reads (examples/sparse_sharpe.cu
+    load_mat, variable `data`) decode to the same values as scipy's reader."""
+    sio = pytest.importorskip("scipy.io")
+    mats = sorted(DATASETS.glob("*.mat"))
+    assert mats
+    for f in mats:
+        D = instances.load_mat(f, "data")
+        S = np.asarray(sio.loadmat(f)["data"], float)
+        assert D.shape == S.shape and np.array_equal(D, S), f.name

@@ -3,6 +3,8 @@ examples/sparse_sharpe.cu:266-546) in the oracle, pinned by enumeration: the
 forward vertex, the in-face vertex over the minimal face of a point, and the
 DICG maximum step; the instance builder on the reference's data shape."""
 import itertools
+import os
+import pathlib
 
 import numpy as np
 import pytest
@@ -147,3 +149,33 @@ def test_sparse_sharpe_builder_bounds_the_level_set():
     f = 0.5 * vstar @ H @ vstar - mu @ vstar
     assert abs(f - inst.settings.natural_lower_bound) <= 1e-9 * (1 + abs(f))
     assert inst.problem.int_vars == list(range(32, 62))
+
+
+US_ALL = pathlib.Path(os.environ.get("GPUBOSCIA_REFERENCE", "/root/reference")) / "DataSets" / "US_all_monthly.mat"
+
+
+@pytest.mark.skipif(not US_ALL.is_file(), reason="reference data set not present")
+@pytest.mark.parametrize("assets,card", [(20, 4), (40, 5)])
+def test_sparse_sharpe_on_the_reference_returns(assets, card):
+    """The example's model on its own data (US_all_monthly.mat, last 60 months,
+    the first `assets` columns, epsilon 1e-3): the oracle B&B closes the gap,
+    the device frontier's restated search reaches the same optimum, and the
+    optimum holds at most `card` assets inside their bounds."""
+    import _frontier_oracle as F
+    P = instances.load_mat(US_ALL, "data")
+    inst = instances.sparse_sharpe(P, assets=assets, cardinality=card, observations=60)
+    s = inst.settings
+    s.gpu_batch_size = 32
+    s.num_streams = 1
+    s.gpu_max_iters = 2000
+    s.time_limit_seconds = 60
+    o = O.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert not o.reached_time_limit
+    assert o.dual_bound >= o.objective - max(s.abs_gap_tol, s.rel_gap_tol * abs(o.objective))
+    assert s.natural_lower_bound <= o.objective
+    f = F.solve(inst.problem, inst.objective, inst.lmo, s, 2)
+    assert abs(f["objective"] - o.objective) <= 1e-9 * max(1.0, abs(o.objective))
+    h = inst.problem.n_vars // 2
+    v, y = o.x[:assets], o.x[h:h + assets]
+    assert np.array_equal(y, np.round(y)) and y.sum() <= card
+    assert np.all(v >= -1e-12) and np.all(v <= inst.lmo.upper[:assets] * y + 1e-9)
