@@ -148,3 +148,35 @@ def test_reference_datasets():
         D = instances.load_mat(f, "data")
         S = np.asarray(sio.loadmat(f)["data"], float)
         assert D.shape == S.shape and np.array_equal(D, S), f.name
+
+
+@pytest.mark.skipif(not REF.is_dir(), reason="reference instance files not present")
+@pytest.mark.parametrize("name", ["latin_3_9.mat", "paley_power_9.mat", "paley_prime_13.mat"])
+def test_reference_instance_is_solved(name):
+    """examples/main.cu's flow on the reference's own graphs (B = A under a
+    seeded permutation): the oracle B&B and the device frontier's restated
+    search find an isomorphism (objective 0) with a closed certified gap."""
+    import sys
+    sys.path.insert(0, str(pathlib.Path(__file__).resolve().parent))
+    import _frontier_oracle as F
+    import _oracle as O
+    from gpuboscia_gb300 import _abi as A
+    inst = instances.graph_matching_from_file(REF / name, seed=3)
+    s = inst.settings
+    s.algorithm = A.ALG_DICG
+    s.line_search = A.LS_QUADRATIC_EXACT
+    s.gpu_batch_size = 16
+    s.num_streams = 1
+    s.gpu_max_iters = 500
+    s.abs_gap_tol = 1e-6
+    s.rel_gap_tol = 1e-6
+    s.time_limit_seconds = 60
+    o = O.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert o.objective <= 1e-9 and o.reached_tolerance and not o.reached_time_limit
+    f = F.solve(inst.problem, inst.objective, inst.lmo, s, 2)
+    assert f["objective"] <= 1e-9
+    m = inst.lmo.order
+    for x in (o.x, f["x"]):
+        X = np.asarray(x).reshape(m, m)
+        assert np.array_equal(X.sum(0), np.ones(m)) and np.array_equal(X.sum(1), np.ones(m))
+        assert np.array_equal(inst.objective.A @ X, X @ inst.objective.B)
