@@ -12,6 +12,7 @@ import dataclasses
 import numpy as np
 
 from . import api
+from ._abi import ALG_DICG
 
 SEEDS = {1: 1001, 2: 1002, 3: 1003, 4: 1004, 5: 1005}
 
@@ -335,3 +336,34 @@ def synthetic_gross_returns(months: int, assets: int, seed: int = SEEDS[3]) -> n
     vol = 0.03 + 0.08 * rng.random(assets)
     alpha = normal(rng, assets, 0.0, 0.004)
     return 1.0 + f @ beta.T + alpha[None, :] + normal(rng, (months, assets)) * vol[None, :]
+
+
+def weighted_clique(vertices: int = 20, cardinality: int = 5, seed: int = 222222222) -> Instance:
+    """examples/weighted_clique.cu:64-150: the maximum-weight induced subgraph
+    with exactly `cardinality` vertices, as a convex binary quadratic.
+
+    Edge weights w_ij ~ U[0, 1). f(x) = 2 sum_{i<j} (1 - w_ij) x_i x_j
+    + lam sum_i x_i (x_i - 1), lam = vertices - 1: in 0.5 x'Qx + c'x form Q has
+    2 lam on the diagonal and 2 (1 - w_ij) off it, c = -lam. The lam term is
+    zero at binary points and makes Q diagonally dominant (convex). Over the
+    equality simplex sum x = cardinality, x binary; DICG, the example's
+    tolerances and its natural bound lam (cardinality^2 / vertices - cardinality)
+    (Cauchy-Schwarz on sum x_i^2). The weights come from PCG64, not the
+    example's mt19937_64, so the instance has the example's shape, not its
+    exact numbers."""
+    rng = _rng(seed)
+    n = vertices
+    W = np.zeros((n, n))
+    iu = np.triu_indices(n, 1)
+    W[iu] = rng.random(len(iu[0]))
+    W = W + W.T
+    lam = float(n - 1)
+    Q = 2.0 * (1.0 - W)
+    np.fill_diagonal(Q, 2.0 * lam)
+    c = np.full(n, -lam)
+    prob = api.Problem(n, np.zeros(n), np.ones(n), list(range(n)))
+    s = api.Settings(algorithm=ALG_DICG, gpu_batch_size=1024, num_streams=2, gpu_max_iters=1000,
+                     abs_gap_tol=1e-7, rel_gap_tol=1e-3,
+                     natural_lower_bound=lam * (cardinality * cardinality / n - cardinality))
+    return Instance(f"weighted_clique_{n}_{cardinality}", prob, api.DenseQuadraticObjective(Q, c),
+                    api.EqualitySimplexLMO(float(cardinality), list(range(n))), s)

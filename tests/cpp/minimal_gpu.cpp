@@ -1,10 +1,12 @@
 // The reference's examples/minimal.cu (min (x0-.3)^2 + (x1-.7)^2 over binaries:
 // x = [0, 1], f = .18) through the C++ drop-in headers, once with the host
 // frontier and once with the device frontier; and a graph-matching pair of
-// order 5 solved both ways to the same certified optimum; and a small
-// sparse-Sharpe portfolio through the reference's LinkedCardinalityLMO.
+// order 5 solved both ways to the same certified optimum; a small
+// sparse-Sharpe portfolio through the reference's LinkedCardinalityLMO; and
+// the weighted-clique example's model over EqualitySimplexLMO.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <stdexcept>
@@ -130,6 +132,60 @@ int main() {
         CHECK(std::fabs(r.objective + 0.125) <= 1e-6);
         CHECK(r.x.size() == Vars && r.x[MaxAssets] == 1.0 && r.x[MaxAssets + 1] == 0.0 && r.x[MaxAssets + 2] == 0.0);
     }
+
+    // weighted clique (examples/weighted_clique.cu): 20 vertices, exactly 5;
+    // f = 2 sum_{i<j} (1 - w_ij) x_i x_j + lam sum x_i (x_i - 1), lam = 19,
+    // over EqualitySimplexLMO<20> with integer variables, DICG; the optimum is
+    // checked against enumeration of all 5-subsets
+    constexpr int Vc = 20, Kc = 5;
+    std::vector<double> W(Vc * Vc, 0.0), Qc(Vc * Vc, 0.0), lc(Vc, -(Vc - 1.0));
+    unsigned long long state = 88172645463325252ull;   // xorshift64 weights in [0, 1)
+    for (int i = 0; i < Vc; ++i)
+        for (int j = i + 1; j < Vc; ++j) {
+            state ^= state << 13; state ^= state >> 7; state ^= state << 17;
+            W[i * Vc + j] = W[j * Vc + i] = (double)(state >> 11) * 0x1.0p-53;
+        }
+    for (int i = 0; i < Vc; ++i)
+        for (int j = 0; j < Vc; ++j) Qc[i * Vc + j] = i == j ? 2.0 * (Vc - 1.0) : 2.0 * (1.0 - W[i * Vc + j]);
+    double best = 1e300;
+    for (int a = 0; a < Vc; ++a) for (int b = a + 1; b < Vc; ++b) for (int c = b + 1; c < Vc; ++c)
+        for (int d = c + 1; d < Vc; ++d) for (int e = d + 1; e < Vc; ++e) {
+            const int S[Kc] = {a, b, c, d, e};
+            double f = 0.0;
+            for (int p = 0; p < Kc; ++p)
+                for (int q = p + 1; q < Kc; ++q) f += Qc[S[p] * Vc + S[q]];
+            best = std::min(best, f);
+        }
+    double* dQc = upload(Qc);
+    double* dlc = upload(lc);
+    GlobalCachedDenseQuadraticObjective<Vc, 32> clique(dQc, dlc, 1.0, 1.0, 0.0);
+    Problem cp;
+    cp.n_vars = Vc;
+    cp.lb.assign(Vc, 0.0);
+    cp.ub.assign(Vc, 1.0);
+    for (int i = 0; i < Vc; ++i) cp.int_vars.push_back(i);
+    EqualitySimplexLMO<Vc> card((double)Kc, Vc, cp.int_vars);
+    for (int dev = 0; dev < 2; ++dev) {
+        auto s = gpuboscia::create_default_settings();
+        s.algorithm = FWAlgorithmKind::DICG;
+        s.time_limit_seconds = 60;
+        s.device.gpu_batch_size = 1024;
+        s.device.num_streams = 2;
+        s.device.gpu_max_iters = 1000;
+        s.device.abs_gap_tol = 1e-7;
+        s.device.rel_gap_tol = 1e-3;
+        s.device.device_frontier = dev != 0;
+        s.natural_lower_bound = (Vc - 1.0) * ((double)Kc * Kc / Vc - Kc);
+        const auto r = gpuboscia::solve(cp, clique, card, s);
+        double chosen = 0.0;
+        for (double v : r.x) chosen += v;
+        std::printf("weighted clique device_frontier=%d: f=%.12f enumerated=%.12f bound=%.12f nodes=%d\n", dev,
+                    r.objective, best, r.dual_bound, r.nodes_processed);
+        CHECK(!r.reached_time_limit && r.x.size() == Vc && chosen == Kc);
+        CHECK(r.objective - best <= 1e-3 * std::fabs(best) + 1e-7 && r.dual_bound <= best + 1e-9);
+    }
+    cudaFree(dQc);
+    cudaFree(dlc);
     cudaFree(dQs);
     cudaFree(dls);
     cudaFree(dU);
