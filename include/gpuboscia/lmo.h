@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../gpuboscia_gb300.h"
+#include "lmo_dicg.h"
 
 namespace gpuboscia {
 // What the relaxation kernel needs to know about an LMO (host data).
@@ -29,6 +30,20 @@ struct BoxLMO {
     bool relaxation_feasible_cpu(const std::vector<double>&, const std::vector<double>&,
                                  const std::vector<double>&, double) const {
         return true;  // the public API checks the box bounds itself
+    }
+    // host restatements of the kernel's oracles (the reference's *_cpu members)
+    void compute_v_cpu(const std::vector<double>& grad, const std::vector<double>& lb,
+                       const std::vector<double>& ub, std::vector<double>& v) const {
+        for (size_t j = 0; j < grad.size(); ++j) v[j] = grad[j] > 0.0 ? lb[j] : ub[j];
+    }
+    void compute_inface_v_cpu(const std::vector<double>& grad, const std::vector<double>& x,
+                              const std::vector<double>& lb, const std::vector<double>& ub, std::vector<double>& a,
+                              double atol = 1e-6, double rtol = 1e-4) const {
+        box_inface_lmo_cpu(grad, x, lb, ub, a, atol, rtol);
+    }
+    double dicg_maximum_step_cpu(const std::vector<double>& direction, const std::vector<double>& x,
+                                 const std::vector<double>& lb, const std::vector<double>& ub) const {
+        return box_dicg_maximum_step_cpu(direction, x, lb, ub);
     }
     gpuboscia::LMOSpec spec(int) const { return {GBX_LMO_BOX, 1.0, {}, 0}; }
 };
@@ -53,13 +68,59 @@ struct UnitSimplexLMO {
     }
     bool relaxation_feasible_cpu(const std::vector<double>& x, const std::vector<double>&,
                                  const std::vector<double>&, double tol) const {
+        return dicg_linear_feasible_cpu(x, tol);
+    }
+    bool dicg_linear_feasible_cpu(const std::vector<double>& v, double tol = 1e-3) const {
+        return RequireEquality ? equality_simplex_linear_feasible_cpu(right_side, v, tol)
+                               : unit_simplex_linear_feasible_cpu(right_side, v, tol);
+    }
+    bool dicg_inface_feasible_cpu(const std::vector<double>& a, const std::vector<double>& x, double atol = 1e-6,
+                                  double rtol = 1e-4) const {
+        return RequireEquality
+                   ? equality_simplex_linear_feasible_cpu(right_side, a, atol + rtol * std::abs(right_side))
+                   : unit_simplex_inface_feasible_cpu(right_side, a, x, atol, rtol);
+    }
+    // Forward oracle on the host: integer coordinates start at lb, the rest of
+    // the mass goes greedily in (gradient, index) order -- to non-positive
+    // gradients only unless the mass is fixed -- integer coordinates up to
+    // ub (whole units under the equality), continuous ones taking all of it.
+    void compute_v_cpu(const std::vector<double>& grad, const std::vector<double>& lb,
+                       const std::vector<double>& ub, std::vector<double>& v) const {
+        const int n = (int)grad.size(), m = std::min(n, MaxN);
         double mass = 0.0;
-        if (RequireEquality) {
-            for (double v : x) { if (v < -tol) return false; mass += v; }
-            return std::isfinite(mass) && std::abs(mass - right_side) <= tol;
+        std::vector<int> order;
+        order.reserve(m);
+        for (int j = 0; j < n; ++j) {
+            v[j] = j < m && is_int[j] ? lb[j] : 0.0;
+            if (j < m && is_int[j]) mass += v[j];
+            if (j < m && (RequireEquality || !(grad[j] > 0.0))) order.push_back(j);
         }
-        for (double v : x) { if (v < 0.0) return false; mass += v; }
-        return mass <= right_side + tol;
+        std::stable_sort(order.begin(), order.end(), [&](int p, int q) { return grad[p] < grad[q]; });
+        double remaining = right_side - mass;
+        for (int j : order) {
+            if (!(remaining > 0.0)) break;
+            double add = remaining;
+            if (is_int[j]) {
+                const double room = std::max(ub[j] - lb[j], 0.0);
+                add = std::min(room, RequireEquality ? std::floor(remaining + 1e-9) : remaining);
+            }
+            v[j] += add;
+            remaining -= add;
+        }
+    }
+    void compute_inface_v_cpu(const std::vector<double>& grad, const std::vector<double>& x,
+                              const std::vector<double>& lb, const std::vector<double>& ub, std::vector<double>& a,
+                              double atol = 1e-6, double rtol = 1e-4) const {
+        const int n = std::min((int)grad.size(), MaxN);
+        unit_simplex_inface_lmo_cpu(right_side, std::vector<unsigned char>(is_int, is_int + n), grad, x, lb, ub, a,
+                                    atol, rtol, RequireEquality);
+    }
+    double dicg_maximum_step_cpu(const std::vector<double>& direction, const std::vector<double>& x,
+                                 const std::vector<double>& lb, const std::vector<double>& ub,
+                                 double tol = 1e-6) const {
+        const int n = std::min((int)direction.size(), MaxN);
+        return unit_simplex_dicg_maximum_step_cpu(right_side, std::vector<unsigned char>(is_int, is_int + n),
+                                                  direction, x, lb, ub, tol, RequireEquality);
     }
     gpuboscia::LMOSpec spec(int n) const {
         gpuboscia::LMOSpec s;

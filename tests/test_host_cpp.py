@@ -52,3 +52,52 @@ def test_host_rules_match_reference_fixture(exe):
     out = _table(exe, [f"quad {g!r} {c!r} {m!r}" for g, c, m, _ in GOLDEN["quad_step"]])
     for k, (*_, e) in enumerate(GOLDEN["quad_step"]):
         assert float(out[k]) == e
+
+
+def test_logger_header_drives_like_the_examples(tmp_path):
+    """include/gpuboscia/logger.h: the examples' Logger / LoggerParams /
+    SolutionStats calls compile warning-free; rows are throttled by the node
+    interval except for new incumbents; a disabled logger prints nothing."""
+    out = tmp_path / "logger_demo"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
+                    str(ROOT / "tests" / "cpp" / "logger_demo.cpp"), "-o", str(out)], check=True)
+    text = subprocess.run([str(out)], capture_output=True, text=True, check=True).stdout
+    rows = [line.split() for line in text.splitlines() if line.startswith("  ") and line.split()[-1][0].isdigit()]
+    nodes = [int(r[1]) if r[0] == "*" else int(r[0]) for r in rows]
+    # rows at 0, every >= 100 nodes, and the new incumbent at 120 (marked)
+    assert nodes == [0, 120, 240, 360]
+    assert [r[0] == "*" for r in rows] == [False, True, False, False]
+    assert "Decomposition-Invariant Frank-Wolfe" in text and "secant" in text
+    assert "Reached tolerance" in text and "2 of 20 entries nonzero" in text
+    assert text.count("variables 20") == 1    # the disabled logger printed nothing
+
+
+def _fmt(v):
+    return " ".join(repr(float(e)) for e in v)
+
+
+def test_host_lmo_oracles_match_the_reference_outputs(tmp_path):
+    """BoxLMO / UnitSimplexLMO / EqualitySimplexLMO compute_v_cpu,
+    compute_inface_v_cpu and dicg_maximum_step_cpu (include/gpuboscia/lmo.h over
+    lmo_dicg.h) reproduce, exactly, the reference's own CPU oracles on the
+    golden cases (tests/golden/reference_cpu.json: forward vertex, in-face
+    vertex, and the maximum step along inface(g) - forward(-g))."""
+    exe = tmp_path / "lmo_cpu"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
+                    str(ROOT / "tests" / "cpp" / "lmo_cpu.cpp"), "-o", str(exe)], check=True)
+    lines, want = [], []
+    for c in GOLDEN["box"]:
+        n = len(c["g"])
+        lines.append(f"box {n} {_fmt(c['g'])} {_fmt(c['lb'])} {_fmt(c['ub'])} {_fmt(c['x'])}")
+        want.append(c["forward"] + c["inface"] + [c["step"]])
+    for c in GOLDEN["simplex"]:
+        n = len(c["g"])
+        lines.append(f"simplex {c['equality']} {c['rhs']!r} {n} {len(c['ints'])} {' '.join(map(str, c['ints']))} "
+                     f"{_fmt(c['g'])} {_fmt(c['lb'])} {_fmt(c['ub'])} {_fmt(c['x'])}")
+        want.append(c["forward"] + c["inface"] + [c["step"]])
+    r = subprocess.run([str(exe)], input="\n".join(lines) + "\n", capture_output=True, text=True, check=True)
+    got = [[float(t) for t in line.split()] for line in r.stdout.splitlines()]
+    assert len(got) == len(want) == len(GOLDEN["box"]) + len(GOLDEN["simplex"])
+    for i, (g, w) in enumerate(zip(got, want)):
+        assert len(g) == len(w), i
+        assert all(_eq(a, b) for a, b in zip(g, w)), (i, g, w)
