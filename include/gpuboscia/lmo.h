@@ -154,6 +154,105 @@ struct BirkhoffLMO {
         return true;
     }
     gpuboscia::LMOSpec spec(int) const { return {GBX_LMO_BIRKHOFF, 1.0, {}, Order}; }
+
+    // Host oracles (the reference's *_cpu members): the minimum-cost
+    // permutation under the branch bounds (lb > 1/2 forces an edge, ub < 1/2
+    // forbids it) -- and, in face mode, the face of x (x_e >= 1 - 1e-9 forced,
+    // x_e <= 1e-9 forbidden) -- as the relaxation kernel computes it; all zeros
+    // when no permutation exists.
+    void compute_v_cpu(const std::vector<double>& grad, const std::vector<double>& lb,
+                       const std::vector<double>& ub, std::vector<double>& v) const {
+        v.resize(variable_count);
+        if (!assign(grad, lb, ub, v, nullptr)) std::fill(v.begin(), v.end(), 0.0);
+    }
+    void compute_inface_v_cpu(const std::vector<double>& direction, const std::vector<double>& x,
+                              const std::vector<double>& lb, const std::vector<double>& ub,
+                              std::vector<double>& v) const {
+        v.resize(variable_count);
+        if (!assign(direction, lb, ub, v, &x)) std::fill(v.begin(), v.end(), 0.0);
+    }
+    double dicg_maximum_step_cpu(const std::vector<double>& direction, const std::vector<double>& x,
+                                 const std::vector<double>& lb, const std::vector<double>& ub) const {
+        double gamma = 1.0;
+        for (int e = 0; e < variable_count; ++e) {
+            const double d = direction[e];
+            if (d > 0.0) gamma = std::min(gamma, (x[e] - lb[e]) / d);
+            else if (d < 0.0) gamma = std::min(gamma, (ub[e] - x[e]) / -d);
+        }
+        return std::max(0.0, gamma);
+    }
+
+private:
+    // Forced edges are placed first; the free rows and columns are then matched
+    // by the shortest-augmenting-path Hungarian with row / column potentials
+    // (one Dijkstra pass per free row). Reduced costs are (cost - u_row) - v_col;
+    // the next column is the unreached one of least slack, the lowest index on
+    // ties; columns no allowed edge reaches are never chosen.
+    static bool assign(const std::vector<double>& cost, const std::vector<double>& lb,
+                       const std::vector<double>& ub, std::vector<double>& out, const std::vector<double>* face) {
+        const size_t N = (size_t)variable_count;
+        if (cost.size() != N || lb.size() != N || ub.size() != N || (face && face->size() != N)) return false;
+        std::fill(out.begin(), out.end(), 0.0);
+        std::vector<int> row_of_col(Order, -1), col_of_row(Order, -1);
+        for (int r = 0; r < Order; ++r)
+            for (int c = 0; c < Order; ++c) {
+                const int e = r * Order + c;
+                if (lb[e] > ub[e] + 1e-9) return false;
+                if (lb[e] > 0.5 || (face && (*face)[e] >= 1.0 - 1e-9)) {
+                    if (ub[e] < 0.5 || col_of_row[r] >= 0 || row_of_col[c] >= 0) return false;
+                    col_of_row[r] = c;
+                    row_of_col[c] = r;
+                    out[e] = 1.0;
+                }
+            }
+        std::vector<int> R, C;
+        for (int i = 0; i < Order; ++i) {
+            if (col_of_row[i] < 0) R.push_back(i);
+            if (row_of_col[i] < 0) C.push_back(i);
+        }
+        if (R.size() != C.size()) return false;
+        const int k = (int)R.size();
+        const double none = 1e300;   // slack of a column no allowed edge has reached
+        // index 0 is the virtual column of the row being inserted
+        std::vector<double> pot_r(k + 1, 0.0), pot_c(k + 1, 0.0), slack(k + 1);
+        std::vector<int> match(k + 1, 0), prev(k + 1, 0);
+        std::vector<char> done(k + 1);
+        for (int row = 1; row <= k; ++row) {
+            match[0] = row;
+            std::fill(slack.begin(), slack.end(), none);
+            std::fill(done.begin(), done.end(), 0);
+            int col = 0;
+            while (true) {
+                done[col] = 1;
+                const int r = match[col];
+                for (int j = 1; j <= k; ++j) {
+                    if (done[j]) continue;
+                    const int e = R[r - 1] * Order + C[j - 1];
+                    if (!(ub[e] >= 0.5) || (face && !((*face)[e] > 1e-9))) continue;
+                    const double red = cost[e] - pot_r[r] - pot_c[j];
+                    if (red < slack[j]) { slack[j] = red; prev[j] = col; }
+                }
+                int next = -1;
+                for (int j = 1; j <= k; ++j)
+                    if (!done[j] && slack[j] < none && (next < 0 || slack[j] < slack[next])) next = j;
+                if (next < 0 || !std::isfinite(slack[next])) return false;
+                const double delta = slack[next];
+                for (int j = 0; j <= k; ++j) {
+                    if (done[j]) { pot_r[match[j]] += delta; pot_c[j] -= delta; }
+                    else slack[j] -= delta;
+                }
+                col = next;
+                if (match[col] == 0) break;
+            }
+            for (int j = col; j != 0;) {   // flip the augmenting path
+                const int pj = prev[j];
+                match[j] = match[pj];
+                j = pj;
+            }
+        }
+        for (int j = 1; j <= k; ++j) out[R[match[j] - 1] * Order + C[j - 1]] = 1.0;
+        return true;
+    }
 };
 
 // Cardinality-constrained simplex over x = (w, z), n = 2*Assets:

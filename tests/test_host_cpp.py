@@ -77,11 +77,12 @@ def _fmt(v):
 
 
 def test_host_lmo_oracles_match_the_reference_outputs(tmp_path):
-    """BoxLMO / UnitSimplexLMO / EqualitySimplexLMO compute_v_cpu,
+    """BoxLMO / UnitSimplexLMO / EqualitySimplexLMO / BirkhoffLMO compute_v_cpu,
     compute_inface_v_cpu and dicg_maximum_step_cpu (include/gpuboscia/lmo.h over
     lmo_dicg.h) reproduce, exactly, the reference's own CPU oracles on the
     golden cases (tests/golden/reference_cpu.json: forward vertex, in-face
-    vertex, and the maximum step along inface(g) - forward(-g))."""
+    vertex, and for box and simplex the maximum step along inface(g) -
+    forward(-g); Birkhoff orders 3-36 with forced, forbidden and face edges)."""
     exe = tmp_path / "lmo_cpu"
     subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
                     str(ROOT / "tests" / "cpp" / "lmo_cpu.cpp"), "-o", str(exe)], check=True)
@@ -95,9 +96,12 @@ def test_host_lmo_oracles_match_the_reference_outputs(tmp_path):
         lines.append(f"simplex {c['equality']} {c['rhs']!r} {n} {len(c['ints'])} {' '.join(map(str, c['ints']))} "
                      f"{_fmt(c['g'])} {_fmt(c['lb'])} {_fmt(c['ub'])} {_fmt(c['x'])}")
         want.append(c["forward"] + c["inface"] + [c["step"]])
+    for c in GOLDEN["birkhoff"]:
+        lines.append(f"birkhoff {c['order']} {_fmt(c['cost'])} {_fmt(c['lb'])} {_fmt(c['ub'])} {_fmt(c['x'])}")
+        want.append(c["forward"] + c["inface"])
     r = subprocess.run([str(exe)], input="\n".join(lines) + "\n", capture_output=True, text=True, check=True)
     got = [[float(t) for t in line.split()] for line in r.stdout.splitlines()]
-    assert len(got) == len(want) == len(GOLDEN["box"]) + len(GOLDEN["simplex"])
+    assert len(got) == len(want) == len(GOLDEN["box"]) + len(GOLDEN["simplex"]) + len(GOLDEN["birkhoff"])
     for i, (g, w) in enumerate(zip(got, want)):
         assert len(g) == len(w), i
         assert all(_eq(a, b) for a, b in zip(g, w)), (i, g, w)
