@@ -56,6 +56,18 @@
                                      std::to_string(__LINE__) + " - " + cudaGetErrorString(_e)); \
     } while (0)
 
+// Per-node status bytes of a relaxation (device_resident_solver.cuh:192-202):
+// the C ABI's GBX_NODE_* values under the reference's names.
+enum DRSNodeState : uint8_t {
+    DRSFractionalUnconverged = GBX_NODE_FRACTIONAL_UNCONVERGED,
+    DRSFractionalConverged = GBX_NODE_FRACTIONAL_CONVERGED,
+    DRSInfeasible = GBX_NODE_INFEASIBLE,
+    DRSIntegralUnconverged = GBX_NODE_INTEGRAL_UNCONVERGED,
+    DRSIntegralConverged = GBX_NODE_INTEGRAL_CONVERGED
+};
+// input flag: the node's x holds a start point (a warm start or a continuation)
+constexpr uint8_t DRSInitialPointSupplied = GBX_NODE_INITIAL_POINT_SUPPLIED;
+
 enum class FWExecutionMode { SingleBlock, MultiBlock };
 
 struct DeviceResidentConfig {

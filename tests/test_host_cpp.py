@@ -152,3 +152,19 @@ int main() {
                     "-I", "/usr/local/cuda/include", str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     assert out == ["1", "3", "2", "|", "3", "1", "|", "5", "0"]
+
+
+def test_node_state_names_have_the_reference_values(tmp_path):
+    """DRSNodeState / DRSInitialPointSupplied (device_resident_solver.cuh:192-202)
+    under the drop-in header: the reference's values, usable as status bytes."""
+    src = tmp_path / "ns.cpp"
+    src.write_text(r'''
+#include <gpuboscia/device_resident_solver.cuh>
+static_assert(DRSFractionalUnconverged == 0 && DRSFractionalConverged == 1 && DRSInfeasible == 2 &&
+              DRSIntegralUnconverged == 3 && DRSIntegralConverged == 4 && DRSInitialPointSupplied == 0x80, "");
+int main() { const uint8_t s = DRSIntegralUnconverged | DRSInitialPointSupplied; return s == 0x83 ? 0 : 1; }
+''')
+    exe = tmp_path / "ns"
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
+                    "-I", "/usr/local/cuda/include", str(src), "-o", str(exe)], check=True)
+    subprocess.run([str(exe)], check=True)
