@@ -658,6 +658,9 @@ private:
         nodes_done_.store(r.nodes_processed);
         reached_tolerance_ = r.reached_tolerance != 0;
         reached_time_limit_ = r.reached_time_limit != 0;
+        // the search ran on the device: one progress report, at its end
+        if (progress_cb_)
+            progress_cb_(r.nodes_processed, 0, r.dual_bound, incumbent_.get(), r.has_incumbent != 0);
         signal_done();
     }
 
