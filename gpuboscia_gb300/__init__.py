@@ -5,13 +5,15 @@ the C ABI of include/gpuboscia_gb300.h). This package builds it in-tree and
 mirrors the reference's public API in Python; C++ users include
 include/gpuboscia/gpuboscia.h instead.
 """
-from . import _abi, scorer
-from .api import (BirkhoffLMO, BoxLMO, CardinalityLMO, DenseQuadraticObjective, EqualitySimplexLMO, GraphMatchingObjective,
-                  ILSObjective, Problem, RelaxWorkspace, Result, Settings, UnitSimplexLMO, lmo_batch,
-                  node_feasible_batch, objective_gradient_batch, relax_batch, solve)
+from . import _abi, instances, scorer
+from .api import (BatchRelaxer, BirkhoffLMO, BoxLMO, CardinalityLMO, DenseQuadraticObjective, EqualitySimplexLMO,
+                  GraphMatchingObjective, ILSObjective, LinkedCardinalityLMO, Problem, RelaxWorkspace, Result,
+                  Settings, UnitSimplexLMO, lmo_batch, node_feasible_batch, objective_gradient_batch,
+                  objective_gradient_batch_f32, relax_batch, set_launch_shape, solve)
 
 __all__ = [
-    "BirkhoffLMO", "BoxLMO", "CardinalityLMO", "DenseQuadraticObjective", "EqualitySimplexLMO", "GraphMatchingObjective",
-    "ILSObjective", "Problem", "RelaxWorkspace", "Result", "Settings", "UnitSimplexLMO", "lmo_batch",
-    "node_feasible_batch", "objective_gradient_batch", "relax_batch", "solve", "scorer", "_abi",
+    "BatchRelaxer", "BirkhoffLMO", "BoxLMO", "CardinalityLMO", "DenseQuadraticObjective", "EqualitySimplexLMO",
+    "GraphMatchingObjective", "ILSObjective", "LinkedCardinalityLMO", "Problem", "RelaxWorkspace", "Result",
+    "Settings", "UnitSimplexLMO", "lmo_batch", "node_feasible_batch", "objective_gradient_batch",
+    "objective_gradient_batch_f32", "relax_batch", "set_launch_shape", "solve", "instances", "scorer", "_abi",
 ]
