@@ -31,11 +31,11 @@ WORKLOADS = {
     # name: instance family and size, nodes per batch, algorithm, line search, iterations per launch
     "birkhoff_gnp36": dict(kind="birkhoff", order=36, nodes=256, alg=1, ls=4, iters=100),
     "birkhoff_regular120": dict(kind="birkhoff", order=120, nodes=256, alg=1, ls=4, iters=20),
-    # config 5 shape (10-regular, B = P A P'); mixed precision keeps the oracle costs in the
+    # isomorphic 10-regular pair on 400 vertices (B = P A P'); mixed precision keeps the oracle costs in the
     # workspace and runs the FP32 gradient over the nonzero lists at this order
     "birkhoff_regular400": dict(kind="birkhoff", order=400, nodes=152, alg=1, ls=4, iters=5),
-    # config 1 (box BQP, n = 64, 1024-node batches) and config 3 (cardinality portfolio,
-    # 100 assets, 64 nodes per launch): Frank-Wolfe, FP64
+    # the 64-variable box BQP (1024-node batches) and the 100-asset cardinality portfolio
+    # (64 nodes per launch): Frank-Wolfe, FP64
     "box_qp64": dict(kind="box", n=64, nodes=1024, alg=0, ls=4, iters=200),
     "portfolio100": dict(kind="portfolio", n=200, nodes=64, alg=0, ls=4, iters=500),
 }

@@ -1,4 +1,4 @@
-"""Seeded synthetic instances of the five benchmark configurations.
+"""Seeded synthetic instances of the benchmark workloads and the reference's example models.
 
 Every draw comes from numpy's PCG64 generator (bit-stable across platforms);
 normals use an explicit Box-Muller transform so no library sampler decides
@@ -101,7 +101,7 @@ class Instance:
 
 
 def box_qp(n: int = 64, seed: int = SEEDS[1]) -> Instance:
-    """Config 1: f = x'Qx/2 + c'x, Q = M'M/64 + 0.1 I, x binary in [0,1]^n."""
+    """Box-constrained binary QP: f = x'Qx/2 + c'x, Q = M'M/64 + 0.1 I, x binary in [0,1]^n."""
     rng = _rng(seed)
     M = normal(rng, (n, n))
     Q = M.T @ M / 64.0 + 0.1 * np.eye(n)
@@ -113,7 +113,7 @@ def box_qp(n: int = 64, seed: int = SEEDS[1]) -> Instance:
 
 
 def portfolio(assets: int = 100, months: int = 600, cardinality: int = 10, seed: int = SEEDS[3]) -> Instance:
-    """Config 3: cardinality-constrained mean-variance portfolio.
+    """Cardinality-constrained mean-variance portfolio.
 
     Returns of a 3-factor model: factor returns N(0.5 %, 4 %) per month, betas
     N(1, 0.3), idiosyncratic volatility U[4 %, 10 %]. Sigma and mu are the sample
@@ -163,7 +163,7 @@ def graph_matching(order: int, A: np.ndarray, B: np.ndarray, name: str, known=No
 
 
 def birkhoff_gnp(order: int = 36, seed: int = SEEDS[2]) -> Instance:
-    """Config 2: A = G(order, 1/2), B = P A P', optimum 0 at X = P'."""
+    """Graph matching on a random graph: A = G(order, 1/2), B = P A P', optimum 0 at X = P'."""
     rng = _rng(seed)
     A = gnp_graph(rng, order, 0.5)
     p = permutation(rng, order)
@@ -175,7 +175,7 @@ def birkhoff_gnp(order: int = 36, seed: int = SEEDS[2]) -> Instance:
 
 def birkhoff_regular_perturbed(order: int = 120, degree: int = 8, swaps: int = 20,
                                seed: int = SEEDS[4]) -> Instance:
-    """Config 4: A d-regular, B = A after `swaps` double-edge swaps, then permuted (optimum > 0)."""
+    """Graph matching on d-regular graphs: A d-regular, B = A after `swaps` double-edge swaps, then permuted (optimum > 0)."""
     rng = _rng(seed)
     A = random_regular(rng, order, degree)
     B = permute(double_edge_swaps(rng, A, swaps), permutation(rng, order))
@@ -183,7 +183,7 @@ def birkhoff_regular_perturbed(order: int = 120, degree: int = 8, swaps: int = 2
 
 
 def birkhoff_regular_isomorphic(order: int = 400, degree: int = 10, seed: int = SEEDS[5]) -> Instance:
-    """Config 5: A d-regular, B = P A P' (optimum 0)."""
+    """Isomorphic d-regular pair: A d-regular, B = P A P' (optimum 0)."""
     rng = _rng(seed)
     A = random_regular(rng, order, degree)
     p = permutation(rng, order)

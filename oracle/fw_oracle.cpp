@@ -363,7 +363,7 @@ struct LMO {
         return true;
     }
 
-    // ---- cardinality-linked simplex (config 3; no reference counterpart):
+    // ---- cardinality-linked simplex (the portfolio set; no reference counterpart):
     // x = (w, z), sum w = 1, 0 <= w <= z, sum z <= K. Vertex = w on one asset a
     // plus z on the forced assets and on the most negative free z-costs while
     // slots remain; values summed in the kernel's order (base over forced

@@ -1,4 +1,4 @@
-"""Cardinality-linked simplex LMO (config 3) on the CPU: the oracle against
+"""Cardinality-linked simplex LMO (the portfolio set) on the CPU: the oracle against
 enumeration of every vertex, with forced and forbidden assets and ties. The
 set has no counterpart in the reference, so enumeration pins it."""
 import itertools

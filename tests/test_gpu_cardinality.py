@@ -1,4 +1,4 @@
-"""Config 3 (cardinality-constrained portfolio) on the GPU against the oracle:
+"""The cardinality-constrained portfolio on the GPU against the oracle:
 the cardinality LMO and the feasibility test bit for bit, Frank-Wolfe node
 relaxations bit for bit, and the whole branch and bound (one stream: the same
 tree as the oracle's)."""

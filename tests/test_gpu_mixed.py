@@ -172,7 +172,7 @@ def test_mixed_rejects_other_kinds(cuda_lib):
 
 @pytest.mark.parametrize("order,degree,N,iters", [(180, 8, 4, 10), (400, 10, 3, 4)])
 def test_mixed_large_order_costs_in_workspace(cuda_lib, order, degree, N, iters):
-    """Orders whose oracle costs exceed shared memory (config 5 shape at 400):
+    """Orders whose oracle costs exceed shared memory (the 10-regular pair at 400):
     costs and edge codes in the workspace, FP32 gradient over the nonzero
     lists, 16 columns per lane in the integer Hungarian above 256; the
     certificate is still the exact FP64 one at the returned iterate."""

@@ -257,7 +257,7 @@ def test_birkhoff_order64_workspace_path_bitwise(cuda_lib):
 
 
 def test_birkhoff_order400_nodes_bitwise(cuda_lib):
-    """Config-5 shape (10-regular graphs on 400 vertices): the FP64 path with the
+    """Isomorphic 10-regular graphs on 400 vertices: the FP64 path with the
     zero-skipping gradient and the four-warp Hungarian at 400 free columns."""
     inst = instances.birkhoff_regular_isomorphic(order=400)
     lb, ub = instances.birkhoff_node_batch(400, 2, seed=5)
