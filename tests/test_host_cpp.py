@@ -11,6 +11,14 @@ ROOT = pathlib.Path(__file__).resolve().parent.parent
 GOLDEN = json.loads((ROOT / "tests" / "golden" / "reference_cpu.json").read_text())
 
 
+def _cuda_include():
+    from gpuboscia_gb300 import build
+    return str(build._cuda_home() / "include")
+
+
+CUDA_INCLUDE = _cuda_include()
+
+
 @pytest.fixture(scope="module")
 def exe(tmp_path_factory):
     out = tmp_path_factory.mktemp("cpp") / "test_host"
@@ -123,7 +131,7 @@ def test_every_reference_header_name_compiles_alone(tmp_path, name):
     src = tmp_path / "one.cpp"
     src.write_text(f"#include <gpuboscia/{name}>\nint main() {{ return 0; }}\n")
     subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
-                    "-I", "/usr/local/cuda/include", str(src)], check=True)
+                    "-I", CUDA_INCLUDE, str(src)], check=True)
 
 
 def test_node_selection_policies(tmp_path):
@@ -149,7 +157,7 @@ int main() {
 ''')
     exe = tmp_path / "sel"
     subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
-                    "-I", "/usr/local/cuda/include", str(src), "-o", str(exe)], check=True)
+                    "-I", CUDA_INCLUDE, str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     assert out == ["1", "3", "2", "|", "3", "1", "|", "5", "0"]
 
@@ -166,5 +174,5 @@ int main() { const uint8_t s = DRSIntegralUnconverged | DRSInitialPointSupplied;
 ''')
     exe = tmp_path / "ns"
     subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
-                    "-I", "/usr/local/cuda/include", str(src), "-o", str(exe)], check=True)
+                    "-I", CUDA_INCLUDE, str(src), "-o", str(exe)], check=True)
     subprocess.run([str(exe)], check=True)
