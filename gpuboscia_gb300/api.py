@@ -264,10 +264,27 @@ def problem_to_c(p: Problem, keep: _Keep) -> A.Problem:
                      keep.ptr(iv, "host") if len(iv) else None, len(iv))
 
 
+def check_problem(problem: Problem, settings: Settings) -> None:
+    """The sizes the C ABI cannot see: gbx_solve reads n_vars doubles from lb,
+    ub and the root point, and indexes with the integer variables."""
+    n = problem.n_vars
+    if not isinstance(n, (int, np.integer)) or n <= 0:
+        raise ValueError(f"n_vars must be a positive integer, got {n!r}")
+    for name, arr in (("lb", problem.lb), ("ub", problem.ub)):
+        if np.asarray(arr).shape != (n,):
+            raise ValueError(f"problem.{name} must have shape ({n},), got {np.asarray(arr).shape}")
+    iv = np.asarray(list(problem.int_vars), dtype=np.int64)
+    if iv.size and (iv.min() < 0 or iv.max() >= n):
+        raise ValueError(f"integer variable index out of range [0, {n})")
+    if settings.root_initial_point is not None and np.asarray(settings.root_initial_point).shape != (n,):
+        raise ValueError(f"root_initial_point must have shape ({n},)")
+
+
 def solve(problem: Problem, objective, lmo, settings: Optional[Settings] = None) -> Result:
     """gpuboscia::solve on the GPU (gbx_solve)."""
-    lib = A.load()
     settings = settings or Settings()
+    check_problem(problem, settings)
+    lib = A.load()
     keep = _Keep()
     n = problem.n_vars
     o = objective.to_c("cuda", keep)

@@ -180,3 +180,23 @@ def test_device_frontier_rejects_bad_settings_without_launching(lib):
     blmo = A.LMO(A.LMO_BIRKHOFF, n, 1.0, None, 3)
     rc = lib.gbx_solve(C.byref(prob), C.byref(obj), C.byref(blmo), C.byref(s), C.byref(res))
     assert rc == A.ERR_INVALID
+
+
+def test_python_solve_checks_sizes_before_the_gpu():
+    """api.solve rejects arrays whose sizes disagree with n_vars (the C side
+    would read past them) before any device work: these raise on a CPU-only
+    machine as ValueError, not as a CUDA error."""
+    obj = api.DenseQuadraticObjective(np.eye(3))
+    good = api.Problem(3, np.zeros(3), np.ones(3), [0, 1, 2])
+    cases = [
+        (api.Problem(3, np.zeros(2), np.ones(3), [0]), api.Settings(), "lb"),
+        (api.Problem(3, np.zeros(3), np.ones(4), [0]), api.Settings(), "ub"),
+        (api.Problem(3, np.zeros(3), np.ones(3), [0, 3]), api.Settings(), "out of range"),
+        (api.Problem(3, np.zeros(3), np.ones(3), [-1]), api.Settings(), "out of range"),
+        (api.Problem(0, np.zeros(0), np.ones(0), []), api.Settings(), "n_vars"),
+        (good, api.Settings(root_initial_point=np.zeros(2)), "root_initial_point"),
+    ]
+    for prob, s, word in cases:
+        with pytest.raises(ValueError, match=word):
+            api.solve(prob, obj, api.BoxLMO(), s)
+    api.check_problem(good, api.Settings(root_initial_point=np.zeros(3)))
