@@ -322,6 +322,36 @@ def _stream_ptr(stream) -> int:
     return s.cuda_stream
 
 
+def check_node_tensors(x, lb, ub, eps, iterations, status, integer_flags=None) -> tuple:
+    """The node batch as gbx_relax_batch reads it (gbx_node_batch): x is
+    [N, n] float64 and lb / ub hold N*n float64, eps N float64, iterations N
+    int32, status N uint8, integer_flags n uint8 -- contiguous, on x's CUDA
+    device. A mismatch would make the kernel read or write outside a buffer,
+    so it is refused here. Returns (N, n)."""
+    import torch
+    if not isinstance(x, torch.Tensor) or x.dim() != 2:
+        raise ValueError("x must be a 2-D tensor [nodes, n_vars]")
+    N, n = x.shape
+    spec = [("x", x, torch.float64, N * n), ("lb", lb, torch.float64, N * n), ("ub", ub, torch.float64, N * n),
+            ("eps", eps, torch.float64, N), ("iterations", iterations, torch.int32, N),
+            ("status", status, torch.uint8, N)]
+    if integer_flags is not None:
+        spec.append(("integer_flags", integer_flags, torch.uint8, n))
+    for name, t, dtype, count in spec:
+        if not isinstance(t, torch.Tensor):
+            raise ValueError(f"{name} must be a torch tensor")
+        if t.dtype != dtype:
+            raise ValueError(f"{name} must be {dtype}, got {t.dtype}")
+        if t.numel() != count:
+            raise ValueError(f"{name} must hold {count} elements, got {t.numel()}")
+        if not t.is_contiguous():
+            raise ValueError(f"{name} must be contiguous")
+    for name, t, _, _ in spec:
+        if not t.is_cuda or t.device != x.device:
+            raise ValueError(f"{name} must be on x's CUDA device ({x.device}), got {t.device}")
+    return N, n
+
+
 def relax_batch(objective, lmo, algorithm: A.Algorithm, x, lb, ub, eps, iterations, status,
                 max_iters: int, integer_flags=None, candidate_tol: float = 1e-6,
                 workspace: Optional[RelaxWorkspace] = None, stream=None, keep: Optional[_Keep] = None,
@@ -332,9 +362,9 @@ def relax_batch(objective, lmo, algorithm: A.Algorithm, x, lb, ub, eps, iteratio
     Returns dict(gap, value, best_vertex, best_vertex_val) of new device tensors.
     """
     import torch
+    N, n = check_node_tensors(x, lb, ub, eps, iterations, status, integer_flags)
     lib = A.load()
     keep = keep or _Keep()
-    N, n = x.shape
     o = objective.to_c("cuda", keep)
     lm = lmo.to_c(n, "cuda", keep)
     dev = x.device
@@ -442,9 +472,9 @@ class BatchRelaxer:
     def __init__(self, objective, lmo, algorithm: A.Algorithm, x, lb, ub, eps, iterations, status,
                  max_iters: int, integer_flags=None, candidate_tol: float = 1e-6, stream=None):
         import torch
+        N, n = check_node_tensors(x, lb, ub, eps, iterations, status, integer_flags)
         self.lib = A.load()
         self.keep = _Keep()
-        N, n = x.shape
         self.obj = objective.to_c("cuda", self.keep)
         self.lmo = lmo.to_c(n, "cuda", self.keep)
         self.alg = algorithm

@@ -200,3 +200,46 @@ def test_python_solve_checks_sizes_before_the_gpu():
         with pytest.raises(ValueError, match=word):
             api.solve(prob, obj, api.BoxLMO(), s)
     api.check_problem(good, api.Settings(root_initial_point=np.zeros(3)))
+
+
+def test_node_batch_tensors_are_checked_before_the_gpu():
+    """relax_batch / BatchRelaxer refuse node tensors whose dtype, size,
+    layout or device differ from what gbx_node_batch describes (the kernel
+    would read or write outside a buffer): ValueError, before any device work."""
+    torch = pytest.importorskip("torch")
+    N, n = 3, 4
+    good = dict(x=torch.zeros(N, n, dtype=torch.float64), lb=torch.zeros(N, n, dtype=torch.float64),
+                ub=torch.ones(N, n, dtype=torch.float64), eps=torch.full((N,), 1e-6, dtype=torch.float64),
+                iterations=torch.zeros(N, dtype=torch.int32), status=torch.zeros(N, dtype=torch.uint8),
+                integer_flags=torch.ones(n, dtype=torch.uint8))
+    bad = [
+        ("x", torch.zeros(N * n, dtype=torch.float64), "2-D"),
+        ("lb", torch.zeros(N, n, dtype=torch.float32), "float64"),
+        ("ub", torch.ones(N, n - 1, dtype=torch.float64), "elements"),
+        ("eps", torch.full((N + 1,), 1e-6, dtype=torch.float64), "elements"),
+        ("iterations", torch.zeros(N, dtype=torch.int64), "int32"),
+        ("status", torch.zeros(N, dtype=torch.int32), "uint8"),
+        ("integer_flags", torch.ones(n + 1, dtype=torch.uint8), "elements"),
+        ("lb", torch.zeros(n, N, dtype=torch.float64).t(), "contiguous"),
+        ("eps", [1e-6] * N, "tensor"),
+    ]
+    obj = api.DenseQuadraticObjective(np.eye(n))
+    alg = A.Algorithm(A.ALG_FRANK_WOLFE, A.LS_OPEN_LOOP, 4, 1e-10, 1e-14, A.PRECISION_FP64)
+    for name, value, word in bad:
+        args = dict(good, **{name: value})
+        with pytest.raises(ValueError, match=word):
+            api.check_node_tensors(**args)
+        with pytest.raises(ValueError, match=word):
+            api.relax_batch(obj, api.BoxLMO(), alg, args["x"], args["lb"], args["ub"], args["eps"],
+                            args["iterations"], args["status"], 10, args["integer_flags"])
+    # a (1, n) batch may carry its bounds as flat n-vectors: same memory, accepted
+    one = dict(good, x=torch.zeros(1, n, dtype=torch.float64), lb=torch.zeros(n, dtype=torch.float64),
+               ub=torch.ones(n, dtype=torch.float64), eps=torch.full((1,), 1e-6, dtype=torch.float64),
+               iterations=torch.zeros(1, dtype=torch.int32), status=torch.zeros(1, dtype=torch.uint8))
+    # everything right but the device: host tensors are refused last
+    for args in (good, one):
+        with pytest.raises(ValueError, match="CUDA device"):
+            api.check_node_tensors(**args)
+        with pytest.raises(ValueError, match="CUDA device"):
+            api.BatchRelaxer(obj, api.BoxLMO(), alg, args["x"], args["lb"], args["ub"], args["eps"],
+                             args["iterations"], args["status"], 10, args["integer_flags"])
