@@ -322,16 +322,50 @@ def _stream_ptr(stream) -> int:
     return s.cuda_stream
 
 
-def check_node_tensors(x, lb, ub, eps, iterations, status, integer_flags=None) -> tuple:
+def _check_rows(lead, rows, dtype, extra=(), n_vars=None):
+    """lead: the [cases, n] tensor that sets the shape; rows: (name, tensor or
+    None) pairs that must hold cases*n elements of dtype; extra: (name,
+    tensor, dtype, count) checked as given; n_vars: the objective's variable
+    count, which n must equal (the kernels size vectors from the objective).
+    All contiguous on lead's CUDA device. Returns (cases, n)."""
+    import torch
+    name0, t0 = lead
+    if not isinstance(t0, torch.Tensor) or t0.dim() != 2:
+        raise ValueError(f"{name0} must be a 2-D tensor [cases, n]")
+    cases, n = t0.shape
+    if n_vars is not None and n_vars != n:
+        raise ValueError(f"the objective has {n_vars} variables, the rows of {name0} {n}")
+    spec = [(name0, t0, dtype, cases * n)]
+    spec += [(nm, t, dtype, cases * n) for nm, t in rows if t is not None]
+    spec += [e for e in extra if e[1] is not None]
+    for name, t, dt, count in spec:
+        if not isinstance(t, torch.Tensor):
+            raise ValueError(f"{name} must be a torch tensor")
+        if t.dtype != dt:
+            raise ValueError(f"{name} must be {dt}, got {t.dtype}")
+        if t.numel() != count:
+            raise ValueError(f"{name} must hold {count} elements, got {t.numel()}")
+        if not t.is_contiguous():
+            raise ValueError(f"{name} must be contiguous")
+    for name, t, _, _ in spec:
+        if not t.is_cuda or t.device != t0.device:
+            raise ValueError(f"{name} must be on {name0}'s CUDA device ({t0.device}), got {t.device}")
+    return cases, n
+
+
+def check_node_tensors(x, lb, ub, eps, iterations, status, integer_flags=None, n_vars=None) -> tuple:
     """The node batch as gbx_relax_batch reads it (gbx_node_batch): x is
     [N, n] float64 and lb / ub hold N*n float64, eps N float64, iterations N
     int32, status N uint8, integer_flags n uint8 -- contiguous, on x's CUDA
-    device. A mismatch would make the kernel read or write outside a buffer,
-    so it is refused here. Returns (N, n)."""
+    device, n equal to the objective's n_vars when given. A mismatch would
+    make the kernel read or write outside a buffer, so it is refused here.
+    Returns (N, n)."""
     import torch
     if not isinstance(x, torch.Tensor) or x.dim() != 2:
         raise ValueError("x must be a 2-D tensor [nodes, n_vars]")
     N, n = x.shape
+    if n_vars is not None and n_vars != n:
+        raise ValueError(f"the objective has {n_vars} variables, the node vectors {n}")
     spec = [("x", x, torch.float64, N * n), ("lb", lb, torch.float64, N * n), ("ub", ub, torch.float64, N * n),
             ("eps", eps, torch.float64, N), ("iterations", iterations, torch.int32, N),
             ("status", status, torch.uint8, N)]
@@ -362,7 +396,7 @@ def relax_batch(objective, lmo, algorithm: A.Algorithm, x, lb, ub, eps, iteratio
     Returns dict(gap, value, best_vertex, best_vertex_val) of new device tensors.
     """
     import torch
-    N, n = check_node_tensors(x, lb, ub, eps, iterations, status, integer_flags)
+    N, n = check_node_tensors(x, lb, ub, eps, iterations, status, integer_flags, getattr(objective, "n", None))
     lib = A.load()
     keep = keep or _Keep()
     o = objective.to_c("cuda", keep)
@@ -394,9 +428,11 @@ def relax_batch(objective, lmo, algorithm: A.Algorithm, x, lb, ub, eps, iteratio
 def lmo_batch(lmo, mode: int, direction, lb, ub, x=None, want_step: bool = False, stream=None):
     """Batched forward (mode 0) or in-face (mode 1) oracle over device tensors [cases, n]."""
     import torch
+    if mode == 1 and x is None:
+        raise ValueError("the in-face oracle (mode 1) needs x")
+    cases, n = _check_rows(("direction", direction), [("lb", lb), ("ub", ub), ("x", x)], torch.float64)
     lib = A.load()
     keep = _Keep()
-    cases, n = direction.shape
     lm = lmo.to_c(n, "cuda", keep)
     out = torch.zeros(cases, n, dtype=torch.float64, device=direction.device)
     step = torch.zeros(cases, dtype=torch.float64, device=direction.device) if want_step else None
@@ -424,9 +460,9 @@ def set_launch_shape(objective, lmo, algorithm: A.Algorithm, n: int, tensor_core
 def objective_gradient_batch(objective, x, precision: int = A.PRECISION_FP64, stream=None):
     """Gradients of the objective at the rows of the device tensor x [cases, n]."""
     import torch
+    cases, n = _check_rows(("x", x), [], torch.float64, n_vars=getattr(objective, "n", None))
     lib = A.load()
     keep = _Keep()
-    cases, n = x.shape
     o = objective.to_c("cuda", keep)
     g = torch.empty(cases, n, dtype=torch.float64, device=x.device)
     rc = lib.gbx_objective_gradient_batch(C.byref(o), precision, cases, x.data_ptr(), g.data_ptr(),
@@ -442,7 +478,7 @@ def objective_gradient_batch_f32(objective, x, stream=None):
     lib = A.load()
     keep = _Keep()
     X = x.to(dtype=torch.float32).contiguous()
-    cases, n = X.shape
+    cases, n = _check_rows(("x", X), [], torch.float32, n_vars=getattr(objective, "n", None))
     o = objective.to_c("cuda", keep)
     g = torch.empty(cases, n, dtype=torch.float32, device=X.device)
     rc = lib.gbx_objective_gradient_batch_f32(C.byref(o), cases, X.data_ptr(), g.data_ptr(), _stream_ptr(stream))
@@ -452,9 +488,10 @@ def objective_gradient_batch_f32(objective, x, stream=None):
 
 def node_feasible_batch(lmo, lb, ub, integer_flags=None, stream=None):
     import torch
+    cases, n = _check_rows(("lb", lb), [("ub", ub)], torch.float64,
+                           [("integer_flags", integer_flags, torch.uint8, lb.shape[1] if lb.dim() == 2 else -1)])
     lib = A.load()
     keep = _Keep()
-    cases, n = lb.shape
     lm = lmo.to_c(n, "cuda", keep)
     out = torch.zeros(cases, dtype=torch.uint8, device=lb.device)
     rc = lib.gbx_node_feasible_batch(C.byref(lm), cases, lb.data_ptr(), ub.data_ptr(),
@@ -472,7 +509,8 @@ class BatchRelaxer:
     def __init__(self, objective, lmo, algorithm: A.Algorithm, x, lb, ub, eps, iterations, status,
                  max_iters: int, integer_flags=None, candidate_tol: float = 1e-6, stream=None):
         import torch
-        N, n = check_node_tensors(x, lb, ub, eps, iterations, status, integer_flags)
+        N, n = check_node_tensors(x, lb, ub, eps, iterations, status, integer_flags,
+                                  getattr(objective, "n", None))
         self.lib = A.load()
         self.keep = _Keep()
         self.obj = objective.to_c("cuda", self.keep)

@@ -243,3 +243,44 @@ def test_node_batch_tensors_are_checked_before_the_gpu():
         with pytest.raises(ValueError, match="CUDA device"):
             api.BatchRelaxer(obj, api.BoxLMO(), alg, args["x"], args["lb"], args["ub"], args["eps"],
                              args["iterations"], args["status"], 10, args["integer_flags"])
+
+
+def test_lmo_feasibility_gradient_tensors_are_checked():
+    """lmo_batch, node_feasible_batch and the gradient entry points refuse
+    tensors that disagree with each other or with the objective's variable
+    count (the C side sizes its reads from them): ValueError before any
+    device work, the device checked last."""
+    torch = pytest.importorskip("torch")
+    c, n = 4, 9
+    f64 = lambda *s: torch.zeros(*s, dtype=torch.float64)
+    lmo = api.BirkhoffLMO(3)
+    with pytest.raises(ValueError, match="elements"):
+        api.lmo_batch(lmo, 0, f64(c, n), f64(c, n - 1), f64(c, n))
+    with pytest.raises(ValueError, match="float64"):
+        api.lmo_batch(lmo, 1, f64(c, n), f64(c, n), f64(c, n), x=torch.zeros(c, n, dtype=torch.float32))
+    with pytest.raises(ValueError, match="needs x"):
+        api.lmo_batch(lmo, 1, f64(c, n), f64(c, n), f64(c, n))
+    with pytest.raises(ValueError, match="CUDA device"):
+        api.lmo_batch(lmo, 0, f64(c, n), f64(c, n), f64(c, n))
+    with pytest.raises(ValueError, match="integer_flags"):
+        api.node_feasible_batch(lmo, f64(c, n), f64(c, n), torch.ones(n - 1, dtype=torch.uint8))
+    with pytest.raises(ValueError, match="2-D"):
+        api.node_feasible_batch(lmo, f64(c * n), f64(c * n))
+    with pytest.raises(ValueError, match="CUDA device"):
+        api.node_feasible_batch(lmo, f64(c, n), f64(c, n), torch.ones(n, dtype=torch.uint8))
+    gm = api.GraphMatchingObjective(np.eye(3), np.eye(3))
+    with pytest.raises(ValueError, match="CUDA device"):
+        api.objective_gradient_batch(gm, f64(c, n))
+    with pytest.raises(ValueError, match="variables"):
+        api.objective_gradient_batch(gm, f64(c, 16))
+    with pytest.raises(ValueError, match="float64"):
+        api.objective_gradient_batch(gm, torch.zeros(c, n, dtype=torch.float32))
+    with pytest.raises(ValueError, match="variables"):
+        api.objective_gradient_batch_f32(gm, torch.zeros(c, 16))
+    # relax_batch: node vectors must match the objective's size
+    N = 2
+    with pytest.raises(ValueError, match="variables"):
+        api.relax_batch(api.DenseQuadraticObjective(np.eye(5)), api.BoxLMO(),
+                        A.Algorithm(A.ALG_FRANK_WOLFE, A.LS_OPEN_LOOP, 4, 1e-10, 1e-14, A.PRECISION_FP64),
+                        f64(N, 4), f64(N, 4), f64(N, 4), f64(N), torch.zeros(N, dtype=torch.int32),
+                        torch.zeros(N, dtype=torch.uint8), 10)
