@@ -71,6 +71,7 @@ class Scorer:
     def forward(self, features, bf16: bool = False, stream=None):
         """Scores of device (or numpy) features [rows, F]; returns a device tensor."""
         import torch
+        _check_features(features)
         X = _dev_f32(features)
         out = torch.empty(X.shape[0], dtype=torch.float32, device="cuda")
         sc = self.to_c()
@@ -82,10 +83,15 @@ class Scorer:
     def gradient(self, features, group_ptr, target, stream=None):
         """(dL/dparams, L) of the listwise loss; device tensors."""
         import torch
-        X = _dev_f32(features)
-        gp = torch.as_tensor(np.asarray(group_ptr, np.int32)).cuda() if not isinstance(group_ptr, torch.Tensor) \
-            else group_ptr
-        t = _dev_f32(target)
+        gpn = _check_groups(features, group_ptr, target)
+        gp = torch.as_tensor(gpn.astype(np.int32)).cuda() if not isinstance(group_ptr, torch.Tensor) \
+            else group_ptr.to(device="cuda", dtype=torch.int32).contiguous()
+        return self._gradient(_dev_f32(features), gp, _dev_f32(target), stream)
+
+    def _gradient(self, X, gp, t, stream=None):
+        """gradient() on checked device tensors: X [rows, F] float32, gp the
+        int32 group offsets from 0 to rows, t [rows] float32."""
+        import torch
         rows, groups = X.shape[0], gp.numel() - 1
         sc = self.to_c()
         lib = A.load()
@@ -108,15 +114,39 @@ class Scorer:
     def train(self, data: "Dataset", epochs: int = 200, lr: float = 3e-3) -> List[float]:
         """Full-batch Adam on the dataset; returns the loss per epoch."""
         import torch
+        _check_groups(data.features, data.group_ptr, data.target)
         X = _dev_f32(data.features)
         gp = torch.as_tensor(data.group_ptr.astype(np.int32)).cuda()
         t = _dev_f32(data.target)
         losses = []
         for _ in range(epochs):
-            g, l = self.gradient(X, gp, t)
+            g, l = self._gradient(X, gp, t)
             self.adam(g, lr)
             losses.append(float(l.item()) / max(1, data.groups))
         return losses
+
+
+def _check_features(features) -> int:
+    """Feature rows as the scorer kernels read them: [rows, F]. Returns rows."""
+    shape = tuple(features.shape) if hasattr(features, "shape") else np.shape(features)
+    if len(shape) != 2 or shape[1] != F:
+        raise ValueError(f"features must be [rows, {F}], got {shape}")
+    return int(shape[0])
+
+
+def _check_groups(features, group_ptr, target) -> np.ndarray:
+    """Listwise batch as the gradient kernel reads it: features [rows, F],
+    group offsets rising from 0 to rows, one target per row. Returns the
+    offsets on the host."""
+    rows = _check_features(features)
+    if hasattr(group_ptr, "detach"):
+        group_ptr = group_ptr.detach().cpu().numpy()
+    gpn = np.asarray(group_ptr).astype(np.int64).ravel()
+    if gpn.size < 1 or gpn[0] != 0 or gpn[-1] != rows or np.any(np.diff(gpn) < 0):
+        raise ValueError(f"group_ptr must rise from 0 to the row count {rows}")
+    if int(np.prod(np.shape(target))) != rows:
+        raise ValueError(f"target must hold one value per row ({rows})")
+    return gpn
 
 
 def _dev_f32(a):
@@ -129,8 +159,12 @@ def _dev_f32(a):
 def features(x, lb, ub, order: int, depth: int, gap: float, value: float, vars_) -> np.ndarray:
     """Host features of candidates vars_ of one node (gbx_branch_features)."""
     lib = A.load()
-    x, lb, ub = (np.ascontiguousarray(v, np.float64) for v in (x, lb, ub))
-    vs = np.ascontiguousarray(vars_, np.int32)
+    x, lb, ub = (np.ascontiguousarray(v, np.float64).ravel() for v in (x, lb, ub))
+    vs = np.ascontiguousarray(vars_, np.int32).ravel()
+    if lb.size != x.size or ub.size != x.size:
+        raise ValueError("x, lb and ub must have the same length")
+    if vs.size and (vs.min() < 0 or vs.max() >= x.size):
+        raise ValueError(f"candidate variable index out of range [0, {x.size})")
     out = np.zeros((len(vs), F), np.float32)
     lib.gbx_branch_features(len(x), x.ctypes.data, lb.ctypes.data, ub.ctypes.data, order, depth, gap, value,
                             len(vs), vs.ctypes.data, out.ctypes.data)

@@ -50,3 +50,32 @@ def test_branch_features_known_answer():
     np.testing.assert_allclose(f[0, 6:15], [2 / 3, 2 / 3, .5, .5, 1, 1, 1, 1, 2 / 3], rtol=1e-6)
     # x[1][1] = .25: row 1 all three fractional, column 1 three fractional, maxima .5 and .5
     np.testing.assert_allclose(f[1, [0, 6, 7, 8, 9, 10, 11, 12, 13]], [.25, 1, 1, .5, .5, 0, 0, .5, .5], rtol=1e-6)
+
+
+def test_scorer_entry_points_check_their_inputs():
+    """features(), Scorer.forward and Scorer.gradient refuse inputs the
+    library would read past (short bounds, candidate indices out of range,
+    rows without F features, group offsets that do not span the rows) before
+    any device work."""
+    import pytest
+    from gpuboscia_gb300 import scorer
+    x, lb, ub = np.full(6, 0.5), np.zeros(6), np.ones(6)
+    with pytest.raises(ValueError, match="same length"):
+        scorer.features(x, lb[:5], ub, 0, 1, 0.1, 1.0, [0])
+    with pytest.raises(ValueError, match="out of range"):
+        scorer.features(x, lb, ub, 0, 1, 0.1, 1.0, [6])
+    with pytest.raises(ValueError, match="out of range"):
+        scorer.features(x, lb, ub, 0, 1, 0.1, 1.0, [-1])
+    F = scorer.F
+    sc = scorer.Scorer.__new__(scorer.Scorer)   # the checks run before the parameters are needed
+    with pytest.raises(ValueError, match="features must be"):
+        sc.forward(np.zeros((4, F - 1), np.float32))
+    rows = 5
+    X, t = np.zeros((rows, F), np.float32), np.full(rows, 0.2, np.float32)
+    for gp in ([0, 2, 4], [1, 2, 5], [0, 3, 2, 5], []):
+        with pytest.raises(ValueError, match="group_ptr"):
+            sc.gradient(X, np.asarray(gp, np.int32), t)
+    with pytest.raises(ValueError, match="target"):
+        sc.gradient(X, np.asarray([0, 2, 5], np.int32), t[:4])
+    # a well-formed batch passes the host checks
+    assert scorer._check_groups(X, np.asarray([0, 2, 2, 5], np.int32), t).tolist() == [0, 2, 2, 5]
