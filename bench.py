@@ -1,13 +1,24 @@
 #!/usr/bin/env python
-"""Benchmark of the node-relaxation hot path on GB300.
+"""Benchmark of the node-relaxation hot path on GB300, on the metric's own
+configuration.
 
-A step is one batched relaxation launch: every open B&B node of a synthetic
-batch (uneven fixings, depth-dependent FW tolerances) is relaxed by FW/DICG
-for up to --iters iterations. value = node relaxations per second with the
-batch resident in HBM; e2e = the same through the C ABI with the node data
-in pinned host memory (H2D and D2H inside the timed region).
+Default workload: Birkhoff graph matching on an isomorphic pair of 10-regular
+graphs on 400 vertices (160,000 binary variables, B = P A P'), branch and bound
+with 1024-node batches, mixed precision, the learned branching scorer, the
+device frontier and the incumbent cutoff. A step is one round of that search
+(pop a batch, relax it, branch and merge the batch of the round before), timed
+on the device by CUDA events on the search's stream; the first rounds grow the
+frontier to full batches and are the warm-up, the last --steps rounds are timed.
+value = B&B nodes per second over the timed rounds (whole batches resident in
+HBM); e2e = nodes per second of the whole gbx_solve call through the Python API
+(instance uploaded from host arrays, incumbent read back).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload NAME]
+
+Other workloads (`--workload`): birkhoff_regular120 (the same search on the
+order-120 pair, 256-node batches) and, one relaxation launch per step,
+birkhoff_gnp36, box_qp64 and portfolio100.
 """
 from __future__ import annotations
 
@@ -28,24 +39,17 @@ sys.path.insert(0, ROOT)
 METRIC = "time to certified 1e-6 gap & B&B nodes/s: batched+learned vs plain, 1 GB300"
 
 WORKLOADS = {
-    # name: instance family and size, nodes per batch, algorithm, line search, iterations per launch
-    "birkhoff_gnp36": dict(kind="birkhoff", order=36, nodes=256, alg=1, ls=4, iters=100),
-    "birkhoff_regular120": dict(kind="birkhoff", order=120, nodes=256, alg=1, ls=4, iters=20),
-    # isomorphic 10-regular pair on 400 vertices (B = P A P'); mixed precision keeps the oracle costs in the
-    # workspace and runs the FP32 gradient over the nonzero lists at this order
-    "birkhoff_regular400": dict(kind="birkhoff", order=400, nodes=152, alg=1, ls=4, iters=5),
-    # the 64-variable box BQP (1024-node batches) and the 100-asset cardinality portfolio
-    # (64 nodes per launch): Frank-Wolfe, FP64
-    "box_qp64": dict(kind="box", n=64, nodes=1024, alg=0, ls=4, iters=200),
-    "portfolio100": dict(kind="portfolio", n=200, nodes=64, alg=0, ls=4, iters=500),
+    # name: instance family and size, nodes per batch, algorithm (0 FW, 1 DICG), line search (4 quadratic
+    # exact), FW iterations per dispatch, and the measurement: "bnb" times rounds of a gbx_solve search,
+    # "relax" times one gbx_relax_batch launch over a synthetic batch of open nodes
+    "birkhoff_regular400": dict(kind="birkhoff", order=400, nodes=1024, alg=1, ls=4, iters=20, mode="bnb"),
+    "birkhoff_regular120": dict(kind="birkhoff", order=120, nodes=256, alg=1, ls=4, iters=100, mode="bnb"),
+    "birkhoff_gnp36": dict(kind="birkhoff", order=36, nodes=256, alg=1, ls=4, iters=100, mode="relax"),
+    "box_qp64": dict(kind="box", n=64, nodes=1024, alg=0, ls=4, iters=200, mode="relax"),
+    "portfolio100": dict(kind="portfolio", n=200, nodes=64, alg=0, ls=4, iters=500, mode="relax"),
 }
-
-
-# dram__bytes_read.sum + dram__bytes_write.sum of the relaxation kernel per node,
-# from the committed ncu captures (profiles/: 256 nodes at order 36, 152 nodes at
-# order 120); independent of the iteration count, scaled by the nodes of a launch
-TRAFFIC_PER_NODE = {("birkhoff_gnp36", "mixed"): 8247552 / 256,
-                    ("birkhoff_regular120", "mixed"): (139682816 + 191056640) / 152}
+DEFAULT_WORKLOAD = "birkhoff_regular400"
+BRANCH_K = 3   # branch_pow2's default: 8 children per branched node
 
 
 def load_peaks():
@@ -65,24 +69,32 @@ def workload_flags(name, n):
     return flags
 
 
-def make_workload(name, nodes, rank):
+def make_instance(name):
     from gpuboscia_gb300 import instances
     w = WORKLOADS[name]
     if w["kind"] == "box":
-        inst = instances.box_qp(n=w["n"])
+        return instances.box_qp(n=w["n"])
+    if w["kind"] == "portfolio":
+        return instances.portfolio(assets=w["n"] // 2)
+    if name.startswith("birkhoff_gnp"):
+        return instances.birkhoff_gnp(order=w["order"])
+    if w["order"] == 400:
+        return instances.birkhoff_regular_isomorphic(order=w["order"])
+    return instances.birkhoff_regular_perturbed(order=w["order"])
+
+
+def make_workload(name, nodes, rank):
+    """The instance and a batch of open nodes with uneven fixings and
+    depth-dependent tolerances (lb, ub, eps)."""
+    from gpuboscia_gb300 import instances
+    w = WORKLOADS[name]
+    inst = make_instance(name)
+    if w["kind"] == "box":
         lb, ub = instances.box_node_batch(w["n"], nodes, seed=4242 + rank)
     elif w["kind"] == "portfolio":
-        inst = instances.portfolio(assets=w["n"] // 2)
         lb, ub = instances.portfolio_node_batch(w["n"] // 2, 10, nodes, seed=4242 + rank)
     else:
-        order = w["order"]
-        if name.startswith("birkhoff_gnp"):
-            inst = instances.birkhoff_gnp(order=order)
-        elif order == 400:
-            inst = instances.birkhoff_regular_isomorphic(order=order)
-        else:
-            inst = instances.birkhoff_regular_perturbed(order=order)
-        lb, ub = instances.birkhoff_node_batch(order, nodes, seed=4242 + rank)
+        lb, ub = instances.birkhoff_node_batch(w["order"], nodes, seed=4242 + rank)
     rng = np.random.Generator(np.random.PCG64(77 + rank))
     depth = rng.integers(0, 13, nodes)
     eps = np.maximum(1e-6, 1e-3 * 0.8 ** depth)
@@ -95,8 +107,9 @@ class ClockSampler:
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device_index):
+    def __init__(self, device_index, period_ms=50):
         self.dev = device_index
+        self.period = period_ms
         self.proc = None
 
     def __enter__(self):
@@ -104,7 +117,7 @@ class ClockSampler:
         self.first = ""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.period)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             # the timed region starts once sampling runs (the first sample is the state entering it)
             if select.select([self.proc.stdout], [], [], 5.0)[0]:
@@ -167,16 +180,24 @@ def cpu_sample(inst, lb, ub, eps, alg_kind, ls, iters, budget_s=12.0, flags=None
     return done / dt, threads, done, dt
 
 
+def ref_sample_nodes(args):
+    """Nodes of the CPU samples: one batch's worth, at most 32 at order 400."""
+    w = WORKLOADS[args.workload]
+    return min(args.nodes, 32) if w.get("order", 0) >= 400 else args.nodes
+
+
 def run_reference(args, rank, world):
-    """--impl reference: the oracle port of the reference's relaxation on the host cores."""
+    """--impl reference: the oracle port of the reference's relaxation on the
+    host cores (a B&B node is one relaxation; the host bookkeeping around it is
+    negligible at these sizes)."""
     if rank != 0:
         return
-    inst, lb, ub, eps = make_workload(args.workload, args.nodes, 0)
+    inst, lb, ub, eps = make_workload(args.workload, ref_sample_nodes(args), 0)
     w = WORKLOADS[args.workload]
     for _ in range(args.warmup):
         cpu_sample(inst, lb, ub, eps, w["alg"], w["ls"], args.iters, budget_s=0.0,
                    flags=workload_flags(args.workload, lb.shape[1]))
-    vals, times = [], []
+    vals, times, done = [], [], 0
     for _ in range(args.steps):
         v, threads, done, dt = cpu_sample(inst, lb, ub, eps, w["alg"], w["ls"], args.iters, budget_s=args.ref_budget,
                                           flags=workload_flags(args.workload, lb.shape[1]))
@@ -188,7 +209,8 @@ def run_reference(args, rank, world):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": dict(config_dict(args), precision="fp64 (CPU oracle)"),
             "cpu_baseline": {"value": value, "unit": "nodes/s", "cores": threads, "kind": "port",
-                             "sample": f"{done} of {args.nodes} nodes per step, {args.iters} iterations max"},
+                             "sample": f"{done} open nodes of the workload per step (uneven fixings), "
+                                       f"relaxed with {args.iters} iterations max each"},
             "e2e": {"value": value, "unit": "nodes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -202,7 +224,13 @@ def config_dict(args):
         d.update(variables=w["n"])
     d.update({"nodes_per_batch": args.nodes, "max_iters_per_dispatch": args.iters,
               "algorithm": "DICG" if w["alg"] == 1 else "Frank-Wolfe", "line_search": "quadratic_exact",
-              "precision": args.precision, "l2": "flushed between timed steps (256 MiB write)"})
+              "precision": args.precision})
+    if w["mode"] == "bnb":
+        d.update({"step": "one round of the branch-and-bound search (a batch popped, relaxed, branched, merged)",
+                  "search": "device frontier, learned branching scorer (branch_pow2, k=3), incumbent cutoff",
+                  "l2": "inputs larger than L2 (each round streams its batch's node vectors)"})
+    else:
+        d["l2"] = "flushed between timed steps (256 MiB write)"
     if getattr(args, "launch_shape", "auto") != "auto":
         d["launch_shape"] = args.launch_shape
         if getattr(args, "tuned_shape", None):
@@ -210,6 +238,319 @@ def config_dict(args):
     return d
 
 
+# ---------------------------------------------------------------- learned scorer and graph pairs
+def _pair(seed, order=9):
+    from gpuboscia_gb300 import instances
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return instances.graph_matching(order, instances.gnp_graph(rng, order, 0.5),
+                                    instances.gnp_graph(rng, order, 0.5), f"pair{order}_{seed}")
+
+
+def _trained_scorer():
+    """The learned scorer: strong-branching labels of four G(9, 1/2) pairs (seeds
+    100-103, disjoint from the held-out pairs 200-203), 400 Adam epochs. Its 16
+    features do not depend on the order, so the same network ranks candidates
+    at every order."""
+    from gpuboscia_gb300 import scorer
+    data = scorer.Dataset.concat([scorer.collect_strong_branching(_pair(100 + k), max_nodes=30, max_candidates=64)
+                                  for k in range(4)])
+    sc = scorer.Scorer(32, seed=0)
+    sc.train(data, epochs=400, lr=3e-3)
+    return sc
+
+
+def _solve_timed(inst, prec, scorer_obj, batch, streams, limit, device_frontier=0, cutoff=0, iters=500,
+                 node_limit=0, trace=0, capacity=0, autotune=1):
+    from gpuboscia_gb300 import _abi as A
+    from gpuboscia_gb300 import api
+    s = inst.settings
+    s.gpu_batch_size = batch
+    s.num_streams = streams
+    s.gpu_max_iters = iters
+    s.line_search = A.LS_QUADRATIC_EXACT
+    s.abs_gap_tol = 1e-6
+    s.rel_gap_tol = 1e-6
+    s.time_limit_seconds = limit
+    s.precision = prec
+    s.scorer = scorer_obj
+    s.device_frontier = device_frontier
+    s.incumbent_cutoff = cutoff
+    s.node_limit = node_limit
+    s.round_trace = trace
+    s.frontier_capacity = capacity
+    s.autotune = autotune
+    t0 = time.perf_counter()
+    r = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    wall = time.perf_counter() - t0
+    gap = abs(r.objective - r.dual_bound) if math.isfinite(r.objective) else math.inf
+    certified = bool(not r.reached_time_limit and not r.reached_node_limit
+                     and (gap <= 1e-6 or gap <= 1e-6 * abs(r.objective)))
+    return wall, r, certified
+
+
+def _solve_summary(wall, r, cert):
+    return {"seconds": wall, "nodes": r.nodes_processed, "nodes_per_s": r.nodes_processed / wall,
+            "batches": r.batches, "objective": r.objective, "dual_bound": r.dual_bound, "certified": cert,
+            "time_limit": bool(r.reached_time_limit), "node_limit": bool(r.reached_node_limit)}
+
+
+# time-to-gap configurations over the held-out pairs:
+# precision, learned scorer, batch, streams, device frontier, incumbent cutoff
+PAIR_CONFIGS = {
+    "plain_fp64": (0, False, 64, 1, 0, 0),
+    "mixed": (1, False, 64, 1, 0, 0),
+    "mixed_learned": (1, True, 64, 1, 0, 0),
+    "mixed_learned_256x4": (1, True, 256, 4, 0, 0),
+    "device_frontier_mixed_1024": (1, False, 1024, 1, 1, 0),
+    "device_frontier_mixed_learned_1024": (1, True, 1024, 1, 1, 0),
+    "full_stack": (1, True, 1024, 1, 1, 1),
+}
+
+
+def _solve_pairs(name, sc, limit):
+    prec, use, batch, streams, dev, cut = PAIR_CONFIGS[name]
+    tot_s, tot_n, cert = 0.0, 0, True
+    for k in range(4):
+        wall, r, c = _solve_timed(_pair(200 + k), prec, sc if use else None, batch, streams, limit, dev, cut)
+        tot_s += wall
+        tot_n += r.nodes_processed
+        cert = cert and c
+    return {"seconds": tot_s, "nodes": tot_n, "certified": cert}
+
+
+def certified_cases(sc, limit):
+    """Instances whose 1e-6 gap closes within a bench run, plain against the
+    full stack: the order-36 G(36, 1/2) pair (the root's LMO vertex is the
+    isomorphism) and four held-out G(9, 1/2) pairs (non-isomorphic: the tree
+    branches, ~3-4k nodes each)."""
+    from gpuboscia_gb300 import _abi as A
+    from gpuboscia_gb300 import instances
+    out = {}
+    gnp = instances.birkhoff_gnp(order=36)
+    for name, prec in (("plain_fp64", A.PRECISION_FP64), ("mixed", A.PRECISION_MIXED)):
+        wall, r, cert = _solve_timed(gnp, prec, None, 256, 2, limit)
+        out.setdefault("gnp36", {})[name] = _solve_summary(wall, r, cert)
+    pairs = {"instances": "4 held-out G(9,1/2) pairs; batch 64 x 1 stream, host frontier, unless named; "
+                          "full_stack = mixed + learned + device frontier (1024-node rounds) + incumbent cutoff"}
+    for name in PAIR_CONFIGS:
+        pairs[name] = _solve_pairs(name, sc, limit)
+    pairs["full_vs_plain"] = pairs["plain_fp64"]["seconds"] / max(pairs["full_stack"]["seconds"], 1e-9)
+    out["graph_pairs"] = pairs
+    return out
+
+
+# ---------------------------------------------------------------- relaxation arms on one batch
+def relax_arms(inst, lb, ub, eps, w, iters, check_nodes=4):
+    """The same open nodes relaxed by the plain FP64 method and by mixed
+    precision at the same iteration budget (one gbx_relax_batch launch each,
+    CUDA events on the launching stream): nodes/s, mean certified bound
+    f(x) - gap, converged fraction. The mixed certificate of a sample of nodes
+    is re-evaluated by the oracle at the returned iterate (an FP64 certificate:
+    the error is that of the GPU's FP64 arithmetic against the oracle's)."""
+    import torch
+    from gpuboscia_gb300 import _abi as A
+    from gpuboscia_gb300 import api
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    dev = torch.device("cuda")
+    N, n = lb.shape
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_lb, d_ub, d_eps = T(lb), T(ub), T(eps)
+    d_flags = T(np.ones(n, np.uint8))
+    stream = torch.cuda.current_stream()
+    out = {}
+    for name, prec in (("plain_fp64", A.PRECISION_FP64), ("mixed", A.PRECISION_MIXED)):
+        alg = A.Algorithm(w["alg"], w["ls"], 4, 1e-10, 1e-14, prec)
+        x = d_lb.clone()
+        it = torch.zeros(N, dtype=torch.int32, device=dev)
+        st = torch.zeros(N, dtype=torch.uint8, device=dev)
+        rl = api.BatchRelaxer(inst.objective, inst.lmo, alg, x, d_lb, d_ub, d_eps, it, st, iters, d_flags, 1e-6,
+                              stream)
+        rl.launch()   # warm-up (module load, launch attributes)
+        x.copy_(d_lb)
+        it.zero_()
+        st.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        rl.launch()
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        val, gap, stat = rl.value.cpu().numpy(), rl.gap.cpu().numpy(), st.cpu().numpy()
+        ok = np.isfinite(gap) & (stat != 2)
+        out[name] = {"nodes": N, "ms": ms, "nodes_per_s": N / (ms / 1000.0),
+                     "node_iterations": int(it.sum().item()),
+                     "mean_certified_bound": float(np.mean((val - gap)[ok])) if ok.any() else None,
+                     "converged_fraction": float(np.isin(stat, (1, 4)).mean())}
+        if name == "mixed" and check_nodes > 0:
+            import _oracle as O
+            k = min(check_nodes, N)
+            oalg = O.algorithm(w["alg"], w["ls"])
+            xs = x.cpu().numpy()[:k]
+            ref = O.relax(inst.objective, inst.lmo, oalg, xs, lb[:k], ub[:k], eps[:k],
+                          iterations=it.cpu().numpy()[:k], status=np.full(k, 0x80, np.uint8), max_iters=0,
+                          threads=os.cpu_count() or 1)
+            out[name]["certificate_check"] = {
+                "nodes": k, "max_abs_gap_error": float(np.max(np.abs(ref["gap"] - gap[:k]))),
+                "max_abs_value_error": float(np.max(np.abs(ref["value"] - val[:k])))}
+    return out
+
+
+# ---------------------------------------------------------------- the search (bnb mode)
+def _host_available_bytes():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def run_bnb(args, rank, world):
+    """Rounds of the full-stack search on the workload's instance (see the
+    module docstring), plus the plain method, the relaxation arms, the other
+    large configuration and the certified cases on the same GPU."""
+    import torch
+    from gpuboscia_gb300 import _abi as A
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    w = WORKLOADS[args.workload]
+    order, B, I = w["order"], args.nodes, args.iters
+    n = order * order
+    inst = make_instance(args.workload)
+    t0 = time.perf_counter()
+    sc = _trained_scorer()
+    train_s = time.perf_counter() - t0
+
+    # ramp: the search grows 1, 8, 64, ... nodes per round until batches are full
+    ramp, g = 0, 1
+    while g < B:
+        ramp += g
+        g <<= BRANCH_K
+    warm_rounds = max(args.warmup, 3)
+    limit = ramp + (warm_rounds + args.steps + 1) * B
+    # open nodes the pool must hold: each processed node opens 2^k children
+    capacity = limit * (1 << BRANCH_K) + 2 * B + 1
+
+    # the full stack once for module loading and graph capture (untimed)
+    _solve_timed(inst, A.PRECISION_MIXED, sc, B, 1, math.inf, 1, 1, I, node_limit=1)
+    with ClockSampler(torch.cuda.current_device(), period_ms=200) as clk:
+        torch.cuda.synchronize()
+        wall, r, cert = _solve_timed(inst, A.PRECISION_MIXED, sc, B, 1, math.inf, 1, 1, I, node_limit=limit,
+                                     trace=4096, capacity=capacity)
+        torch.cuda.synchronize()
+    ms, nodes = r.round_ms.astype(np.float64), r.round_nodes.astype(np.int64)
+    full = np.nonzero(nodes == B)[0]
+    timed = full[-args.steps:] if len(full) >= args.steps else full
+    if len(timed) == 0:
+        raise RuntimeError("the search ended before a full batch")
+    first_timed = int(timed[0])
+    t_local = torch.tensor([float(ms[timed].sum())], dtype=torch.float64, device="cuda")
+    n_local = float(nodes[timed].sum())
+    if world > 1:
+        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
+    total_ms = float(t_local.item())
+    value = n_local * world / (total_ms / 1000.0)
+    main = _solve_summary(wall, r, cert)
+    main.update(rounds=len(ms), warmup_rounds=first_timed, timed_rounds=len(timed),
+                round_ms_mean=float(ms[timed].mean()))
+
+    # whole calls with the same node budget: the plain method (the reference's
+    # configuration: FP64, host frontier, most fractional, no cutoff, no tuner)
+    # against the full stack. The host frontier keeps every open node's bounds
+    # in host memory (two FP64 vectors): the budget stays within a quarter of
+    # the host's available memory
+    small = ramp + B
+    per_node = (1 << BRANCH_K) * 2 * n * 8
+    avail = _host_available_bytes()
+    if avail and small * per_node > avail // 4:
+        small = max(ramp, int(avail // 4 // per_node))
+    wall_f, r_f, c_f = _solve_timed(inst, A.PRECISION_MIXED, sc, B, 1, math.inf, 1, 1, I, node_limit=small,
+                                    capacity=capacity)
+    wall_p, r_p, c_p = _solve_timed(inst, A.PRECISION_FP64, None, B, 1, math.inf, 0, 0, I, node_limit=small,
+                                    autotune=0)
+    plain = _solve_summary(wall_p, r_p, c_p)
+    full_small = _solve_summary(wall_f, r_f, c_f)
+
+    # e2e: the main search's whole call through the Python API (instance from host arrays)
+    h2d = 2 * n * 8 + 2 * n * 8 + len(inst.problem.int_vars) * 4    # A, B, root lb, ub, integer indices
+    d2h = n * 8                                                       # the incumbent
+    e2e_value = r.nodes_processed / wall
+
+    other = {}
+    if args.workload == "birkhoff_regular400" and args.other_limit > 0:
+        # the order-120 pair (non-isomorphic 8-regular graphs), 256-node batches, a fixed time budget
+        inst4 = make_instance("birkhoff_regular120")
+        w4 = WORKLOADS["birkhoff_regular120"]
+        o4 = {}
+        for name, prec, scx, devf, cut in (("plain_fp64", A.PRECISION_FP64, None, 0, 0),
+                                           ("full_stack", A.PRECISION_MIXED, sc, 1, 1)):
+            wl, rr, cc = _solve_timed(inst4, prec, scx, w4["nodes"], 1, args.other_limit, devf, cut, w4["iters"],
+                                      autotune=0)
+            o4[name] = _solve_summary(wl, rr, cc)
+        o4["full_vs_plain_nodes_per_s"] = o4["full_stack"]["nodes_per_s"] / max(o4["plain_fp64"]["nodes_per_s"], 1e-9)
+        o4["note"] = (f"time budget {args.other_limit:g} s per arm, {w4['iters']} iterations per dispatch; "
+                      "for two d-regular graphs the doubly stochastic J/n gives AX = XB, so every FW bound is 0 "
+                      "while the optimum is positive: the gap cannot close by this method")
+        other["birkhoff_regular120"] = o4
+
+    _, lb_r, ub_r, eps_r = make_workload(args.workload, min(args.relax_nodes, B), rank)
+    arms = relax_arms(inst, lb_r, ub_r, eps_r, w, I, check_nodes=args.check_nodes)
+    cases = certified_cases(sc, args.ttg_limit) if args.ttg_limit > 0 else None
+    if rank != 0:
+        return
+
+    hbm_peak, bf16_peak, peak_kind = load_peaks()
+    mx = arms["mixed"]
+    # the relaxation kernel's algorithmic bytes: the iteration's m*m arrays
+    # streamed once each -- FP32 iterate read, FP32 gradient written and read,
+    # integer oracle costs written and read (20 m^2 bytes per node-iteration)
+    per_it = 20.0 * order * order
+    achieved = mx["node_iterations"] * per_it / (mx["ms"] / 1000.0) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                "kernel": "relax_kernel<GRAPH_MATCHING,BIRKHOFF,mixed>",
+                "work": f"{mx['node_iterations']} node-iterations x 20*{order}^2 bytes in "
+                        f"{mx['ms']:.1f} ms ({mx['nodes']} nodes, one launch)",
+                "note": "latency-bound: the two exact integer Hungarians per iteration are a dependent chain of "
+                        "Dijkstra steps; the gradient runs in FP32 over the graphs' nonzero lists (no tensor "
+                        "cores at this order)"}
+    cpu_v, cores, done, dt = cpu_sample(inst, lb_r[:ref_sample_nodes(args)], ub_r[:ref_sample_nodes(args)],
+                                        eps_r[:ref_sample_nodes(args)], w["alg"], w["ls"], I,
+                                        budget_s=args.cpu_budget)
+    ttg = {args.workload: {
+        "plain_fp64": plain, "full_stack": full_small, "full_stack_long": main,
+        "certified": bool(main["certified"] or full_small["certified"]),
+        "note": ("the optimum is 0 and every FW bound is 0 (J/n is a fractional isomorphism of two regular "
+                 "graphs), so the gap closes only when an LMO vertex is the isomorphism itself; at the root the "
+                 "iterate's mass on it stays at 1/order, and only nodes whose fixings already name two correct "
+                 "pairs reach it within a few hundred iterations")}}
+    if cases:
+        ttg.update(cases)
+    line = {"metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": world, "steps": len(timed),
+            "warmup": first_timed, "ms_per_step": total_ms / len(timed), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f64", "data": "synthetic",
+            "config": config_dict(args),
+            "e2e": {"value": e2e_value, "unit": "nodes/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "what": "whole gbx_solve call of the timed search (ramp rounds included) through the Python "
+                            "API, instance uploaded from host arrays, incumbent read back"},
+            "roofline": roofline,
+            "cpu_baseline": {"value": cpu_v, "unit": "nodes/s", "cores": cores, "kind": "port",
+                             "sample": f"{done} open nodes of the workload (uneven fixings), {I} iterations max "
+                                       f"each, {dt:.1f} s"},
+            "clocks": clk.summary(),
+            # per round: select, gather, relax, learned branching, decide, expand, merge, status
+            "gpu_launches": 8 * len(timed),
+            "full_vs_plain_nodes_per_s": full_small["nodes_per_s"] / max(plain["nodes_per_s"], 1e-9),
+            "plain_fp64": plain, "full_stack_same_budget": full_small, "search": main,
+            "relax_arms": arms, "other_configs": other, "time_to_gap": ttg,
+            "scorer_training_seconds": train_s}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- one relaxation launch (relax mode)
 def time_plain(args, inst, lb, x0, d_lb, d_ub, d_eps, d_flags, flush, w, stream):
     """The plain method (FP64 gradient and Hungarian) on the same batch, for the ratio."""
     import torch
@@ -241,98 +582,9 @@ def time_plain(args, inst, lb, x0, d_lb, d_ub, d_eps, d_flags, flush, w, stream)
             "node_iterations_per_step": int(it.sum().item())}
 
 
-def _solve_timed(inst, prec, scorer_obj, batch, streams, limit, device_frontier=0, cutoff=0):
-    from gpuboscia_gb300 import _abi as A
-    from gpuboscia_gb300 import api
-    s = inst.settings
-    s.gpu_batch_size = batch
-    s.num_streams = streams
-    s.gpu_max_iters = 500   # the reference's graph-matching example (examples/main.cu:218)
-    s.line_search = A.LS_QUADRATIC_EXACT
-    s.abs_gap_tol = 1e-6
-    s.rel_gap_tol = 1e-6
-    s.time_limit_seconds = limit
-    s.precision = prec
-    s.scorer = scorer_obj
-    s.device_frontier = device_frontier
-    s.incumbent_cutoff = cutoff
-    t0 = time.perf_counter()
-    r = api.solve(inst.problem, inst.objective, inst.lmo, s)
-    wall = time.perf_counter() - t0
-    gap = abs(r.objective - r.dual_bound) if math.isfinite(r.objective) else math.inf
-    certified = bool(not r.reached_time_limit and (gap <= 1e-6 or gap <= 1e-6 * abs(r.objective)))
-    return wall, r, certified
-
-
-def time_to_gap(args, inst):
-    """Wall time of gpuboscia::solve (through gbx_solve) from entry to the certified
-    1e-6 gap. (1) The workload's instance, plain FP64 against mixed precision.
-    (2) Held-out G(9, 1/2) graph pairs (non-isomorphic, the tree branches):
-    plain (FP64 gradients, most-fractional branching) against mixed precision
-    and mixed precision + the learned scorer (trained first on strong-branching
-    labels of four other pairs); same engine settings for all."""
-    from gpuboscia_gb300 import _abi as A
-    out = {}
-    for name, prec in (("plain_fp64", A.PRECISION_FP64), ("mixed", A.PRECISION_MIXED)):
-        wall, r, cert = _solve_timed(inst, prec, None, 256, 2, args.ttg_limit)
-        out[name] = {"seconds": wall, "nodes": r.nodes_processed, "objective": r.objective,
-                     "dual_bound": r.dual_bound, "certified": cert, "time_limit": bool(r.reached_time_limit)}
-
-    t0 = time.perf_counter()
-    sc = _trained_scorer()
-    train_s = time.perf_counter() - t0
-    pairs = {"instances": "4 held-out G(9,1/2) pairs; batch 64 x 1 stream, host frontier, unless named; "
-                          "full_stack = mixed + learned + device frontier (1024-node rounds) + incumbent cutoff",
-             "scorer_training_seconds": train_s}
-    for name in PAIR_CONFIGS:
-        pairs[name] = _solve_pairs(name, sc, args.ttg_limit)
-    out["graph_pairs"] = pairs
-    return out
-
-
-def _pair(seed, order=9):
-    from gpuboscia_gb300 import instances
-    rng = np.random.Generator(np.random.PCG64(seed))
-    return instances.graph_matching(order, instances.gnp_graph(rng, order, 0.5),
-                                    instances.gnp_graph(rng, order, 0.5), f"pair{order}_{seed}")
-
-
-def _trained_scorer():
-    """The learned scorer: strong-branching labels of four G(9, 1/2) pairs (seeds
-    100-103, disjoint from the held-out pairs 200-203), 400 Adam epochs."""
-    from gpuboscia_gb300 import scorer
-    data = scorer.Dataset.concat([scorer.collect_strong_branching(_pair(100 + k), max_nodes=30, max_candidates=64)
-                                  for k in range(4)])
-    sc = scorer.Scorer(32, seed=0)
-    sc.train(data, epochs=400, lr=3e-3)
-    return sc
-
-
-# time-to-gap configurations over the held-out pairs:
-# precision, learned scorer, batch, streams, device frontier, incumbent cutoff
-PAIR_CONFIGS = {
-    "plain_fp64": (0, False, 64, 1, 0, 0),
-    "mixed": (1, False, 64, 1, 0, 0),
-    "mixed_learned": (1, True, 64, 1, 0, 0),
-    "mixed_learned_256x4": (1, True, 256, 4, 0, 0),
-    "device_frontier_mixed_1024": (1, False, 1024, 1, 1, 0),
-    "device_frontier_mixed_learned_1024": (1, True, 1024, 1, 1, 0),
-    "full_stack": (1, True, 1024, 1, 1, 1),
-}
-
-
-def _solve_pairs(name, sc, limit):
-    prec, use, batch, streams, dev, cut = PAIR_CONFIGS[name]
-    tot_s, tot_n, cert = 0.0, 0, True
-    for k in range(4):
-        wall, r, c = _solve_timed(_pair(200 + k), prec, sc if use else None, batch, streams, limit, dev, cut)
-        tot_s += wall
-        tot_n += r.nodes_processed
-        cert = cert and c
-    return {"seconds": tot_s, "nodes": tot_n, "certified": cert}
-
-
-def run_gpu(args, rank, world):
+def run_relax(args, rank, world):
+    """A step is one gbx_relax_batch launch over the workload's batch of open
+    nodes, up to --iters iterations each; value = node relaxations per second."""
     import torch
     from gpuboscia_gb300 import _abi as A
     from gpuboscia_gb300 import api
@@ -443,21 +695,26 @@ def run_gpu(args, rank, world):
     plain = None
     if args.plain_steps > 0 and prec != A.PRECISION_FP64 and birkhoff:
         plain = time_plain(args, inst, lb, x0, d_lb, d_ub, d_eps, d_flags, flush, w, stream)
-    ttg = time_to_gap(args, inst) if rank == 0 and args.ttg_limit > 0 and birkhoff else None
     if rank != 0:
         return
     hbm_peak, bf16_peak, peak_kind = load_peaks()
     grads = node_iters + N  # iterations plus the final certificate gradient of each node
-    if birkhoff:
+    if birkhoff and prec == A.PRECISION_MIXED and order > 64:
+        # the mixed gradient runs on the tensor cores (orders 65..128 by default)
         flops = grads * 8.0 * order ** 3
         achieved_tf = flops / (kernel_ms / 1000.0) / 1e12
         roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": bf16_peak, "unit": "TFLOP/s",
-                    "frac": achieved_tf / bf16_peak,
-                    "traffic": (TRAFFIC_PER_NODE[(args.workload, args.precision)] * N
-                                if (args.workload, args.precision) in TRAFFIC_PER_NODE else None),
-                    "peak_kind": peak_kind,
-                    "kernel": "relax_kernel<GRAPH_MATCHING,BIRKHOFF>",
+                    "frac": achieved_tf / bf16_peak, "traffic": None, "peak_kind": peak_kind,
+                    "kernel": "relax_kernel<GRAPH_MATCHING,BIRKHOFF,mixed>",
                     "work": f"{grads} gradients x 8*{order}^3 flop per launch"}
+    elif birkhoff:
+        # FP32 SIMT or FP64 gradient: the iteration's m*m arrays streamed once each
+        per_it = 20.0 * order * order
+        achieved = node_iters * per_it / (kernel_ms / 1000.0) / 1e9
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                    "kernel": "relax_kernel<GRAPH_MATCHING,BIRKHOFF,%s>" % args.precision,
+                    "work": f"{node_iters} node-iterations x 20*{order}^2 bytes per launch"}
     else:
         # the box / simplex LMO phase: g, lb, ub in and v out, 32 bytes per variable per call
         lmo_bytes = grads * 32.0 * n
@@ -480,7 +737,7 @@ def run_gpu(args, rank, world):
             # relax_kernel, plus sparse_build_kernel for graph matching
             "clocks": clk.summary(), "gpu_launches": (2 if birkhoff else 1) * args.steps,
             "node_iterations_per_step": node_iters,
-            "plain_fp64": plain, "time_to_gap": ttg,
+            "plain_fp64": plain,
             "status_counts": {str(s): int((statuses == s).sum()) for s in np.unique(statuses)}}
     print(json.dumps(line), flush=True)
 
@@ -488,26 +745,34 @@ def run_gpu(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="birkhoff_gnp36", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--nodes", type=int, default=None)
     ap.add_argument("--iters", type=int, default=None)
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--plain-steps", type=int, default=2,
-                    help="timed steps of the plain FP64 method on the same batch (0 skips it)")
+                    help="relax mode: timed steps of the plain FP64 method on the same batch (0 skips it)")
     ap.add_argument("--ttg-limit", type=float, default=30.0,
-                    help="time limit of each time-to-gap solve in seconds (0 skips them)")
+                    help="bnb mode: time limit of each certified time-to-gap solve in seconds (0 skips them)")
+    ap.add_argument("--other-limit", type=float, default=10.0,
+                    help="bnb mode: time budget of each order-120 search arm in seconds (0 skips them)")
+    ap.add_argument("--relax-nodes", type=int, default=152,
+                    help="bnb mode: open nodes of the relaxation-arm comparison (one wave of 152 SMs)")
+    ap.add_argument("--check-nodes", type=int, default=4,
+                    help="bnb mode: nodes whose mixed certificate the oracle re-evaluates")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-budget", type=float, default=8.0)
     ap.add_argument("--launch-shape", default="auto", choices=["auto", "tc", "simt", "tuned"],
-                    help="mixed Birkhoff gradient: the default rule, tensor cores, FP32 SIMT "
+                    help="relax mode, mixed Birkhoff gradient: the default rule, tensor cores, FP32 SIMT "
                          "(over the nonzero lists for sparse graphs above order 64), or the "
                          "autotuner's choice on the batch (gbx_relax_autotune)")
     ap.add_argument("--solve", default=None, choices=sorted(PAIR_CONFIGS),
                     help="only solve the held-out graph pairs with this time-to-gap configuration "
                          "(one JSON line; for profiling the search)")
+    ap.add_argument("--mode", default=None, choices=["bnb", "relax"],
+                    help="override the workload's measurement (relax: one relaxation launch per step)")
     args = ap.parse_args()
     if args.solve:
         from gpuboscia_gb300 import build
@@ -519,8 +784,10 @@ def main():
         print(json.dumps({"solve": args.solve, **_solve_pairs(args.solve, sc, args.ttg_limit or 60.0)}))
         return
     w = WORKLOADS[args.workload]
+    mode = args.mode or w["mode"]
     if w["kind"] != "birkhoff":
         args.precision = "fp64"   # mixed precision covers graph matching over Birkhoff only
+        mode = "relax"
     args.nodes = args.nodes or w["nodes"]
     args.iters = args.iters or w["iters"]
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -537,7 +804,10 @@ def main():
         if world > 1:
             import torch
             torch.distributed.barrier()
-        run_gpu(args, rank, world)
+        if mode == "bnb":
+            run_bnb(args, rank, world)
+        else:
+            run_relax(args, rank, world)
     if world > 1 and args.impl == "gb300":
         import torch
         torch.distributed.destroy_process_group()

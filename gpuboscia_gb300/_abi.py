@@ -109,6 +109,12 @@ class Scorer(C.Structure):
     ]
 
 
+class RoundTrace(C.Structure):
+    _fields_ = [
+        ("capacity", C.c_int), ("count", C.c_int), ("ms", C.c_void_p), ("nodes", C.c_void_p),
+    ]
+
+
 class Settings(C.Structure):
     _fields_ = [
         ("gpu_batch_size", C.c_int), ("num_streams", C.c_int), ("gpu_max_iters", C.c_int),
@@ -120,7 +126,8 @@ class Settings(C.Structure):
         ("branch_k", C.c_int), ("use_cuda_graph", C.c_int),
         ("scorer", C.c_void_p), ("autotune", C.c_int),
         ("device_frontier", C.c_int), ("incumbent_cutoff", C.c_int), ("frontier_capacity", C.c_int),
-        ("frontier_slots", C.c_int),
+        ("frontier_slots", C.c_int), ("node_limit", C.c_int),
+        ("trace", C.c_void_p),
     ]
 
 
@@ -129,7 +136,8 @@ class Result(C.Structure):
         ("objective", C.c_double), ("dual_bound", C.c_double),
         ("nodes_processed", C.c_int), ("elapsed_seconds", C.c_double),
         ("reached_tolerance", C.c_int), ("reached_time_limit", C.c_int),
-        ("has_incumbent", C.c_int), ("x", C.c_void_p),
+        ("has_incumbent", C.c_int), ("x", C.c_void_p), ("reached_node_limit", C.c_int),
+        ("batches", C.c_int),
     ]
 
 
@@ -158,6 +166,8 @@ def default_settings() -> Settings:
     s.incumbent_cutoff = 0
     s.frontier_capacity = 0
     s.frontier_slots = 2
+    s.node_limit = 0
+    s.trace = None
     return s
 
 

@@ -225,6 +225,8 @@ class Settings:
     incumbent_cutoff: int = 0       # stop node relaxations whose FW bound clears the incumbent
     frontier_capacity: int = 0      # pool size in nodes (0: automatic)
     frontier_slots: int = 2         # device frontier: batches in flight (1 or 2)
+    node_limit: int = 0             # stop after this many processed nodes (0: none)
+    round_trace: int = 0            # device frontier: record the timing of up to this many rounds
 
     def algorithm_c(self) -> A.Algorithm:
         return A.Algorithm(self.algorithm, self.line_search, self.secant_iters, self.secant_tol,
@@ -235,7 +237,7 @@ class Settings:
         for f in ("gpu_batch_size", "num_streams", "gpu_max_iters", "gpu_eps", "gpu_eps_decay", "gpu_eps_min",
                   "integer_tol", "abs_gap_tol", "rel_gap_tol", "time_limit_seconds", "natural_lower_bound",
                   "branch_k", "use_cuda_graph", "autotune", "device_frontier", "incumbent_cutoff",
-                  "frontier_capacity", "frontier_slots"):
+                  "frontier_capacity", "frontier_slots", "node_limit"):
             setattr(s, f, getattr(self, f))
         s.algorithm = self.algorithm_c()
         s.root_initial_point = keep.ptr(_f64(self.root_initial_point) if self.root_initial_point is not None
@@ -256,6 +258,10 @@ class Result:
     elapsed_seconds: float
     reached_tolerance: bool
     reached_time_limit: bool
+    reached_node_limit: bool = False
+    batches: int = 0                  # relaxation launches of the search
+    round_ms: Optional[np.ndarray] = None     # device time of each round (Settings.round_trace)
+    round_nodes: Optional[np.ndarray] = None  # nodes each round finished
 
 
 def problem_to_c(p: Problem, keep: _Keep) -> A.Problem:
@@ -294,12 +300,22 @@ def solve(problem: Problem, objective, lmo, settings: Optional[Settings] = None)
     x = np.zeros(n, dtype=np.float64)
     r = A.Result()
     r.x = x.ctypes.data
+    tr = None
+    if settings.round_trace > 0:
+        cap = int(settings.round_trace)
+        tms, tnodes = np.zeros(cap, np.float32), np.zeros(cap, np.int32)
+        tr = A.RoundTrace(cap, 0, tms.ctypes.data, tnodes.ctypes.data)
+        s.trace = C.addressof(tr)
     rc = lib.gbx_solve(C.byref(pr), C.byref(o), C.byref(lm), C.byref(s), C.byref(r))
     if rc == A.ERR_INVALID:
         raise ValueError(lib.gbx_last_error().decode())
     A.check(lib, rc, "gbx_solve")
-    return Result(r.objective, x if r.has_incumbent else np.zeros(0), r.dual_bound, r.nodes_processed,
-                  r.elapsed_seconds, bool(r.reached_tolerance), bool(r.reached_time_limit))
+    out = Result(r.objective, x if r.has_incumbent else np.zeros(0), r.dual_bound, r.nodes_processed,
+                 r.elapsed_seconds, bool(r.reached_tolerance), bool(r.reached_time_limit),
+                 bool(r.reached_node_limit), int(r.batches))
+    if tr is not None:
+        out.round_ms, out.round_nodes = tms[:tr.count].copy(), tnodes[:tr.count].copy()
+    return out
 
 
 # ---------------------------------------------------------------- batched kernels
@@ -325,7 +341,8 @@ def _stream_ptr(stream) -> int:
 def _check_rows(lead, rows, dtype, extra=(), n_vars=None):
     """lead: the [cases, n] tensor that sets the shape; rows: (name, tensor or
     None) pairs that must hold cases*n elements of dtype; extra: (name,
-    tensor, dtype, count) checked as given; n_vars: the objective's variable
+    tensor, dtype, count) checked as given (count None: n elements, one per
+    variable); n_vars: the objective's variable
     count, which n must equal (the kernels size vectors from the objective).
     All contiguous on lead's CUDA device. Returns (cases, n)."""
     import torch
@@ -337,7 +354,7 @@ def _check_rows(lead, rows, dtype, extra=(), n_vars=None):
         raise ValueError(f"the objective has {n_vars} variables, the rows of {name0} {n}")
     spec = [(name0, t0, dtype, cases * n)]
     spec += [(nm, t, dtype, cases * n) for nm, t in rows if t is not None]
-    spec += [e for e in extra if e[1] is not None]
+    spec += [(nm, t, dt, n if count is None else count) for nm, t, dt, count in extra if t is not None]
     for name, t, dt, count in spec:
         if not isinstance(t, torch.Tensor):
             raise ValueError(f"{name} must be a torch tensor")
@@ -475,6 +492,8 @@ def objective_gradient_batch(objective, x, precision: int = A.PRECISION_FP64, st
 def objective_gradient_batch_f32(objective, x, stream=None):
     """Pipelined tensor-core gradients of FP32 points x [cases, n] (orders <= 128)."""
     import torch
+    if not isinstance(x, torch.Tensor):
+        raise ValueError("x must be a 2-D tensor [cases, n]")
     lib = A.load()
     keep = _Keep()
     X = x.to(dtype=torch.float32).contiguous()
@@ -488,8 +507,7 @@ def objective_gradient_batch_f32(objective, x, stream=None):
 
 def node_feasible_batch(lmo, lb, ub, integer_flags=None, stream=None):
     import torch
-    cases, n = _check_rows(("lb", lb), [("ub", ub)], torch.float64,
-                           [("integer_flags", integer_flags, torch.uint8, lb.shape[1] if lb.dim() == 2 else -1)])
+    cases, n = _check_rows(("lb", lb), [("ub", ub)], torch.float64, [("integer_flags", integer_flags, torch.uint8, None)])
     lib = A.load()
     keep = _Keep()
     lm = lmo.to_c(n, "cuda", keep)

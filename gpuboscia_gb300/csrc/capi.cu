@@ -68,7 +68,11 @@ const char* gbx_last_error(void) { return g_err.c_str(); }
 
 size_t gbx_relax_workspace_bytes(const gbx_objective* obj, const gbx_lmo* lmo,
                                  const gbx_algorithm* alg, int n_nodes) {
-    if (validate(obj, lmo, alg) != GBX_OK || n_nodes < 0) return 0;
+    if (validate(obj, lmo, alg) != GBX_OK) return 0;
+    if (n_nodes < 0) {
+        g_err = "n_nodes must be non-negative";
+        return 0;
+    }
     gbx::Layout L;
     std::string err;
     if (gbx::make_layout(*obj, *lmo, *alg, n_nodes, &L, &err) != GBX_OK) {

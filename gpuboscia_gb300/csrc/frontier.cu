@@ -29,6 +29,14 @@
 // completion). Kernels of a finished search return at once. Nothing waits on
 // another CTA: every round is ordered by streams and events alone.
 //
+// Pool layout. A binary problem (every integer variable's root bounds in
+// {0, 1}) stores an open node's bounds as one byte per variable (bit 0: lb = 1,
+// bit 1: ub = 1; continuous variables keep the root's bounds), 16x less than
+// two FP64 vectors: at order 400 a node takes 160 KB instead of 2.56 MB, so a
+// search that opens 10^5 nodes fits in HBM. The iterate of a continued node
+// (an unconverged integral node requeued with its x) goes to a small separate
+// pool. Other problems keep FP64 bounds and an iterate slot per node.
+//
 // Two batch slots (default): round r pops slot r % 2 and relaxes it on that
 // slot's stream while the control stream branches, decides and merges the
 // other slot, so the GPU is not idle behind a batch's slowest node. The
@@ -55,9 +63,13 @@ namespace {
 constexpr int kMaxBatch = 1024;    // nodes per round: one decide CTA
 constexpr int kMaxK = 8;           // branch_pow2 variables per node on this path
 constexpr int kEpsDepths = 4096;   // node tolerance by depth (deeper nodes use the last)
+// rounds per graph replay: the host checks the time limit between replays,
+// so problems whose rounds are long (large node vectors) replay two at a time
 constexpr int kRoundsPerReplay = 4;
+constexpr int kRoundsPerReplayLarge = 2;
+constexpr long long kLargeRoundDoubles = 1ll << 24;   // batch * n above which a round counts as long
 
-enum Why { RUNNING = 0, EXHAUSTED = 1, TOLERANCE = 2, CAPACITY = 3 };
+enum Why { RUNNING = 0, EXHAUSTED = 1, TOLERANCE = 2, CAPACITY = 3, NODE_LIMIT = 4 };
 
 // device control block (read by the host after every replay). Two batch
 // slots can be in flight: one relaxing while the other is decided and merged.
@@ -75,6 +87,9 @@ struct FState {
     int inc_src;           // batch index whose best vertex is the new incumbent (-1)
     int has_inc;
     int rounds;
+    int batches;           // rounds whose slot held at least one node
+    int xfree_top;         // free continuation-iterate slots (compact pool)
+    long long round_nodes[4];   // nodes_done after each of the last four rounds
     int n_batch[2];        // nodes popped into each slot
     int n_new[2];          // entries each slot pushes
     int pop_at[2];         // frontier position the slot's nodes were popped from
@@ -110,8 +125,19 @@ struct Slot {
 
 struct Tree {
     int n, cap, B, k, n_int, id_stride;
+    long long node_limit;  // processed nodes that end the search (0: none)
     double abs_tol, rel_tol, int_tol;
-    // pool of open nodes [cap * n] and their records [cap]
+    // pool of open nodes and their records [cap]. Compact pool: pcode
+    // [cap * n] bound codes, px [xcap * n] continuation iterates addressed by
+    // mxslot, free x slots on xfree. Otherwise plb / pub / px [cap * n].
+    int compact;
+    int xcap;
+    unsigned char* pcode;
+    const double* root_lb;  // [n]
+    const double* root_ub;
+    const unsigned char* isint;  // [n]
+    int* mxslot;
+    int* xfree;
     double* plb;
     double* pub;
     double* px;
@@ -185,22 +211,38 @@ __global__ void select_kernel(Tree T, int s) {
     S->slot_cut[s] = S->incumbent;   // fixed for the slot's relaxation: the result is timing-independent
     S->head += N;
     S->free_top += N;
+    if (N > 0) S->batches += 1;
 }
 
 // one CTA per batch node
 __global__ void __launch_bounds__(256) gather_kernel(Tree T, int s) {
-    const FState* S = T.S;
+    FState* S = T.S;
     const Slot& B = T.sl[s];
     const int i = blockIdx.x;
     if (i >= S->n_batch[s]) return;
     const int slot = T.fslot[S->cur][S->pop_at[s] + i];
     const size_t n = T.n, src = (size_t)slot * n, dst = (size_t)i * n;
     const bool hx = T.mhasx[slot] != 0;
-    for (size_t j = threadIdx.x; j < n; j += blockDim.x) {
-        const double l = T.plb[src + j];
-        B.lb[dst + j] = l;
-        B.ub[dst + j] = T.pub[src + j];
-        B.x[dst + j] = hx ? T.px[src + j] : l;
+    if (T.compact) {
+        const int xs = hx ? T.mxslot[slot] : -1;
+        const double* xsrc = T.px + (size_t)(xs < 0 ? 0 : xs) * n;
+        for (size_t j = threadIdx.x; j < n; j += blockDim.x) {
+            const unsigned char c = T.pcode[src + j];
+            const bool in = T.isint[j] != 0;
+            const double l = in ? ((c & 1) ? 1.0 : 0.0) : T.root_lb[j];
+            B.lb[dst + j] = l;
+            B.ub[dst + j] = in ? ((c & 2) ? 1.0 : 0.0) : T.root_ub[j];
+            B.x[dst + j] = xs >= 0 ? xsrc[j] : l;
+        }
+        // the iterate now lives in the batch: its x slot goes back to the free stack
+        if (threadIdx.x == 0 && xs >= 0) T.xfree[atomicAdd(&S->xfree_top, 1)] = xs;
+    } else {
+        for (size_t j = threadIdx.x; j < n; j += blockDim.x) {
+            const double l = T.plb[src + j];
+            B.lb[dst + j] = l;
+            B.ub[dst + j] = T.pub[src + j];
+            B.x[dst + j] = hx ? T.px[src + j] : l;
+        }
     }
     if (threadIdx.x == 0) {
         const int d = T.mdepth[slot];
@@ -541,10 +583,15 @@ __global__ void __launch_bounds__(kMaxBatch) decide_kernel(Tree T, int s) {
     }
     const int node = s_node[i];
     const int gcnt = (node < N) ? s_cnt[node] : 0;
-    int E = 0;
+    const int gcont = (gcnt > 0 && B.st[node] >= GBX_NODE_INTEGRAL_UNCONVERGED) ? 1 : 0;
+    // free-stack tops, read before the scans' barriers: thread 0 rewrites them
+    // below (the batch's pool slots were returned by gather)
+    const int top = S->free_top;
+    const int xtop = S->xfree_top;
+    int E = 0, ncont = 0;
     const int off = block_scan_sum(gcnt, wi, &E) - gcnt;
-    const int top = S->free_top;   // the batch's pool slots were returned by gather
-    if (E > top) {
+    const int crank = block_scan_sum(gcont, wi, &ncont) - gcont;   // continuation rank, sorted order
+    if (E > top || (T.compact && ncont > xtop)) {
         if (i == 0) { S->done = 1; S->why = CAPACITY; }
         return;
     }
@@ -567,10 +614,12 @@ __global__ void __launch_bounds__(kMaxBatch) decide_kernel(Tree T, int s) {
             T.mid[slot] = id;
             T.miters[slot] = gc ? B.it[g] : 0;
             T.mhasx[slot] = gc ? 1 : 0;
+            if (T.compact) T.mxslot[slot] = gc ? T.xfree[xtop - 1 - crank] : -1;
         }
     }
     if (i == 0) {
         S->free_top = top - E;
+        if (T.compact) S->xfree_top = xtop - ncont;
         S->n_new[s] = E;
         S->next_id += n_branched * T.id_stride;
         S->nodes_done += N - n_cont;
@@ -605,6 +654,7 @@ __global__ void __launch_bounds__(256) expand_kernel(Tree T, int s) {
         if ((int)threadIdx.x < nv) s_vars[threadIdx.x] = B.bvars[g * kMaxK + threadIdx.x];
         __syncthreads();
         const size_t src = (size_t)g * n, dst = (size_t)slot * n;
+        double* xdst = T.px + (T.compact ? (size_t)(mask < 0 ? T.mxslot[slot] : 0) * n : dst);
         for (size_t j = threadIdx.x; j < n; j += blockDim.x) {
             double l = B.lb[src + j], u = B.ub[src + j];
             for (int b = 0; b < nv; ++b) {
@@ -614,9 +664,14 @@ __global__ void __launch_bounds__(256) expand_kernel(Tree T, int s) {
                     else u = floor(xv);
                 }
             }
-            T.plb[dst + j] = l;
-            T.pub[dst + j] = u;
-            if (mask < 0) T.px[dst + j] = B.x[src + j];
+            if (T.compact) {
+                // integer variables of a binary problem: l, u in {0, 1}
+                T.pcode[dst + j] = (unsigned char)((l >= 0.5 ? 1 : 0) | (u >= 0.5 ? 2 : 0));
+            } else {
+                T.plb[dst + j] = l;
+                T.pub[dst + j] = u;
+            }
+            if (mask < 0) xdst[j] = B.x[src + j];
         }
     }
 }
@@ -669,6 +724,7 @@ __global__ void status_kernel(Tree T, int s) {
     S->cur = cur ^ 1;
     S->n_front = live;
     S->head = 0;
+    S->round_nodes[S->rounds & 3] = S->nodes_done;
     S->rounds += 1;
     S->inc_src = -1;
     S->n_batch[s] = 0;
@@ -680,6 +736,7 @@ __global__ void status_kernel(Tree T, int s) {
     S->bound = bound;
     if (live == 0 && !other) { S->done = 1; S->why = EXHAUSTED; }
     else if (within_tolerance(bound, inc, T.abs_tol, T.rel_tol)) { S->done = 1; S->why = TOLERANCE; }
+    else if (T.node_limit > 0 && S->nodes_done >= T.node_limit) { S->done = 1; S->why = NODE_LIMIT; }
 }
 
 struct DeviceBuffers {
@@ -697,9 +754,21 @@ struct DeviceBuffers {
 
 }  // namespace
 
-size_t frontier_slot_bytes(int n) {
-    return 3 * (size_t)n * sizeof(double) + sizeof(double) + 3 * sizeof(int) + 1  // pool
-           + 2 * (sizeof(double) + 2 * sizeof(int)) + sizeof(int);                 // frontier, free stack
+size_t frontier_slot_bytes(int n, int compact) {
+    const size_t vectors = compact ? (size_t)n + sizeof(int)        // bound codes, x-pool index
+                                   : 3 * (size_t)n * sizeof(double); // lb, ub, iterate
+    return vectors + sizeof(double) + 3 * sizeof(int) + 1              // pool records
+           + 2 * (sizeof(double) + 2 * sizeof(int)) + sizeof(int);     // frontier, free stack
+}
+
+// Binary problem: every integer variable's root bounds are 0 or 1, so every
+// node's bounds are too and fit the one-byte codes of the compact pool.
+static bool frontier_compact(const gbx_problem& pr) {
+    for (int q = 0; q < pr.n_int; ++q) {
+        const double l = pr.lb[pr.int_vars[q]], u = pr.ub[pr.int_vars[q]];
+        if (!((l == 0.0 || l == 1.0) && (u == 0.0 || u == 1.0))) return false;
+    }
+    return true;
 }
 
 int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const gbx_lmo& lmo,
@@ -742,13 +811,17 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{st};
 
     // pool capacity: the caller's, else a quarter of free memory up to 2^18 nodes
+    // (less the continuation iterates of a compact pool: two batches' worth)
+    const int compact = frontier_compact(pr) ? 1 : 0;
     long long cap = s.frontier_capacity;
     const int E_max = B << k;
     if (cap <= 0) {
         size_t fr = 0, tot = 0;
         e = cudaMemGetInfo(&fr, &tot);
         if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
-        cap = std::min<long long>(1 << 18, (long long)(fr / 4 / frontier_slot_bytes(n)));
+        const size_t xbytes = compact ? (size_t)2 * B * n * sizeof(double) : 0;
+        const size_t room = fr / 4 > xbytes ? fr / 4 - xbytes : 0;
+        cap = std::min<long long>(1 << 18, (long long)(room / frontier_slot_bytes(n, compact)));
         cap = std::max<long long>(cap, (long long)E_max + B + 1);
     }
     if (cap < (long long)E_max + 1 || cap > (1ll << 30)) {
@@ -761,10 +834,20 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     T.n = n; T.cap = (int)cap; T.B = B; T.k = k; T.n_int = pr.n_int;
     T.id_stride = std::max(8, 1 << k);
     T.abs_tol = s.abs_gap_tol; T.rel_tol = s.rel_gap_tol; T.int_tol = s.integer_tol;
+    T.node_limit = s.node_limit;
     const size_t C = (size_t)cap, Nn = (size_t)n;
-    T.plb = D.get<double>(C * Nn, &e);
-    T.pub = D.get<double>(C * Nn, &e);
-    T.px = D.get<double>(C * Nn, &e);
+    T.compact = compact;
+    T.xcap = compact ? (int)std::min<long long>(cap, 2ll * B) : 0;
+    if (compact) {
+        T.pcode = D.get<unsigned char>(C * Nn, &e);
+        T.mxslot = D.get<int>(C, &e);
+        T.xfree = D.get<int>((size_t)T.xcap, &e);
+        T.px = D.get<double>((size_t)T.xcap * Nn, &e);
+    } else {
+        T.plb = D.get<double>(C * Nn, &e);
+        T.pub = D.get<double>(C * Nn, &e);
+        T.px = D.get<double>(C * Nn, &e);
+    }
     T.mbound = D.get<double>(C, &e);
     T.mdepth = D.get<int>(C, &e);
     T.mid = D.get<int>(C, &e);
@@ -807,6 +890,11 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     T.inc_x = D.get<double>(Nn, &e);
     T.S = D.get<FState>(1, &e);
     unsigned char* d_flags = D.get<unsigned char>(Nn, &e);
+    double* d_root_lb = compact ? D.get<double>(Nn, &e) : nullptr;
+    double* d_root_ub = compact ? D.get<double>(Nn, &e) : nullptr;
+    T.root_lb = d_root_lb;
+    T.root_ub = d_root_ub;
+    T.isint = d_flags;
     if (e != cudaSuccess) { *err = std::string("device frontier allocation: ") + cudaGetErrorString(e); return GBX_ERR_CUDA; }
     T.int_vars = d_int_vars;
     T.eps_tab = d_eps;
@@ -827,6 +915,21 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     S0.next_id = 1;
     S0.inc_src = -1;
     S0.slot_bound[0] = S0.slot_bound[1] = std::numeric_limits<double>::infinity();
+    // compact pool: the root's codes; its start point (if any) in x slot 0
+    std::vector<unsigned char> root_code;
+    std::vector<int> xstack;
+    int root_xslot = -1;
+    if (compact) {
+        root_code.assign(Nn, 0);
+        for (int q = 0; q < pr.n_int; ++q) {
+            const int j = pr.int_vars[q];
+            root_code[j] = (unsigned char)((pr.lb[j] == 1.0 ? 1 : 0) | (pr.ub[j] == 1.0 ? 2 : 0));
+        }
+        const int first = root_x ? 1 : 0;
+        for (int q = T.xcap - 1; q >= first; --q) xstack.push_back(q);   // lowest free slot on top
+        root_xslot = root_x ? 0 : -1;
+        S0.xfree_top = (int)xstack.size();
+    }
     const double root_bound = s.natural_lower_bound;
     const int zero = 0;
     const unsigned char hx = root_x ? 1 : 0;
@@ -837,8 +940,16 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     up(d_int_vars, pr.int_vars, sizeof(int) * pr.n_int);
     up(d_eps, eps.data(), sizeof(double) * kEpsDepths);
     up(T.free_stack, stack.data(), sizeof(int) * stack.size());
-    up(T.plb, pr.lb, sizeof(double) * Nn);
-    up(T.pub, pr.ub, sizeof(double) * Nn);
+    if (compact) {
+        up(T.pcode, root_code.data(), Nn);
+        up(T.mxslot, &root_xslot, sizeof(int));
+        up(T.xfree, xstack.data(), sizeof(int) * xstack.size());
+        up(d_root_lb, pr.lb, sizeof(double) * Nn);
+        up(d_root_ub, pr.ub, sizeof(double) * Nn);
+    } else {
+        up(T.plb, pr.lb, sizeof(double) * Nn);
+        up(T.pub, pr.ub, sizeof(double) * Nn);
+    }
     if (root_x) up(T.px, root_x, sizeof(double) * Nn);
     up(T.mbound, &root_bound, sizeof(double));
     up(T.mdepth, &zero, sizeof(int));
@@ -902,6 +1013,17 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_fork[q], cudaEventDisableTiming);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_join[q], cudaEventDisableTiming);
         }
+    // per-round timing (gbx_settings.trace): an event at the start of every
+    // replay and one after each of its rounds, all on the frontier's stream
+    const bool tracing = s.trace && s.trace->capacity > 0 && s.trace->ms && s.trace->nodes;
+    cudaEvent_t ev_round[kRoundsPerReplay + 1] = {};
+    struct RoundEvents {
+        cudaEvent_t* ev;
+        ~RoundEvents() { for (int i = 0; i <= kRoundsPerReplay; ++i) if (ev[i]) cudaEventDestroy(ev[i]); }
+    } reg{ev_round};
+    if (tracing)
+        for (int i = 0; i <= kRoundsPerReplay && e == cudaSuccess; ++i) e = cudaEventCreate(&ev_round[i]);
+    if (s.trace) s.trace->count = 0;
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
     int rc = GBX_OK;
 
@@ -937,8 +1059,13 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     // A replay holds an even number of rounds and ends by joining its last
     // relaxation, so the next replay's first round finishes it in stream order.
     // With one slot a round is pop, relax, finish on one stream.
+    const int rpr = (long long)B * n > kLargeRoundDoubles ? kRoundsPerReplayLarge : kRoundsPerReplay;
     auto round = [&](int r) -> int {
         const int q = NS == 1 ? 0 : (r & 1);
+        if (tracing && r % rpr == 0) {
+            const cudaError_t ee = cudaEventRecord(ev_round[0], st);
+            if (ee != cudaSuccess) { *err = cudaGetErrorString(ee); return GBX_ERR_CUDA; }
+        }
         select_kernel<<<1, 1, 0, st>>>(T, q);
         gather_kernel<<<B, 256, 0, st>>>(T, q);
         if (NS == 1) {
@@ -952,13 +1079,17 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
             int rr = launch_relax(P[q], rs[q], err);
             if (rr) return rr;
             ee = cudaEventRecord(ev_join[q], rs[q]);
-            if (ee == cudaSuccess && r % kRoundsPerReplay != 0) ee = cudaStreamWaitEvent(st, ev_join[q ^ 1], 0);
+            if (ee == cudaSuccess && r % rpr != 0) ee = cudaStreamWaitEvent(st, ev_join[q ^ 1], 0);
             if (ee != cudaSuccess) { *err = cudaGetErrorString(ee); return GBX_ERR_CUDA; }
             finish(q ^ 1);
-            if (r % kRoundsPerReplay == kRoundsPerReplay - 1) {   // join the last relaxation of the replay
+            if (r % rpr == rpr - 1) {   // join the last relaxation of the replay
                 ee = cudaStreamWaitEvent(st, ev_join[q], 0);
                 if (ee != cudaSuccess) { *err = cudaGetErrorString(ee); return GBX_ERR_CUDA; }
             }
+        }
+        if (tracing) {
+            const cudaError_t ee = cudaEventRecord(ev_round[r % rpr + 1], st);
+            if (ee != cudaSuccess) { *err = cudaGetErrorString(ee); return GBX_ERR_CUDA; }
         }
         const cudaError_t le = cudaGetLastError();
         if (le != cudaSuccess) { *err = cudaGetErrorString(le); return GBX_ERR_CUDA; }
@@ -971,7 +1102,7 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
         cudaGraph_t g = nullptr;
         e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
         int crc = e == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
-        for (int r = 0; r < kRoundsPerReplay && crc == GBX_OK; ++r) crc = round(r);
+        for (int r = 0; r < rpr && crc == GBX_OK; ++r) crc = round(r);
         const cudaError_t ee = cudaStreamEndCapture(st, &g);
         if (crc == GBX_OK && ee == cudaSuccess && g) {
             if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) exec = nullptr;
@@ -986,13 +1117,15 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
     struct HostGuard { FState* p; ~HostGuard() { cudaFreeHost(p); } } hg{hS};
     bool timed_out = false;
+    int rounds_seen = 0;
+    long long nodes_seen = 0;
     const auto t_search = std::chrono::steady_clock::now();   // the time limit counts from here
     for (;;) {
         if (exec) {
             e = cudaGraphLaunch(exec, st);
             if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
         } else {
-            for (int r = 0; r < kRoundsPerReplay; ++r) {
+            for (int r = 0; r < rpr; ++r) {
                 rc = round(r);
                 if (rc) return rc;
             }
@@ -1000,6 +1133,26 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
         e = cudaMemcpyAsync(hS, T.S, sizeof(FState), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+        if (tracing) {
+            // the rounds this replay completed (a finished search skips the rest)
+            const int nr = std::min(hS->rounds - rounds_seen, rpr);
+            float prev = 0.f;
+            for (int i = 0; i < nr; ++i) {
+                float t = 0.f;
+                e = cudaEventElapsedTime(&t, ev_round[0], ev_round[i + 1]);
+                if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+                const long long after = hS->round_nodes[(rounds_seen + i) & 3];
+                gbx_round_trace* tr = s.trace;
+                if (tr->count < tr->capacity) {
+                    tr->ms[tr->count] = t - prev;
+                    tr->nodes[tr->count] = (int)(after - nodes_seen);
+                    tr->count += 1;
+                }
+                prev = t;
+                nodes_seen = after;
+            }
+            rounds_seen = hS->rounds;
+        }
         if (hS->done) break;
         const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_search).count();
         if (std::isfinite(s.time_limit_seconds) && el >= s.time_limit_seconds) { timed_out = true; break; }
@@ -1013,6 +1166,8 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     res->nodes_processed = (int)hS->nodes_done;
     res->reached_tolerance = hS->why == TOLERANCE ? 1 : 0;
     res->reached_time_limit = timed_out ? 1 : 0;
+    res->reached_node_limit = hS->why == NODE_LIMIT ? 1 : 0;
+    res->batches = hS->batches;
     res->has_incumbent = hS->has_inc;
     if (res->x && hS->has_inc) {
         e = cudaMemcpy(res->x, T.inc_x, sizeof(double) * Nn, cudaMemcpyDeviceToHost);

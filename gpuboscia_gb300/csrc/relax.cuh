@@ -189,7 +189,7 @@ int launch_gradient_batch_f32(const gbx_objective& o, int cases, const float* x,
 // is the validated root start point or null
 int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const gbx_lmo& lmo,
                           const gbx_settings& s, const double* root_x, gbx_result* res, std::string* err);
-size_t frontier_slot_bytes(int n);
+size_t frontier_slot_bytes(int n, int compact);
 int launch_node_feasible(const gbx_lmo& l, int cases, const double* lb, const double* ub,
                          const uint8_t* flags, uint8_t* out, void* stream, std::string* err);
 

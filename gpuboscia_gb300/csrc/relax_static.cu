@@ -66,8 +66,12 @@ extern "C" int gbx_relax_batch_static(const gbx_objective* obj, const gbx_lmo* l
         gbx::set_last_error("batch: null descriptor");
         return GBX_ERR_INVALID;
     }
+    if (batch->n_nodes < 0 || batch->max_iters < 0) {
+        gbx::set_last_error("batch: n_nodes and max_iters must be non-negative");
+        return GBX_ERR_INVALID;
+    }
     const size_t need = gbx_relax_workspace_bytes(obj, lmo, alg, batch->n_nodes);
-    if (need == 0) return GBX_ERR_INVALID;  // message set by the sizing call
+    if (need == 0) return GBX_ERR_INVALID;  // bad descriptors: the sizing call set the message
     if (need > GBX_STATIC_SCRATCH_BYTES) {
         gbx::set_last_error("batch needs " + std::to_string(need) + " bytes of scratch; the static scratch holds " +
                             std::to_string((size_t)GBX_STATIC_SCRATCH_BYTES) +

@@ -191,6 +191,8 @@ void gbx_default_settings(gbx_settings* s) {
     s->incumbent_cutoff = 0;
     s->frontier_capacity = 0;
     s->frontier_slots = 2;
+    s->node_limit = 0;
+    s->trace = nullptr;
 }
 
 int gbx_solve(const gbx_problem* problem, const gbx_objective* obj, const gbx_lmo* lmo,
@@ -205,6 +207,9 @@ int gbx_solve(const gbx_problem* problem, const gbx_objective* obj, const gbx_lm
                     || s->algorithm.line_search == GBX_LS_SAFEGUARDED_SCALED_OPEN_LOOP))
             throw std::invalid_argument("scaled open-loop is available only for DICG");
         if (s->branch_k < 1 || s->branch_k > 16) throw std::invalid_argument("branch_k must be in [1, 16]");
+        if (s->node_limit < 0) throw std::invalid_argument("node_limit must be non-negative");
+        res->reached_node_limit = 0;
+        res->batches = 0;
         Problem prob;
         prob.n_vars = n;
         prob.lb.assign(problem->lb, problem->lb + n);
@@ -252,6 +257,7 @@ int gbx_solve(const gbx_problem* problem, const gbx_objective* obj, const gbx_lm
         cfg.use_cuda_graph = s->use_cuda_graph != 0;
         cfg.autotune = s->autotune != 0;
         cfg.incumbent_cutoff = s->incumbent_cutoff != 0;
+        cfg.node_limit = s->node_limit;
 
         const double tol = s->integer_tol;
         const int k = s->branch_k;
@@ -289,6 +295,8 @@ int gbx_solve(const gbx_problem* problem, const gbx_objective* obj, const gbx_lm
         res->nodes_processed = engine.nodes_processed();
         res->reached_tolerance = engine.reached_tolerance();
         res->reached_time_limit = engine.reached_time_limit();
+        res->reached_node_limit = engine.reached_node_limit();
+        res->batches = (int)engine.gpu_batches();
         const auto x = engine.incumbent_x();
         res->has_incumbent = !x.empty();
         if (res->x && !x.empty()) std::copy(x.begin(), x.end(), res->x);

@@ -72,8 +72,9 @@ class Scorer:
         """Scores of device (or numpy) features [rows, F]; returns a device tensor."""
         import torch
         _check_features(features)
-        X = _dev_f32(features)
-        out = torch.empty(X.shape[0], dtype=torch.float32, device="cuda")
+        dev = self.params.device
+        X = _dev_f32(features, dev)
+        out = torch.empty(X.shape[0], dtype=torch.float32, device=dev)
         sc = self.to_c()
         lib = A.load()
         A.check(lib, lib.gbx_scorer_forward(C.byref(sc), X.shape[0], X.data_ptr(), out.data_ptr(), int(bf16),
@@ -84,9 +85,10 @@ class Scorer:
         """(dL/dparams, L) of the listwise loss; device tensors."""
         import torch
         gpn = _check_groups(features, group_ptr, target)
-        gp = torch.as_tensor(gpn.astype(np.int32)).cuda() if not isinstance(group_ptr, torch.Tensor) \
-            else group_ptr.to(device="cuda", dtype=torch.int32).contiguous()
-        return self._gradient(_dev_f32(features), gp, _dev_f32(target), stream)
+        dev = self.params.device
+        gp = _on(group_ptr if isinstance(group_ptr, torch.Tensor) else gpn.astype(np.int32), dev, torch.int32,
+                 "group_ptr")
+        return self._gradient(_dev_f32(features, dev), gp, _dev_f32(target, dev, "target"), stream)
 
     def _gradient(self, X, gp, t, stream=None):
         """gradient() on checked device tensors: X [rows, F] float32, gp the
@@ -96,9 +98,10 @@ class Scorer:
         sc = self.to_c()
         lib = A.load()
         nb = lib.gbx_scorer_workspace_bytes(C.byref(sc), rows)
-        ws = torch.empty(nb, dtype=torch.uint8, device="cuda")
-        grad = torch.empty(self.count, dtype=torch.float32, device="cuda")
-        loss = torch.empty(1, dtype=torch.float32, device="cuda")
+        dev = self.params.device
+        ws = torch.empty(nb, dtype=torch.uint8, device=dev)
+        grad = torch.empty(self.count, dtype=torch.float32, device=dev)
+        loss = torch.empty(1, dtype=torch.float32, device=dev)
         A.check(lib, lib.gbx_scorer_gradient(C.byref(sc), rows, X.data_ptr(), groups, gp.data_ptr(), t.data_ptr(),
                                              grad.data_ptr(), loss.data_ptr(), ws.data_ptr(), nb, _stream(stream)),
                 "gbx_scorer_gradient")
@@ -115,9 +118,10 @@ class Scorer:
         """Full-batch Adam on the dataset; returns the loss per epoch."""
         import torch
         _check_groups(data.features, data.group_ptr, data.target)
-        X = _dev_f32(data.features)
-        gp = torch.as_tensor(data.group_ptr.astype(np.int32)).cuda()
-        t = _dev_f32(data.target)
+        dev = self.params.device
+        X = _dev_f32(data.features, dev)
+        gp = _on(data.group_ptr.astype(np.int32), dev, torch.int32, "group_ptr")
+        t = _dev_f32(data.target, dev, "target")
         losses = []
         for _ in range(epochs):
             g, l = self._gradient(X, gp, t)
@@ -149,11 +153,21 @@ def _check_groups(features, group_ptr, target) -> np.ndarray:
     return gpn
 
 
-def _dev_f32(a):
+def _on(a, device, dtype, name):
+    """a (tensor or array) as a contiguous tensor of dtype on the scorer's
+    device. Host data is copied there; a tensor already on another CUDA
+    device is refused (the kernels read every operand on one device)."""
     import torch
     if isinstance(a, torch.Tensor):
-        return a.to(device="cuda", dtype=torch.float32).contiguous()
-    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+        if a.is_cuda and a.device != device:
+            raise ValueError(f"{name} is on {a.device}, the scorer's parameters on {device}")
+        return a.to(device=device, dtype=dtype).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device=device, dtype=dtype).contiguous()
+
+
+def _dev_f32(a, device, name="features"):
+    import torch
+    return _on(a, device, torch.float32, name)
 
 
 def features(x, lb, ub, order: int, depth: int, gap: float, value: float, vars_) -> np.ndarray:

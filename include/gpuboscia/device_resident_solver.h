@@ -100,6 +100,10 @@ struct DeviceResidentConfig {
     // stop a node's relaxation once its FW bound clears the incumbent
     // (gbx_node_batch.cutoff): the node is pruned at any bound above it
     bool incumbent_cutoff = false;
+    // stop once this many nodes are processed (0: no limit; no counterpart in
+    // the reference): the search ends with the batch that reaches it, and the
+    // reported dual bound is the live bound at that point
+    int node_limit = 0;
 };
 
 enum class DRSSchedulingEventType { Dispatched, CompletionDetached, PostprocessStarted };
@@ -142,6 +146,7 @@ public:
             throw std::invalid_argument("invalid tolerance configuration");
         if (std::isnan(time_limit_seconds_) || time_limit_seconds_ <= 0.0)
             throw std::invalid_argument("time limit must be positive");
+        if (cfg_.node_limit < 0) throw std::invalid_argument("node_limit must be non-negative");
         if (cfg_.gpu_block_threads != 0 && (cfg_.gpu_block_threads < 32 || cfg_.gpu_block_threads % 32 != 0))
             throw std::invalid_argument("gpu_block_threads must be zero or a positive multiple of 32");
         if (obj_.n != prob_.n_vars)
@@ -224,6 +229,7 @@ public:
     bool last_gpu_converged() const { return last_gpu_converged_.load(); }
     bool reached_tolerance() const { return reached_tolerance_; }
     bool reached_time_limit() const { return reached_time_limit_; }
+    bool reached_node_limit() const { return reached_node_limit_; }
     int effective_gpu_batch_size() const { return cfg_.gpu_batch_size; }
     int effective_num_streams() const { return cfg_.num_streams; }
     // Batches whose forward and in-face oracles ran concurrently in one launch.
@@ -366,6 +372,15 @@ private:
         if (el < time_limit_seconds_) return false;
         final_dual_bound_ = global_live_bound(incumbent_.get());
         reached_time_limit_ = true;
+        signal_done();
+        return true;
+    }
+
+    // the node limit ends the search like a time limit: live bound, no tolerance
+    bool finish_if_node_limit_reached() {
+        if (cfg_.node_limit <= 0 || nodes_done_.load() < cfg_.node_limit) return false;
+        final_dual_bound_ = global_live_bound(incumbent_.get());
+        reached_node_limit_ = true;
         signal_done();
         return true;
     }
@@ -561,7 +576,7 @@ private:
         call_branch_hook(batch);
         emit_scheduling_event(DRSSchedulingEventType::PostprocessStarted, batch.slot_id, batch.generation, N);
         for (int i = 0; i < N; ++i) {
-            if (finish_if_time_limit_reached()) return;
+            if (finish_if_time_limit_reached() || finish_if_node_limit_reached()) return;
             Node nd = batch.nodes[i];
             const double active_bound = nd.dual_bound;
             if (batch.status[i] == GBX_NODE_INFEASIBLE || pruned_early_parents_.count(nd.parent_id)) {
@@ -647,6 +662,7 @@ private:
         s.incumbent_cutoff = cfg_.incumbent_cutoff ? 1 : 0;
         s.frontier_capacity = cfg_.frontier_capacity;
         s.frontier_slots = cfg_.frontier_slots;
+        s.node_limit = cfg_.node_limit;
         std::vector<double> x(prob_.n_vars);
         gbx_result r{};
         r.x = x.data();
@@ -658,6 +674,8 @@ private:
         nodes_done_.store(r.nodes_processed);
         reached_tolerance_ = r.reached_tolerance != 0;
         reached_time_limit_ = r.reached_time_limit != 0;
+        reached_node_limit_ = r.reached_node_limit != 0;
+        batches_launched_ = r.batches;
         // the search ran on the device: one progress report, at its end
         if (progress_cb_)
             progress_cb_(r.nodes_processed, 0, r.dual_bound, incumbent_.get(), r.has_incumbent != 0);
@@ -737,6 +755,7 @@ private:
     double final_dual_bound_ = -std::numeric_limits<double>::infinity();
     bool reached_tolerance_ = false;
     bool reached_time_limit_ = false;
+    bool reached_node_limit_ = false;
     Clock::time_point solve_started_{};
     std::function<void(int, int, double, double, bool)> progress_cb_;
     std::function<void(const DRSSchedulingEvent&)> scheduling_cb_;

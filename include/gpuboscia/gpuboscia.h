@@ -45,6 +45,8 @@ struct Result {
     double elapsed_seconds = 0.0;
     bool reached_tolerance = false;
     bool reached_time_limit = false;
+    // DeviceResidentConfig::node_limit stopped the search (no counterpart in the reference)
+    bool reached_node_limit = false;
 };
 
 inline Settings create_default_settings() { return Settings{}; }
@@ -136,6 +138,7 @@ Result solve_with_algorithm(const Problem& problem, DeviceObjective objective, L
     r.nodes_processed = solver.nodes_processed();
     r.reached_tolerance = solver.reached_tolerance();
     r.reached_time_limit = solver.reached_time_limit();
+    r.reached_node_limit = solver.reached_node_limit();
     return r;
 }
 

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GBX_ABI_VERSION 3
+#define GBX_ABI_VERSION 4
 
 /* ---- status codes ------------------------------------------------------ */
 enum {
@@ -302,6 +302,19 @@ int gbx_scorer_gradient(const gbx_scorer* s, int rows, const float* features, in
 int gbx_scorer_adam(gbx_scorer* s, const float* grad, float* m, float* v, int step, float lr,
                     void* stream);
 
+/* Per-round timing of a device-frontier search (no counterpart in the
+ * reference): round r pops a batch, relaxes it and branches the batch popped
+ * the round before. ms[r] is the round's device time (CUDA events on the
+ * search's stream; the host's reads between graph replays are not counted),
+ * nodes[r] the nodes whose processing the round finished. The host frontier
+ * records nothing (count 0). */
+typedef struct gbx_round_trace {
+    int capacity;             /* entries ms and nodes hold                    */
+    int count;                /* out: rounds recorded (at most capacity)      */
+    float* ms;                /* host [capacity]                              */
+    int* nodes;               /* host [capacity]                              */
+} gbx_round_trace;
+
 typedef struct gbx_settings {
     /* DeviceResidentConfig (device_resident_solver.cuh:1004-1025) */
     int gpu_batch_size;       /* 1024 */
@@ -333,6 +346,11 @@ typedef struct gbx_settings {
     int frontier_capacity;    /* open nodes the pool holds (0: a quarter of free memory, <= 2^18) */
     int frontier_slots;       /* device frontier: batches in flight, 1 or 2 (2: one relaxes while
                                  the other is branched and merged); 2 */
+    /* stop once this many nodes are processed (0: no limit; no counterpart in
+     * the reference). The search stops at the end of the batch that reaches
+     * it; the result's dual bound is the live bound then, a valid bound. */
+    int node_limit;           /* 0 */
+    gbx_round_trace* trace;   /* device frontier: per-round timing, or NULL */
 } gbx_settings;
 
 typedef struct gbx_result {
@@ -344,6 +362,8 @@ typedef struct gbx_result {
     int reached_time_limit;
     int has_incumbent;
     double* x;                /* host [n_vars], caller-owned, filled when has_incumbent */
+    int reached_node_limit;   /* gbx_settings.node_limit stopped the search */
+    int batches;              /* relaxation launches (batches of nodes) the search made */
 } gbx_result;
 
 /* ---- graph-matching instance files (examples/main.cu:41-129 reads the

@@ -11,9 +11,13 @@ mkdir -p "$here/_build"
 g++ -std=c++17 -O2 -ffp-contract=off -fPIC -shared -pthread \
     -o "$here/_build/liboracle.so" "$here/fw_oracle.cpp"
 
+# the reference tree where it lies (GPUBOSCIA_REFERENCE overrides); its root
+# is recorded beside the library so the CPU tests that read the reference's
+# data files find them without naming a path of their own
 ref="${GPUBOSCIA_REFERENCE:-/root/reference}"
 if [ -d "$ref/include/gpuboscia" ]; then
     mkdir -p "$here/_ref"
     nvcc -std=c++17 -O2 -Xcompiler -fPIC -Xcompiler -ffp-contract=off -shared \
         -I "$ref/include" -o "$here/_ref/libgbref.so" "$here/ref_shim.cu"
+    printf '%s\n' "$(cd "$ref" && pwd)" > "$here/_ref/reference_root.txt"
 fi

@@ -1,6 +1,6 @@
 // ref_shim.cu -- TEST INFRASTRUCTURE. Exposes the reference project's own
 // CPU functions through a C ABI so the oracle can be pinned against them.
-// Built by oracle/build_ref.sh from the reference headers where they lie
+// Built by oracle/build.sh from the reference headers where they lie
 // (nothing is copied); the output goes to oracle/_ref/ and is never shipped.
 //
 // Wrapped reference functions (reference project paths):

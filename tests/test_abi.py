@@ -40,7 +40,7 @@ def test_library_exports_every_declared_symbol(lib):
     assert not missing, missing
     for f in declared_functions():
         assert hasattr(lib, f)
-    assert lib.gbx_abi_version() == 3
+    assert lib.gbx_abi_version() == 4
 
 
 _LAYOUT_C = r"""
@@ -58,7 +58,8 @@ int main(void) {
   S(gbx_settings) O(gbx_settings, algorithm) O(gbx_settings, time_limit_seconds) O(gbx_settings, use_cuda_graph)
   O(gbx_settings, scorer) O(gbx_settings, autotune) O(gbx_settings, device_frontier)
   O(gbx_settings, frontier_capacity) O(gbx_settings, incumbent_cutoff) O(gbx_node_batch, cutoff)
-  O(gbx_settings, frontier_slots)
+  O(gbx_settings, frontier_slots) O(gbx_settings, node_limit) O(gbx_result, reached_node_limit)
+  O(gbx_result, batches) O(gbx_settings, trace) S(gbx_round_trace) O(gbx_round_trace, nodes)
   S(gbx_scorer) O(gbx_scorer, params) O(gbx_scorer, params_bf16)
   S(gbx_result) O(gbx_result, x)
   return 0;
@@ -77,7 +78,7 @@ def test_struct_layouts_match_ctypes(tmp_path):
                                                        check=True).stdout.splitlines())
     M = {"gbx_objective": A.Objective, "gbx_lmo": A.LMO, "gbx_algorithm": A.Algorithm,
          "gbx_node_batch": A.NodeBatch, "gbx_problem": A.Problem, "gbx_settings": A.Settings,
-         "gbx_result": A.Result, "gbx_scorer": A.Scorer}
+         "gbx_result": A.Result, "gbx_scorer": A.Scorer, "gbx_round_trace": A.RoundTrace}
     for key, val in got.items():
         if "." in key:
             t, f = key.split(".")
@@ -94,7 +95,7 @@ def test_default_settings_match_reference_defaults(lib):
         if f == "algorithm":
             for g, _ in A.Algorithm._fields_:
                 assert getattr(s.algorithm, g) == getattr(d.algorithm, g), g
-        elif f != "root_initial_point":
+        elif f not in ("root_initial_point", "trace"):
             assert getattr(s, f) == getattr(d, f), f
 
 
@@ -115,6 +116,25 @@ def test_workspace_sizing_is_host_only(lib):
     bad = A.LMO(A.LMO_BIRKHOFF, 36 * 36, 1.0, None, 35)
     assert lib.gbx_relax_workspace_bytes(C.byref(obj), C.byref(bad), C.byref(alg), 4) == 0
     assert b"order" in lib.gbx_last_error()
+    assert lib.gbx_relax_workspace_bytes(C.byref(obj), C.byref(lmo), C.byref(alg), -1) == 0
+    assert b"n_nodes" in lib.gbx_last_error()
+
+
+def test_static_entry_rejects_negative_sizes_with_a_message(lib):
+    """The allocation-free entry checks the batch's sizes itself, before it
+    sizes the scratch or touches a device, and says why it refused."""
+    keep = api._Keep()
+    obj = api.DenseQuadraticObjective(np.eye(4)).to_c("host", keep)
+    lmo = api.BoxLMO().to_c(4, "host", keep)
+    alg = A.Algorithm(A.ALG_FRANK_WOLFE, A.LS_OPEN_LOOP, 4, 1e-10, 1e-14, A.PRECISION_FP64)
+    for n_nodes, iters in ((-1, 5), (3, -2)):
+        lib.gbx_relax_workspace_bytes(C.byref(obj), C.byref(A.LMO(A.LMO_BIRKHOFF, 16, 1.0, None, 3)),
+                                      C.byref(alg), 1)   # leaves an unrelated message behind
+        b = A.NodeBatch()
+        b.n_nodes, b.max_iters = n_nodes, iters
+        assert lib.gbx_relax_batch_static(C.byref(obj), C.byref(lmo), C.byref(alg), C.byref(b), None) \
+            == A.ERR_INVALID
+        assert b"non-negative" in lib.gbx_last_error()
 
 
 def test_relax_rejects_bad_arguments_without_launching(lib):

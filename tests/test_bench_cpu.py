@@ -9,12 +9,12 @@ import sys
 
 ROOT = pathlib.Path(__file__).resolve().parent.parent
 ARGS = ["--impl", "reference", "--steps", "2", "--warmup", "1", "--nodes", "16", "--iters", "5",
-        "--ref-budget", "0.2"]
+        "--ref-budget", "0.2", "--workload", "birkhoff_gnp36"]
 
 
-def _run(env_extra=None):
+def _run(env_extra=None, args=ARGS):
     env = dict(os.environ, **(env_extra or {}))
-    return subprocess.run([sys.executable, str(ROOT / "bench.py"), *ARGS], capture_output=True, text=True,
+    return subprocess.run([sys.executable, str(ROOT / "bench.py"), *args], capture_output=True, text=True,
                           env=env, cwd=ROOT, timeout=600)
 
 
@@ -42,3 +42,15 @@ def test_reference_arm_other_ranks_exit_quietly():
     r = _run({"WORLD_SIZE": "2", "RANK": "1", "LOCAL_RANK": "1"})
     assert r.returncode == 0, r.stderr
     assert not [l for l in r.stdout.splitlines() if l.startswith("{")]
+
+
+def test_default_workload_is_the_order_400_search():
+    """Without --workload the bench measures the order-400 isomorphic 10-regular
+    pair with 1024-node batches; the reference arm times the oracle on a
+    bounded sample of that workload's open nodes."""
+    r = _run(args=["--impl", "reference", "--steps", "1", "--warmup", "1", "--iters", "1", "--ref-budget", "0"])
+    assert r.returncode == 0, r.stderr
+    d = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][0])
+    cfg = d["config"]
+    assert cfg["workload"] == "birkhoff_regular400" and cfg["order"] == 400 and cfg["nodes_per_batch"] == 1024
+    assert d["value"] > 0 and d["cpu_baseline"]["sample"]

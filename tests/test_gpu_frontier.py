@@ -343,3 +343,76 @@ def test_fp64_search_matches_the_restated_frontier(cuda_lib, problem, slots, cut
     assert g.dual_bound == ref["dual_bound"]
     assert g.reached_tolerance == ref["tolerance"]
     assert np.array_equal(g.x, ref["x"])
+
+
+@pytest.mark.parametrize("device_frontier", [0, 1])
+def test_node_limit_stops_with_a_valid_bound(cuda_lib, device_frontier):
+    """Settings.node_limit ends the search with the batch that reaches it (both
+    frontiers): flagged, at least that many nodes and at most one batch more,
+    and the reported bound still below the proved optimum."""
+    inst = instances.box_qp(n=16, seed=21)
+    s = inst.settings
+    s.num_streams = 1
+    s.gpu_batch_size = 8
+    s.gpu_max_iters = 2000
+    s.rel_gap_tol = 0.0
+    s.device_frontier = device_frontier
+    whole = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert _proved(whole) and not whole.reached_node_limit and whole.nodes_processed > 40
+    s.node_limit = 20
+    part = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert part.reached_node_limit and not part.reached_tolerance
+    assert 20 <= part.nodes_processed <= 20 + 2 * s.gpu_batch_size
+    assert part.dual_bound <= whole.objective + 1e-9
+    assert part.objective >= whole.objective - 1e-9
+
+
+def test_round_trace_accounts_for_every_node(cuda_lib):
+    """Settings.round_trace: one entry per round of the device search, device
+    times from CUDA events, and the rounds' node counts summing to the nodes
+    processed."""
+    inst = instances.box_qp(n=16, seed=21)
+    s = inst.settings
+    s.gpu_batch_size = 8
+    s.gpu_max_iters = 2000
+    s.rel_gap_tol = 0.0
+    s.device_frontier = 1
+    s.round_trace = 4096
+    r = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    assert _proved(r)
+    assert len(r.round_ms) == len(r.round_nodes) > 0
+    assert int(r.round_nodes.sum()) == r.nodes_processed
+    assert np.all(r.round_ms >= 0) and r.round_ms.sum() > 0
+    # a batch of continued nodes only finishes no new node
+    assert r.batches >= int(np.count_nonzero(r.round_nodes))
+
+
+@pytest.mark.parametrize("slots,iters", [(1, 2000), (2, 2000), (2, 4)])
+def test_compact_pool_equals_the_fp64_pool(cuda_lib, slots, iters):
+    """A binary problem keeps its open nodes' bounds as one byte per variable;
+    the same problem with one more integer variable fixed at 2 (zero objective
+    weight) must keep FP64 bounds. Both searches are the same tree: node count,
+    incumbent, bound and solution agree exactly. A budget of 4 iterations per
+    dispatch leaves integral nodes unconverged, so continued nodes (their
+    iterates in the separate pool) are exercised as well."""
+    inst = instances.box_qp(n=16, seed=21)
+    Q, c = inst.objective.Q, inst.objective.c
+    n = 16
+    Q2 = np.zeros((n + 1, n + 1))
+    Q2[:n, :n] = Q
+    obj2 = api.DenseQuadraticObjective(Q2, np.concatenate([c, [0.0]]), inst.objective.scale,
+                                       inst.objective.linear_scale, inst.objective.constant)
+    prob2 = api.Problem(n + 1, np.concatenate([inst.problem.lb, [2.0]]), np.concatenate([inst.problem.ub, [2.0]]),
+                        list(inst.problem.int_vars) + [n])
+    s = inst.settings
+    s.gpu_batch_size = 8
+    s.gpu_max_iters = iters
+    s.rel_gap_tol = 0.0
+    s.device_frontier = 1
+    s.frontier_slots = slots
+    a = api.solve(inst.problem, inst.objective, inst.lmo, s)
+    b = api.solve(prob2, obj2, inst.lmo, s)
+    assert _proved(a) and _proved(b)
+    assert a.nodes_processed == b.nodes_processed
+    assert a.objective == b.objective and a.dual_bound == b.dual_bound
+    assert np.array_equal(a.x, b.x[:n]) and b.x[n] == 2.0

@@ -11,8 +11,9 @@ import numpy as np
 import pytest
 
 from gpuboscia_gb300 import instances
+from _refdata import reference_path
 
-REF = pathlib.Path(os.environ.get("GPUBOSCIA_REFERENCE", "/root/reference")) / "test_instances"
+REF = reference_path("test_instances")
 
 
 def _element(t, payload):

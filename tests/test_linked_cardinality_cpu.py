@@ -11,6 +11,7 @@ import pytest
 
 import _oracle as O
 from gpuboscia_gb300 import api, instances
+from _refdata import reference_path
 
 A_, HALF, M = 6, 8, 3            # active assets, padded half, cardinality
 
@@ -151,7 +152,7 @@ def test_sparse_sharpe_builder_bounds_the_level_set():
     assert inst.problem.int_vars == list(range(32, 62))
 
 
-US_ALL = pathlib.Path(os.environ.get("GPUBOSCIA_REFERENCE", "/root/reference")) / "DataSets" / "US_all_monthly.mat"
+US_ALL = reference_path("DataSets", "US_all_monthly.mat")
 
 
 @pytest.mark.skipif(not US_ALL.is_file(), reason="reference data set not present")

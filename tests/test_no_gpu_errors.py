@@ -49,7 +49,7 @@ def test_c_abi_reports_cuda_errors_and_stays_usable():
                 A.check(lib, rc, "gbx_solve")
         # host-only entry points are unaffected
         assert lib.gbx_relax_workspace_bytes(C.byref(obj), C.byref(lmo), C.byref(s.algorithm), 8) > 0
-        assert lib.gbx_abi_version() == 3
+        assert lib.gbx_abi_version() == 4
 
 
 def test_cpp_dropin_throws_runtime_error(tmp_path):
