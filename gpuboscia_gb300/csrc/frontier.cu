@@ -1015,6 +1015,7 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
         }
     // per-round timing (gbx_settings.trace): an event at the start of every
     // replay and one after each of its rounds, all on the frontier's stream
+    // (recorded as external events, so that a captured replay records them too)
     const bool tracing = s.trace && s.trace->capacity > 0 && s.trace->ms && s.trace->nodes;
     cudaEvent_t ev_round[kRoundsPerReplay + 1] = {};
     struct RoundEvents {
@@ -1063,7 +1064,7 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     auto round = [&](int r) -> int {
         const int q = NS == 1 ? 0 : (r & 1);
         if (tracing && r % rpr == 0) {
-            const cudaError_t ee = cudaEventRecord(ev_round[0], st);
+            const cudaError_t ee = cudaEventRecordWithFlags(ev_round[0], st, cudaEventRecordExternal);
             if (ee != cudaSuccess) { *err = cudaGetErrorString(ee); return GBX_ERR_CUDA; }
         }
         select_kernel<<<1, 1, 0, st>>>(T, q);
@@ -1088,7 +1089,7 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
             }
         }
         if (tracing) {
-            const cudaError_t ee = cudaEventRecord(ev_round[r % rpr + 1], st);
+            const cudaError_t ee = cudaEventRecordWithFlags(ev_round[r % rpr + 1], st, cudaEventRecordExternal);
             if (ee != cudaSuccess) { *err = cudaGetErrorString(ee); return GBX_ERR_CUDA; }
         }
         const cudaError_t le = cudaGetLastError();

@@ -1158,7 +1158,7 @@ struct BnB {
     double inc = kInf;
     std::vector<double> inc_x;
     int active = 0, next_id = 1, nodes_done = 0;
-    bool done = false, reached_tol = false, reached_time = false;
+    bool done = false, reached_tol = false, reached_time = false, reached_nodes = false;
     double final_bound = -kInf;
     std::chrono::steady_clock::time_point started;
     // the single slot
@@ -1183,6 +1183,15 @@ struct BnB {
         if (el < s->time_limit_seconds) return false;
         final_bound = live_bound(inc);
         reached_time = true;
+        signal_done();
+        return true;
+    }
+    // gbx_settings.node_limit (the library's extension, same rule as its engine:
+    // checked where the time limit is, between batches)
+    bool nodes_up() {
+        if (s->node_limit <= 0 || nodes_done < s->node_limit) return false;
+        final_bound = live_bound(inc);
+        reached_nodes = true;
         signal_done();
         return true;
     }
@@ -1329,7 +1338,7 @@ struct BnB {
 
     void worker() {
         while (!done) {
-            if (time_up()) return;
+            if (time_up() || nodes_up()) return;
             std::vector<Batch> completed;
             if (in_use) completed.push_back(detach());  // launch completed synchronously
             fill();
@@ -1458,6 +1467,8 @@ int oracle_solve(const gbx_problem* prob, const gbx_objective* obj, const gbx_lm
     res->elapsed_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - bb.started).count();
     res->reached_tolerance = bb.reached_tol;
     res->reached_time_limit = bb.reached_time;
+    res->reached_node_limit = bb.reached_nodes;
+    res->batches = bb.generation;
     res->has_incumbent = !bb.inc_x.empty();
     if (res->x && res->has_incumbent)
         std::copy(bb.inc_x.begin(), bb.inc_x.end(), res->x);

@@ -170,7 +170,8 @@ def solve(problem, objective, lmo, settings: api.Settings | None = None) -> api.
     if rc != 0:
         raise ValueError(L.oracle_last_error().decode())
     return api.Result(r.objective, x if r.has_incumbent else np.zeros(0), r.dual_bound, r.nodes_processed,
-                      r.elapsed_seconds, bool(r.reached_tolerance), bool(r.reached_time_limit))
+                      r.elapsed_seconds, bool(r.reached_tolerance), bool(r.reached_time_limit),
+                      bool(r.reached_node_limit), int(r.batches))
 
 
 INF = math.inf

@@ -350,7 +350,7 @@ def test_node_limit_stops_with_a_valid_bound(cuda_lib, device_frontier):
     """Settings.node_limit ends the search with the batch that reaches it (both
     frontiers): flagged, at least that many nodes and at most one batch more,
     and the reported bound still below the proved optimum."""
-    inst = instances.box_qp(n=16, seed=21)
+    inst = instances.box_qp(n=40, seed=5)   # a tree of ~90 nodes
     s = inst.settings
     s.num_streams = 1
     s.gpu_batch_size = 8
@@ -358,11 +358,11 @@ def test_node_limit_stops_with_a_valid_bound(cuda_lib, device_frontier):
     s.rel_gap_tol = 0.0
     s.device_frontier = device_frontier
     whole = api.solve(inst.problem, inst.objective, inst.lmo, s)
-    assert _proved(whole) and not whole.reached_node_limit and whole.nodes_processed > 40
-    s.node_limit = 20
+    assert _proved(whole) and not whole.reached_node_limit and whole.nodes_processed > 60
+    s.node_limit = 30
     part = api.solve(inst.problem, inst.objective, inst.lmo, s)
     assert part.reached_node_limit and not part.reached_tolerance
-    assert 20 <= part.nodes_processed <= 20 + 2 * s.gpu_batch_size
+    assert 30 <= part.nodes_processed <= 30 + 2 * s.gpu_batch_size
     assert part.dual_bound <= whole.objective + 1e-9
     assert part.objective >= whole.objective - 1e-9
 
