@@ -367,6 +367,262 @@ __device__ bool int_hungarian_warp(const IHW& w, int m, const int* costs, int sh
     return true;
 }
 
+// int_hungarian_warp with the per-column state (potential, slack, predecessor,
+// matched row with its potential and offset, the D at which a column joined
+// the tree) in shared memory `cs` (colstate_bytes(CPL) bytes, one warp): the
+// same shortest-augmenting-path steps, ties and results, in about 40
+// registers instead of ~9*CPL, so that two large-order nodes fit on an SM.
+// The owner of the step's column is read straight from shared memory instead
+// of being shuffled from its lane.
+template <int CPL, int FACE>
+__device__ bool int_hungarian_warp_cs(const IHW& w, int* cs, int m, const int* costs, int shift,
+                                      const uint8_t* code, bool restrict_same) {
+    const int lane = threadIdx.x & 31;
+    auto S = [&](int a, int t) -> int& { return cs[(a * CPL + t) * 32 + lane]; };
+    auto O = [&](int a, int t, int l) -> int { return cs[(a * CPL + t) * 32 + l]; };
+    auto cost_at = [&](int e) -> int {
+        const int c0 = costs[e];
+        if constexpr (FACE == 2) return (c0 < kIntInf && (code[e] & kFaceIn)) ? -c0 : kIntInf;
+        else return c0;
+    };
+    const unsigned lt = (1u << lane) - 1u;
+    int k;
+    if (restrict_same && w.scal[2] > 0) {
+        k = w.scal[2] - 1;
+    } else {
+        for (int i = lane; i < m; i += 32) { w.fcol[i] = -1; w.frow[i] = -1; }
+        __syncwarp();
+        bool ok = true;
+        const int nn = m * m;
+        for (int e = lane; e < nn; e += 32) {
+            const uint8_t c = code[e];
+            if (c & kBad) ok = false;
+            const bool forced = (c & kForced) || (FACE != 0 && (c & kFaceOne));
+            if (forced) {
+                const int r = e / m, col = e - r * m;
+                if (!(c & kAllowed)) ok = false;
+                if (atomicCAS(&w.fcol[r], -1, col) != -1) ok = false;
+                if (atomicCAS(&w.frow[col], -1, r) != -1) ok = false;
+            }
+        }
+        ok = __all_sync(kFull, ok);
+        __syncwarp();
+        if (!ok) return false;
+        k = 0;
+        int kc = 0;
+        for (int base = 0; base < m; base += 32) {
+            const int i = base + lane;
+            const bool fr = i < m && w.fcol[i] < 0;
+            const bool fc = i < m && w.frow[i] < 0;
+            const unsigned mr = __ballot_sync(kFull, fr), mc = __ballot_sync(kFull, fc);
+            if (fr) w.rows[k + __popc(mr & lt)] = i;
+            if (i < m) w.rowpos[i] = fr ? k + __popc(mr & lt) + 1 : 0;
+            if (fc) w.cols[kc + __popc(mc & lt)] = i;
+            k += __popc(mr);
+            kc += __popc(mc);
+        }
+        if (k != kc || k > 32 * CPL) return false;
+        for (int i = lane + 1; i <= k; i += 32) w.rowb[i] = w.rows[i - 1] * m;
+        if (lane == 0) w.scal[2] = k + 1;
+        __syncwarp();
+    }
+    const bool warm = w.scal[0] != 0;
+    const int dshift = shift - w.scal[1];
+    for (int t = 0; t < CPL; ++t) {
+        const int j = lane + 1 + 32 * t;
+        const bool valid = j <= k;
+        const int col = valid ? w.cols[j - 1] : 0;
+        long long v = 0;
+        if (valid && warm) {
+            v = w.colpot[col];
+            if (dshift > 0) v = dshift >= 24 ? 0 : v * (1ll << dshift);
+            else if (dshift < 0) v = -dshift >= 40 ? 0 : (v >> (-dshift));
+            v = max(-kPotLimit, min(kPotLimit, v));
+        }
+        S(CS_COL, t) = col;
+        S(CS_PV, t) = (int)v;
+        S(CS_PJ, t) = 0;
+        S(CS_UR, t) = 0;
+        S(CS_RBR, t) = 0;
+        if (valid) w.pvs[j] = (int)v;
+    }
+    __syncwarp();
+    // row potentials u_i = min_j (c_ij - v_j), one row per lane
+    bool rows_ok = true;
+    for (int i = lane + 1; i <= k; i += 32) {
+        const int rb = w.rowb[i];
+        int best = kIntInf, barg = 0;
+        int j = 1;
+        for (; j + 7 <= k; j += 8) {
+            int cc[8], pp[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) { cc[q] = cost_at(rb + w.cols[j - 1 + q]); pp[q] = w.pvs[j + q]; }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (cc[q] < kIntInf && cc[q] - pp[q] < best) { best = cc[q] - pp[q]; barg = j + q; }
+        }
+        for (; j <= k; ++j) {
+            const int c = cost_at(rb + w.cols[j - 1]);
+            if (c < kIntInf && c - w.pvs[j] < best) { best = c - w.pvs[j]; barg = j; }
+        }
+        if (best >= kIntInf) rows_ok = false;
+        w.u[i] = best;
+        w.pinv[i - 1] = barg;   // a tight column of row i (pinv is free during the call)
+        w.rmatch[i] = 0;
+    }
+    if (!__all_sync(kFull, rows_ok)) return false;
+    __syncwarp();
+    // keep the previous matching where its edge is still allowed and tight
+    if (warm) {
+        for (int t = 0; t < CPL; ++t) {
+            if (lane + 1 + 32 * t > k) continue;
+            const int col = S(CS_COL, t);
+            const int r = w.match[col];
+            if (r < 0 || r >= m) continue;
+            const int i = w.rowpos[r];
+            if (i <= 0) continue;
+            const int c = cost_at(r * m + col);
+            const int ui = w.u[i];
+            if (c < kIntInf && c - ui - S(CS_PV, t) == 0) {
+                S(CS_PJ, t) = i;
+                S(CS_UR, t) = ui;
+                S(CS_RBR, t) = w.rowb[i];
+                w.rmatch[i] = 1;
+            }
+        }
+    }
+    __syncwarp();
+    // greedy tight matching: every free row claims its tight column, the lowest
+    // row wins a contested free column
+    {
+        int* claim = w.pi;   // per compacted column; pi is rewritten at the end
+        for (int t = 0; t < CPL; ++t)
+            if (lane + 1 + 32 * t <= k) claim[lane + 32 * t] = S(CS_PJ, t) ? 0 : 0x7fffffff;
+        __syncwarp();
+        for (int i = lane + 1; i <= k; i += 32)
+            if (!w.rmatch[i]) atomicMin(&claim[w.pinv[i - 1] - 1], i);
+        __syncwarp();
+        for (int t = 0; t < CPL; ++t) {
+            if (lane + 1 + 32 * t > k || S(CS_PJ, t)) continue;
+            const int r = claim[lane + 32 * t];
+            if (r != 0x7fffffff) {
+                S(CS_PJ, t) = r;
+                S(CS_UR, t) = w.u[r];
+                S(CS_RBR, t) = w.rowb[r];
+                w.rmatch[r] = 1;
+            }
+        }
+        __syncwarp();
+    }
+    bool feasible = true;
+    for (int i = 1; i <= k && feasible; ++i) {
+        if (w.rmatch[i]) continue;
+        for (int t = 0; t < CPL; ++t) {
+            S(CS_MRAW, t) = kIntInf;
+            S(CS_WAY, t) = 0;
+            S(CS_USED, t) = -1;
+        }
+        int j0 = 0, D = 0;
+        int ui0 = w.u[i], rb = w.rowb[i];
+        bool augmented = false;
+        for (int step = 0; step <= k; ++step) {
+            int bv = kIntInf, bj = 0x7fffffff;
+            // all of this lane's costs of the row at once (invalid slots read
+            // column 0 of the same row), then the scan
+            int cv[CPL];
+#pragma unroll
+            for (int t = 0; t < CPL; ++t) cv[t] = cost_at(rb + S(CS_COL, t));
+#pragma unroll
+            for (int t = 0; t < CPL; ++t) {
+                const bool live = lane + 1 + 32 * t <= k && S(CS_USED, t) < 0;
+                const int c = cv[t];
+                int mr = S(CS_MRAW, t);
+                if (live && c < kIntInf) {
+                    const int cur = c - ui0 - S(CS_PV, t) + D;
+                    if (cur < mr) { mr = cur; S(CS_MRAW, t) = cur; S(CS_WAY, t) = j0; }
+                }
+                if (live && mr < bv) { bv = mr; bj = lane + 1 + 32 * t; }
+            }
+            int gmin, j1;
+            const int key = bv < kPackLimit ? (bv << 10) | bj : 0x7fffffff;
+            const int kmin = __reduce_min_sync(kFull, key);
+            if (kmin != 0x7fffffff) {
+                gmin = kmin >> 10;
+                j1 = kmin & 1023;
+            } else {
+                gmin = __reduce_min_sync(kFull, bv);
+                if (gmin >= kIntInf) { feasible = false; break; }
+                j1 = __reduce_min_sync(kFull, bv == gmin ? bj : 0x7fffffff);
+            }
+            D = gmin;
+            const int owner = (j1 - 1) & 31, slot = (j1 - 1) >> 5;
+            const int pnext = O(CS_PJ, slot, owner);
+            const int unext = O(CS_UR, slot, owner);
+            const int rnext = O(CS_RBR, slot, owner);
+            if (lane == owner) S(CS_USED, slot) = D;
+            j0 = j1;
+            if (pnext == 0) { augmented = true; break; }
+            ui0 = unext;
+            rb = rnext;
+        }
+        if (!feasible || !augmented) { feasible = false; break; }
+        // apply the potentials of this path (before the matching flips)
+        const int uroot = w.u[i] + D;
+        for (int t = 0; t < CPL; ++t) {
+            const int ua = S(CS_USED, t);
+            if (ua < 0) continue;
+            const int d = D - ua;
+            S(CS_PV, t) -= d;
+            S(CS_UR, t) += d;
+        }
+        __syncwarp();
+        // flip the path: column j takes the row (and its potential / offset) of way[j]
+        int j = j0;
+        for (int guard = 0; guard <= k && j != 0; ++guard) {
+            const int owner = (j - 1) & 31, slot = (j - 1) >> 5;
+            const int jp = O(CS_WAY, slot, owner);
+            int np = i, nu = uroot, nr = w.rowb[i];
+            if (jp != 0) {
+                const int po = (jp - 1) & 31, ps = (jp - 1) >> 5;
+                np = O(CS_PJ, ps, po);
+                nu = O(CS_UR, ps, po);
+                nr = O(CS_RBR, ps, po);
+            }
+            __syncwarp();
+            if (lane == owner) { S(CS_PJ, slot) = np; S(CS_UR, slot) = nu; S(CS_RBR, slot) = nr; }
+            __syncwarp();
+            j = jp;
+        }
+        __syncwarp();
+    }
+    if (!__all_sync(kFull, feasible)) return false;
+    // outputs and the warm state for the next call (original indices)
+    for (int i = lane; i < m; i += 32)
+        if (w.fcol[i] >= 0) { w.pi[i] = w.fcol[i]; w.match[w.fcol[i]] = i; }
+    int lo = kIntInf;
+    for (int t = 0; t < CPL; ++t) {
+        if (lane + 1 + 32 * t > k) continue;
+        const int col = S(CS_COL, t);
+        const int r = w.rows[S(CS_PJ, t) - 1];
+        w.pi[r] = col;
+        w.match[col] = r;
+        lo = min(lo, S(CS_PV, t));
+    }
+    lo = __reduce_min_sync(kFull, lo);
+    if (lo >= kIntInf) lo = 0;
+    bool sane = true;
+    for (int t = 0; t < CPL; ++t) {
+        if (lane + 1 + 32 * t > k) continue;
+        const int v = S(CS_PV, t) - lo;
+        w.colpot[S(CS_COL, t)] = v;
+        sane = sane && v <= kPotLimit;
+    }
+    sane = __all_sync(kFull, sane);
+    if (lane == 0) { w.scal[0] = sane ? 1 : 0; w.scal[1] = shift; }
+    __syncwarp();
+    return true;
+}
+
 // Block-wide max of |v| over n floats (broadcast).
 static __device__ float bmax_abs(const float* v, int n, double* red) {
     float mx = 0.f;

@@ -51,6 +51,9 @@ struct Layout {
     // offsets, the gradient runs over the nonzero lists in FP32
     int cost_global;
     size_t mx_cost_off, mx_code_off;
+    // those orders keep each oracle warp's per-column Hungarian state in
+    // shared memory (cs_bytes per warp at sm_cs), so two nodes fit on an SM
+    size_t sm_cs, cs_bytes;
     // the certificate's FP64 Hungarian reads the gradient staged in the cost
     // region (1), or straight from the node's gradient vector (0) when staging
     // would cost a resident node per SM
@@ -114,6 +117,13 @@ GBX_HD inline SparseAB sparse_at(unsigned char* base, int m, int cap) {
     }
     return S;
 }
+
+// Column state of one integer-Hungarian warp held in shared memory instead of
+// registers (the large-order kernel, 8 or 16 columns per lane): eight
+// [CPL][32] int arrays, lane-contiguous so a warp's access to one slot is
+// conflict-free.
+enum { CS_COL, CS_PV, CS_MRAW, CS_WAY, CS_PJ, CS_USED, CS_UR, CS_RBR, CS_COUNT };
+GBX_HD inline size_t colstate_bytes(int cpl) { return (size_t)CS_COUNT * cpl * 32 * sizeof(int); }
 
 // bytes of one FP64 Hungarian workspace (potentials, minv, path, forced maps)
 GBX_HD inline size_t hung_ws_bytes(int m) {

@@ -144,6 +144,13 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
             cost_bytes = staged;
         }
         fixed_bytes += (L.cost_global ? 0 : cost_bytes + code_bytes) + 2 * L.ihw_bytes;
+        if (L.cost_global) {
+            // large orders: only the certificate's forward oracle runs in FP64
+            // (one workspace), and the integer oracles' column state moves to
+            // shared memory (below) -- two nodes per SM
+            L.hung_warps = 1;
+            fixed_bytes -= L.hung_bytes;
+        }
     }
     size_t obj_doubles = o.kind == GBX_OBJ_GRAPH_MATCHING ? 2 * (size_t)o.order * o.order
                                                           : (size_t)n * n;
@@ -194,11 +201,13 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
         L.sm_idx = p; p += align16((size_t)L.sort_size * 4);
         L.sm_fixed = p; p += align16((size_t)n);
     }
-    L.sm_hung = p; p += 2 * L.hung_bytes;
+    L.sm_hung = p; p += (size_t)L.hung_warps * L.hung_bytes;
     L.sm_mx = p; if (mixed && !L.mx_global) p += mx_bytes;
     L.sm_cost = p; if (!L.cost_global) p += cost_bytes;
     L.sm_code = p; if (!L.cost_global) p += code_bytes;
     L.sm_ihw = p; p += mixed ? 2 * L.ihw_bytes : 0;
+    L.cs_bytes = mixed && L.cost_global ? colstate_bytes(l.order <= 256 ? 8 : 16) : 0;
+    L.sm_cs = p; p += 2 * L.cs_bytes;
     L.sm_total = p;
     L.mixed_node_bytes = L.mx_global ? (mx_bytes + 255) / 256 * 256 : 0;
     if (L.tc) L.mixed_node_bytes += kTcImageBytes;

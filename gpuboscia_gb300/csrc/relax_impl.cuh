@@ -1733,11 +1733,12 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
             const IHW& w = fwd ? w0 : w1;
             const bool same = fwd || c.flag[4] == 0;
             bool ok;
-            if constexpr (BIG) {
-                if (m <= 256) ok = fwd ? int_hungarian_warp<8, 0>(w, m, costf, shift, code, same)
-                                       : int_hungarian_warp<8, 1>(w, m, costa, shift, code, same);
-                else ok = fwd ? int_hungarian_warp<16, 0>(w, m, costf, shift, code, same)
-                              : int_hungarian_warp<16, 1>(w, m, costa, shift, code, same);
+            if constexpr (BIG) {   // column state in shared memory: two nodes per SM
+                int* cs = reinterpret_cast<int*>(dsm + L.sm_cs + (fwd ? 0 : L.cs_bytes));
+                if (m <= 256) ok = fwd ? int_hungarian_warp_cs<8, 0>(w, cs, m, costf, shift, code, same)
+                                       : int_hungarian_warp_cs<8, 1>(w, cs, m, costa, shift, code, same);
+                else ok = fwd ? int_hungarian_warp_cs<16, 0>(w, cs, m, costf, shift, code, same)
+                              : int_hungarian_warp_cs<16, 1>(w, cs, m, costa, shift, code, same);
             } else if constexpr (TC) {   // orders 17..128, costs beside the operand images
                 if (m <= 64) ok = fwd ? int_hungarian_warp<2, 0>(w, m, costf, shift, code, same)
                                       : int_hungarian_warp<2, 1>(w, m, costa, shift, code, same);
@@ -2196,12 +2197,22 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
             // a 0/1 point with unit row and column sums is a permutation: its
             // value in O(m^2) is bit-identical to the generic one
             const bool perm = graph_perm && c.tol < 0.5 && __syncthreads_and(zero_one);
+            int* cpi = hw1.pi;
+            int* cpinv = hw1.pinv;
+            if constexpr (kMixedLoop) {
+                if (L.hung_warps < 2) {
+                    // one FP64 workspace: the in-face integer oracle's arrays are free now
+                    const IHW wi = ihw_at(dsm + L.sm_ihw + L.ihw_bytes, c.m);
+                    cpi = wi.pi;
+                    cpinv = wi.pinv;
+                }
+            }
             if (perm) {
                 for (int j = tid; j < n; j += kThreads)
-                    if (CAND[j] == 1.0) hw1.pi[j / c.m] = j - (j / c.m) * c.m;
+                    if (CAND[j] == 1.0) cpi[j / c.m] = j - (j / c.m) * c.m;
                 __syncthreads();
             }
-            const double cv = integer_value(c, CAND, LB, UB, perm ? hw1.pi : nullptr, hw1.pinv);
+            const double cv = integer_value(c, CAND, LB, UB, perm ? cpi : nullptr, cpinv);
             if (cv < best_val) {
                 for (int j = tid; j < n; j += kThreads) best[j] = CAND[j];
                 if (tid == 0) P.b.best_vertex_val[node] = cv;
@@ -2225,7 +2236,7 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
 // One CTA per node (grid = nodes), or a persistent grid whose CTAs take the
 // next node from an atomic queue in the workspace until the batch is done.
 template <int OK, int LK, int MIX>
-__global__ void __launch_bounds__(kThreads, MIX == 1 ? 2 : 1) relax_kernel(const __grid_constant__ Params P) {
+__global__ void __launch_bounds__(kThreads, (MIX == 1 || MIX == 3) ? 2 : 1) relax_kernel(const __grid_constant__ Params P) {
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ Scalars sh;
     // a batch assembled on the device (frontier rounds) carries its size in

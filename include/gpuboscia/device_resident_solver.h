@@ -576,7 +576,7 @@ private:
         call_branch_hook(batch);
         emit_scheduling_event(DRSSchedulingEventType::PostprocessStarted, batch.slot_id, batch.generation, N);
         for (int i = 0; i < N; ++i) {
-            if (finish_if_time_limit_reached() || finish_if_node_limit_reached()) return;
+            if (finish_if_time_limit_reached()) return;
             Node nd = batch.nodes[i];
             const double active_bound = nd.dual_bound;
             if (batch.status[i] == GBX_NODE_INFEASIBLE || pruned_early_parents_.count(nd.parent_id)) {
@@ -692,7 +692,7 @@ private:
 
     void gpu_worker() {
         while (!done_.load(std::memory_order_relaxed)) {
-            if (finish_if_time_limit_reached()) return;
+            if (finish_if_time_limit_reached() || finish_if_node_limit_reached()) return;
             std::vector<Completed> completed;
             for (Slot* s : ready_slots()) completed.push_back(detach_completed_slot(*s));
             // refill released slots before any CPU work on their results

@@ -154,7 +154,8 @@ def test_config5_order400_mixed_certificate_equals_the_oracle(cuda_lib):
     its = it.cpu().numpy()
     assert np.all(its == 12)
     ref = O.relax(inst.objective, inst.lmo, O.algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT), x.cpu().numpy(), lb, ub,
-                  eps, iterations=its, status=np.full(N, 0x80, np.uint8), max_iters=0, threads=8)
+                  eps, iterations=its, status=np.full(N, 0x80, np.uint8), max_iters=0,
+                  flags=np.ones(m * m, np.uint8), threads=8)
     assert np.array_equal(out["gap"].cpu().numpy(), ref["gap"])
     assert np.array_equal(out["value"].cpu().numpy(), ref["value"])
     assert np.array_equal(st.cpu().numpy(), ref["status"])
