@@ -742,6 +742,38 @@ def run_relax(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_gradient(args):
+    """--mode gradient: the batched graph-matching gradient entry points alone
+    (for profiling), on a G(order, 1/2) pair and --cases random points:
+    --gradient f32 times gbx_objective_gradient_batch_f32 (the pipelined
+    tensor-core kernel), mixed times gbx_objective_gradient_batch with FP64
+    points in mixed precision. One JSON line (not the benchmark's line)."""
+    import torch
+    from gpuboscia_gb300 import _abi as A
+    from gpuboscia_gb300 import api, instances
+    m, N = args.order, args.cases
+    inst = instances.birkhoff_gnp(order=m, seed=5)
+    rng = np.random.Generator(np.random.PCG64(9))
+    x = torch.from_numpy(rng.random((N, m * m))).cuda()
+    xf = x.float()
+    call = ((lambda: api.objective_gradient_batch_f32(inst.objective, xf)) if args.gradient == "f32"
+            else (lambda: api.objective_gradient_batch(inst.objective, x, A.PRECISION_MIXED)))
+    for _ in range(args.warmup):
+        call()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        call()
+        b.record()
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    t = statistics.mean(ms)
+    print(json.dumps({"mode": "gradient", "entry": args.gradient, "order": m, "cases": N, "ms": t,
+                      "tflops_algorithmic": N * 8.0 * m ** 3 / (t / 1000.0) / 1e12}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -771,9 +803,18 @@ def main():
     ap.add_argument("--solve", default=None, choices=sorted(PAIR_CONFIGS),
                     help="only solve the held-out graph pairs with this time-to-gap configuration "
                          "(one JSON line; for profiling the search)")
-    ap.add_argument("--mode", default=None, choices=["bnb", "relax"],
-                    help="override the workload's measurement (relax: one relaxation launch per step)")
+    ap.add_argument("--mode", default=None, choices=["bnb", "relax", "gradient"],
+                    help="override the workload's measurement (relax: one relaxation launch per step; "
+                         "gradient: the batched gradient entry points alone, for profiling)")
+    ap.add_argument("--order", type=int, default=128, help="gradient mode: graph order")
+    ap.add_argument("--cases", type=int, default=4096, help="gradient mode: points per call")
+    ap.add_argument("--gradient", default="f32", choices=["f32", "mixed"], help="gradient mode: entry point")
     args = ap.parse_args()
+    if args.mode == "gradient":
+        from gpuboscia_gb300 import build
+        build.build()
+        run_gradient(args)
+        return
     if args.solve:
         from gpuboscia_gb300 import build
         build.build()

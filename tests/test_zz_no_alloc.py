@@ -89,3 +89,43 @@ def test_static_scratch_rejects_oversized_batches():
     rc = lib.gbx_relax_batch_static(C.byref(obj), C.byref(lmo), C.byref(alg), C.byref(b), None)
     assert rc == A.ERR_WORKSPACE
     assert b"static scratch" in lib.gbx_last_error()
+
+
+@pytest.mark.parametrize("order,nodes", [(120, 3), (400, 2)])
+def test_static_scratch_mixed_precision_twice(order, nodes):
+    """The mixed path keeps more in the scratch than the FP64 path: its FP32
+    arrays, the integer oracles' warm state and, at order 400, the oracle
+    costs, edge codes and the graphs' nonzero lists. Two calls in a row on
+    different batches must equal the caller-workspace variant (the mixed
+    path is deterministic at a fixed launch shape), so no word of the shared
+    array is read before the call writes it."""
+    import torch
+    assert torch.cuda.is_available()
+    from gpuboscia_gb300 import build
+    build.build()
+    lib = A.load()
+    dev = torch.device("cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    inst = (instances.birkhoff_regular_perturbed(order=order) if order == 120
+            else instances.birkhoff_regular_isomorphic(order=order))
+    keep = api._Keep()
+    obj = inst.objective.to_c("cuda", keep)
+    lmo = inst.lmo.to_c(order * order, "cuda", keep)
+    alg = A.Algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT, 4, 1e-10, 1e-14, A.PRECISION_MIXED)
+    for seed in (7, 8):
+        lb, ub = instances.birkhoff_node_batch(order, nodes, seed=seed)
+        eps = np.full(nodes, 1e-6)
+        need = lib.gbx_relax_workspace_bytes(C.byref(obj), C.byref(lmo), C.byref(alg), nodes)
+        assert 256 < need <= A.STATIC_SCRATCH_BYTES
+        b_ref, t_ref = _batch(lb, ub, eps, dev)
+        ws = torch.empty(need, dtype=torch.uint8, device=dev)
+        rc = lib.gbx_relax_batch(C.byref(obj), C.byref(lmo), C.byref(alg), C.byref(b_ref), ws.data_ptr(), need,
+                                 stream)
+        assert rc == A.OK, lib.gbx_last_error()
+        b_st, t_st = _batch(lb, ub, eps, dev)
+        rc = lib.gbx_relax_batch_static(C.byref(obj), C.byref(lmo), C.byref(alg), C.byref(b_st), stream)
+        assert rc == A.OK, lib.gbx_last_error()
+        torch.cuda.synchronize()
+        ref, got = _host(t_ref), _host(t_st)
+        for k in ref:
+            assert np.array_equal(ref[k], got[k]), k
