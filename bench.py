@@ -396,6 +396,52 @@ def relax_arms(inst, lb, ub, eps, w, iters, check_nodes=4):
     return out
 
 
+def cluster_arms(inst, w, lb, ub, eps, iters, sizes=(1, 38, 152)):
+    """Large orders, mixed precision: the cluster shape (four CTAs per node, the
+    oracle costs split across their shared memories) against one CTA per node
+    (two nodes per SM), on the first N nodes of the batch, one launch each
+    (CUDA events). Identical results; the question is time per launch."""
+    import torch
+    from gpuboscia_gb300 import _abi as A
+    from gpuboscia_gb300 import api
+    m = w["order"]
+    n = m * m
+    alg = A.Algorithm(w["alg"], w["ls"], 4, 1e-10, 1e-14, A.PRECISION_MIXED)
+    out = {}
+    try:
+        for N in sizes:
+            if N > lb.shape[0]:
+                continue
+            row = {}
+            for name, shape in (("one_cta", 0), ("cluster4", 2)):
+                api.set_launch_shape(inst.objective, inst.lmo, alg, n, -1, shape)
+                T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+                d_lb, d_ub, d_eps = T(lb[:N]), T(ub[:N]), T(eps[:N])
+                flags = T(np.ones(n, np.uint8))
+                x = d_lb.clone()
+                it = torch.zeros(N, dtype=torch.int32, device="cuda")
+                st = torch.zeros(N, dtype=torch.uint8, device="cuda")
+                rl = api.BatchRelaxer(inst.objective, inst.lmo, alg, x, d_lb, d_ub, d_eps, it, st, iters, flags, 1e-6,
+                                      torch.cuda.current_stream())
+                rl.launch()
+                x.copy_(d_lb)
+                it.zero_()
+                st.zero_()
+                torch.cuda.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                rl.launch()
+                b.record()
+                torch.cuda.synchronize()
+                ms = a.elapsed_time(b)
+                row[name] = {"ms": ms, "nodes_per_s": N / (ms / 1000.0), "x_sum": float(x.sum().item())}
+            row["same_iterates"] = row["one_cta"]["x_sum"] == row["cluster4"]["x_sum"]
+            out[f"nodes_{N}"] = row
+    finally:
+        api.set_launch_shape(inst.objective, inst.lmo, alg, n, -1, 0)
+    return out
+
+
 # ---------------------------------------------------------------- the search (bnb mode)
 def _host_available_bytes():
     try:
@@ -498,6 +544,8 @@ def run_bnb(args, rank, world):
 
     _, lb_r, ub_r, eps_r = make_workload(args.workload, min(args.relax_nodes, B), rank)
     arms = relax_arms(inst, lb_r, ub_r, eps_r, w, I, check_nodes=args.check_nodes)
+    if 128 < order <= 404 and args.cluster_arms:
+        arms["cluster_vs_one_cta"] = cluster_arms(inst, w, lb_r, ub_r, eps_r, I)
     cases = certified_cases(sc, args.ttg_limit) if args.ttg_limit > 0 else None
     if rank != 0:
         return
@@ -608,6 +656,8 @@ def run_relax(args, rank, world):
     stream = torch.cuda.current_stream()
     if args.launch_shape in ("tc", "simt"):
         api.set_launch_shape(inst.objective, inst.lmo, alg, n, 1 if args.launch_shape == "tc" else 0, 0)
+    elif args.launch_shape == "cluster":
+        api.set_launch_shape(inst.objective, inst.lmo, alg, n, -1, 2)
     relaxer = api.BatchRelaxer(inst.objective, inst.lmo, alg, x, d_lb, d_ub, d_eps, it, st, args.iters, d_flags,
                                1e-6, stream)
     if args.launch_shape == "tuned":
@@ -792,14 +842,17 @@ def main():
                     help="bnb mode: time budget of each order-120 search arm in seconds (0 skips them)")
     ap.add_argument("--relax-nodes", type=int, default=152,
                     help="bnb mode: open nodes of the relaxation-arm comparison (one wave of 152 SMs)")
+    ap.add_argument("--cluster-arms", type=int, default=1,
+                    help="bnb mode, orders 129..404: time the cluster shape against one CTA per node (0 skips)")
     ap.add_argument("--check-nodes", type=int, default=4,
                     help="bnb mode: nodes whose mixed certificate the oracle re-evaluates")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-budget", type=float, default=8.0)
-    ap.add_argument("--launch-shape", default="auto", choices=["auto", "tc", "simt", "tuned"],
-                    help="relax mode, mixed Birkhoff gradient: the default rule, tensor cores, FP32 SIMT "
-                         "(over the nonzero lists for sparse graphs above order 64), or the "
-                         "autotuner's choice on the batch (gbx_relax_autotune)")
+    ap.add_argument("--launch-shape", default="auto", choices=["auto", "tc", "simt", "tuned", "cluster"],
+                    help="relax mode, mixed Birkhoff: the default rule, tensor-core gradient, FP32 SIMT "
+                         "gradient (over the nonzero lists for sparse graphs above order 64), the "
+                         "autotuner's choice on the batch (gbx_relax_autotune), or a cluster of four CTAs "
+                         "per node (orders 129..404)")
     ap.add_argument("--solve", default=None, choices=sorted(PAIR_CONFIGS),
                     help="only solve the held-out graph pairs with this time-to-gap configuration "
                          "(one JSON line; for profiling the search)")

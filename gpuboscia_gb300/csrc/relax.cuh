@@ -54,6 +54,12 @@ struct Layout {
     // those orders keep each oracle warp's per-column Hungarian state in
     // shared memory (cs_bytes per warp at sm_cs), so two nodes fit on an SM
     size_t sm_cs, cs_bytes;
+    // a cluster of `cluster` CTAs per node (0: one CTA): cl_cols columns of
+    // packed oracle costs per CTA at sm_slice (the FP64 workspace shares it),
+    // two per-oracle workspaces of chw_bytes at sm_chw, the leader's
+    // row->column maps of both oracles at sm_lpi, the control block at sm_cl
+    int cluster, cl_cols;
+    size_t sm_slice, sm_chw, chw_bytes, sm_lpi, sm_cl;
     // the certificate's FP64 Hungarian reads the gradient staged in the cost
     // region (1), or straight from the node's gradient vector (0) when staging
     // would cost a resident node per SM
@@ -125,6 +131,33 @@ GBX_HD inline SparseAB sparse_at(unsigned char* base, int m, int cap) {
 enum { CS_COL, CS_PV, CS_MRAW, CS_WAY, CS_PJ, CS_USED, CS_UR, CS_RBR, CS_COUNT };
 GBX_HD inline size_t colstate_bytes(int cpl) { return (size_t)CS_COUNT * cpl * 32 * sizeof(int); }
 
+// Thread-block-cluster shape of the large-order mixed kernel (cluster.cuh):
+// kClCtas CTAs per node, each holding up to 32 * kClCpl columns of the
+// integer oracle costs.
+constexpr int kClCtas = 4;              // CTAs of a node's cluster
+constexpr int kClCpl = 4;               // columns per lane of a CTA's slice (slices of <= 128 columns)
+enum { CL_ORACLE = 1, CL_EXIT = 2 };
+
+// control block of a CTA (the leader's fields are the ones read remotely)
+struct ClCtl {
+    uint64_t bar_go;      // helpers: the leader posted a command (1 arrival)
+    uint64_t bar_done;    // leader: every helper acknowledged the exit (kClCtas - 1 arrivals)
+    int cmd[4];           // leader: op, cost shift, in-face restriction unchanged, DICG
+    int released;         // leader: the helpers have left
+    int err;              // a bounded wait gave up
+};
+
+// scal: [0] warm state valid, [1] shift of the stored potentials, [2] k+1 of the
+// cached restriction (0: none), [3] first compacted column of this slice,
+// [4] compacted columns of this slice, [5] phase events so far, [6] step
+// exchanges so far, [8..11] / [12..15] receive slots of the final reductions
+
+GBX_HD inline size_t chw_bytes(int m) {
+    return align16((size_t)13 * (m + 1) * sizeof(int)) + align16(3 * 128 * sizeof(int)) + 16 * sizeof(int)
+           + align16((size_t)CS_COUNT * kClCpl * 32 * sizeof(int)) + align16(2 * kClCtas * 8 * sizeof(int))
+           + 16 * sizeof(int) + 2 * kClCtas * sizeof(int) + align16((size_t)m + 1);
+}
+
 // bytes of one FP64 Hungarian workspace (potentials, minv, path, forced maps)
 GBX_HD inline size_t hung_ws_bytes(int m) {
     size_t b = 0;
@@ -162,7 +195,7 @@ void set_last_error(const std::string& msg);
 // Launch shape chosen by the autotuner (-1: the default rule).
 struct Variant {
     int tc = -1;          // mixed Birkhoff: 1 tensor-core gradient, 0 FP32 SIMT gradient
-    int persistent = -1;  // 1 persistent grid, 0 one CTA per node
+    int persistent = -1;  // 1 persistent grid, 0 one CTA per node, 2 a cluster of kClCtas CTAs per node
 };
 int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a,
                 int n_nodes, Layout* L, std::string* err, const Variant* v = nullptr);

@@ -10,6 +10,8 @@ extern template int launch_mix<GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BIRKHOFF, 2>(cons
                                                                              std::string*);
 extern template int launch_mix<GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BIRKHOFF, 3>(const Params&, cudaStream_t,
                                                                              std::string*);
+extern template int launch_cluster<GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BIRKHOFF>(const Params&, cudaStream_t,
+                                                                            std::string*);
 template int launch_one<GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BIRKHOFF>(const Params&, cudaStream_t, std::string*);
 template int launch_one<GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BOX>(const Params&, cudaStream_t, std::string*);
 }  // namespace gbx

@@ -209,6 +209,35 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
     L.cs_bytes = mixed && L.cost_global ? colstate_bytes(l.order <= 256 ? 8 : 16) : 0;
     L.sm_cs = p; p += 2 * L.cs_bytes;
     L.sm_total = p;
+    if (v.persistent == 2) {
+        // a cluster of kClCtas CTAs per node (large orders, mixed precision):
+        // each CTA holds a slice of the packed oracle costs; the leader's FP64
+        // workspace (feasibility, certificate) shares the slice's memory, used
+        // only while no oracle runs
+        if (!mixed || !L.cost_global || L.tc || o.kind != GBX_OBJ_GRAPH_MATCHING || l.kind != GBX_LMO_BIRKHOFF) {
+            *err = "a cluster per node covers mixed-precision graph matching over the Birkhoff polytope above order 128";
+            return GBX_ERR_UNSUPPORTED;
+        }
+        const int S = (l.order + kClCtas - 1) / kClCtas;
+        const size_t slice = align16((size_t)l.order * S * sizeof(int));
+        const size_t chw = align16(chw_bytes(l.order));
+        const size_t lpi = align16(4 * (size_t)l.order * sizeof(int));
+        const size_t total = slice + 2 * chw + lpi + align16(sizeof(ClCtl));
+        if (S > 32 * kClCpl || total > kSmemBudget || L.hung_bytes > slice) {
+            *err = "a cluster per node: the cost slices of this order do not fit in shared memory (orders 129..404)";
+            return GBX_ERR_UNSUPPORTED;
+        }
+        L.cluster = kClCtas;
+        L.cl_cols = S;
+        L.chw_bytes = chw;
+        L.persistent = 0;
+        L.sm_slice = 0;
+        L.sm_hung = 0;
+        L.sm_chw = slice;
+        L.sm_lpi = slice + 2 * chw;
+        L.sm_cl = L.sm_lpi + lpi;
+        L.sm_total = L.sm_cl + align16(sizeof(ClCtl));
+    }
     L.mixed_node_bytes = L.mx_global ? (mx_bytes + 255) / 256 * 256 : 0;
     if (L.tc) L.mixed_node_bytes += kTcImageBytes;
     L.mx_cost_off = L.mx_code_off = 0;
@@ -273,6 +302,12 @@ std::vector<Variant> candidate_variants(const gbx_objective& o, const gbx_lmo& l
             v.persistent = pers;
             out.push_back(v);
         }
+    // a cluster of CTAs per node where it applies (large-order mixed graph matching)
+    Variant cl;
+    cl.persistent = 2;
+    Layout L;
+    std::string err;
+    if (make_layout(o, l, a, 1, &L, &err, &cl) == GBX_OK) out.push_back(cl);
     return out;
 }
 

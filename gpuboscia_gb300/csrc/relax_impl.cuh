@@ -295,6 +295,7 @@ static __device__ double perm_value(const Ctx& c, const int* pi, int* pinv) {
 }  // namespace gbx
 #include "mixed.cuh"
 #include "tc_grad.cuh"
+#include "cluster.cuh"
 namespace gbx {
 
 // ------------------------------------------------------------------ Hungarian
@@ -1562,13 +1563,15 @@ static __device__ inline uint8_t* mixed_codes(const Params& P, unsigned char* ds
 // iterate X in place and returns the cumulative iteration count; the caller
 // then computes the FP64 certificate at the returned iterate. MODE 1: FP32
 // SIMT gradient; 2: tensor-core gradient; 3: large orders (costs in the
-// workspace, FP32 gradient over the nonzero lists, 16 columns per lane).
+// workspace, FP32 gradient over the nonzero lists, 16 columns per lane);
+// 4: large orders on a cluster of CTAs (the leader's side; cluster.cuh).
 template <int MODE>
 static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, int node, double* X,
                           const double* LB, const double* UB, double* best, double& best_val,
                           double eps, int it0, bool dicg, int ls, double cutv) {
     constexpr bool TC = MODE == 2;
-    constexpr bool BIG = MODE == 3;
+    constexpr bool CL = MODE == 4;
+    constexpr bool BIG = MODE == 3 || CL;
     const Layout& L = P.L;
     const int n = c.n, m = c.m, tid = c.tid;
     unsigned char* mx = L.mx_global ? P.mixed + (size_t)node * L.mixed_node_bytes : dsm + L.sm_mx;
@@ -1584,8 +1587,17 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
     int* costa = costf + n;   // in-face oracle costs (negated, face only), unless derived on the fly
     uint8_t* code = mixed_codes(P, dsm, node);   // edge codes, with the iterate's face bits
     const bool derive = L.derive_inface != 0;
-    const IHW w0 = ihw_at(dsm + L.sm_ihw, m);
-    const IHW w1 = ihw_at(dsm + L.sm_ihw + L.ihw_bytes, m);
+    // the oracles' row->column maps (and scratch inverses): the integer
+    // Hungarian workspaces, or on a cluster the leader's four arrays
+    IHW w0 = ihw_at(dsm + L.sm_ihw, m);
+    IHW w1 = ihw_at(dsm + L.sm_ihw + L.ihw_bytes, m);
+    if constexpr (CL) {
+        int* lpi = reinterpret_cast<int*>(dsm + L.sm_lpi);
+        w0.pi = lpi;
+        w0.pinv = lpi + m;
+        w1.pi = lpi + 2 * m;
+        w1.pinv = lpi + 3 * m;
+    }
     const double tol = c.tol;
     // tensor-core gradient: operand images in the cost matrices' shared memory,
     // the node's A / -B images after its FP32 arrays in the workspace
@@ -1650,15 +1662,17 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
         asm volatile("mov.u32 %0, %%warpid;" : "=r"(slot));
         s_owarp = ((slot >> 3) & 1) ? 2 : 0;
     }
-    if (tid == 0) { w0.scal[0] = 0; w0.scal[1] = 0; w0.scal[2] = 0; }
-    if (tid == 32) { w1.scal[0] = 0; w1.scal[1] = 0; w1.scal[2] = 0; }
-    // warm state of every column: the in-face oracle's free columns change with
-    // the face, so a column may be read before any call has written it
-    for (int j = tid; j < m; j += kThreads) {
-        w0.colpot[j] = 0;
-        w1.colpot[j] = 0;
-        w0.match[j] = -1;
-        w1.match[j] = -1;
+    if constexpr (!CL) {   // (a cluster's oracles reset their state at launch)
+        if (tid == 0) { w0.scal[0] = 0; w0.scal[1] = 0; w0.scal[2] = 0; }
+        if (tid == 32) { w1.scal[0] = 0; w1.scal[1] = 0; w1.scal[2] = 0; }
+        // warm state of every column: the in-face oracle's free columns change with
+        // the face, so a column may be read before any call has written it
+        for (int j = tid; j < m; j += kThreads) {
+            w0.colpot[j] = 0;
+            w1.colpot[j] = 0;
+            w0.match[j] = -1;
+            w1.match[j] = -1;
+        }
     }
     if (tid == 0) c.flag[4] = 0;  // set when a face-forced bit of x changes
     if (tid == 0) c.flag[5] = 0;  // set when a tensor-core wait timed out
@@ -1720,6 +1734,35 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
             frexpf(limit / gmx, &ex);
             shift = max(-120, min(120, ex - 1));
         }
+        if constexpr (CL) {
+            // post the command, stage this CTA's slice, run the oracle warps
+            // with the helpers (each CTA scales its own slice of the costs)
+            ClCtl* ctl = reinterpret_cast<ClCtl*>(dsm + L.sm_cl);
+            if (tid == 0) {
+                ctl->cmd[0] = CL_ORACLE;
+                ctl->cmd[1] = shift;
+                ctl->cmd[2] = c.flag[4] == 0 ? 1 : 0;
+                ctl->cmd[3] = dicg ? 1 : 0;
+            }
+            __threadfence();
+            __syncthreads();
+            if (tid == 0) {
+                cl_fence();
+                for (int r = 1; r < kClCtas; ++r) cl_arrive(cl_map(&ctl->bar_go, (unsigned)r));
+            }
+            int* slice = reinterpret_cast<int*>(dsm + L.sm_slice);
+            cl_stage(slice, L.cl_cols, 0, m, gf, code, shift);
+            __syncthreads();
+            const int wid = tid >> 5;
+            if (wid == 0 || (dicg && wid == 1)) {
+                const bool ok = wid == 0
+                    ? cl_hungarian<0>(chw_at(dsm + L.sm_chw, m), slice, L.cl_cols, m, shift, code, true, w0.pi,
+                                      &ctl->err)
+                    : cl_hungarian<2>(chw_at(dsm + L.sm_chw + L.chw_bytes, m), slice, L.cl_cols, m, shift, code,
+                                      c.flag[4] == 0, w1.pi, &ctl->err);
+                if ((tid & 31) == 0) c.flag[wid == 0 ? 0 : 2] = ok;
+            }
+        } else {
         for (int e = tid; e < n; e += kThreads) {
             const int ci = __float2int_rn(scalbnf(gf[e], shift));
             const bool allowed = (code[e] & kAllowed) != 0;
@@ -1753,6 +1796,7 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
             }
             if ((threadIdx.x & 31) == 0) c.flag[fwd ? 0 : 2] = ok;
         }
+        }   // one CTA's oracles
         __syncthreads();
         if (tid == 0) c.flag[4] = 0;
         if (!c.flag[0] || (dicg && !c.flag[2])) break;
@@ -1865,6 +1909,7 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
         }
         __syncthreads();
     }
+    if constexpr (CL) cl_release(reinterpret_cast<ClCtl*>(dsm + L.sm_cl));   // the helpers leave
     if constexpr (tcg) {
         // a gradient that timed out may still have MMAs in flight: wait (bounded)
         // for them before the accumulator columns are released
@@ -2200,7 +2245,11 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
             int* cpi = hw1.pi;
             int* cpinv = hw1.pinv;
             if constexpr (kMixedLoop) {
-                if (L.hung_warps < 2) {
+                if (L.cluster) {
+                    // the leader's in-face map arrays are free now
+                    cpi = reinterpret_cast<int*>(dsm + L.sm_lpi) + 2 * c.m;
+                    cpinv = cpi + c.m;
+                } else if (L.hung_warps < 2) {
                     // one FP64 workspace: the in-face integer oracle's arrays are free now
                     const IHW wi = ihw_at(dsm + L.sm_ihw + L.ihw_bytes, c.m);
                     cpi = wi.pi;
@@ -2255,6 +2304,40 @@ __global__ void __launch_bounds__(kThreads, (MIX == 1 || MIX == 3) ? 2 : 1) rela
         if (node >= n_nodes) return;
         relax_node<OK, LK, MIX>(P, node, dsm, sh);
         __syncthreads();
+    }
+}
+
+// A cluster of kClCtas CTAs per node (the large-order mixed relaxation of
+// cluster.cuh): CTA 0 relaxes the node, the others serve its oracles until
+// it lets them go. Every CTA resets its oracle state and barriers before the
+// cluster barrier that opens the launch, so no remote arrive meets an
+// uninitialised barrier.
+template <int OK, int LK>
+__global__ void __cluster_dims__(kClCtas, 1, 1) __launch_bounds__(kThreads, 1)
+    relax_cluster_kernel(const __grid_constant__ Params P) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ Scalars sh;
+    const Layout& L = P.L;
+    const int m = P.obj.order;
+    ClCtl* ctl = reinterpret_cast<ClCtl*>(dsm + L.sm_cl);
+    if (threadIdx.x == 0) {
+        cl_bar_init(&ctl->bar_go, 1);
+        cl_bar_init(&ctl->bar_done, kClCtas - 1);
+        ctl->released = 0;
+        ctl->err = 0;
+        chw_reset(chw_at(dsm + L.sm_chw, m));
+        chw_reset(chw_at(dsm + L.sm_chw + L.chw_bytes, m));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    cl_sync_all();
+    const int node = (int)(blockIdx.x / kClCtas);
+    const int n_nodes = P.live_count ? min(*P.live_count, P.b.n_nodes) : P.b.n_nodes;
+    if (cl_rank() == 0) {
+        if (node < n_nodes) relax_node<OK, LK, 4>(P, node, dsm, sh);
+        cl_release(ctl);   // (an infeasible or absent node lets the helpers go here)
+    } else {
+        cl_helper(P, node, dsm);
     }
 }
 
@@ -2374,9 +2457,29 @@ int launch_mix(const Params& p, cudaStream_t st, std::string* err) {
     return GBX_OK;
 }
 
+// The cluster launch: kClCtas CTAs per node (grid = nodes * kClCtas).
+template <int OK, int LK>
+int launch_cluster(const Params& p, cudaStream_t st, std::string* err) {
+    if constexpr (OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF) {
+        auto k = relax_cluster_kernel<OK, LK>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.L.sm_total);
+        if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+        k<<<p.b.n_nodes * kClCtas, kThreads, p.L.sm_total, st>>>(p);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+        return GBX_OK;
+    } else {
+        (void)p;
+        (void)st;
+        *err = "a cluster per node covers mixed-precision graph matching over the Birkhoff polytope";
+        return GBX_ERR_UNSUPPORTED;
+    }
+}
+
 template <int OK, int LK>
 int launch_one(const Params& p, cudaStream_t st, std::string* err) {
     if constexpr (OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF) {
+        if (p.L.cluster) return launch_cluster<OK, LK>(p, st, err);
         if (p.L.mixed) {
             if (p.L.tc) return launch_mix<OK, LK, 2>(p, st, err);
             if (p.L.cost_global) return launch_mix<OK, LK, 3>(p, st, err);

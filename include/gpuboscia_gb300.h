@@ -191,19 +191,25 @@ int gbx_relax_batch_static(const gbx_objective* obj, const gbx_lmo* lmo,
 /* Autotuner (no counterpart in the reference): times each candidate launch
  * shape of this problem on the caller's batch -- the tensor-core or FP32 SIMT
  * gradient where both apply (mixed precision, Birkhoff orders 17..90), one CTA
- * per node or a persistent grid pulling nodes from a queue -- keeping the
+ * per node or a persistent grid pulling nodes from a queue, and for mixed
+ * precision at Birkhoff orders 129..404 a cluster of four CTAs per node that
+ * splits the assignment oracles' columns (the replacement of the reference's
+ * MultiBlock backend, include/gpuboscia/multiblock.cuh:36-103) -- keeping the
  * fastest of `repeats` runs each, and makes the winner the shape that later
  * gbx_relax_batch calls of the same problem shape use (process-wide). The
  * batch's x, iterations and status are restored, so the caller still owns an
  * unrelaxed batch. workspace: gbx_relax_workspace_bytes (it covers every
- * shape). chosen (may be NULL) receives {tensor-core gradient, persistent}. */
+ * shape). chosen (may be NULL) receives {tensor-core gradient, persistent}
+ * with persistent 2 for the cluster shape. */
 int gbx_relax_autotune(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
                        const gbx_node_batch* batch, void* workspace, size_t workspace_bytes,
                        void* stream, int repeats, int* chosen);
 
 /* Pins the launch shape of this problem shape by hand (what the autotuner
  * would store): tensor_core -1/0/1 (default rule / FP32 SIMT / tensor-core
- * gradient; mixed precision only), persistent 0/1. */
+ * gradient; mixed precision only), persistent 0/1/2 (one CTA per node /
+ * persistent grid / a cluster of four CTAs per node: mixed precision, Birkhoff
+ * orders 129..404; GBX_ERR_UNSUPPORTED elsewhere). */
 int gbx_relax_set_launch_shape(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
                                int tensor_core, int persistent);
 

@@ -304,3 +304,25 @@ def test_lmo_feasibility_gradient_tensors_are_checked():
                         A.Algorithm(A.ALG_FRANK_WOLFE, A.LS_OPEN_LOOP, 4, 1e-10, 1e-14, A.PRECISION_FP64),
                         f64(N, 4), f64(N, 4), f64(N, 4), f64(N), torch.zeros(N, dtype=torch.int32),
                         torch.zeros(N, dtype=torch.uint8), 10)
+
+
+def test_cluster_launch_shape_only_where_it_applies(lib):
+    """Persistent 2 (a cluster of four CTAs per node) pins only for mixed
+    precision graph matching over the Birkhoff polytope at orders 129..404;
+    elsewhere it is refused on the host, without a GPU."""
+    keep = api._Keep()
+    mixed = A.Algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT, 4, 1e-10, 1e-14, A.PRECISION_MIXED)
+    fp64 = A.Algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT, 4, 1e-10, 1e-14, A.PRECISION_FP64)
+    for order, alg, ok in ((400, mixed, True), (300, mixed, True), (36, mixed, False), (400, fp64, False),
+                           (500, mixed, False)):
+        o = api.GraphMatchingObjective(np.zeros((order, order)), np.zeros((order, order))).to_c("host", keep)
+        lm = api.BirkhoffLMO(order).to_c(order * order, "host", keep)
+        rc = lib.gbx_relax_set_launch_shape(C.byref(o), C.byref(lm), C.byref(alg), -1, 2)
+        assert (rc == A.OK) == ok, (order, lib.gbx_last_error())
+        if ok:
+            # the cluster shape needs no workspace beyond the one-CTA shape's
+            assert lib.gbx_relax_workspace_bytes(C.byref(o), C.byref(lm), C.byref(alg), 4) > 0
+        assert lib.gbx_relax_set_launch_shape(C.byref(o), C.byref(lm), C.byref(alg), -1, 0) == A.OK
+    o = api.GraphMatchingObjective(np.zeros((400, 400)), np.zeros((400, 400))).to_c("host", keep)
+    lm = api.BirkhoffLMO(400).to_c(400 * 400, "host", keep)
+    assert lib.gbx_relax_set_launch_shape(C.byref(o), C.byref(lm), C.byref(mixed), -1, 3) == A.ERR_INVALID
