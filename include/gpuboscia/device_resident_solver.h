@@ -116,6 +116,29 @@ struct DRSSchedulingEvent {
 };
 
 namespace gpuboscia {
+
+// How the engine relaxes a batch when the objective is not a built-in kind:
+// the workspace it needs and the launch (user_relax.cuh provides both for
+// user-written device objectives). Empty: the library's gbx_relax_batch.
+struct RelaxHooks {
+    std::function<size_t(const gbx_lmo&, int)> workspace_bytes;
+    std::function<int(const gbx_lmo&, const gbx_algorithm&, const gbx_node_batch&, void*, size_t, cudaStream_t)>
+        launch;
+};
+
+// Built-in objective kinds describe themselves to the C ABI (descriptor());
+// any other objective type is a user-written device objective.
+template <class T, class = void>
+struct HasDescriptor : std::false_type {};
+template <class T>
+struct HasDescriptor<T, std::void_t<decltype(std::declval<const T&>().descriptor())>> : std::true_type {};
+
+// The relaxation of a user objective type: defined by <gpuboscia/user_relax.cuh>,
+// which the translation unit that calls solve() with such a type must include
+// (compiled by nvcc).
+template <class Obj, class = void>
+struct UserRelax;
+
 namespace detail {
 
 inline void gbx_check(int rc, const char* what) {
@@ -130,9 +153,9 @@ inline void gbx_check(int rc, const char* what) {
 class BnBEngine {
 public:
     BnBEngine(const Problem& prob, const gbx_objective& obj, const LMOSpec& lmo, const gbx_algorithm& alg,
-              BranchStrategy branch, DeviceResidentConfig cfg, double time_limit_seconds)
+              BranchStrategy branch, DeviceResidentConfig cfg, double time_limit_seconds, RelaxHooks hooks = {})
         : prob_(prob), obj_(obj), lmo_spec_(lmo), alg_(alg), branch_sel_(std::move(branch)), cfg_(cfg),
-          time_limit_seconds_(time_limit_seconds) {
+          time_limit_seconds_(time_limit_seconds), hooks_(std::move(hooks)) {
         if (cfg_.gpu_max_iters <= 0 || cfg_.gpu_batch_size <= 0 || cfg_.num_streams <= 0)
             throw std::invalid_argument("GPU iterations, batch size and streams must be positive");
         for (int j : prob_.int_vars)
@@ -154,6 +177,12 @@ public:
         if (cfg_.execution_mode == FWExecutionMode::MultiBlock && cfg_.blocks_per_node < 1)
             throw std::invalid_argument("MultiBlock blocks_per_node must be positive");
         alg_.precision = cfg_.precision;
+        if (hooks_.launch) {
+            if (cfg_.precision != GBX_PRECISION_FP64)
+                throw std::invalid_argument("mixed precision covers the built-in graph-matching objective only");
+            if (cfg_.device_frontier)
+                throw std::invalid_argument("the device frontier relaxes the built-in objective kinds only");
+        }
         const int n = prob_.n_vars;
         lmo_ = gbx_lmo{};
         lmo_.kind = lmo_spec_.kind;
@@ -170,7 +199,8 @@ public:
             GBX_CUDA_CHECK(cudaMemcpy(d_lmo_is_int_, lmo_spec_.is_int.data(), n, cudaMemcpyHostToDevice));
             lmo_.is_int = d_lmo_is_int_;
         }
-        ws_bytes_ = gbx_relax_workspace_bytes(&obj_, &lmo_, &alg_, cfg_.gpu_batch_size);
+        ws_bytes_ = hooks_.launch ? hooks_.workspace_bytes(lmo_, cfg_.gpu_batch_size)
+                                  : gbx_relax_workspace_bytes(&obj_, &lmo_, &alg_, cfg_.gpu_batch_size);
         if (ws_bytes_ == 0) gbx_check(GBX_ERR_INVALID, "gbx_relax_workspace_bytes");
         slots_.resize(cfg_.num_streams);
         for (int i = 0; i < cfg_.num_streams; ++i) alloc_slot(slots_[i], i);
@@ -299,7 +329,7 @@ private:
             return nullptr;
         }
         cudaMemcpyAsync(s.d, s.h, s.o_gap, cudaMemcpyHostToDevice, s.stream);
-        const int rc = gbx_relax_batch(&obj_, &lmo_, &alg_, &b, s.ws, ws_bytes_, s.stream);
+        const int rc = relax_call(b, s);
         cudaMemcpyAsync(s.h + s.o_x, s.d + s.o_x, s.end - s.o_x, cudaMemcpyDeviceToHost, s.stream);
         const cudaError_t e = cudaStreamEndCapture(s.stream, &graph);
         cudaGraphExec_t exec = nullptr;
@@ -347,6 +377,12 @@ private:
         return depth_dependent_tolerance(cfg_.gpu_eps, cfg_.gpu_eps_decay, cfg_.gpu_eps_min, nd.depth);
     }
     bool should_prune(const Node& nd) const { return nd.dual_bound >= incumbent_.get(); }
+    // one batch relaxation on the slot's stream: the library's kernel, or the
+    // user objective's template kernel
+    int relax_call(const gbx_node_batch& b, Slot& s) {
+        if (hooks_.launch) return hooks_.launch(lmo_, alg_, b, s.ws, ws_bytes_, s.stream);
+        return gbx_relax_batch(&obj_, &lmo_, &alg_, &b, s.ws, ws_bytes_, s.stream);
+    }
     double global_live_bound(double inc) const {
         return std::min(queue_.best_bound(inc), active_bounds_.best_bound(inc));
     }
@@ -445,7 +481,7 @@ private:
         b.best_vertex_val = at<double>(s.d, s.o_bvv);
         b.integer_flags = d_flags_;
         b.cutoff = cfg_.incumbent_cutoff ? at<double>(s.d, s.o_cut) : nullptr;
-        if (cfg_.autotune && !tuned_ && N == cfg_.gpu_batch_size) {
+        if (cfg_.autotune && !tuned_ && N == cfg_.gpu_batch_size && !hooks_.launch) {
             // once, on the first full batch: the tuner relaxes it under every launch
             // shape and restores it, and later launches (and graphs) use the winner
             tuned_ = true;
@@ -458,7 +494,7 @@ private:
             GBX_CUDA_CHECK(cudaGraphLaunch(exec, s.stream));
         } else {
             GBX_CUDA_CHECK(cudaMemcpyAsync(s.d, s.h, s.o_gap, cudaMemcpyHostToDevice, s.stream));
-            gbx_check(gbx_relax_batch(&obj_, &lmo_, &alg_, &b, s.ws, ws_bytes_, s.stream), "gbx_relax_batch");
+            gbx_check(relax_call(b, s), "gbx_relax_batch");
             GBX_CUDA_CHECK(cudaMemcpyAsync(s.h + s.o_x, s.d + s.o_x, s.end - s.o_x, cudaMemcpyDeviceToHost,
                                            s.stream));
         }
@@ -736,6 +772,7 @@ private:
     BranchStrategy branch_sel_;
     DeviceResidentConfig cfg_;
     double time_limit_seconds_;
+    RelaxHooks hooks_;
 
     ConcurrentQueue queue_;
     ConcurrentBoundSet active_bounds_;
@@ -783,10 +820,25 @@ public:
                                DeviceResidentConfig cfg = {}, LMO lmo = {},
                                double time_limit_seconds = std::numeric_limits<double>::infinity(),
                                Heuristic = {})
-        : BnBEngine(check_size(prob), obj.descriptor(), lmo.spec(prob.n_vars), alg.descriptor(),
-                    std::move(branch_sel), cfg, time_limit_seconds) {}
+        : BnBEngine(check_size(prob), objective_descriptor(obj), lmo.spec(prob.n_vars), alg.descriptor(),
+                    std::move(branch_sel), cfg, time_limit_seconds, hooks_for(obj)) {}
 
 private:
+    // built-in kinds go to the library; a user objective (the reference's
+    // device-struct extension point) to its template kernel (user_relax.cuh)
+    static gbx_objective objective_descriptor(const DeviceObjective& obj) {
+        if constexpr (gpuboscia::HasDescriptor<DeviceObjective>::value) {
+            return obj.descriptor();
+        } else {
+            gbx_objective o{};
+            o.n = DeviceObjective::n_vars;
+            return o;
+        }
+    }
+    static gpuboscia::RelaxHooks hooks_for(const DeviceObjective& obj) {
+        if constexpr (gpuboscia::HasDescriptor<DeviceObjective>::value) return {};
+        else return gpuboscia::UserRelax<DeviceObjective>::hooks(obj);
+    }
     static const Problem& check_size(const Problem& prob) {
         if (prob.n_vars != DeviceObjective::n_vars)
             throw std::runtime_error("DeviceObjective::n_vars does not match Problem::n_vars");
