@@ -233,6 +233,8 @@ def config_dict(args):
         d["l2"] = "flushed between timed steps (256 MiB write)"
     if getattr(args, "launch_shape", "auto") != "auto":
         d["launch_shape"] = args.launch_shape
+    if getattr(args, "oracle_warps", -1) != -1:
+        d["oracle_warps"] = args.oracle_warps
         if getattr(args, "tuned_shape", None):
             d["tuned_shape"] = {"tensor_core": args.tuned_shape[0], "persistent": args.tuned_shape[1]}
     return d
@@ -397,10 +399,11 @@ def relax_arms(inst, lb, ub, eps, w, iters, check_nodes=4):
 
 
 def cluster_arms(inst, w, lb, ub, eps, iters, sizes=(1, 38, 152)):
-    """Large orders, mixed precision: the cluster shape (four CTAs per node, the
-    oracle costs split across their shared memories) against one CTA per node
-    (two nodes per SM), on the first N nodes of the batch, one launch each
-    (CUDA events). Identical results; the question is time per launch."""
+    """Large orders, mixed precision: one CTA per node (two nodes per SM) with
+    each integer oracle on four warps (the default) or on one warp, and the
+    cluster shape (four CTAs per node, the oracle costs split across their
+    shared memories), on the first N nodes of the batch, one launch each (CUDA
+    events). Identical results; the question is time per launch."""
     import torch
     from gpuboscia_gb300 import _abi as A
     from gpuboscia_gb300 import api
@@ -413,8 +416,8 @@ def cluster_arms(inst, w, lb, ub, eps, iters, sizes=(1, 38, 152)):
             if N > lb.shape[0]:
                 continue
             row = {}
-            for name, shape in (("one_cta", 0), ("cluster4", 2)):
-                api.set_launch_shape(inst.objective, inst.lmo, alg, n, -1, shape)
+            for name, shape, ow in (("one_cta", 0, -1), ("one_cta_one_warp_oracles", 0, 1), ("cluster4", 2, -1)):
+                api.set_launch_shape(inst.objective, inst.lmo, alg, n, -1, shape, oracle_warps=ow)
                 T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
                 d_lb, d_ub, d_eps = T(lb[:N]), T(ub[:N]), T(eps[:N])
                 flags = T(np.ones(n, np.uint8))
@@ -435,7 +438,7 @@ def cluster_arms(inst, w, lb, ub, eps, iters, sizes=(1, 38, 152)):
                 torch.cuda.synchronize()
                 ms = a.elapsed_time(b)
                 row[name] = {"ms": ms, "nodes_per_s": N / (ms / 1000.0), "x_sum": float(x.sum().item())}
-            row["same_iterates"] = row["one_cta"]["x_sum"] == row["cluster4"]["x_sum"]
+            row["same_iterates"] = len({r["x_sum"] for r in row.values()}) == 1
             out[f"nodes_{N}"] = row
     finally:
         api.set_launch_shape(inst.objective, inst.lmo, alg, n, -1, 0)
@@ -658,6 +661,9 @@ def run_relax(args, rank, world):
         api.set_launch_shape(inst.objective, inst.lmo, alg, n, 1 if args.launch_shape == "tc" else 0, 0)
     elif args.launch_shape == "cluster":
         api.set_launch_shape(inst.objective, inst.lmo, alg, n, -1, 2)
+    if args.oracle_warps != -1:
+        api.set_launch_shape(inst.objective, inst.lmo, alg, n, -1, 2 if args.launch_shape == "cluster" else 0,
+                             oracle_warps=args.oracle_warps)
     relaxer = api.BatchRelaxer(inst.objective, inst.lmo, alg, x, d_lb, d_ub, d_eps, it, st, args.iters, d_flags,
                                1e-6, stream)
     if args.launch_shape == "tuned":
@@ -853,6 +859,8 @@ def main():
                          "gradient (over the nonzero lists for sparse graphs above order 64), the "
                          "autotuner's choice on the batch (gbx_relax_autotune), or a cluster of four CTAs "
                          "per node (orders 129..404)")
+    ap.add_argument("--oracle-warps", type=int, default=-1, choices=[-1, 1, 4],
+                    help="relax mode, mixed Birkhoff orders 129..512: warps per integer oracle (-1 default: 4)")
     ap.add_argument("--solve", default=None, choices=sorted(PAIR_CONFIGS),
                     help="only solve the held-out graph pairs with this time-to-gap configuration "
                          "(one JSON line; for profiling the search)")

@@ -225,6 +225,20 @@ int gbx_relax_set_launch_shape(const gbx_objective* obj, const gbx_lmo* lmo, con
     return GBX_OK;
 }
 
+int gbx_relax_set_oracle_warps(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg, int warps) {
+    const int rc = validate(obj, lmo, alg);
+    if (rc) return rc;
+    if (warps != -1 && warps != 1 && warps != 4) return fail(GBX_ERR_INVALID, "oracle warps: -1, 1 or 4");
+    gbx::Variant v = gbx::tuned_variant(*obj, *lmo, *alg);
+    v.oracle_warps = warps;
+    gbx::Layout L;
+    std::string err;
+    const int r = gbx::make_layout(*obj, *lmo, *alg, 1, &L, &err, &v);
+    if (r) return fail(r, err);
+    gbx::store_variant(*obj, *lmo, *alg, v);
+    return GBX_OK;
+}
+
 int gbx_lmo_batch(const gbx_lmo* lmo, int cases, int mode, const double* direction,
                   const double* x, const double* lb, const double* ub, double* out,
                   double* out_step, void* stream) {

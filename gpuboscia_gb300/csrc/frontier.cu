@@ -53,6 +53,7 @@
 #include <vector>
 
 #include "../../include/gpuboscia/gap_utils.h"
+#include "../../include/gpuboscia/nvtx.h"
 #include "features.h"
 #include "relax.cuh"
 #include "scorer_mlp.cuh"
@@ -1122,6 +1123,7 @@ int solve_device_frontier(const gbx_problem& pr, const gbx_objective& obj, const
     long long nodes_seen = 0;
     const auto t_search = std::chrono::steady_clock::now();   // the time limit counts from here
     for (;;) {
+        gpuboscia::detail::NvtxRange replay_range("gbx.frontier_rounds");
         if (exec) {
             e = cudaGraphLaunch(exec, st);
             if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }

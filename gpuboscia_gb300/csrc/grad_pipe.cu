@@ -146,11 +146,16 @@ __global__ void __launch_bounds__(kPipeThreads, 1) grad_pipe_kernel(const unsign
                     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(nx), "r"(bytes) : "memory");
             }
             // converter warp cw owns columns 32 cw .. 32 cw + 31; per instruction a
-            // warp covers 8 rows x 32 columns (lane -> row 8 rg + lane % 8, column
-            // block 4 cw + lane / 8): the 16-byte image stores of the 8 lanes of a
-            // row block fill one 128-byte core matrix
+            // warp covers 8 rows x 32 columns. Lane (Q, q) = (lane / 8, lane % 8)
+            // converts row 8 rg + q, column block cb = (Q + q / 2) % 4, and reads
+            // the half h = q % 2 of its 8 columns first: the eight 16-byte reads of
+            // a quarter warp then fall on eight different bank groups of the staged
+            // rows (all rows share the banks: the row stride is 128 floats), and
+            // its eight 16-byte image stores on eight different rows of core
+            // matrices -- neither side has a bank conflict
             const int cw = warp - 8;
-            const int c0 = 8 * (4 * cw + (lane >> 3));
+            const int cb = ((lane >> 3) + ((lane & 7) >> 1)) & 3, h = lane & 1;
+            const int c0 = 8 * (4 * cw + cb);
             const bool vec = (m & 3) == 0 && c0 + 8 <= m;
             bool stop = false;
             for (int q = 0; q < 4 && staged; ++q) {
@@ -163,10 +168,11 @@ __global__ void __launch_bounds__(kPipeThreads, 1) grad_pipe_kernel(const unsign
                     const int lr = 8 * t + (lane & 7), r = kStageRows * q + lr;
                     float v[8];
                     if (r < m && vec) {
-                        const float4 a = *reinterpret_cast<const float4*>(st + lr * m + c0);
-                        const float4 b4 = *reinterpret_cast<const float4*>(st + lr * m + c0 + 4);
-                        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-                        v[4] = b4.x; v[5] = b4.y; v[6] = b4.z; v[7] = b4.w;
+                        const float4 a = *reinterpret_cast<const float4*>(st + lr * m + c0 + 4 * h);
+                        const float4 b4 = *reinterpret_cast<const float4*>(st + lr * m + c0 + 4 * (1 - h));
+                        const float4 lo4 = h ? b4 : a, hi4 = h ? a : b4;
+                        v[0] = lo4.x; v[1] = lo4.y; v[2] = lo4.z; v[3] = lo4.w;
+                        v[4] = hi4.x; v[5] = hi4.y; v[6] = hi4.z; v[7] = hi4.w;
                     } else {
 #pragma unroll
                         for (int e = 0; e < 8; ++e) v[e] = (r < m && c0 + e < m) ? st[lr * m + c0 + e] : 0.f;

@@ -622,6 +622,306 @@ __device__ bool int_hungarian_warp_cs(const IHW& w, int* cs, int m, const int* c
     __syncwarp();
     return true;
 }
+// ---- the same integer Hungarian on a group of four warps (large orders).
+// At orders above 128 the costs come from L2 and a Dijkstra step of one warp
+// scans up to 16 columns per lane; on four warps (one per SM sub-partition)
+// a lane scans a quarter of them, and the four warps' best keys meet in
+// shared memory behind one named barrier per step. Group g is threads
+// [128g, 128g+128) with named barrier 1+g; thread gt of the group owns the
+// compacted columns gt+1, gt+129, ... (CPL per thread, k <= 128*CPL), its
+// column state at cs[(a*CPL + t)*128 + gt] (colstate_bytes(4*CPL) bytes, the
+// single-warp layout of 4*CPL columns per lane). The steps, the tie rule
+// (lowest column) and the warm state are those of int_hungarian_warp_cs, so
+// the assignment, the kept potentials and the matching are identical; every
+// early return is group-uniform. All 128 threads of the group call it.
+__device__ __forceinline__ void oracle_group_bar(int g) {
+    asm volatile("bar.sync %0, 128;" :: "r"(1 + g) : "memory");
+}
+
+template <int CPL, int FACE>
+__device__ bool int_hungarian_group_cs(const IHW& w, int* cs, int m, const int* costs, int shift,
+                                       const uint8_t* code, bool restrict_same, int g) {
+    constexpr int GT = 128, GW = 4;
+    __shared__ int s_key[2][2][GW];   // [group][step parity][warp]: packed (slack, column) keys
+    __shared__ int s_fbv[2][2][GW];   // the two-reduction path: slack and column per warp
+    __shared__ int s_fbj[2][2][GW];
+    __shared__ int s_red[2][GW];      // group min / and
+    __shared__ int s_k[2];
+    const int gt = (int)threadIdx.x - GT * g, lane = gt & 31, gw = gt >> 5;
+    auto S = [&](int a, int t) -> int& { return cs[(a * CPL + t) * GT + gt]; };
+    auto O = [&](int a, int t, int o) -> int& { return cs[(a * CPL + t) * GT + o]; };
+    auto cost_at = [&](int e) -> int {
+        const int c0 = costs[e];
+        if constexpr (FACE == 2) return (c0 < kIntInf && (code[e] & kFaceIn)) ? -c0 : kIntInf;
+        else return c0;
+    };
+    auto group_min = [&](int v) -> int {
+        v = __reduce_min_sync(kFull, v);
+        if (lane == 0) s_red[g][gw] = v;
+        oracle_group_bar(g);
+        int r = s_red[g][0];
+#pragma unroll
+        for (int q = 1; q < GW; ++q) r = min(r, s_red[g][q]);
+        oracle_group_bar(g);
+        return r;
+    };
+    auto group_all = [&](bool b) -> bool { return group_min(b ? 1 : 0) != 0; };
+    int k;
+    if (restrict_same && w.scal[2] > 0) {
+        k = w.scal[2] - 1;
+    } else {
+        for (int i = gt; i < m; i += GT) { w.fcol[i] = -1; w.frow[i] = -1; }
+        oracle_group_bar(g);
+        bool ok = true;
+        const int nn = m * m;
+        for (int e = gt; e < nn; e += GT) {
+            const uint8_t c = code[e];
+            if (c & kBad) ok = false;
+            const bool forced = (c & kForced) || (FACE != 0 && (c & kFaceOne));
+            if (forced) {
+                const int r = e / m, col = e - r * m;
+                if (!(c & kAllowed)) ok = false;
+                if (atomicCAS(&w.fcol[r], -1, col) != -1) ok = false;
+                if (atomicCAS(&w.frow[col], -1, r) != -1) ok = false;
+            }
+        }
+        if (!group_all(ok)) return false;
+        if (gw == 0) {   // compaction in index order on the first warp
+            const unsigned lt = (1u << lane) - 1u;
+            int kr = 0, kc = 0;
+            for (int base = 0; base < m; base += 32) {
+                const int i = base + lane;
+                const bool fr = i < m && w.fcol[i] < 0;
+                const bool fc = i < m && w.frow[i] < 0;
+                const unsigned mr = __ballot_sync(kFull, fr), mc = __ballot_sync(kFull, fc);
+                if (fr) w.rows[kr + __popc(mr & lt)] = i;
+                if (i < m) w.rowpos[i] = fr ? kr + __popc(mr & lt) + 1 : 0;
+                if (fc) w.cols[kc + __popc(mc & lt)] = i;
+                kr += __popc(mr);
+                kc += __popc(mc);
+            }
+            if (lane == 0) s_k[g] = (kr != kc || kr > GT * CPL) ? -1 : kr;
+        }
+        oracle_group_bar(g);
+        k = s_k[g];
+        if (k < 0) return false;
+        for (int i = gt + 1; i <= k; i += GT) w.rowb[i] = w.rows[i - 1] * m;
+        if (gt == 0) w.scal[2] = k + 1;
+        oracle_group_bar(g);
+    }
+    const bool warm = w.scal[0] != 0;
+    const int dshift = shift - w.scal[1];
+    for (int t = 0; t < CPL; ++t) {
+        const int j = gt + 1 + GT * t;
+        const bool valid = j <= k;
+        const int col = valid ? w.cols[j - 1] : 0;
+        long long v = 0;
+        if (valid && warm) {
+            v = w.colpot[col];
+            if (dshift > 0) v = dshift >= 24 ? 0 : v * (1ll << dshift);
+            else if (dshift < 0) v = -dshift >= 40 ? 0 : (v >> (-dshift));
+            v = max(-kPotLimit, min(kPotLimit, v));
+        }
+        S(CS_COL, t) = col;
+        S(CS_PV, t) = (int)v;
+        S(CS_PJ, t) = 0;
+        S(CS_UR, t) = 0;
+        S(CS_RBR, t) = 0;
+        if (valid) w.pvs[j] = (int)v;
+    }
+    oracle_group_bar(g);
+    // row potentials u_i = min_j (c_ij - v_j), one row per thread
+    bool rows_ok = true;
+    for (int i = gt + 1; i <= k; i += GT) {
+        const int rb = w.rowb[i];
+        int best = kIntInf, barg = 0;
+        int j = 1;
+        for (; j + 7 <= k; j += 8) {
+            int cc[8], pp[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) { cc[q] = cost_at(rb + w.cols[j - 1 + q]); pp[q] = w.pvs[j + q]; }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (cc[q] < kIntInf && cc[q] - pp[q] < best) { best = cc[q] - pp[q]; barg = j + q; }
+        }
+        for (; j <= k; ++j) {
+            const int c = cost_at(rb + w.cols[j - 1]);
+            if (c < kIntInf && c - w.pvs[j] < best) { best = c - w.pvs[j]; barg = j; }
+        }
+        if (best >= kIntInf) rows_ok = false;
+        w.u[i] = best;
+        w.pinv[i - 1] = barg;   // a tight column of row i (pinv is free during the call)
+        w.rmatch[i] = 0;
+    }
+    if (!group_all(rows_ok)) return false;
+    // keep the previous matching where its edge is still allowed and tight
+    if (warm) {
+        for (int t = 0; t < CPL; ++t) {
+            if (gt + 1 + GT * t > k) continue;
+            const int col = S(CS_COL, t);
+            const int r = w.match[col];
+            if (r < 0 || r >= m) continue;
+            const int i = w.rowpos[r];
+            if (i <= 0) continue;
+            const int c = cost_at(r * m + col);
+            const int ui = w.u[i];
+            if (c < kIntInf && c - ui - S(CS_PV, t) == 0) {
+                S(CS_PJ, t) = i;
+                S(CS_UR, t) = ui;
+                S(CS_RBR, t) = w.rowb[i];
+                w.rmatch[i] = 1;
+            }
+        }
+    }
+    oracle_group_bar(g);
+    // greedy tight matching: every free row claims its tight column, the lowest
+    // row wins a contested free column
+    {
+        int* claim = w.pi;   // per compacted column; pi is rewritten at the end
+        for (int t = 0; t < CPL; ++t)
+            if (gt + 1 + GT * t <= k) claim[gt + GT * t] = S(CS_PJ, t) ? 0 : 0x7fffffff;
+        oracle_group_bar(g);
+        for (int i = gt + 1; i <= k; i += GT)
+            if (!w.rmatch[i]) atomicMin(&claim[w.pinv[i - 1] - 1], i);
+        oracle_group_bar(g);
+        for (int t = 0; t < CPL; ++t) {
+            if (gt + 1 + GT * t > k || S(CS_PJ, t)) continue;
+            const int r = claim[gt + GT * t];
+            if (r != 0x7fffffff) {
+                S(CS_PJ, t) = r;
+                S(CS_UR, t) = w.u[r];
+                S(CS_RBR, t) = w.rowb[r];
+                w.rmatch[r] = 1;
+            }
+        }
+        oracle_group_bar(g);
+    }
+    bool feasible = true;
+    int par = 0;
+    for (int i = 1; i <= k && feasible; ++i) {
+        if (w.rmatch[i]) continue;
+        for (int t = 0; t < CPL; ++t) {
+            S(CS_MRAW, t) = kIntInf;
+            S(CS_WAY, t) = 0;
+            S(CS_USED, t) = -1;
+        }
+        int j0 = 0, D = 0;
+        int ui0 = w.u[i], rb = w.rowb[i];
+        bool augmented = false;
+        for (int step = 0; step <= k; ++step) {
+            int bv = kIntInf, bj = 0x7fffffff;
+            int cv[CPL];
+#pragma unroll
+            for (int t = 0; t < CPL; ++t) cv[t] = cost_at(rb + S(CS_COL, t));
+#pragma unroll
+            for (int t = 0; t < CPL; ++t) {
+                const bool live = gt + 1 + GT * t <= k && S(CS_USED, t) < 0;
+                const int c = cv[t];
+                int mr = S(CS_MRAW, t);
+                if (live && c < kIntInf) {
+                    const int cur = c - ui0 - S(CS_PV, t) + D;
+                    if (cur < mr) { mr = cur; S(CS_MRAW, t) = cur; S(CS_WAY, t) = j0; }
+                }
+                if (live && mr < bv) { bv = mr; bj = gt + 1 + GT * t; }
+            }
+            const int key = bv < kPackLimit ? (bv << 10) | bj : 0x7fffffff;
+            const int wk = __reduce_min_sync(kFull, key);
+            if (lane == 0) s_key[g][par][gw] = wk;
+            oracle_group_bar(g);
+            int kmin = s_key[g][par][0];
+#pragma unroll
+            for (int q = 1; q < GW; ++q) kmin = min(kmin, s_key[g][par][q]);
+            int gmin, j1;
+            if (kmin != 0x7fffffff) {
+                gmin = kmin >> 10;
+                j1 = kmin & 1023;
+            } else {
+                // every slack is large: minimum slack, then the lowest column at it
+                const int wb = __reduce_min_sync(kFull, bv);
+                const int wj = __reduce_min_sync(kFull, bv == wb ? bj : 0x7fffffff);
+                if (lane == 0) { s_fbv[g][par][gw] = wb; s_fbj[g][par][gw] = wj; }
+                oracle_group_bar(g);
+                gmin = s_fbv[g][par][0];
+                j1 = s_fbj[g][par][0];
+#pragma unroll
+                for (int q = 1; q < GW; ++q) {
+                    const int vq = s_fbv[g][par][q], jq = s_fbj[g][par][q];
+                    if (vq < gmin || (vq == gmin && jq < j1)) { gmin = vq; j1 = jq; }
+                }
+                if (gmin >= kIntInf) { feasible = false; break; }
+            }
+            par ^= 1;
+            D = gmin;
+            const int owner = (j1 - 1) & (GT - 1), slot = (j1 - 1) >> 7;
+            const int pnext = O(CS_PJ, slot, owner);
+            const int unext = O(CS_UR, slot, owner);
+            const int rnext = O(CS_RBR, slot, owner);
+            if (gt == owner) S(CS_USED, slot) = D;
+            j0 = j1;
+            if (pnext == 0) { augmented = true; break; }
+            ui0 = unext;
+            rb = rnext;
+        }
+        if (!feasible || !augmented) { feasible = false; break; }
+        // apply the potentials of this path (before the matching flips)
+        const int uroot = w.u[i] + D;
+        for (int t = 0; t < CPL; ++t) {
+            const int ua = S(CS_USED, t);
+            if (ua < 0) continue;
+            const int d = D - ua;
+            S(CS_PV, t) -= d;
+            S(CS_UR, t) += d;
+        }
+        oracle_group_bar(g);
+        // flip the path on one thread: column j takes the row (and its
+        // potential / offset) of way[j], from the path's end back to its root
+        if (gt == 0) {
+            int j = j0;
+            for (int guard = 0; guard <= k && j != 0; ++guard) {
+                const int owner = (j - 1) & (GT - 1), slot = (j - 1) >> 7;
+                const int jp = O(CS_WAY, slot, owner);
+                int np = i, nu = uroot, nr = w.rowb[i];
+                if (jp != 0) {
+                    const int po = (jp - 1) & (GT - 1), ps = (jp - 1) >> 7;
+                    np = O(CS_PJ, ps, po);
+                    nu = O(CS_UR, ps, po);
+                    nr = O(CS_RBR, ps, po);
+                }
+                O(CS_PJ, slot, owner) = np;
+                O(CS_UR, slot, owner) = nu;
+                O(CS_RBR, slot, owner) = nr;
+                j = jp;
+            }
+        }
+        oracle_group_bar(g);
+    }
+    if (!feasible) return false;
+    // outputs and the warm state for the next call (original indices)
+    for (int i = gt; i < m; i += GT)
+        if (w.fcol[i] >= 0) { w.pi[i] = w.fcol[i]; w.match[w.fcol[i]] = i; }
+    int lo = kIntInf;
+    for (int t = 0; t < CPL; ++t) {
+        if (gt + 1 + GT * t > k) continue;
+        const int col = S(CS_COL, t);
+        const int r = w.rows[S(CS_PJ, t) - 1];
+        w.pi[r] = col;
+        w.match[col] = r;
+        lo = min(lo, S(CS_PV, t));
+    }
+    lo = group_min(lo);
+    if (lo >= kIntInf) lo = 0;
+    bool sane = true;
+    for (int t = 0; t < CPL; ++t) {
+        if (gt + 1 + GT * t > k) continue;
+        const int v = S(CS_PV, t) - lo;
+        w.colpot[S(CS_COL, t)] = v;
+        sane = sane && v <= kPotLimit;
+    }
+    sane = group_all(sane);
+    if (gt == 0) { w.scal[0] = sane ? 1 : 0; w.scal[1] = shift; }
+    oracle_group_bar(g);
+    return true;
+}
 
 // Block-wide max of |v| over n floats (broadcast).
 static __device__ float bmax_abs(const float* v, int n, double* red) {

@@ -54,6 +54,10 @@ struct Layout {
     // those orders keep each oracle warp's per-column Hungarian state in
     // shared memory (cs_bytes per warp at sm_cs), so two nodes fit on an SM
     size_t sm_cs, cs_bytes;
+    // ... and run each integer oracle on a group of four warps (forward on
+    // warps 0-3, in-face on 4-7: a quarter of the columns per lane and step)
+    // instead of one warp
+    int oracle_group;
     // a cluster of `cluster` CTAs per node (0: one CTA): cl_cols columns of
     // packed oracle costs per CTA at sm_slice (the FP64 workspace shares it),
     // two per-oracle workspaces of chw_bytes at sm_chw, the leader's
@@ -196,6 +200,7 @@ void set_last_error(const std::string& msg);
 struct Variant {
     int tc = -1;          // mixed Birkhoff: 1 tensor-core gradient, 0 FP32 SIMT gradient
     int persistent = -1;  // 1 persistent grid, 0 one CTA per node, 2 a cluster of kClCtas CTAs per node
+    int oracle_warps = -1;  // large-order mixed Birkhoff: warps per integer oracle, 1 or 4
 };
 int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a,
                 int n_nodes, Layout* L, std::string* err, const Variant* v = nullptr);

@@ -209,6 +209,16 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
     L.cs_bytes = mixed && L.cost_global ? colstate_bytes(l.order <= 256 ? 8 : 16) : 0;
     L.sm_cs = p; p += 2 * L.cs_bytes;
     L.sm_total = p;
+    // large orders: each integer oracle on four warps unless pinned to one
+    L.oracle_group = (L.cs_bytes && v.oracle_warps != 1) ? 1 : 0;
+    if (v.oracle_warps != -1 && v.oracle_warps != 1 && v.oracle_warps != 4) {
+        *err = "oracle warps: 1 or 4";
+        return GBX_ERR_INVALID;
+    }
+    if (v.oracle_warps == 4 && !L.cs_bytes) {
+        *err = "four warps per oracle cover mixed-precision Birkhoff orders 129..512";
+        return GBX_ERR_UNSUPPORTED;
+    }
     if (v.persistent == 2) {
         // a cluster of kClCtas CTAs per node (large orders, mixed precision):
         // each CTA holds a slice of the packed oracle costs; the leader's FP64
@@ -228,6 +238,7 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
             return GBX_ERR_UNSUPPORTED;
         }
         L.cluster = kClCtas;
+        L.oracle_group = 0;
         L.cl_cols = S;
         L.chw_bytes = chw;
         L.persistent = 0;
@@ -295,13 +306,20 @@ std::vector<Variant> candidate_variants(const gbx_objective& o, const gbx_lmo& l
     if (a.precision == GBX_PRECISION_MIXED && o.kind == GBX_OBJ_GRAPH_MATCHING && l.kind == GBX_LMO_BIRKHOFF
             && l.order > 16 && l.order <= 128)
         tcs = {l.order > 64 ? 1 : 0, l.order > 64 ? 0 : 1};
+    // large-order mixed Birkhoff: one or four warps per integer oracle
+    std::vector<int> ows = {-1};
+    if (a.precision == GBX_PRECISION_MIXED && o.kind == GBX_OBJ_GRAPH_MATCHING && l.kind == GBX_LMO_BIRKHOFF
+            && l.order > 128 && l.order <= 512)
+        ows = {4, 1};
     for (int tc : tcs)
-        for (int pers : {0, 1}) {
-            Variant v;
-            v.tc = tc;
-            v.persistent = pers;
-            out.push_back(v);
-        }
+        for (int ow : ows)
+            for (int pers : {0, 1}) {
+                Variant v;
+                v.tc = tc;
+                v.persistent = pers;
+                v.oracle_warps = ow;
+                out.push_back(v);
+            }
     // a cluster of CTAs per node where it applies (large-order mixed graph matching)
     Variant cl;
     cl.persistent = 2;

@@ -1771,7 +1771,25 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
         }
         __syncthreads();
         const int owarp = (int)(threadIdx.x >> 5) - s_owarp;
-        if (owarp == 0 || (dicg && owarp == 1)) {
+        bool group_done = false;
+        if constexpr (BIG) {
+            if (L.oracle_group) {   // forward oracle on warps 0-3, in-face on warps 4-7
+                group_done = true;
+                const int g = tid >> 7;
+                if (g == 0 || dicg) {
+                    int* cs = reinterpret_cast<int*>(dsm + L.sm_cs + (g == 0 ? 0 : L.cs_bytes));
+                    bool ok;
+                    if (m <= 256)
+                        ok = g == 0 ? int_hungarian_group_cs<2, 0>(w0, cs, m, costf, shift, code, true, 0)
+                                    : int_hungarian_group_cs<2, 1>(w1, cs, m, costa, shift, code, c.flag[4] == 0, 1);
+                    else
+                        ok = g == 0 ? int_hungarian_group_cs<4, 0>(w0, cs, m, costf, shift, code, true, 0)
+                                    : int_hungarian_group_cs<4, 1>(w1, cs, m, costa, shift, code, c.flag[4] == 0, 1);
+                    if ((tid & 127) == 0) c.flag[g == 0 ? 0 : 2] = ok;
+                }
+            }
+        }
+        if (!group_done && (owarp == 0 || (dicg && owarp == 1))) {
             const bool fwd = owarp == 0;
             const IHW& w = fwd ? w0 : w1;
             const bool same = fwd || c.flag[4] == 0;

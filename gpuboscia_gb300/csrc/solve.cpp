@@ -115,6 +115,7 @@ public:
             GBX_CUDA_CHECK(cudaMalloc(&d_feat_, cap_ * F * sizeof(float)));
             GBX_CUDA_CHECK(cudaMalloc(&d_score_, cap_ * sizeof(float)));
         }
+        gpuboscia::detail::NvtxRange range("gbx.scorer");
         GBX_CUDA_CHECK(cudaMemcpyAsync(d_feat_, h_feat_.data(), R * F * sizeof(float), cudaMemcpyHostToDevice, st_));
         if (gbx_scorer_forward(s_, (int)R, d_feat_, d_score_, s_->params_bf16 ? 1 : 0, st_) != GBX_OK)
             throw std::runtime_error(std::string("scorer: ") + gbx_last_error());

@@ -39,6 +39,7 @@
 #include "algorithms.h"
 #include "atomic_incumbent.h"
 #include "bnb.h"
+#include "nvtx.h"
 #include "branching.h"
 #include "concurrent_queue.h"
 #include "dense_quadratic_objectives.h"
@@ -440,6 +441,7 @@ private:
     }
 
     void submit_slot(Slot& s, std::vector<Node> batch) {
+        detail::NvtxRange range("gbx.dispatch");
         const int n = prob_.n_vars;
         const int N = (int)batch.size();
         layout(s, N);
@@ -491,10 +493,18 @@ private:
         }
         cudaGraphExec_t exec = cfg_.use_cuda_graph ? slot_graph(s, N, b) : nullptr;
         if (exec) {
+            detail::NvtxRange r("gbx.graph_replay");   // upload, relaxation, download
             GBX_CUDA_CHECK(cudaGraphLaunch(exec, s.stream));
         } else {
-            GBX_CUDA_CHECK(cudaMemcpyAsync(s.d, s.h, s.o_gap, cudaMemcpyHostToDevice, s.stream));
-            gbx_check(relax_call(b, s), "gbx_relax_batch");
+            {
+                detail::NvtxRange r("gbx.h2d");
+                GBX_CUDA_CHECK(cudaMemcpyAsync(s.d, s.h, s.o_gap, cudaMemcpyHostToDevice, s.stream));
+            }
+            {
+                detail::NvtxRange r("gbx.relax");
+                gbx_check(relax_call(b, s), "gbx_relax_batch");
+            }
+            detail::NvtxRange r("gbx.d2h");
             GBX_CUDA_CHECK(cudaMemcpyAsync(s.h + s.o_x, s.d + s.o_x, s.end - s.o_x, cudaMemcpyDeviceToHost,
                                            s.stream));
         }
@@ -607,6 +617,7 @@ private:
     }
 
     void process_completed_batch(Completed& batch) {
+        detail::NvtxRange range("gbx.complete");
         const int n = prob_.n_vars;
         const int N = (int)batch.nodes.size();
         call_branch_hook(batch);

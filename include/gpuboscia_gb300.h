@@ -213,6 +213,17 @@ int gbx_relax_autotune(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_a
 int gbx_relax_set_launch_shape(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
                                int tensor_core, int persistent);
 
+/* Pins how many warps run each integer assignment oracle of a large-order
+ * mixed-precision Birkhoff relaxation (orders 129..512, one CTA per node or the
+ * persistent grid): 1 (one warp per oracle, the forward and in-face oracles on
+ * two warps) or 4 (a group of four warps per oracle, one per SM sub-partition,
+ * each lane scanning a quarter of the columns of a Dijkstra step); -1 restores
+ * the default (4). The assignments are identical either way. Keeps the pinned
+ * or tuned tensor-core / persistent choice; gbx_relax_set_launch_shape resets
+ * this to the default. GBX_ERR_UNSUPPORTED for 4 outside those orders. */
+int gbx_relax_set_oracle_warps(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
+                               int warps);
+
 /* Batched LMO calls, one case per row (the probes of tests/test_pipeline.cu:
  * 96-163). mode 0: forward v = argmin <direction, v> over the node's set
  * (LMO::compute_v); mode 1: in-face away oracle (LMO::compute_inface_v) on

@@ -326,3 +326,25 @@ def test_cluster_launch_shape_only_where_it_applies(lib):
     o = api.GraphMatchingObjective(np.zeros((400, 400)), np.zeros((400, 400))).to_c("host", keep)
     lm = api.BirkhoffLMO(400).to_c(400 * 400, "host", keep)
     assert lib.gbx_relax_set_launch_shape(C.byref(o), C.byref(lm), C.byref(mixed), -1, 3) == A.ERR_INVALID
+
+
+def test_oracle_warps_only_where_they_apply(lib):
+    """Four warps per integer oracle pin only for the large-order mixed
+    Birkhoff kernel (orders 129..512); one warp and the default pin anywhere;
+    other counts are argument errors. All checked on the host."""
+    keep = api._Keep()
+    mixed = A.Algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT, 4, 1e-10, 1e-14, A.PRECISION_MIXED)
+    fp64 = A.Algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT, 4, 1e-10, 1e-14, A.PRECISION_FP64)
+    for order, alg, ok in ((400, mixed, True), (200, mixed, True), (500, mixed, True), (120, mixed, False),
+                           (36, mixed, False), (400, fp64, False)):
+        o = api.GraphMatchingObjective(np.zeros((order, order)), np.zeros((order, order))).to_c("host", keep)
+        lm = api.BirkhoffLMO(order).to_c(order * order, "host", keep)
+        rc = lib.gbx_relax_set_oracle_warps(C.byref(o), C.byref(lm), C.byref(alg), 4)
+        assert (rc == A.OK) == ok, (order, lib.gbx_last_error())
+        if not ok:
+            assert rc == A.ERR_UNSUPPORTED
+        assert lib.gbx_relax_set_oracle_warps(C.byref(o), C.byref(lm), C.byref(alg), 1) == A.OK
+        assert lib.gbx_relax_set_oracle_warps(C.byref(o), C.byref(lm), C.byref(alg), -1) == A.OK
+        for bad in (0, 2, 8):
+            assert lib.gbx_relax_set_oracle_warps(C.byref(o), C.byref(lm), C.byref(alg), bad) == A.ERR_INVALID
+            assert "oracle warps" in lib.gbx_last_error().decode()

@@ -1,7 +1,8 @@
-"""The large-order mixed relaxation on a thread-block cluster (four CTAs per
-node, the oracle costs split across their shared memories, each Dijkstra
-step's argmin reduced through distributed shared memory) against the one-CTA
-kernel: the split oracles compute the same assignments, tie-breaks and warm
+"""The large-order mixed relaxation's launch shapes against each other: a
+thread-block cluster (four CTAs per node, the oracle costs split across their
+shared memories, each Dijkstra step's argmin reduced through distributed shared
+memory) against the one-CTA kernel, and four warps per integer oracle against
+one. The split oracles compute the same assignments, tie-breaks and warm
 state, so the relaxations are identical bit for bit -- iterate, gap, value,
 status, iterations and best vertex."""
 import numpy as np
@@ -20,7 +21,8 @@ def _dev(a, dtype=None):
 
 def _relax(inst, alg, lb, ub, iters, shape):
     m = inst.lmo.order
-    api.set_launch_shape(inst.objective, inst.lmo, alg, m * m, -1, shape)
+    if shape is not None:
+        api.set_launch_shape(inst.objective, inst.lmo, alg, m * m, -1, shape)
     N = lb.shape[0]
     x = _dev(lb.copy())
     it = _dev(np.zeros(N), np.int32)
@@ -51,3 +53,33 @@ def test_cluster_relaxation_equals_one_cta(cuda_lib, order, alg_kind):
     assert np.all(one["iterations"][:4] == 8)
     for k in one:
         assert np.array_equal(one[k], cl[k]), k
+
+
+def _relax_warps(inst, alg, lb, ub, iters, warps, persistent=0):
+    m = inst.lmo.order
+    api.set_launch_shape(inst.objective, inst.lmo, alg, m * m, -1, persistent, oracle_warps=warps)
+    return _relax(inst, alg, lb, ub, iters, None)
+
+
+@pytest.mark.parametrize("order,alg_kind,persistent", [(400, A.ALG_DICG, 0), (400, A.ALG_FRANK_WOLFE, 0),
+                                                        (300, A.ALG_DICG, 1), (200, A.ALG_DICG, 0)])
+def test_four_warp_oracles_equal_one_warp(cuda_lib, order, alg_kind, persistent):
+    """Each integer oracle on a group of four warps (a quarter of the columns
+    per lane and Dijkstra step, the warps' best keys meeting in shared memory)
+    computes the same assignments, ties and warm state as on one warp: the
+    relaxations are identical bit for bit."""
+    inst = (instances.birkhoff_regular_isomorphic(order=order) if order == 400
+            else instances.birkhoff_regular_perturbed(order=order, degree=10, swaps=20))
+    alg = A.Algorithm(alg_kind, A.LS_QUADRATIC_EXACT, 4, 1e-10, 1e-14, A.PRECISION_MIXED)
+    lb, ub = instances.birkhoff_node_batch(order, 6, seed=67)
+    lb[5, 0 * order + 0] = 1.0   # infeasible: a row forced twice
+    lb[5, 0 * order + 1] = 1.0
+    try:
+        one = _relax_warps(inst, alg, lb, ub, 10, 1, persistent)
+        four = _relax_warps(inst, alg, lb, ub, 10, 4, persistent)
+    finally:
+        api.set_launch_shape(inst.objective, inst.lmo, alg, order * order, -1, 0)
+    assert one["status"][5] == A.NODE_INFEASIBLE
+    assert np.all(one["iterations"][:5] >= 1)
+    for k in one:
+        assert np.array_equal(one[k], four[k]), k

@@ -176,3 +176,31 @@ int main() { const uint8_t s = DRSIntegralUnconverged | DRSInitialPointSupplied;
     subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
                     "-I", CUDA_INCLUDE, str(src), "-o", str(exe)], check=True)
     subprocess.run([str(exe)], check=True)
+
+
+@pytest.mark.parametrize("defines", [[], ["-DGBX_NO_NVTX"]])
+def test_nvtx_ranges_nest_and_compile_out(tmp_path, defines):
+    """The solver's NVTX ranges (dispatch, upload, relaxation, download,
+    completion, frontier replays) come from a header-only helper: ranges
+    nest and close on scope exit, cost nothing without a profiler attached,
+    and compile out under GBX_NO_NVTX."""
+    src = tmp_path / "nv.cpp"
+    src.write_text(r'''
+#include <gpuboscia/nvtx.h>
+#include <stdexcept>
+static int work(int k) {
+    gpuboscia::detail::NvtxRange r("gbx.test.outer");
+    { gpuboscia::detail::NvtxRange q("gbx.test.inner"); k += 1; }
+    if (k > 2) throw std::runtime_error("early exit closes the range");
+    return k;
+}
+int main() {
+    int s = work(0) + work(1);
+    try { work(5); } catch (const std::exception&) { s += 10; }
+    return s == 13 ? 0 : 1;
+}
+''')
+    exe = tmp_path / "nv"
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", *defines, "-I", str(ROOT / "include"),
+                    "-I", CUDA_INCLUDE, str(src), "-o", str(exe)], check=True)
+    subprocess.run([str(exe)], check=True)
