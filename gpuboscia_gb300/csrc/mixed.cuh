@@ -35,6 +35,17 @@ constexpr uint8_t kFaceIn = 32;    // x > 1e-9
 constexpr uint8_t kFaceOne = 64;   // x >= 1 - 1e-9
 constexpr uint8_t kFaceBits = kFaceIn | kFaceOne;
 
+// Packed costs (large orders): one array serves both oracles of an
+// iteration, (cost << 1) | face bit for an allowed edge, kIntInf otherwise.
+// FACE 3 reads it as the forward costs, FACE 4 as the in-face costs (the
+// negated cost on the iterate's face, kIntInf elsewhere) -- the values FACE 0
+// and FACE 1 read from two separate arrays, so the assignments are identical.
+__device__ __forceinline__ int packed_forward(int v) { return v >= kIntInf ? kIntInf : (v >> 1); }
+__device__ __forceinline__ int packed_inface(int v) { return (v < kIntInf && (v & 1)) ? -(v >> 1) : kIntInf; }
+__device__ __forceinline__ int pack_cost(int ci, bool allowed, bool face) {
+    return allowed ? (int)(((unsigned)ci << 1) | (face ? 1u : 0u)) : kIntInf;
+}
+
 struct IHW {
     int *u, *rowb, *pvs;                         // [m+1] row potentials, row offsets r*m, column potentials
     int *rows, *cols, *rowpos, *fcol, *frow, *pi, *colpot, *match, *pinv;  // [m]
@@ -103,6 +114,8 @@ __device__ bool int_hungarian_warp(const IHW& w, int m, const int* costs, int sh
     auto cost_at = [&](int e) -> int {
         const int c0 = costs[e];
         if constexpr (FACE == 2) return (c0 < kIntInf && (code[e] & kFaceIn)) ? -c0 : kIntInf;
+        else if constexpr (FACE == 3) return packed_forward(c0);
+        else if constexpr (FACE == 4) return packed_inface(c0);
         else return c0;
     };
     const unsigned lt = (1u << lane) - 1u;
@@ -117,7 +130,7 @@ __device__ bool int_hungarian_warp(const IHW& w, int m, const int* costs, int sh
         for (int e = lane; e < nn; e += 32) {
             const uint8_t c = code[e];
             if (c & kBad) ok = false;
-            const bool forced = (c & kForced) || (FACE != 0 && (c & kFaceOne));
+            const bool forced = (c & kForced) || (FACE != 0 && FACE != 3 && (c & kFaceOne));
             if (forced) {
                 const int r = e / m, col = e - r * m;
                 if (!(c & kAllowed)) ok = false;
@@ -383,6 +396,8 @@ __device__ bool int_hungarian_warp_cs(const IHW& w, int* cs, int m, const int* c
     auto cost_at = [&](int e) -> int {
         const int c0 = costs[e];
         if constexpr (FACE == 2) return (c0 < kIntInf && (code[e] & kFaceIn)) ? -c0 : kIntInf;
+        else if constexpr (FACE == 3) return packed_forward(c0);
+        else if constexpr (FACE == 4) return packed_inface(c0);
         else return c0;
     };
     const unsigned lt = (1u << lane) - 1u;
@@ -397,7 +412,7 @@ __device__ bool int_hungarian_warp_cs(const IHW& w, int* cs, int m, const int* c
         for (int e = lane; e < nn; e += 32) {
             const uint8_t c = code[e];
             if (c & kBad) ok = false;
-            const bool forced = (c & kForced) || (FACE != 0 && (c & kFaceOne));
+            const bool forced = (c & kForced) || (FACE != 0 && FACE != 3 && (c & kFaceOne));
             if (forced) {
                 const int r = e / m, col = e - r * m;
                 if (!(c & kAllowed)) ok = false;
@@ -653,6 +668,8 @@ __device__ bool int_hungarian_group_cs(const IHW& w, int* cs, int m, const int* 
     auto cost_at = [&](int e) -> int {
         const int c0 = costs[e];
         if constexpr (FACE == 2) return (c0 < kIntInf && (code[e] & kFaceIn)) ? -c0 : kIntInf;
+        else if constexpr (FACE == 3) return packed_forward(c0);
+        else if constexpr (FACE == 4) return packed_inface(c0);
         else return c0;
     };
     auto group_min = [&](int v) -> int {
@@ -677,7 +694,7 @@ __device__ bool int_hungarian_group_cs(const IHW& w, int* cs, int m, const int* 
         for (int e = gt; e < nn; e += GT) {
             const uint8_t c = code[e];
             if (c & kBad) ok = false;
-            const bool forced = (c & kForced) || (FACE != 0 && (c & kFaceOne));
+            const bool forced = (c & kForced) || (FACE != 0 && FACE != 3 && (c & kFaceOne));
             if (forced) {
                 const int r = e / m, col = e - r * m;
                 if (!(c & kAllowed)) ok = false;

@@ -1550,6 +1550,214 @@ static __device__ void grad_f32_sparse(const SparseAB& S, int m, float two_s, co
     __syncthreads();
 }
 
+// The same R and G for large orders, where X and R live in the workspace,
+// bit-identical to grad_f32_sparse. X is sparse (a convex combination of a few
+// permutations), so R = A X - X B is built from X's nonzeros: a pass lists
+// each row's nonzeros (ascending columns) in the scratch `xc`, `xv`, `xn`;
+// then warp w takes rows w, w+8, ... and accumulates row i of R in its
+// shared-memory buffer `rows + w*m`: first the rows k of X for the neighbours
+// k of i in A (ascending), then, for each nonzero X[i][l] (ascending l), row l
+// of B. Every element receives the same multiply-adds in the same order as
+// grad_f32_sparse, minus those whose X factor is zero, which leave the sum
+// unchanged (a sum started at +0 never becomes -0). G = 2s (A'R - R B') reads
+// R densely: the rows of R named by column p of A (coalesced, the list held
+// in the lanes' registers), and row p of R staged in the same buffer for the
+// gathers through B's rows. B's rows are staged in `lst` when they fit in
+// `lst_bytes`, otherwise read from the lists in global memory.
+template <int NJ>
+static __device__ void grad_f32_rows(const SparseAB& S, int m, float two_s, const float* X, float* R, float* G,
+                                     float* rows, unsigned char* lst, size_t lst_bytes, uint16_t* xc, float* xv,
+                                     int* xn) {
+    constexpr int PB = 8;   // neighbour rows of X fetched together
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    float* acc = rows + (size_t)warp * m;
+    // B's rows (list 3): staged in shared memory when they fit
+    const int nb = S.ptr[3][m];
+    const size_t o_idx = align16((size_t)(m + 1) * sizeof(int));
+    const size_t o_val = o_idx + align16((size_t)nb * sizeof(uint16_t));
+    const bool staged = lst && o_val + align16((size_t)nb * sizeof(float)) <= lst_bytes && m <= 65535;
+    const int* bptr = staged ? reinterpret_cast<const int*>(lst) : S.ptr[3];
+    const uint16_t* sidx = reinterpret_cast<const uint16_t*>(lst + o_idx);
+    const float* sval = reinterpret_cast<const float*>(lst + o_val);
+    if (staged) {
+        int* p = reinterpret_cast<int*>(lst);
+        uint16_t* ix = reinterpret_cast<uint16_t*>(lst + o_idx);
+        float* vl = reinterpret_cast<float*>(lst + o_val);
+        for (int q = threadIdx.x; q <= m; q += kThreads) p[q] = S.ptr[3][q];
+        for (int t = threadIdx.x; t < nb; t += kThreads) {
+            ix[t] = (uint16_t)S.idx[3][t];
+            vl[t] = (float)S.val[3][t];
+        }
+    }
+    auto bcol = [&](int t) -> int { return staged ? (int)sidx[t] : S.idx[3][t]; };
+    auto bv = [&](int t) -> float { return staged ? sval[t] : (float)S.val[3][t]; };
+    // X's nonzeros, row by row, ascending columns (NaN counts as nonzero)
+    for (int i = warp; i < m; i += kWarps) {
+        int cnt = 0;
+#pragma unroll 4
+        for (int j0 = 0; j0 < m; j0 += 32) {
+            const int j = j0 + lane;
+            const float v = j < m ? X[(size_t)i * m + j] : 0.f;
+            const bool nz = j < m && v != 0.f;
+            const unsigned b = __ballot_sync(kFull, nz);
+            if (nz) {
+                const int o = cnt + __popc(b & lt);
+                xc[(size_t)i * m + o] = (uint16_t)j;
+                xv[(size_t)i * m + o] = v;
+            }
+            cnt += __popc(b);
+        }
+        if (lane == 0) xn[i] = cnt;
+    }
+    __syncthreads();
+    // R, row by row
+    for (int i = warp; i < m; i += kWarps) {
+        for (int j = lane; j < m; j += 32) acc[j] = 0.f;
+        __syncwarp();
+        const int a0 = S.ptr[0][i], a1 = S.ptr[0][i + 1];
+        for (int tb = a0; tb < a1; tb += PB) {
+            const int tc = min(PB, a1 - tb);
+            int kk = 0, nk = 0;
+            float aa = 0.f;
+            if (lane < tc) {
+                kk = S.idx[0][tb + lane];
+                aa = (float)S.val[0][tb + lane];
+                nk = xn[kk];
+            }
+            // the first 32 nonzeros of each neighbour row, all in flight together
+            int pc[PB];
+            float pv[PB];
+#pragma unroll
+            for (int u = 0; u < PB; ++u) {
+                const int k = __shfl_sync(kFull, kk, u);
+                const int cn = __shfl_sync(kFull, nk, u);
+                pc[u] = -1;
+                pv[u] = 0.f;
+                if (u < tc && lane < cn) {
+                    pc[u] = xc[(size_t)k * m + lane];
+                    pv[u] = xv[(size_t)k * m + lane];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < PB; ++u) {
+                if (u >= tc) break;
+                const float a = __shfl_sync(kFull, aa, u);
+                const int cn = __shfl_sync(kFull, nk, u);
+                if (pc[u] >= 0) acc[pc[u]] = fmaf(a, pv[u], acc[pc[u]]);
+                if (cn > 32) {
+                    const int k = __shfl_sync(kFull, kk, u);
+                    for (int e = 32 + lane; e < cn; e += 32) {
+                        const int j = xc[(size_t)k * m + e];
+                        acc[j] = fmaf(a, xv[(size_t)k * m + e], acc[j]);
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        // - X B: for each nonzero X[i][l], ascending l, row l of B
+        const int ci = xn[i];
+        for (int eb = 0; eb < ci; eb += 32) {
+            int lc = 0;
+            float lx = 0.f;
+            if (eb + lane < ci) {
+                lc = xc[(size_t)i * m + eb + lane];
+                lx = xv[(size_t)i * m + eb + lane];
+            }
+            const int ec = min(32, ci - eb);
+            for (int u = 0; u < ec; ++u) {
+                const int l = __shfl_sync(kFull, lc, u);
+                const float x = __shfl_sync(kFull, lx, u);
+                const int b0 = bptr[l], b1 = bptr[l + 1];
+                for (int t = b0 + lane; t < b1; t += 32) {
+                    const int j = bcol(t);
+                    acc[j] = fmaf(-x, bv(t), acc[j]);
+                }
+                __syncwarp();
+            }
+        }
+        for (int j = lane; j < m; j += 32) R[(size_t)i * m + j] = acc[j];
+        __syncwarp();
+    }
+    __syncthreads();
+    // G's gathers through B's rows read them as a padded table when it fits
+    // (entry u of row q at u*m + q: a warp's reads of one entry are
+    // consecutive, free of bank conflicts)
+    __shared__ int s_dmax;
+    if (threadIdx.x == 0) s_dmax = 0;
+    __syncthreads();
+    {
+        int dl = 0;
+        for (int q = threadIdx.x; q < m; q += kThreads) dl = max(dl, S.ptr[3][q + 1] - S.ptr[3][q]);
+        if (dl) atomicMax(&s_dmax, dl);
+    }
+    __syncthreads();
+    const int D = s_dmax;
+    const size_t e_val = align16((size_t)D * m * sizeof(uint16_t));
+    const size_t e_len = e_val + align16((size_t)D * m * sizeof(float));
+    const bool ell = lst && D > 0 && e_len + align16((size_t)m * sizeof(int)) <= lst_bytes && m <= 65535;
+    uint16_t* eidx = reinterpret_cast<uint16_t*>(lst);
+    float* evl = reinterpret_cast<float*>(lst + e_val);
+    int* elen = reinterpret_cast<int*>(lst + e_len);
+    if (ell) {
+        for (int x = threadIdx.x; x < D * m; x += kThreads) {
+            const int u = x / m, q = x - (x / m) * m;
+            const int b0 = S.ptr[3][q], len = S.ptr[3][q + 1] - b0;
+            eidx[x] = u < len ? (uint16_t)S.idx[3][b0 + u] : (uint16_t)0;
+            evl[x] = u < len ? (float)S.val[3][b0 + u] : 0.f;
+        }
+        for (int q = threadIdx.x; q < m; q += kThreads) elen[q] = S.ptr[3][q + 1] - S.ptr[3][q];
+    }
+    __syncthreads();
+    // G, row by row: A' R through column p of A, then - R B' through B's rows
+    for (int p = warp; p < m; p += kWarps) {
+        for (int j = lane; j < m; j += 32) acc[j] = R[(size_t)p * m + j];
+        __syncwarp();
+        float r[NJ];
+#pragma unroll
+        for (int q = 0; q < NJ; ++q) r[q] = 0.f;
+        const int a0 = S.ptr[2][p], a1 = S.ptr[2][p + 1];
+        for (int tb = a0; tb < a1; tb += 32) {
+            const int tc = min(32, a1 - tb);
+            int kk = 0;
+            float aa = 0.f;
+            if (lane < tc) {
+                kk = S.idx[2][tb + lane];
+                aa = (float)S.val[2][tb + lane];
+            }
+#pragma unroll 2
+            for (int u = 0; u < tc; ++u) {
+                const int k = __shfl_sync(kFull, kk, u);
+                const float a = __shfl_sync(kFull, aa, u);
+                const float* row = R + (size_t)k * m;
+#pragma unroll
+                for (int q = 0; q < NJ; ++q) {
+                    const int j = lane + 32 * q;
+                    if (j < m) r[q] = fmaf(a, row[j], r[q]);
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NJ; ++q) {
+            const int j = lane + 32 * q;
+            if (j >= m) continue;
+            float v = r[q];
+            if (ell) {
+                const int len = elen[j];
+                for (int u = 0; u < len; ++u) v = fmaf(-acc[eidx[u * m + j]], evl[u * m + j], v);
+            } else if (staged) {   // the staged lists are still in place
+                for (int t = bptr[j]; t < bptr[j + 1]; ++t) v = fmaf(-acc[sidx[t]], sval[t], v);
+            } else {
+                for (int t = S.ptr[3][j]; t < S.ptr[3][j + 1]; ++t)
+                    v = fmaf(-acc[S.idx[3][t]], (float)S.val[3][t], v);
+            }
+            G[(size_t)p * m + j] = two_s * v;
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+}
+
 // Oracle costs and edge codes of a mixed-precision node: shared memory, or the
 // node's workspace for large orders.
 static __device__ inline unsigned char* mixed_costs(const Params& P, unsigned char* dsm, int node) {
@@ -1632,7 +1840,7 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
     bool int_ok = true;
     for (int e = tid; e < n; e += kThreads) {
         const int i = e / m, j = e - (e / m) * m;
-        if (!tcg) {
+        if (!tcg && !(BIG && c.use_sp)) {   // the dense FP32 gradient's copies
             Af[e] = (float)c.A[e];
             Bf[e] = (float)c.B[e];
             Btf[e] = (float)c.B[j * m + i];
@@ -1680,9 +1888,52 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
     // integers, so scores and curvatures are exact integer sums (the FP64 sums
     // of the same integers are exact too, hence bit-identical)
     const bool ints = __syncthreads_and(int_ok) != 0;
+    // Large orders with sparse small-integer graphs score permutations and
+    // pairwise directions in O(nnz): ||AP - PB||^2 = ||A||^2 + ||B||^2 -
+    // 2 sum_i sum_{k in row i of A} A[i][k] B[pi[i]][pi[k]], exact integers, so
+    // the sums equal the O(m^2) ones; a permutation's bounds are checked per row
+    // against the one column (if any) that must not be 0 (zreq: -1 none, -2
+    // more than one, found once: the kZeroOk bits do not change in the loop).
+    const bool sparse_ints = BIG && ints && c.use_sp;
+    int* zreq = reinterpret_cast<int*>(Btf) + m;   // after the gradient's row counts
+    double norms = 0.0;                            // ||A||^2 + ||B||^2
+    if (sparse_ints) {
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int r = warp; r < m; r += kWarps) {
+            int cnt = 0, col = -1;
+            for (int j0 = 0; j0 < m; j0 += 32) {
+                const int j = j0 + lane;
+                const unsigned b = __ballot_sync(kFull, j < m && !(code[r * m + j] & kZeroOk));
+                if (b && col < 0) col = j0 + __ffs(b) - 1;
+                cnt += __popc(b);
+            }
+            if (lane == 0) zreq[r] = cnt == 0 ? -1 : (cnt == 1 ? col : -2);
+        }
+        double loc = 0.0;
+        for (int t = tid; t < c.sp.ptr[0][m]; t += kThreads) loc += c.sp.val[0][t] * c.sp.val[0][t];
+        for (int t = tid; t < c.sp.ptr[3][m]; t += kThreads) loc += c.sp.val[3][t] * c.sp.val[3][t];
+        norms = bsum(loc, c.red);   // (a barrier: zreq is visible after it)
+    }
+    auto a_int = [&](int t) -> long long { return (long long)c.sp.val[0][t]; };
 
     auto score = [&](const int* pi, int* pinv) -> double {
         if (!ints) return perm_score(c, code, pi, pinv);
+        if (sparse_ints) {
+            bool valid = true;
+            for (int r = tid; r < m; r += kThreads) {
+                pinv[pi[r]] = r;
+                const int z = zreq[r];
+                if (!(code[r * m + pi[r]] & kOneOk) || z == -2 || (z >= 0 && z != pi[r])) valid = false;
+            }
+            if (!__syncthreads_and(valid)) return kNone;
+            long long cross = 0;
+            for (int i = tid; i < m; i += kThreads) {
+                const int pr = pi[i] * m;
+                for (int t = c.sp.ptr[0][i]; t < c.sp.ptr[0][i + 1]; ++t)
+                    cross += a_int(t) * (long long)Bi[pr + pi[c.sp.idx[0][t]]];
+            }
+            return c.s * bsum((double)(-2 * cross) + (tid == 0 ? norms : 0.0), c.red);
+        }
         bool valid = true;
         for (int r = tid; r < m; r += kThreads) pinv[pi[r]] = r;
         for (int e = tid; e < n; e += kThreads) {
@@ -1699,13 +1950,24 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
         return c.s * bsum((double)acc, c.red);
     };
 
+    // Large orders keep the best vertex as its permutation (m ints after zreq)
+    // and write the n-vector once, after the loop: the last permutation taken
+    // is the one the per-vertex writes would have left.
+    int* best_pi = zreq + m;
+    bool best_lazy = false;
     auto take = [&](const int* pi, double fv) {
         if (fv < best_val) {
             best_val = fv;
             if (tid == 0) P.b.best_vertex_val[node] = fv;
         }
-        if (fv < 1e299 && fv == best_val)
-            for (int e = tid; e < n; e += kThreads) best[e] = pi[e / m] == e - (e / m) * m ? 1.0 : 0.0;
+        if (fv < 1e299 && fv == best_val) {
+            if (sparse_ints) {
+                for (int r = tid; r < m; r += kThreads) best_pi[r] = pi[r];
+                best_lazy = true;
+            } else {
+                for (int e = tid; e < n; e += kThreads) best[e] = pi[e / m] == e - (e / m) * m ? 1.0 : 0.0;
+            }
+        }
         __syncthreads();
     };
 
@@ -1721,7 +1983,25 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
                 __syncthreads();
                 break;
             }
-        } else if (c.use_sp && (BIG || m > 64)) {
+        } else if (c.use_sp && BIG) {
+            // large orders: row by row, the factor's rows and B's lists staged in
+            // shared memory that is free during the gradient (the FP64 Hungarian
+            // workspace and the integer oracles' column state; on a cluster, the
+            // leader's cost slice, staged again after the gradient)
+            unsigned char* base = CL ? dsm + L.sm_slice : dsm + L.sm_hung;
+            const size_t rows_bytes = align16((size_t)kWarps * m * sizeof(float));
+            unsigned char* lst = CL ? base + rows_bytes : dsm + L.sm_cs;
+            const size_t avail = CL ? (size_t)L.cl_cols * m * sizeof(int) : 2 * L.cs_bytes;
+            const size_t lst_bytes = CL ? (avail > rows_bytes ? avail - rows_bytes : 0) : avail;
+            // X's nonzero lists in the dense FP32 copies of A and B, which only
+            // the dense gradient reads
+            uint16_t* xc = reinterpret_cast<uint16_t*>(Af);
+            float* xv = Bf;
+            int* xn = reinterpret_cast<int*>(Btf);
+            float* rb = reinterpret_cast<float*>(base);
+            if (m <= 256) grad_f32_rows<8>(c.sp, m, two_s, xf, Rf, gf, rb, lst, lst_bytes, xc, xv, xn);
+            else grad_f32_rows<16>(c.sp, m, two_s, xf, Rf, gf, rb, lst, lst_bytes, xc, xv, xn);
+        } else if (c.use_sp && m > 64) {
             // sparse graphs above order 64: products over the nonzero lists
             grad_f32_sparse(c.sp, m, two_s, xf, Rf, gf);
         } else {
@@ -1765,9 +2045,16 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
         } else {
         for (int e = tid; e < n; e += kThreads) {
             const int ci = __float2int_rn(scalbnf(gf[e], shift));
-            const bool allowed = (code[e] & kAllowed) != 0;
-            costf[e] = allowed ? ci : kIntInf;
-            if (dicg && !derive) costa[e] = (allowed && (code[e] & kFaceIn)) ? -ci : kIntInf;
+            const uint8_t cd = code[e];
+            const bool allowed = (cd & kAllowed) != 0;
+            if constexpr (BIG) {
+                // one packed array read by both oracles (half the bytes the
+                // Dijkstra steps stream from L2)
+                costf[e] = pack_cost(ci, allowed, (cd & kFaceIn) != 0);
+            } else {
+                costf[e] = allowed ? ci : kIntInf;
+                if (dicg && !derive) costa[e] = (allowed && (cd & kFaceIn)) ? -ci : kIntInf;
+            }
         }
         __syncthreads();
         const int owarp = (int)(threadIdx.x >> 5) - s_owarp;
@@ -1780,11 +2067,11 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
                     int* cs = reinterpret_cast<int*>(dsm + L.sm_cs + (g == 0 ? 0 : L.cs_bytes));
                     bool ok;
                     if (m <= 256)
-                        ok = g == 0 ? int_hungarian_group_cs<2, 0>(w0, cs, m, costf, shift, code, true, 0)
-                                    : int_hungarian_group_cs<2, 1>(w1, cs, m, costa, shift, code, c.flag[4] == 0, 1);
+                        ok = g == 0 ? int_hungarian_group_cs<2, 3>(w0, cs, m, costf, shift, code, true, 0)
+                                    : int_hungarian_group_cs<2, 4>(w1, cs, m, costf, shift, code, c.flag[4] == 0, 1);
                     else
-                        ok = g == 0 ? int_hungarian_group_cs<4, 0>(w0, cs, m, costf, shift, code, true, 0)
-                                    : int_hungarian_group_cs<4, 1>(w1, cs, m, costa, shift, code, c.flag[4] == 0, 1);
+                        ok = g == 0 ? int_hungarian_group_cs<4, 3>(w0, cs, m, costf, shift, code, true, 0)
+                                    : int_hungarian_group_cs<4, 4>(w1, cs, m, costf, shift, code, c.flag[4] == 0, 1);
                     if ((tid & 127) == 0) c.flag[g == 0 ? 0 : 2] = ok;
                 }
             }
@@ -1796,10 +2083,10 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
             bool ok;
             if constexpr (BIG) {   // column state in shared memory: two nodes per SM
                 int* cs = reinterpret_cast<int*>(dsm + L.sm_cs + (fwd ? 0 : L.cs_bytes));
-                if (m <= 256) ok = fwd ? int_hungarian_warp_cs<8, 0>(w, cs, m, costf, shift, code, same)
-                                       : int_hungarian_warp_cs<8, 1>(w, cs, m, costa, shift, code, same);
-                else ok = fwd ? int_hungarian_warp_cs<16, 0>(w, cs, m, costf, shift, code, same)
-                              : int_hungarian_warp_cs<16, 1>(w, cs, m, costa, shift, code, same);
+                if (m <= 256) ok = fwd ? int_hungarian_warp_cs<8, 3>(w, cs, m, costf, shift, code, same)
+                                       : int_hungarian_warp_cs<8, 4>(w, cs, m, costf, shift, code, same);
+                else ok = fwd ? int_hungarian_warp_cs<16, 3>(w, cs, m, costf, shift, code, same)
+                              : int_hungarian_warp_cs<16, 4>(w, cs, m, costf, shift, code, same);
             } else if constexpr (TC) {   // orders 17..128, costs beside the operand images
                 if (m <= 64) ok = fwd ? int_hungarian_warp<2, 0>(w, m, costf, shift, code, same)
                                       : int_hungarian_warp<2, 1>(w, m, costa, shift, code, same);
@@ -1883,7 +2170,29 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
                 const int pa = w1.pi[i], pv = w0.pi[i];
                 if (pa != pv) pl += (double)gf[i * m + pa] - (double)gf[i * m + pv];
             }
-            if (ints) {
+            if (sparse_ints) {
+                // ||A D - D B||^2 for D = P1 - P0 (P1 the in-face vertex): the
+                // squares of the O(m^2) sum expanded into 2||A||^2 + 2||B||^2
+                // and O(nnz) cross sums, exact integers
+                const int* p1 = w1.pi;
+                const int* p0 = w0.pi;
+                const int* p0inv = w0.pinv;
+                long long cross = 0;
+                for (int i = tid; i < m; i += kThreads) {
+                    const int r1 = p1[i] * m, r0 = p0[i] * m;
+                    for (int t = c.sp.ptr[0][i]; t < c.sp.ptr[0][i + 1]; ++t) {
+                        const int k = c.sp.idx[0][t];
+                        const long long a = a_int(t);
+                        const long long a1a0 = (long long)Ai[i * m + p0inv[p1[k]]];
+                        const long long b11 = Bi[r1 + p1[k]], b01 = Bi[r0 + p1[k]];
+                        const long long b10 = Bi[r1 + p0[k]], b00 = Bi[r0 + p0[k]];
+                        cross += a * (-a1a0 - b11 + b01 + b10 - b00);
+                    }
+                    for (int t = c.sp.ptr[3][p1[i]]; t < c.sp.ptr[3][p1[i] + 1]; ++t)
+                        cross -= (long long)c.sp.val[3][t] * (long long)Bi[r0 + c.sp.idx[3][t]];
+                }
+                cl = (double)(2 * cross) + (tid == 0 ? 2.0 * norms : 0.0);
+            } else if (ints) {
                 int acc = 0;
                 for (int e = tid; e < n; e += kThreads) {
                     const int i = e / m, j = e - (e / m) * m;
@@ -1927,6 +2236,9 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
         }
         __syncthreads();
     }
+    if (best_lazy)
+        for (int e = tid; e < n; e += kThreads) best[e] = best_pi[e / m] == e - (e / m) * m ? 1.0 : 0.0;
+    __syncthreads();
     if constexpr (CL) cl_release(reinterpret_cast<ClCtl*>(dsm + L.sm_cl));   // the helpers leave
     if constexpr (tcg) {
         // a gradient that timed out may still have MMAs in flight: wait (bounded)
