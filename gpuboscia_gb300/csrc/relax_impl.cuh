@@ -1592,7 +1592,39 @@ static __device__ void grad_f32_rows(const SparseAB& S, int m, float two_s, cons
     }
     auto bcol = [&](int t) -> int { return staged ? (int)sidx[t] : S.idx[3][t]; };
     auto bv = [&](int t) -> float { return staged ? sval[t] : (float)S.val[3][t]; };
-    // X's nonzeros, row by row, ascending columns (NaN counts as nonzero)
+    // X's nonzeros, row by row, ascending columns (NaN counts as nonzero);
+    // orders divisible by 4 read X as float4 and place each lane's nonzeros
+    // after the prefix count of the lanes before it
+    if ((m & 3) == 0) {
+        for (int i = warp; i < m; i += kWarps) {
+            int cnt = 0;
+            for (int j0 = 0; j0 < m; j0 += 128) {
+                const int j = j0 + 4 * lane;
+                const float4 v = j < m ? *reinterpret_cast<const float4*>(X + (size_t)i * m + j)
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float vv[4] = {v.x, v.y, v.z, v.w};
+                int mine = 0;
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc) mine += vv[cc] != 0.f;
+                int pre = mine;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const int t = __shfl_up_sync(kFull, pre, off);
+                    if (lane >= off) pre += t;
+                }
+                int o = cnt + pre - mine;
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc)
+                    if (vv[cc] != 0.f) {
+                        xc[(size_t)i * m + o] = (uint16_t)(j + cc);
+                        xv[(size_t)i * m + o] = vv[cc];
+                        ++o;
+                    }
+                cnt += __shfl_sync(kFull, pre, 31);
+            }
+            if (lane == 0) xn[i] = cnt;
+        }
+    } else
     for (int i = warp; i < m; i += kWarps) {
         int cnt = 0;
 #pragma unroll 4
@@ -1709,7 +1741,72 @@ static __device__ void grad_f32_rows(const SparseAB& S, int m, float two_s, cons
         for (int q = threadIdx.x; q < m; q += kThreads) elen[q] = S.ptr[3][q + 1] - S.ptr[3][q];
     }
     __syncthreads();
-    // G, row by row: A' R through column p of A, then - R B' through B's rows
+    // G, row by row: A' R through column p of A, then - R B' through B's rows.
+    // Orders divisible by 4 read R's rows as float4 (lane l takes columns
+    // 4l .. 4l+3 of every 128): a quarter of the load instructions.
+    if ((m & 3) == 0) {
+        constexpr int NH = (NJ + 3) / 4;   // 128-column groups per row
+        for (int p = warp; p < m; p += kWarps) {
+            for (int j = 4 * lane; j < m; j += 128)
+                *reinterpret_cast<float4*>(acc + j) = *reinterpret_cast<const float4*>(R + (size_t)p * m + j);
+            __syncwarp();
+            float4 r4[NH];
+#pragma unroll
+            for (int h = 0; h < NH; ++h) r4[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+            const int a0 = S.ptr[2][p], a1 = S.ptr[2][p + 1];
+            for (int tb = a0; tb < a1; tb += 32) {
+                const int tc = min(32, a1 - tb);
+                int kk = 0;
+                float aa = 0.f;
+                if (lane < tc) {
+                    kk = S.idx[2][tb + lane];
+                    aa = (float)S.val[2][tb + lane];
+                }
+#pragma unroll 2
+                for (int u = 0; u < tc; ++u) {
+                    const int k = __shfl_sync(kFull, kk, u);
+                    const float a = __shfl_sync(kFull, aa, u);
+                    const float* row = R + (size_t)k * m;
+#pragma unroll
+                    for (int h = 0; h < NH; ++h) {
+                        const int j = 4 * lane + 128 * h;
+                        if (j < m) {
+                            const float4 x = *reinterpret_cast<const float4*>(row + j);
+                            r4[h].x = fmaf(a, x.x, r4[h].x);
+                            r4[h].y = fmaf(a, x.y, r4[h].y);
+                            r4[h].z = fmaf(a, x.z, r4[h].z);
+                            r4[h].w = fmaf(a, x.w, r4[h].w);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < NH; ++h) {
+                const int j0 = 4 * lane + 128 * h;
+                if (j0 >= m) continue;
+                float v4[4] = {r4[h].x, r4[h].y, r4[h].z, r4[h].w};
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc) {
+                    const int j = j0 + cc;
+                    float v = v4[cc];
+                    if (ell) {
+                        const int len = elen[j];
+                        for (int u = 0; u < len; ++u) v = fmaf(-acc[eidx[u * m + j]], evl[u * m + j], v);
+                    } else if (staged) {
+                        for (int t = bptr[j]; t < bptr[j + 1]; ++t) v = fmaf(-acc[sidx[t]], sval[t], v);
+                    } else {
+                        for (int t = S.ptr[3][j]; t < S.ptr[3][j + 1]; ++t)
+                            v = fmaf(-acc[S.idx[3][t]], (float)S.val[3][t], v);
+                    }
+                    v4[cc] = two_s * v;
+                }
+                *reinterpret_cast<float4*>(G + (size_t)p * m + j0) = make_float4(v4[0], v4[1], v4[2], v4[3]);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        return;
+    }
     for (int p = warp; p < m; p += kWarps) {
         for (int j = lane; j < m; j += 32) acc[j] = R[(size_t)p * m + j];
         __syncwarp();
@@ -2043,6 +2140,19 @@ static __device__ int mixed_loop(Ctx& c, const Params& P, unsigned char* dsm, in
                 if ((tid & 31) == 0) c.flag[wid == 0 ? 0 : 2] = ok;
             }
         } else {
+        if (BIG && (n & 3) == 0) {
+            // four costs per thread and access (orders divisible by 2)
+            for (int e4 = tid; e4 < n / 4; e4 += kThreads) {
+                const float4 g4 = reinterpret_cast<const float4*>(gf)[e4];
+                const uchar4 c4 = reinterpret_cast<const uchar4*>(code)[e4];
+                int4 o;
+                o.x = pack_cost(__float2int_rn(scalbnf(g4.x, shift)), c4.x & kAllowed, c4.x & kFaceIn);
+                o.y = pack_cost(__float2int_rn(scalbnf(g4.y, shift)), c4.y & kAllowed, c4.y & kFaceIn);
+                o.z = pack_cost(__float2int_rn(scalbnf(g4.z, shift)), c4.z & kAllowed, c4.z & kFaceIn);
+                o.w = pack_cost(__float2int_rn(scalbnf(g4.w, shift)), c4.w & kAllowed, c4.w & kFaceIn);
+                reinterpret_cast<int4*>(costf)[e4] = o;
+            }
+        } else
         for (int e = tid; e < n; e += kThreads) {
             const int ci = __float2int_rn(scalbnf(gf[e], shift));
             const uint8_t cd = code[e];
