@@ -178,7 +178,7 @@ STATIC_SCRATCH_BYTES = 32 << 20
 EXPORTED_SYMBOLS = (
     "gbx_abi_version", "gbx_last_error", "gbx_relax_workspace_bytes",
     "gbx_relax_batch", "gbx_relax_batch_static", "gbx_relax_autotune", "gbx_relax_set_launch_shape",
-    "gbx_relax_set_oracle_warps",
+    "gbx_relax_set_oracle_warps", "gbx_relax_set_nodes_per_sm",
     "gbx_lmo_batch",
     "gbx_objective_gradient_batch", "gbx_objective_gradient_batch_f32",
     "gbx_node_feasible_batch",
@@ -219,6 +219,8 @@ def load(path: os.PathLike | str | None = None) -> C.CDLL:
     lib.gbx_relax_set_launch_shape.argtypes = [P(Objective), P(LMO), P(Algorithm), C.c_int, C.c_int]
     lib.gbx_relax_set_oracle_warps.restype = C.c_int
     lib.gbx_relax_set_oracle_warps.argtypes = [P(Objective), P(LMO), P(Algorithm), C.c_int]
+    lib.gbx_relax_set_nodes_per_sm.restype = C.c_int
+    lib.gbx_relax_set_nodes_per_sm.argtypes = [P(Objective), P(LMO), P(Algorithm), C.c_int]
     lib.gbx_lmo_batch.restype = C.c_int
     lib.gbx_lmo_batch.argtypes = [P(LMO), C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]

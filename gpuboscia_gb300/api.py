@@ -462,11 +462,12 @@ def lmo_batch(lmo, mode: int, direction, lb, ub, x=None, want_step: bool = False
 
 
 def set_launch_shape(objective, lmo, algorithm: A.Algorithm, n: int, tensor_core: int = -1, persistent: int = 0,
-                     oracle_warps: int = -1):
+                     oracle_warps: int = -1, nodes_per_sm: int = -1):
     """gbx_relax_set_launch_shape: pin this problem shape's launch shape (tensor_core -1 default rule,
     0 FP32 SIMT gradient -- over the nonzero lists for sparse graphs above order 64 --, 1 tensor cores;
     persistent 0 one CTA per node, 1 persistent grid, 2 a cluster of four CTAs per node), then
-    gbx_relax_set_oracle_warps (-1 default, 1 or 4 warps per integer oracle at orders 129..512)."""
+    gbx_relax_set_oracle_warps (-1 default, 1 or 4 warps per integer oracle at orders 129..512) and
+    gbx_relax_set_nodes_per_sm (-1 default, 1 or 2 nodes per SM for the FP64 kernels)."""
     lib = A.load()
     keep = _Keep()
     o = objective.to_c("cuda", keep)
@@ -480,6 +481,11 @@ def set_launch_shape(objective, lmo, algorithm: A.Algorithm, n: int, tensor_core
         if rc == A.ERR_INVALID:
             raise ValueError(lib.gbx_last_error().decode())
         A.check(lib, rc, "gbx_relax_set_oracle_warps")
+    if nodes_per_sm != -1:
+        rc = lib.gbx_relax_set_nodes_per_sm(C.byref(o), C.byref(lm), C.byref(algorithm), nodes_per_sm)
+        if rc == A.ERR_INVALID:
+            raise ValueError(lib.gbx_last_error().decode())
+        A.check(lib, rc, "gbx_relax_set_nodes_per_sm")
 
 
 def objective_gradient_batch(objective, x, precision: int = A.PRECISION_FP64, stream=None):

@@ -239,6 +239,20 @@ int gbx_relax_set_oracle_warps(const gbx_objective* obj, const gbx_lmo* lmo, con
     return GBX_OK;
 }
 
+int gbx_relax_set_nodes_per_sm(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg, int per_sm) {
+    const int rc = validate(obj, lmo, alg);
+    if (rc) return rc;
+    if (per_sm != -1 && per_sm != 1 && per_sm != 2) return fail(GBX_ERR_INVALID, "nodes per SM: -1, 1 or 2");
+    gbx::Variant v = gbx::tuned_variant(*obj, *lmo, *alg);
+    v.per_sm = per_sm;
+    gbx::Layout L;
+    std::string err;
+    const int r = gbx::make_layout(*obj, *lmo, *alg, 1, &L, &err, &v);
+    if (r) return fail(r, err);
+    gbx::store_variant(*obj, *lmo, *alg, v);
+    return GBX_OK;
+}
+
 int gbx_lmo_batch(const gbx_lmo* lmo, int cases, int mode, const double* direction,
                   const double* x, const double* lb, const double* ub, double* out,
                   double* out_step, void* stream) {

@@ -58,6 +58,9 @@ struct Layout {
     // warps 0-3, in-face on 4-7: a quarter of the columns per lane and step)
     // instead of one warp
     int oracle_group;
+    // FP64 kernels: compiled for two CTAs per SM (a 128-register cap) when
+    // two fit in shared memory, else one (the autotuner times both)
+    int per_sm2;
     // a cluster of `cluster` CTAs per node (0: one CTA): cl_cols columns of
     // packed oracle costs per CTA at sm_slice (the FP64 workspace shares it),
     // two per-oracle workspaces of chw_bytes at sm_chw, the leader's
@@ -201,6 +204,7 @@ struct Variant {
     int tc = -1;          // mixed Birkhoff: 1 tensor-core gradient, 0 FP32 SIMT gradient
     int persistent = -1;  // 1 persistent grid, 0 one CTA per node, 2 a cluster of kClCtas CTAs per node
     int oracle_warps = -1;  // large-order mixed Birkhoff: warps per integer oracle, 1 or 4
+    int per_sm = -1;        // FP64 kernels: nodes (CTAs) per SM the kernel is compiled for, 1 or 2
 };
 int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a,
                 int n_nodes, Layout* L, std::string* err, const Variant* v = nullptr);

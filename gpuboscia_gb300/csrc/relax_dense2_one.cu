@@ -1,0 +1,10 @@
+// relax_dense2_one.cu -- the FP64 kernels of the Birkhoff and cardinality LMOs compiled for one CTA per SM (no
+// register cap), the launch shape the autotuner times against two per SM;
+// a unit of its own so that it compiles in parallel with relax_dense2.cu.
+#include "relax_impl.cuh"
+
+namespace gbx {
+template int launch_mix<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_BIRKHOFF, 0, 1>(const Params&, cudaStream_t, std::string*);
+template int launch_mix<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_CARDINALITY, 0, 1>(const Params&, cudaStream_t, std::string*);
+template int launch_mix<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_LINKED_CARDINALITY, 0, 1>(const Params&, cudaStream_t, std::string*);
+}  // namespace gbx

@@ -4,6 +4,9 @@
 #include "relax_impl.cuh"
 
 namespace gbx {
+// the one-CTA-per-SM FP64 kernels compile in relax_graph_one.cu
+extern template int launch_mix<GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BIRKHOFF, 0, 1>(const Params&, cudaStream_t, std::string*);
+extern template int launch_mix<GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BOX, 0, 1>(const Params&, cudaStream_t, std::string*);
 extern template int launch_mix<GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BIRKHOFF, 1>(const Params&, cudaStream_t,
                                                                              std::string*);
 extern template int launch_mix<GBX_OBJ_GRAPH_MATCHING, GBX_LMO_BIRKHOFF, 2>(const Params&, cudaStream_t,

@@ -209,6 +209,18 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
     L.cs_bytes = mixed && L.cost_global ? colstate_bytes(l.order <= 256 ? 8 : 16) : 0;
     L.sm_cs = p; p += 2 * L.cs_bytes;
     L.sm_total = p;
+    // FP64 kernels: two nodes per SM (a 128-register cap) wherever two fit in
+    // shared memory, unless pinned
+    if (v.per_sm != -1 && v.per_sm != 1 && v.per_sm != 2) {
+        *err = "nodes per SM: 1 or 2";
+        return GBX_ERR_INVALID;
+    }
+    if (v.per_sm == 2 && mixed) {
+        *err = "nodes per SM applies to the FP64 kernels (mixed precision picks its own)";
+        return GBX_ERR_UNSUPPORTED;
+    }
+    L.per_sm2 = !mixed && (v.per_sm == 2 || (v.per_sm == -1 && 2 * (L.sm_total + kSmemPerCtaReserve) <= kSmemPerSm))
+                    ? 1 : 0;
     // large orders: each integer oracle on four warps unless pinned to one
     L.oracle_group = (L.cs_bytes && v.oracle_warps != 1) ? 1 : 0;
     if (v.oracle_warps != -1 && v.oracle_warps != 1 && v.oracle_warps != 4) {
@@ -311,15 +323,28 @@ std::vector<Variant> candidate_variants(const gbx_objective& o, const gbx_lmo& l
     if (a.precision == GBX_PRECISION_MIXED && o.kind == GBX_OBJ_GRAPH_MATCHING && l.kind == GBX_LMO_BIRKHOFF
             && l.order > 128 && l.order <= 512)
         ows = {4, 1};
+    // FP64 kernels: two nodes per SM (where they fit) or one
+    std::vector<int> pss = {-1};
+    if (a.precision != GBX_PRECISION_MIXED) {
+        Variant two;
+        two.per_sm = 2;
+        Layout L2;
+        std::string e2;
+        if (make_layout(o, l, a, 1, &L2, &e2, &two) == GBX_OK
+                && 2 * (L2.sm_total + kSmemPerCtaReserve) <= kSmemPerSm)
+            pss = {2, 1};
+    }
     for (int tc : tcs)
         for (int ow : ows)
-            for (int pers : {0, 1}) {
-                Variant v;
-                v.tc = tc;
-                v.persistent = pers;
-                v.oracle_warps = ow;
-                out.push_back(v);
-            }
+            for (int ps : pss)
+                for (int pers : {0, 1}) {
+                    Variant v;
+                    v.tc = tc;
+                    v.persistent = pers;
+                    v.oracle_warps = ow;
+                    v.per_sm = ps;
+                    out.push_back(v);
+                }
     // a cluster of CTAs per node where it applies (large-order mixed graph matching)
     Variant cl;
     cl.persistent = 2;

@@ -178,12 +178,10 @@ static __device__ void residual(const Ctx& c, const double* X, double* R) {
     }
 }
 
-// g = grad f(x). Graph matching leaves the residual of x in c.R.
-static __device__ void obj_grad(const Ctx& c, const double* x, double* g) {
+// g = 2s (A'R - R B') from the residual in c.R (graph matching).
+static __device__ void grad_from_residual(const Ctx& c, double* g) {
     const int n = c.n;
-    if (c.ok == GBX_OBJ_GRAPH_MATCHING) {
-        residual(c, x, c.R);
-        __syncthreads();
+    {
         const int m = c.m;
         const double two_s = 2.0 * c.s;
         if (c.use_sp && all_finite(c, c.R)) {
@@ -206,6 +204,18 @@ static __device__ void obj_grad(const Ctx& c, const double* x, double* g) {
                 g[e] = two_s * acc;
             }
         }
+    }
+    __syncthreads();
+}
+
+// g = grad f(x). Graph matching leaves the residual of x in c.R.
+static __device__ void obj_grad(const Ctx& c, const double* x, double* g) {
+    const int n = c.n;
+    if (c.ok == GBX_OBJ_GRAPH_MATCHING) {
+        residual(c, x, c.R);
+        __syncthreads();
+        grad_from_residual(c, g);
+        return;
     } else {
         for (int j = c.tid; j < n; j += kThreads) {
             double acc = 0.0;
@@ -1855,6 +1865,165 @@ static __device__ void grad_f32_rows(const SparseAB& S, int m, float two_s, cons
     __syncthreads();
 }
 
+// The certificate's FP64 residual and gradient at large orders, bit-identical
+// to residual() + grad_from_residual(): every element gets the same fused
+// multiply-adds in the same order, minus those whose X factor is zero, which
+// leave a sum started at +0 unchanged. X's nonzeros are listed by row
+// (xc, xv, xn: scratch in global memory); row i of R merges A's row i with
+// X's row i by column index, as the residual's two-list walk does (A's term
+// first on a tie): a neighbour k scatters a * X[k][:], a nonzero X[i][l]
+// scatters -X[i][l] * B[l][:], into the warp's shared-memory row. The gradient
+// reads the rows of R named by column p of A and gathers row p of R (staged)
+// through B's rows; B's rows are staged in `scr` beside the warps' rows
+// (lists for the residual, a padded table for the gradient) when they fit.
+static __device__ void grad64_rows(const Ctx& c, const double* X, double* R, double* g, unsigned char* scr,
+                                   size_t scr_bytes, uint16_t* xc, double* xv, int* xn) {
+    const SparseAB& S = c.sp;
+    const int m = c.m, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const size_t rows_bytes = align16((size_t)kWarps * m * sizeof(double));
+    double* acc = reinterpret_cast<double*>(scr) + (size_t)warp * m;
+    unsigned char* lst = scr + rows_bytes;
+    const size_t lst_bytes = scr_bytes > rows_bytes ? scr_bytes - rows_bytes : 0;
+    const int nb = S.ptr[3][m];
+    // B's rows as lists (residual)
+    const size_t o_idx = align16((size_t)(m + 1) * sizeof(int));
+    const size_t o_val = o_idx + align16((size_t)nb * sizeof(uint16_t));
+    const bool staged = o_val + align16((size_t)nb * sizeof(double)) <= lst_bytes && m <= 65535;
+    const int* bptr = staged ? reinterpret_cast<const int*>(lst) : S.ptr[3];
+    const uint16_t* sidx = reinterpret_cast<const uint16_t*>(lst + o_idx);
+    const double* sval = reinterpret_cast<const double*>(lst + o_val);
+    if (staged) {
+        int* pp = reinterpret_cast<int*>(lst);
+        uint16_t* ix = reinterpret_cast<uint16_t*>(lst + o_idx);
+        double* vl = reinterpret_cast<double*>(lst + o_val);
+        for (int q = threadIdx.x; q <= m; q += kThreads) pp[q] = S.ptr[3][q];
+        for (int t = threadIdx.x; t < nb; t += kThreads) {
+            ix[t] = (uint16_t)S.idx[3][t];
+            vl[t] = S.val[3][t];
+        }
+    }
+    // X's nonzeros by row, ascending columns
+    for (int i = warp; i < m; i += kWarps) {
+        int cnt = 0;
+        for (int j0 = 0; j0 < m; j0 += 32) {
+            const int j = j0 + lane;
+            const double v = j < m ? X[(size_t)i * m + j] : 0.0;
+            const bool nz = j < m && v != 0.0;
+            const unsigned b = __ballot_sync(kFull, nz);
+            if (nz) {
+                const int o = cnt + __popc(b & lt);
+                xc[(size_t)i * m + o] = (uint16_t)j;
+                xv[(size_t)i * m + o] = v;
+            }
+            cnt += __popc(b);
+        }
+        if (lane == 0) xn[i] = cnt;
+    }
+    __syncthreads();
+    // R, row by row: the merged walk over A's row i and X's row i, with the
+    // first 32 entries of both lists held in the lanes
+    for (int i = warp; i < m; i += kWarps) {
+        for (int j = lane; j < m; j += 32) acc[j] = 0.0;
+        __syncwarp();
+        int ia = S.ptr[0][i];
+        const int ea = S.ptr[0][i + 1];
+        int ib = 0;
+        const int eb = xn[i];
+        while (ia < ea || ib < eb) {
+            // the next 32 of each list
+            const int ha = ia + lane, hb = ib + lane;
+            const int lka = ha < ea ? S.idx[0][ha] : m;
+            const double la = ha < ea ? S.val[0][ha] : 0.0;
+            const int lcn = ha < ea ? xn[lka] : 0;
+            const int lkb = hb < eb ? (int)xc[(size_t)i * m + hb] : m;
+            const double lx = hb < eb ? xv[(size_t)i * m + hb] : 0.0;
+            int ua = 0, ub = 0;
+            while ((ua < 32 && ia + ua < ea) || (ub < 32 && ib + ub < eb)) {
+                const bool has_a = ua < 32 && ia + ua < ea, has_b = ub < 32 && ib + ub < eb;
+                // a list whose held window ran out first ends this pass (the
+                // other's next entry may precede the window's successor)
+                if ((!has_a && ia + ua < ea) || (!has_b && ib + ub < eb)) break;
+                const int ka = has_a ? __shfl_sync(kFull, lka, ua) : m;
+                const int kb = has_b ? __shfl_sync(kFull, lkb, ub) : m;
+                if (ka <= kb) {
+                    const double a = __shfl_sync(kFull, la, ua);
+                    const int cn = __shfl_sync(kFull, lcn, ua);
+                    for (int e = lane; e < cn; e += 32) {
+                        const int j = xc[(size_t)ka * m + e];
+                        acc[j] = fma(a, xv[(size_t)ka * m + e], acc[j]);
+                    }
+                    ++ua;
+                } else {
+                    const double x = __shfl_sync(kFull, lx, ub);
+                    const int b0 = bptr[kb], b1 = bptr[kb + 1];
+                    for (int t = b0 + lane; t < b1; t += 32) {
+                        const int j = staged ? (int)sidx[t] : S.idx[3][t];
+                        acc[j] = fma(-x, staged ? sval[t] : S.val[3][t], acc[j]);
+                    }
+                    ++ub;
+                }
+                __syncwarp();
+            }
+            ia += ua;
+            ib += ub;
+        }
+        for (int j = lane; j < m; j += 32) R[(size_t)i * m + j] = acc[j];
+        __syncwarp();
+    }
+    __syncthreads();
+    if (!all_finite(c, R)) {   // as grad_from_residual: the dense sums
+        grad_from_residual(c, g);
+        return;
+    }
+    // B's rows as a padded table (gradient)
+    __shared__ int s_dmax64;
+    if (threadIdx.x == 0) s_dmax64 = 0;
+    __syncthreads();
+    {
+        int dl = 0;
+        for (int q = threadIdx.x; q < m; q += kThreads) dl = max(dl, S.ptr[3][q + 1] - S.ptr[3][q]);
+        if (dl) atomicMax(&s_dmax64, dl);
+    }
+    __syncthreads();
+    const int D = s_dmax64;
+    const size_t e_val = align16((size_t)D * m * sizeof(uint16_t));
+    const size_t e_len = e_val + align16((size_t)D * m * sizeof(double));
+    const bool ell = D > 0 && e_len + align16((size_t)m * sizeof(int)) <= lst_bytes && m <= 65535;
+    uint16_t* eidx = reinterpret_cast<uint16_t*>(lst);
+    double* evl = reinterpret_cast<double*>(lst + e_val);
+    int* elen = reinterpret_cast<int*>(lst + e_len);
+    if (ell) {
+        for (int x = threadIdx.x; x < D * m; x += kThreads) {
+            const int u = x / m, q = x - (x / m) * m;
+            const int b0 = S.ptr[3][q], len = S.ptr[3][q + 1] - b0;
+            eidx[x] = u < len ? (uint16_t)S.idx[3][b0 + u] : (uint16_t)0;
+            evl[x] = u < len ? S.val[3][b0 + u] : 0.0;
+        }
+        for (int q = threadIdx.x; q < m; q += kThreads) elen[q] = S.ptr[3][q + 1] - S.ptr[3][q];
+    }
+    __syncthreads();
+    const double two_s = 2.0 * c.s;
+    for (int p = warp; p < m; p += kWarps) {
+        for (int j = lane; j < m; j += 32) acc[j] = R[(size_t)p * m + j];
+        __syncwarp();
+        const int a0 = S.ptr[2][p], a1 = S.ptr[2][p + 1];
+        for (int j = lane; j < m; j += 32) {
+            double v = 0.0;
+            for (int t = a0; t < a1; ++t) v = fma(S.val[2][t], R[(size_t)S.idx[2][t] * m + j], v);
+            if (ell) {
+                const int len = elen[j];
+                for (int u = 0; u < len; ++u) v = fma(-acc[eidx[u * m + j]], evl[u * m + j], v);
+            } else {
+                for (int t = S.ptr[3][j]; t < S.ptr[3][j + 1]; ++t) v = fma(-acc[S.idx[3][t]], S.val[3][t], v);
+            }
+            g[(size_t)p * m + j] = two_s * v;
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+}
+
 // Oracle costs and edge codes of a mixed-precision node: shared memory, or the
 // node's workspace for large orders.
 static __device__ inline unsigned char* mixed_costs(const Params& P, unsigned char* dsm, int node) {
@@ -2636,7 +2805,21 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
 
     // certificate at the returned iterate (the graph-matching value comes from
     // the residual the gradient leaves behind: the same sums as obj_value)
-    obj_grad(c, X, G);
+    bool rows64 = false;
+    if constexpr (kMixedLoop && MIX == 3) {
+        // large orders: row by row, with the node's FP32 arrays (free now) as
+        // scratch for X's nonzero lists and the shared memory of the integer
+        // oracles and the FP64 Hungarian (not yet in use) for rows and B
+        if (c.use_sp && all_finite(c, X)) {
+            unsigned char* mxb = P.mixed + (size_t)node * L.mixed_node_bytes;
+            grad64_rows(c, X, c.R, G, dsm + L.sm_hung, L.sm_total - L.sm_hung,
+                        reinterpret_cast<uint16_t*>(mxb + 2 * (size_t)n * sizeof(float)),
+                        reinterpret_cast<double*>(mxb),
+                        reinterpret_cast<int*>(mxb + 3 * (size_t)n * sizeof(float)));
+            rows64 = true;
+        }
+    }
+    if (!rows64) obj_grad(c, X, G);
     double fval = 0.0;
     if constexpr (OK == GBX_OBJ_GRAPH_MATCHING) fval = value_from_residual(c);
     bool fok;
@@ -2724,8 +2907,8 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
 
 // One CTA per node (grid = nodes), or a persistent grid whose CTAs take the
 // next node from an atomic queue in the workspace until the batch is done.
-template <int OK, int LK, int MIX>
-__global__ void __launch_bounds__(kThreads, (MIX == 1 || MIX == 3) ? 2 : 1) relax_kernel(const __grid_constant__ Params P) {
+template <int OK, int LK, int MIX, int MB>
+__global__ void __launch_bounds__(kThreads, MB) relax_kernel(const __grid_constant__ Params P) {
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ Scalars sh;
     // a batch assembled on the device (frontier rounds) carries its size in
@@ -2872,9 +3055,11 @@ __global__ void __launch_bounds__(kThreads, 1) feasible_kernel(
 // ------------------------------------------------------------------ launchers
 // One kernel variant (MIX) of a kind; each variant of the graph-matching
 // Birkhoff kernel is instantiated in its own translation unit.
-template <int OK, int LK, int MIX>
+// MB: CTAs per SM the kernel is compiled for (its register cap): two for the
+// SIMT mixed shapes, one for the tensor-core shape, either for FP64.
+template <int OK, int LK, int MIX, int MB = (MIX == 1 || MIX == 3) ? 2 : 1>
 int launch_mix(const Params& p, cudaStream_t st, std::string* err) {
-    auto k = relax_kernel<OK, LK, MIX>;
+    auto k = relax_kernel<OK, LK, MIX, MB>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::max<size_t>(p.L.sm_total, 1));
     if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
@@ -2926,7 +3111,7 @@ int launch_one(const Params& p, cudaStream_t st, std::string* err) {
             return launch_mix<OK, LK, 1>(p, st, err);
         }
     }
-    return launch_mix<OK, LK, 0>(p, st, err);
+    return p.L.per_sm2 ? launch_mix<OK, LK, 0, 2>(p, st, err) : launch_mix<OK, LK, 0, 1>(p, st, err);
 }
 
 template <int LK>

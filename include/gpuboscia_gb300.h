@@ -224,6 +224,16 @@ int gbx_relax_set_launch_shape(const gbx_objective* obj, const gbx_lmo* lmo, con
 int gbx_relax_set_oracle_warps(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
                                int warps);
 
+/* Pins how many nodes (CTAs of 256 threads) each SM holds for the FP64
+ * relaxation kernels: 2 (the default wherever two fit in shared memory: the
+ * kernel is compiled for a 128-register cap, and one node's barrier waits
+ * overlap the other's work) or 1 (no register cap; faster only when a batch
+ * leaves SMs idle anyway); -1 restores the default. Results are identical.
+ * Keeps the other pinned or tuned choices; gbx_relax_set_launch_shape resets
+ * it. GBX_ERR_UNSUPPORTED for 2 in mixed precision (its kernels fix their own). */
+int gbx_relax_set_nodes_per_sm(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
+                               int per_sm);
+
 /* Batched LMO calls, one case per row (the probes of tests/test_pipeline.cu:
  * 96-163). mode 0: forward v = argmin <direction, v> over the node's set
  * (LMO::compute_v); mode 1: in-face away oracle (LMO::compute_inface_v) on

@@ -348,3 +348,22 @@ def test_oracle_warps_only_where_they_apply(lib):
         for bad in (0, 2, 8):
             assert lib.gbx_relax_set_oracle_warps(C.byref(o), C.byref(lm), C.byref(alg), bad) == A.ERR_INVALID
             assert "oracle warps" in lib.gbx_last_error().decode()
+
+
+def test_nodes_per_sm_only_for_fp64(lib):
+    """Two nodes per SM pin for the FP64 kernels; mixed precision refuses 2 (its
+    kernels fix their own occupancy); other counts are argument errors."""
+    keep = api._Keep()
+    fp64 = A.Algorithm(A.ALG_FRANK_WOLFE, A.LS_QUADRATIC_EXACT, 4, 1e-10, 1e-14, A.PRECISION_FP64)
+    mixed = A.Algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT, 4, 1e-10, 1e-14, A.PRECISION_MIXED)
+    q = api.DenseQuadraticObjective(np.eye(64)).to_c("host", keep)
+    box = api.BoxLMO().to_c(64, "host", keep)
+    for v in (2, 1, -1):
+        assert lib.gbx_relax_set_nodes_per_sm(C.byref(q), C.byref(box), C.byref(fp64), v) == A.OK
+    for bad in (0, 3, 4):
+        assert lib.gbx_relax_set_nodes_per_sm(C.byref(q), C.byref(box), C.byref(fp64), bad) == A.ERR_INVALID
+        assert "nodes per SM" in lib.gbx_last_error().decode()
+    o = api.GraphMatchingObjective(np.zeros((36, 36)), np.zeros((36, 36))).to_c("host", keep)
+    lm = api.BirkhoffLMO(36).to_c(36 * 36, "host", keep)
+    assert lib.gbx_relax_set_nodes_per_sm(C.byref(o), C.byref(lm), C.byref(mixed), 2) == A.ERR_UNSUPPORTED
+    assert lib.gbx_relax_set_nodes_per_sm(C.byref(o), C.byref(lm), C.byref(mixed), -1) == A.OK

@@ -123,3 +123,54 @@ def test_graph_replay_matches_direct_launches(cuda_lib):
     assert g.objective == d.objective and g.nodes_processed == d.nodes_processed and g.dual_bound == d.dual_bound
     o = O.solve(inst.problem, inst.objective, inst.lmo, s)
     assert g.objective == o.objective and g.nodes_processed == o.nodes_processed
+
+
+def _nodes_per_sm(lib, inst, alg, per_sm):
+    keep = api._Keep()
+    o = inst.objective.to_c("cuda", keep)
+    lm = inst.lmo.to_c(len(inst.problem.lb), "cuda", keep)
+    A.check(lib, lib.gbx_relax_set_nodes_per_sm(C.byref(o), C.byref(lm), C.byref(alg), per_sm),
+            "gbx_relax_set_nodes_per_sm")
+
+
+@pytest.mark.parametrize("kind", ["box", "birkhoff", "portfolio"])
+def test_fp64_nodes_per_sm_are_bit_identical(cuda_lib, kind):
+    """The FP64 kernels compiled for two nodes per SM (128-register cap, the
+    default where two fit) and for one give the same nodes bit for bit, with
+    more nodes than resident CTAs and against the oracle on a sample."""
+    if kind == "box":
+        inst = instances.box_qp(n=64, seed=21)
+        alg = O.algorithm(A.ALG_FRANK_WOLFE, A.LS_QUADRATIC_EXACT)
+        N, iters = 700, 60
+        rng = np.random.default_rng(5)
+        lb = np.zeros((N, 64))
+        ub = np.ones((N, 64))
+        for i in range(N):
+            fix = rng.choice(64, 6, replace=False)
+            lb[i, fix[:3]] = 1.0
+            ub[i, fix[3:]] = 0.0
+    elif kind == "birkhoff":
+        inst = instances.birkhoff_gnp(order=36, seed=36)
+        alg = O.algorithm(A.ALG_DICG, A.LS_QUADRATIC_EXACT)
+        N, iters = 400, 20
+        lb, ub = instances.birkhoff_node_batch(36, N, seed=13)
+    else:
+        inst = instances.portfolio(assets=100)
+        alg = O.algorithm(A.ALG_FRANK_WOLFE, A.LS_QUADRATIC_EXACT)
+        N, iters = 200, 40
+        lb, ub = instances.portfolio_node_batch(100, 10, N, seed=9)
+    try:
+        _nodes_per_sm(cuda_lib, inst, alg, 2)
+        a = run(inst, alg, lb, ub, iters, N)
+        _nodes_per_sm(cuda_lib, inst, alg, 1)
+        b = run(inst, alg, lb, ub, iters, N)
+    finally:
+        _nodes_per_sm(cuda_lib, inst, alg, -1)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    # a sample against the oracle (the same all-integer flags as run())
+    S = 3
+    o = O.relax(inst.objective, inst.lmo, alg, lb[:S].copy(), lb[:S], ub[:S], 1e-6, np.zeros(S, np.int32),
+                np.zeros(S, np.uint8), iters, np.ones(lb.shape[1], np.uint8))
+    for k in ("x", "gap", "value", "status", "iterations"):
+        assert np.array_equal(a[k][:S], o[k]), k
