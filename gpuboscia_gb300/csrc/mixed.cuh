@@ -844,6 +844,15 @@ __device__ bool int_hungarian_group_cs(const IHW& w, int* cs, int m, const int* 
             const int key = bv < kPackLimit ? (bv << 10) | bj : 0x7fffffff;
             const int wk = __reduce_min_sync(kFull, key);
             if (lane == 0) s_key[g][par][gw] = wk;
+            // the warp's candidate column's matched row holds the next step's
+            // costs if the candidate wins: start bringing it toward the SM (one
+            // 128-byte line per lane) while the warps meet
+            if (wk != 0x7fffffff) {
+                const int wj = wk & 1023;
+                const int wo = (wj - 1) & (GT - 1), ws = (wj - 1) >> 7;
+                if (O(CS_PJ, ws, wo) != 0 && lane * 32 < m)
+                    asm volatile("prefetch.global.L1 [%0];" :: "l"(costs + O(CS_RBR, ws, wo) + lane * 32));
+            }
             oracle_group_bar(g);
             int kmin = s_key[g][par][0];
 #pragma unroll
