@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _dev(a, dtype=None):
-    return torch.from_numpy(np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))).cuda()
+    return torch.from_numpy(np.array(a, dtype=dtype, order="C", copy=True)).cuda()   # a writable copy
 
 
 def _relax(inst, alg, lb, ub, iters, shape):

@@ -33,7 +33,7 @@ def _same(g, o):
 
 
 def _dev(a, dtype=None):
-    return torch.from_numpy(np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))).cuda()
+    return torch.from_numpy(np.array(a, dtype=dtype, order="C", copy=True)).cuda()   # a writable copy
 
 
 def test_config1_box_bqp64_whole_tree_equals_the_oracle(cuda_lib):

@@ -27,7 +27,7 @@ ALGS = [
 
 def _t(a, dtype=None):
     import torch
-    return torch.from_numpy(np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))).cuda()
+    return torch.from_numpy(np.array(a, dtype=dtype, order="C", copy=True)).cuda()   # a writable copy
 
 
 def gpu_relax(obj, lmo, alg, x, lb, ub, eps, iterations, status, max_iters, flags, tol=1e-6):
