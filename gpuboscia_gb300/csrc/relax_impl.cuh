@@ -576,12 +576,15 @@ static __device__ bool hungarian_warp(const HW& w, int m, const double* cost, do
 // ---- the same Hungarian on a group of four warps (one per SM sub-partition:
 // on GB300 each sub-partition executes its own FP64 instructions, so the
 // per-step slack updates of 128 lanes cost what 32 lanes' did). Groups are
-// threads [0,128) (g = 0, named barrier 1) and [128,256) (g = 1, barrier 2).
+// threads [0,128) (g = 0, named barrier 1) and [128,256) (g = 1, barrier 2);
+// a lone oracle (the FP64 forward LMO of Frank-Wolfe, the certificate) runs on
+// the whole CTA as one group of eight warps (GW = 8, g = 0, named barrier 1).
 constexpr int kHungWarps = 4;
 constexpr int kHungThreads = kHungWarps * 32;
 
+template <int GW = kHungWarps>
 __device__ __forceinline__ void group_bar(int g) {
-    asm volatile("bar.sync %0, %1;" :: "r"(1 + g), "r"(kHungThreads) : "memory");
+    asm volatile("bar.sync %0, %1;" :: "r"(1 + g), "r"(GW * 32) : "memory");
 }
 
 __device__ __forceinline__ double key_fp64(unsigned long long key) {
@@ -590,34 +593,35 @@ __device__ __forceinline__ double key_fp64(unsigned long long key) {
 }
 
 // Solve phase: thread gt of the group owns the compacted columns gt+1,
-// gt+1+128, ... (CPL per thread; k <= 128*CPL). Per step every warp reduces its
-// best (slack key, column) with three REDUX, the four warp results meet in
+// gt+1+32*GW, ... (CPL per thread; k <= 32*GW*CPL). Per step every warp reduces
+// its best (slack key, column) with three REDUX, the GW warp results meet in
 // shared memory, and every thread derives the step value from the winning key
 // (the key maps back to the slack exactly, up to the sign of a zero, which no
 // comparison sees). Potential updates and the tie rule are those of the
 // single-warp loop, so the assignment is identical.
-template <int CPL>
+template <int CPL, int GW = kHungWarps>
 static __device__ bool hung_solve_group(const HW& w, int m, int k, const double* cost, double sign,
                                         const double* ub, const double* face, double* out, const uint8_t* code,
                                         int g) {
-    __shared__ unsigned long long s_key[2][kHungWarps];
-    __shared__ int s_j[2][kHungWarps];
+    constexpr int GT = GW * 32;
+    __shared__ unsigned long long s_key[2][GW];
+    __shared__ int s_j[2][GW];
     __shared__ int s_row[2];
-    const int gt = threadIdx.x - kHungThreads * g, lane = gt & 31, gw = gt >> 5;
+    const int gt = threadIdx.x - GT * g, lane = gt & 31, gw = gt >> 5;
     int colE[CPL], way[CPL], pr[CPL];
     double minv[CPL], pv[CPL];
     bool valid[CPL], used[CPL];
 #pragma unroll
     for (int t = 0; t < CPL; ++t) {
-        const int j = gt + 1 + kHungThreads * t;
+        const int j = gt + 1 + GT * t;
         valid[t] = j <= k;
         colE[t] = valid[t] ? w.cols[j - 1] : 0;
         pv[t] = 0.0;
         pr[t] = 0;
         way[t] = 0;
     }
-    for (int j = gt; j <= k; j += kHungThreads) w.u[j] = 0.0;
-    group_bar(g);
+    for (int j = gt; j <= k; j += GT) w.u[j] = 0.0;
+    group_bar<GW>(g);
     for (int i = 1; i <= k; ++i) {
 #pragma unroll
         for (int t = 0; t < CPL; ++t) { minv[t] = kNone; used[t] = false; }
@@ -651,7 +655,7 @@ static __device__ bool hung_solve_group(const HW& w, int m, int k, const double*
                 }
                 if (mv < kNone) {
                     const unsigned long long key = fp64_key(mv);
-                    const int j = gt + 1 + kHungThreads * t;
+                    const int j = gt + 1 + GT * t;
                     if (key < bkey) { bkey = key; bj = j; }
                 }
             }
@@ -660,11 +664,11 @@ static __device__ bool hung_solve_group(const HW& w, int m, int k, const double*
             const unsigned long long wkey = ((unsigned long long)hi << 32) | lo;
             const int wj = (int)__reduce_min_sync(kFull, bkey == wkey ? (unsigned)bj : 0x7fffffffu);
             if (lane == 0) { s_key[g][gw] = wkey; s_j[g][gw] = wj; }
-            group_bar(g);
+            group_bar<GW>(g);
             unsigned long long best = s_key[g][0];
             int j1 = s_j[g][0];
 #pragma unroll
-            for (int q = 1; q < kHungWarps; ++q) {
+            for (int q = 1; q < GW; ++q) {
                 const unsigned long long kq = s_key[g][q];
                 const int jq = s_j[g][q];
                 if (kq < best || (kq == best && jq < j1)) { best = kq; j1 = jq; }
@@ -679,13 +683,13 @@ static __device__ bool hung_solve_group(const HW& w, int m, int k, const double*
                 if (used[t]) { w.u[pr[t]] += bv; pv[t] -= bv; }
                 else minv[t] -= bv;
             }
-            const int owner = (j1 - 1) % kHungThreads, slot = (j1 - 1) / kHungThreads;
+            const int owner = (j1 - 1) % GT, slot = (j1 - 1) / GT;
             if (gt == owner) {
 #pragma unroll
                 for (int t = 0; t < CPL; ++t)
                     if (t == slot) { used[t] = true; s_row[g] = pr[t]; }
             }
-            group_bar(g);
+            group_bar<GW>(g);
             const int pj = s_row[g];
             j0 = j1;
             if (pj == 0) { done = true; break; }
@@ -696,11 +700,11 @@ static __device__ bool hung_solve_group(const HW& w, int m, int k, const double*
 #pragma unroll
         for (int t = 0; t < CPL; ++t)
             if (valid[t]) {
-                const int j = gt + 1 + kHungThreads * t;
+                const int j = gt + 1 + GT * t;
                 w.way[j] = way[t];
                 w.p[j] = pr[t];
             }
-        group_bar(g);
+        group_bar<GW>(g);
         if (gt == 0) {
             w.p[0] = i;
             int jj = j0;
@@ -710,10 +714,10 @@ static __device__ bool hung_solve_group(const HW& w, int m, int k, const double*
                 jj = jp;
             }
         }
-        group_bar(g);
+        group_bar<GW>(g);
 #pragma unroll
         for (int t = 0; t < CPL; ++t)
-            if (valid[t]) pr[t] = w.p[gt + 1 + kHungThreads * t];
+            if (valid[t]) pr[t] = w.p[gt + 1 + GT * t];
     }
 #pragma unroll
     for (int t = 0; t < CPL; ++t) {
@@ -722,33 +726,35 @@ static __device__ bool hung_solve_group(const HW& w, int m, int k, const double*
         out[r * m + colE[t]] = 1.0;
         w.pi[r] = colE[t];
     }
-    group_bar(g);
+    group_bar<GW>(g);
     return true;
 }
 
-// The Hungarian on group g (all 128 of its threads call it): pre-pass on the
-// group's first warp, solve on all four; beyond 512 free columns the first warp
-// runs the shared-memory loop. Same result as hungarian_warp.
+// The Hungarian on group g (all 32*GW of its threads call it): pre-pass on the
+// group's first warp, solve on all of them; beyond 128*GW free columns the
+// first warp runs the shared-memory loop. Same result as hungarian_warp.
+template <int GW = kHungWarps>
 static __device__ bool hungarian_group(const HW& w, int m, const double* cost, double sign, const double* lb,
                                        const double* ub, const double* face, double* out, const uint8_t* code,
                                        int g) {
+    constexpr int GT = GW * 32;
     __shared__ int s_k[2];
-    const int gt = threadIdx.x - kHungThreads * g;
+    const int gt = threadIdx.x - GT * g;
     if (gt < 32) {
         const int k = hung_prepass(w, m, lb, ub, face, out);
         if (gt == 0) s_k[g] = k;
     }
-    group_bar(g);
+    group_bar<GW>(g);
     const int k = s_k[g];
     if (k < 0) return false;
-    if (k <= kHungThreads) return hung_solve_group<1>(w, m, k, cost, sign, ub, face, out, code, g);
-    if (k <= 2 * kHungThreads) return hung_solve_group<2>(w, m, k, cost, sign, ub, face, out, code, g);
-    if (k <= 4 * kHungThreads) return hung_solve_group<4>(w, m, k, cost, sign, ub, face, out, code, g);
+    if (k <= GT) return hung_solve_group<1, GW>(w, m, k, cost, sign, ub, face, out, code, g);
+    if (k <= 2 * GT) return hung_solve_group<2, GW>(w, m, k, cost, sign, ub, face, out, code, g);
+    if (k <= 4 * GT) return hung_solve_group<4, GW>(w, m, k, cost, sign, ub, face, out, code, g);
     if (gt < 32) {
         const bool ok = hung_solve_smem(w, m, k, cost, sign, ub, face, out, code);
         if (gt == 0) s_k[g] = ok ? 1 : 0;
     }
-    group_bar(g);
+    group_bar<GW>(g);
     return s_k[g] != 0;
 }
 
@@ -1239,9 +1245,9 @@ static __device__ bool lmo_forward(const Ctx& c, const double* g, const double* 
         for (int j = c.tid; j < n; j += kThreads) v[j] = 0.0;
         __syncthreads();
         if (n != c.lorder * c.lorder) return false;
-        if (threadIdx.x < kHungThreads) {
+        {   // a lone oracle: the whole CTA as one group of eight warps
             const HW w = hw_at(c.hung[0], c.lorder);
-            const bool ok = hungarian_group(w, c.lorder, g, 1.0, lb, ub, nullptr, v, nullptr, 0);
+            const bool ok = hungarian_group<8>(w, c.lorder, g, 1.0, lb, ub, nullptr, v, nullptr, 0);
             if (threadIdx.x == 0) c.flag[0] = ok;
         }
         __syncthreads();
@@ -2738,14 +2744,17 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
         const double fcut = (cutv < kInfD && iter > 0) ? value_at_grad(c, X, G) : 0.0;
         bool fwd_perm = false, away_perm = false;
         if constexpr (LK == GBX_LMO_BIRKHOFF) {
-            // forward oracle on warp 0, DICG away oracle on warp 1
+            // forward oracle on warps 0-3, DICG away oracle on warps 4-7
             for (int j = tid; j < n; j += kThreads) { V[j] = 0.0; if (dicg) AW[j] = 0.0; }
             __syncthreads();
             if (n == c.lorder * c.lorder) {
-                if (threadIdx.x < kHungThreads) {
+                if (!dicg) {   // Frank-Wolfe: the forward oracle alone, on all eight warps
+                    const bool ok = hungarian_group<8>(hw0, c.lorder, G, 1.0, LB, UB, nullptr, V, nullptr, 0);
+                    if (threadIdx.x == 0) sh.flag[0] = ok;
+                } else if (threadIdx.x < kHungThreads) {
                     const bool ok = hungarian_group(hw0, c.lorder, G, 1.0, LB, UB, nullptr, V, nullptr, 0);
                     if (threadIdx.x == 0) sh.flag[0] = ok;
-                } else if (dicg) {
+                } else {
                     const bool ok = hungarian_group(hw1, c.lorder, G, -1.0, LB, UB, X, AW, nullptr, 1);
                     if (threadIdx.x == kHungThreads) sh.flag[2] = ok;
                 }
@@ -2833,8 +2842,8 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
             V[j] = 0.0;
         }
         __syncthreads();
-        if (threadIdx.x < kHungThreads) {
-            const bool ok = hungarian_group(hw0, c.lorder, Gs, 1.0, LB, UB, nullptr, V, mixed_codes(P, dsm, node), 0);
+        {   // the certificate's lone oracle: the whole CTA as one group of eight warps
+            const bool ok = hungarian_group<8>(hw0, c.lorder, Gs, 1.0, LB, UB, nullptr, V, mixed_codes(P, dsm, node), 0);
             if (threadIdx.x == 0) sh.flag[0] = ok;
         }
         __syncthreads();
