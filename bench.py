@@ -544,6 +544,32 @@ def run_bnb(args, rank, world):
                       "for two d-regular graphs the doubly stochastic J/n gives AX = XB, so every FW bound is 0 "
                       "while the optimum is positive: the gap cannot close by this method")
         other["birkhoff_regular120"] = o4
+        # the box BQP (n = 64): time to a certified gap through gbx_solve, the reference's
+        # configuration (host frontier, 64-node batches, one stream) against 1024-node
+        # device-frontier rounds with the incumbent cutoff; FP64 both (bit-exact relaxations)
+        from gpuboscia_gb300 import instances as I_
+        ob = {}
+        for name, batch, devf, cut in (("plain_fp64", 64, 0, 0), ("batched_fp64", 1024, 1, 1)):
+            instb = I_.box_qp(n=64)
+            wl, rr, cc = _solve_timed(instb, A.PRECISION_FP64, None, batch, 1, args.other_limit, devf, cut, 2000,
+                                      autotune=0)
+            ob[name] = _solve_summary(wl, rr, cc)
+        ob["batched_vs_plain_seconds"] = ob["plain_fp64"]["seconds"] / max(ob["batched_fp64"]["seconds"], 1e-9)
+        ob["note"] = "box BQP n = 64, whole tree to a certified 1e-6 gap, 2000 iterations per dispatch"
+        other["box_qp64"] = ob
+        # the cardinality portfolio (100 assets, 600 months): B&B nodes/s over a fixed time
+        # budget, 64-node batches on one stream against four streams
+        op = {}
+        for name, streams in (("plain_fp64", 1), ("four_streams_fp64", 4)):
+            instp = I_.portfolio()
+            wl, rr, cc = _solve_timed(instp, A.PRECISION_FP64, None, 64, streams, args.other_limit / 2, 0, 0, 500,
+                                      autotune=0)
+            op[name] = _solve_summary(wl, rr, cc)
+        op["four_streams_vs_plain_nodes_per_s"] = (op["four_streams_fp64"]["nodes_per_s"]
+                                                   / max(op["plain_fp64"]["nodes_per_s"], 1e-9))
+        op["note"] = (f"portfolio, 100 assets, cardinality 10, 64-node batches, time budget {args.other_limit / 2:g} s "
+                      "per arm: one 64-node launch fills 64 of 152 SMs, several streams overlap batches")
+        other["portfolio100"] = op
 
     _, lb_r, ub_r, eps_r = make_workload(args.workload, min(args.relax_nodes, B), rank)
     arms = relax_arms(inst, lb_r, ub_r, eps_r, w, I, check_nodes=args.check_nodes)
