@@ -687,6 +687,8 @@ def run_relax(args, rank, world):
         api.set_launch_shape(inst.objective, inst.lmo, alg, n, 1 if args.launch_shape == "tc" else 0, 0)
     elif args.launch_shape == "cluster":
         api.set_launch_shape(inst.objective, inst.lmo, alg, n, -1, 2)
+    elif args.launch_shape == "pair":
+        api.set_launch_shape(inst.objective, inst.lmo, alg, n, -1, 3)
     if args.oracle_warps != -1:
         api.set_launch_shape(inst.objective, inst.lmo, alg, n, -1, 2 if args.launch_shape == "cluster" else 0,
                              oracle_warps=args.oracle_warps)
@@ -880,11 +882,11 @@ def main():
                     help="bnb mode: nodes whose mixed certificate the oracle re-evaluates")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-budget", type=float, default=8.0)
-    ap.add_argument("--launch-shape", default="auto", choices=["auto", "tc", "simt", "tuned", "cluster"],
+    ap.add_argument("--launch-shape", default="auto", choices=["auto", "tc", "simt", "tuned", "cluster", "pair"],
                     help="relax mode, mixed Birkhoff: the default rule, tensor-core gradient, FP32 SIMT "
                          "gradient (over the nonzero lists for sparse graphs above order 64), the "
-                         "autotuner's choice on the batch (gbx_relax_autotune), or a cluster of four CTAs "
-                         "per node (orders 129..404)")
+                         "autotuner's choice on the batch (gbx_relax_autotune), a cluster of four CTAs "
+                         "per node (orders 129..404), or a pair of CTAs per node (FP64 dense quadratic)")
     ap.add_argument("--oracle-warps", type=int, default=-1, choices=[-1, 1, 4],
                     help="relax mode, mixed Birkhoff orders 129..512: warps per integer oracle (-1 default: 4)")
     ap.add_argument("--solve", default=None, choices=sorted(PAIR_CONFIGS),

@@ -465,7 +465,8 @@ def set_launch_shape(objective, lmo, algorithm: A.Algorithm, n: int, tensor_core
                      oracle_warps: int = -1, nodes_per_sm: int = -1):
     """gbx_relax_set_launch_shape: pin this problem shape's launch shape (tensor_core -1 default rule,
     0 FP32 SIMT gradient -- over the nonzero lists for sparse graphs above order 64 --, 1 tensor cores;
-    persistent 0 one CTA per node, 1 persistent grid, 2 a cluster of four CTAs per node), then
+    persistent 0 one CTA per node, 1 persistent grid, 2 a cluster of four CTAs per node, 3 a pair of CTAs
+    per node for the FP64 dense quadratic objective), then
     gbx_relax_set_oracle_warps (-1 default, 1 or 4 warps per integer oracle at orders 129..512) and
     gbx_relax_set_nodes_per_sm (-1 default, 1 or 2 nodes per SM for the FP64 kernels)."""
     lib = A.load()

@@ -212,8 +212,8 @@ int gbx_relax_set_launch_shape(const gbx_objective* obj, const gbx_lmo* lmo, con
                                int tensor_core, int persistent) {
     const int rc = validate(obj, lmo, alg);
     if (rc) return rc;
-    if (tensor_core < -1 || tensor_core > 1 || persistent < 0 || persistent > 2)
-        return fail(GBX_ERR_INVALID, "launch shape: tensor_core in -1..1, persistent in 0..2");
+    if (tensor_core < -1 || tensor_core > 1 || persistent < 0 || persistent > 3)
+        return fail(GBX_ERR_INVALID, "launch shape: tensor_core in -1..1, persistent in 0..3");
     gbx::Variant v;
     v.tc = tensor_core;
     v.persistent = persistent;

@@ -61,6 +61,11 @@ struct Layout {
     // FP64 kernels: compiled for two CTAs per SM (a 128-register cap) when
     // two fit in shared memory, else one (the autotuner times both)
     int per_sm2;
+    // FP64 dense quadratic objective with every node vector in shared memory:
+    // a node on a pair of CTAs (a two-CTA cluster) that split the objective's
+    // products, with a 256-double exchange buffer at sm_xch
+    int pair;
+    size_t sm_xch;
     // a cluster of `cluster` CTAs per node (0: one CTA): cl_cols columns of
     // packed oracle costs per CTA at sm_slice (the FP64 workspace shares it),
     // two per-oracle workspaces of chw_bytes at sm_chw, the leader's
@@ -202,7 +207,8 @@ void set_last_error(const std::string& msg);
 // Launch shape chosen by the autotuner (-1: the default rule).
 struct Variant {
     int tc = -1;          // mixed Birkhoff: 1 tensor-core gradient, 0 FP32 SIMT gradient
-    int persistent = -1;  // 1 persistent grid, 0 one CTA per node, 2 a cluster of kClCtas CTAs per node
+    int persistent = -1;  // 1 persistent grid, 0 one CTA per node, 2 a cluster of kClCtas CTAs per node,
+                          // 3 a pair of CTAs per node (FP64 dense quadratic objective)
     int oracle_warps = -1;  // large-order mixed Birkhoff: warps per integer oracle, 1 or 4
     int per_sm = -1;        // FP64 kernels: nodes (CTAs) per SM the kernel is compiled for, 1 or 2
 };

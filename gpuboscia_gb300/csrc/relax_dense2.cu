@@ -3,6 +3,10 @@
 #include "relax_impl.cuh"
 
 namespace gbx {
+// the pair-per-node kernels compile in relax_pair.cu
+extern template int launch_pair<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_BIRKHOFF>(const Params&, cudaStream_t, std::string*);
+extern template int launch_pair<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_CARDINALITY>(const Params&, cudaStream_t, std::string*);
+extern template int launch_pair<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_LINKED_CARDINALITY>(const Params&, cudaStream_t, std::string*);
 // the one-CTA-per-SM FP64 kernels compile in relax_dense2_one.cu
 extern template int launch_mix<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_BIRKHOFF, 0, 1>(const Params&, cudaStream_t, std::string*);
 extern template int launch_mix<GBX_OBJ_DENSE_QUADRATIC, GBX_LMO_CARDINALITY, 0, 1>(const Params&, cudaStream_t, std::string*);

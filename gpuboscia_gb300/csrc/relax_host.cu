@@ -221,6 +221,21 @@ int make_layout(const gbx_objective& o, const gbx_lmo& l, const gbx_algorithm& a
     }
     L.per_sm2 = !mixed && (v.per_sm == 2 || (v.per_sm == -1 && 2 * (L.sm_total + kSmemPerCtaReserve) <= kSmemPerSm))
                     ? 1 : 0;
+    // a pair of CTAs per node: the dense quadratic objective's products split
+    // between them; every node vector must sit in shared memory (each CTA keeps
+    // its own copy of the node)
+    L.pair = 0;
+    L.sm_xch = 0;
+    if (v.persistent == 3) {
+        if (mixed || o.kind != GBX_OBJ_DENSE_QUADRATIC || !L.vec_smem) {
+            *err = "a pair of CTAs per node covers the FP64 dense quadratic objective with the node in shared memory";
+            return GBX_ERR_UNSUPPORTED;
+        }
+        L.pair = 1;
+        L.persistent = 0;
+        L.sm_xch = align16(L.sm_total);
+        L.sm_total = L.sm_xch + align16((size_t)kThreads * sizeof(double));
+    }
     // large orders: each integer oracle on four warps unless pinned to one
     L.oracle_group = (L.cs_bytes && v.oracle_warps != 1) ? 1 : 0;
     if (v.oracle_warps != -1 && v.oracle_warps != 1 && v.oracle_warps != 4) {
@@ -351,6 +366,10 @@ std::vector<Variant> candidate_variants(const gbx_objective& o, const gbx_lmo& l
     Layout L;
     std::string err;
     if (make_layout(o, l, a, 1, &L, &err, &cl) == GBX_OK) out.push_back(cl);
+    // a pair of CTAs per node where it applies (FP64 dense quadratic, node in shared memory)
+    Variant pr;
+    pr.persistent = 3;
+    if (make_layout(o, l, a, 1, &L, &err, &pr) == GBX_OK) out.push_back(pr);
     return out;
 }
 

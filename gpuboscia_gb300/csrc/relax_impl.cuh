@@ -137,7 +137,37 @@ struct Ctx {
     // problem
     const uint8_t* flags;
     double tol;
+    // a node on a pair of CTAs (a two-CTA cluster, dense quadratic objective):
+    // this CTA's rank (-1: one CTA per node) and the 256-double buffer through
+    // which the pair exchanges per-lane partial sums
+    int pr;
+    double* xch;
 };
+
+// ---- the pair's exchange: the peer's copy of a shared-memory object, a
+// remote FP64 store, and the cluster-wide barrier (both CTAs, all threads)
+__device__ __forceinline__ unsigned pair_addr(const void* p, int rank) {
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+                 : "=r"(r) : "r"((unsigned)__cvta_generic_to_shared(p)), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void pair_store(const double* p, int rank, double v) {
+    asm volatile("st.shared::cluster.f64 [%0], %1;" :: "r"(pair_addr(p, rank)), "d"(v) : "memory");
+}
+__device__ __forceinline__ void pair_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// A per-lane partial computed by the lane's owner (lanes of parity pr) made
+// visible to both CTAs, then the 256-lane sum in the usual order.
+__device__ __forceinline__ double pair_lane_value(const Ctx& c, double v) {
+    if (!((c.tid & 1) ^ c.pr)) {
+        c.xch[c.tid] = v;
+        pair_store(c.xch + c.tid, c.pr ^ 1, v);
+    }
+    pair_sync();
+    return c.xch[c.tid];
+}
 
 // ------------------------------------------------------------------ objective
 static __device__ bool all_finite(const Ctx& c, const double* v) {
@@ -217,12 +247,19 @@ static __device__ void obj_grad(const Ctx& c, const double* x, double* g) {
         grad_from_residual(c, g);
         return;
     } else {
+        // a pair of CTAs computes the elements of its parity and stores them in
+        // both copies of g (g is in shared memory in the pair shape); the first
+        // barrier keeps the peer's previous g until it is done with it
+        if (c.pr >= 0) pair_sync();
         for (int j = c.tid; j < n; j += kThreads) {
+            if (c.pr >= 0 && (j & 1) != c.pr) continue;
             double acc = 0.0;
             for (int k = 0; k < n; ++k) acc = fma(c.Q[(size_t)k * n + j], x[k], acc);
             const double lin = c.c ? c.ls * c.c[j] : 0.0;
             g[j] = c.s * (acc + lin);
+            if (c.pr >= 0) pair_store(g + j, c.pr ^ 1, g[j]);
         }
+        if (c.pr >= 0) pair_sync();
     }
     __syncthreads();
 }
@@ -256,7 +293,9 @@ static __device__ double obj_value(const Ctx& c, const double* x) {
     }
     const double a = 0.5 * c.s, b = c.s * c.ls;
     double quad = 0.0, lin = 0.0;
-    for (int j = c.tid; j < n; j += kThreads) {
+    const bool mine = c.pr < 0 || !((c.tid & 1) ^ c.pr);   // a pair: the lanes of this CTA's parity
+    if (c.pr >= 0) pair_sync();
+    for (int j = c.tid; mine && j < n; j += kThreads) {
         double qx = 0.0;
         for (int k = 0; k < n; ++k) qx = fma(c.Q[(size_t)k * n + j], x[k], qx);
         quad = fma(x[j], qx, quad);
@@ -264,6 +303,7 @@ static __device__ double obj_value(const Ctx& c, const double* x) {
     }
     double val = a * quad + b * lin;
     if (c.tid == 0) val += c.k0;
+    if (c.pr >= 0) val = pair_lane_value(c, val);
     return bsum(val, c.red);
 }
 
@@ -277,11 +317,14 @@ static __device__ double obj_curvature(const Ctx& c, const double* d) {
         return (2.0 * c.s) * bsum(loc, c.red);
     }
     double curv = 0.0;
-    for (int j = c.tid; j < n; j += kThreads) {
+    const bool mine = c.pr < 0 || !((c.tid & 1) ^ c.pr);
+    if (c.pr >= 0) pair_sync();
+    for (int j = c.tid; mine && j < n; j += kThreads) {
         double prod = 0.0;
         for (int k = 0; k < n; ++k) prod = fma(c.Q[(size_t)k * n + j], d[k], prod);
         curv = fma(c.s * d[j], prod, curv);
     }
+    if (c.pr >= 0) curv = pair_lane_value(c, curv);
     return bsum(curv, c.red);
 }
 
@@ -2604,6 +2647,16 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
     c.hung_bytes = L.hung_bytes;
     c.flags = P.b.integer_flags;
     c.tol = P.b.candidate_tol;
+    c.pr = -1;
+    c.xch = nullptr;
+    if (L.pair) {   // a two-CTA cluster per node: this CTA's rank, the exchange buffer
+        unsigned rk;
+        asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rk));
+        c.pr = (int)rk;
+        c.xch = reinterpret_cast<double*>(dsm + L.sm_xch);
+    }
+    // in a pair, rank 0 alone writes the node's results (rank 1 computes the same)
+    const bool writer = c.pr <= 0;
 
     // stage node data and objective matrices
     for (int j = tid; j < n; j += kThreads) {
@@ -2638,11 +2691,11 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
     const int it0 = P.b.iterations[node];
     const bool supplied = (P.b.status[node] & GBX_NODE_INITIAL_POINT_SUPPLIED) != 0;
     __syncthreads();
-    if (tid == 0) P.b.best_vertex_val[node] = kNone;
+    if (tid == 0 && writer) P.b.best_vertex_val[node] = kNone;
     double best_val = kNone;
 
     if (!node_feasible<LK>(c, LB, UB, V)) {
-        if (tid == 0) {
+        if (tid == 0 && writer) {
             P.b.status[node] = GBX_NODE_INFEASIBLE;
             P.b.value[node] = CUDART_INF;
             P.b.gap[node] = 0.0;
@@ -2676,9 +2729,9 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
         const double fv = integer_value(c, vert, LB, UB, pi, pinv);
         if (fv < best_val) {
             best_val = fv;
-            if (tid == 0) P.b.best_vertex_val[node] = fv;
+            if (tid == 0 && writer) P.b.best_vertex_val[node] = fv;
         }
-        if (fv < 1e299 && fv == best_val)
+        if (fv < 1e299 && fv == best_val && writer)
             for (int j = tid; j < n; j += kThreads) best[j] = vert[j];
         __syncthreads();
     };
@@ -2894,7 +2947,7 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
                 __syncthreads();
             }
             const double cv = integer_value(c, CAND, LB, UB, perm ? cpi : nullptr, cpinv);
-            if (cv < best_val) {
+            if (cv < best_val && writer) {
                 for (int j = tid; j < n; j += kThreads) best[j] = CAND[j];
                 if (tid == 0) P.b.best_vertex_val[node] = cv;
             }
@@ -2905,6 +2958,7 @@ static __device__ __forceinline__ void relax_node(const Params& P, const int nod
         if (!isfinite(X[j]) || (c.flags && c.flags[j] && fabs(X[j] - round(X[j])) > c.tol))
             integral = false;
     if (__syncthreads_and(integral)) st = st ? GBX_NODE_INTEGRAL_CONVERGED : GBX_NODE_INTEGRAL_UNCONVERGED;
+    if (!writer) return;
     for (int j = tid; j < n; j += kThreads) gx[j] = X[j];
     if (tid == 0) {
         P.b.value[node] = fval;
@@ -2937,6 +2991,24 @@ __global__ void __launch_bounds__(kThreads, MB) relax_kernel(const __grid_consta
         relax_node<OK, LK, MIX>(P, node, dsm, sh);
         __syncthreads();
     }
+}
+
+// A pair of CTAs per node (a two-CTA cluster, FP64 dense quadratic objective):
+// both run the node's relaxation on their own copy of it, each computing half
+// of the objective's products and the lanes of its parity in the sums, which
+// the pair exchanges through distributed shared memory; rank 0 writes the
+// results. Every decision follows from values both CTAs compute identically, so
+// they meet every cluster barrier; the last one keeps either CTA's shared
+// memory alive until the peer's final stores into it are done.
+template <int OK, int LK>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
+    relax_pair_kernel(const __grid_constant__ Params P) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ Scalars sh;
+    const int n_nodes = P.live_count ? min(*P.live_count, P.b.n_nodes) : P.b.n_nodes;
+    const int node = (int)(blockIdx.x >> 1);
+    if (node < n_nodes) relax_node<OK, LK, 0>(P, node, dsm, sh);
+    pair_sync();
 }
 
 // A cluster of kClCtas CTAs per node (the large-order mixed relaxation of
@@ -3004,6 +3076,8 @@ __global__ void __launch_bounds__(kThreads, 1) lmo_probe_kernel(
     c.hung[1] = dsm + L.sm_hung + L.hung_bytes;
     c.flags = nullptr;
     c.tol = 0.0;
+    c.pr = -1;
+    c.xch = nullptr;
     double* o = out + off;
     if (mode == 0) {
         lmo_forward<LK>(c, dir + off, lb + off, ub + off, o);
@@ -3056,6 +3130,8 @@ __global__ void __launch_bounds__(kThreads, 1) feasible_kernel(
     c.hung[1] = dsm + L.sm_hung + L.hung_bytes;
     c.flags = flags;
     c.tol = 0.0;
+    c.pr = -1;
+    c.xch = nullptr;
     const bool ok = node_feasible<LK>(c, lb + (size_t)cs * n, ub + (size_t)cs * n, ws + (size_t)cs * n);
     if (threadIdx.x == 0) out[cs] = ok ? 1 : 0;
 }
@@ -3091,6 +3167,25 @@ int launch_mix(const Params& p, cudaStream_t st, std::string* err) {
     return GBX_OK;
 }
 
+// The pair launch: two CTAs per node (grid = 2 * nodes).
+template <int OK, int LK>
+int launch_pair(const Params& p, cudaStream_t st, std::string* err) {
+    if constexpr (OK == GBX_OBJ_DENSE_QUADRATIC) {
+        auto k = relax_pair_kernel<OK, LK>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.L.sm_total);
+        if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+        k<<<p.b.n_nodes * 2, kThreads, p.L.sm_total, st>>>(p);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) { *err = cudaGetErrorString(e); return GBX_ERR_CUDA; }
+        return GBX_OK;
+    } else {
+        (void)p;
+        (void)st;
+        *err = "a pair of CTAs per node covers the dense quadratic objective";
+        return GBX_ERR_UNSUPPORTED;
+    }
+}
+
 // The cluster launch: kClCtas CTAs per node (grid = nodes * kClCtas).
 template <int OK, int LK>
 int launch_cluster(const Params& p, cudaStream_t st, std::string* err) {
@@ -3112,6 +3207,8 @@ int launch_cluster(const Params& p, cudaStream_t st, std::string* err) {
 
 template <int OK, int LK>
 int launch_one(const Params& p, cudaStream_t st, std::string* err) {
+    if constexpr (OK == GBX_OBJ_DENSE_QUADRATIC)
+        if (p.L.pair) return launch_pair<OK, LK>(p, st, err);
     if constexpr (OK == GBX_OBJ_GRAPH_MATCHING && LK == GBX_LMO_BIRKHOFF) {
         if (p.L.cluster) return launch_cluster<OK, LK>(p, st, err);
         if (p.L.mixed) {

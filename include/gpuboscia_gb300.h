@@ -207,9 +207,11 @@ int gbx_relax_autotune(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_a
 
 /* Pins the launch shape of this problem shape by hand (what the autotuner
  * would store): tensor_core -1/0/1 (default rule / FP32 SIMT / tensor-core
- * gradient; mixed precision only), persistent 0/1/2 (one CTA per node /
+ * gradient; mixed precision only), persistent 0/1/2/3 (one CTA per node /
  * persistent grid / a cluster of four CTAs per node: mixed precision, Birkhoff
- * orders 129..404; GBX_ERR_UNSUPPORTED elsewhere). */
+ * orders 129..404 / a pair of CTAs per node splitting the objective's
+ * products: FP64 dense quadratic objective with the node in shared memory, for
+ * batches smaller than the GPU; GBX_ERR_UNSUPPORTED elsewhere). */
 int gbx_relax_set_launch_shape(const gbx_objective* obj, const gbx_lmo* lmo, const gbx_algorithm* alg,
                                int tensor_core, int persistent);
 

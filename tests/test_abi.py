@@ -325,7 +325,14 @@ def test_cluster_launch_shape_only_where_it_applies(lib):
         assert lib.gbx_relax_set_launch_shape(C.byref(o), C.byref(lm), C.byref(alg), -1, 0) == A.OK
     o = api.GraphMatchingObjective(np.zeros((400, 400)), np.zeros((400, 400))).to_c("host", keep)
     lm = api.BirkhoffLMO(400).to_c(400 * 400, "host", keep)
-    assert lib.gbx_relax_set_launch_shape(C.byref(o), C.byref(lm), C.byref(mixed), -1, 3) == A.ERR_INVALID
+    assert lib.gbx_relax_set_launch_shape(C.byref(o), C.byref(lm), C.byref(mixed), -1, 4) == A.ERR_INVALID
+    # persistent 3, a pair of CTAs per node, is the FP64 dense quadratic objective's
+    assert lib.gbx_relax_set_launch_shape(C.byref(o), C.byref(lm), C.byref(mixed), -1, 3) == A.ERR_UNSUPPORTED
+    fp64 = A.Algorithm(A.ALG_FRANK_WOLFE, A.LS_QUADRATIC_EXACT, 4, 1e-10, 1e-14, A.PRECISION_FP64)
+    q = api.DenseQuadraticObjective(np.eye(200)).to_c("host", keep)
+    box = api.BoxLMO().to_c(200, "host", keep)
+    assert lib.gbx_relax_set_launch_shape(C.byref(q), C.byref(box), C.byref(fp64), -1, 3) == A.OK
+    assert lib.gbx_relax_set_launch_shape(C.byref(q), C.byref(box), C.byref(fp64), -1, 0) == A.OK
 
 
 def test_oracle_warps_only_where_they_apply(lib):

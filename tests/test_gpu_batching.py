@@ -174,3 +174,46 @@ def test_fp64_nodes_per_sm_are_bit_identical(cuda_lib, kind):
                 np.zeros(S, np.uint8), iters, np.ones(lb.shape[1], np.uint8))
     for k in ("x", "gap", "value", "status", "iterations"):
         assert np.array_equal(a[k][:S], o[k]), k
+
+
+@pytest.mark.parametrize("kind", ["portfolio", "box", "portfolio_secant"])
+def test_pair_of_ctas_per_node_is_bit_identical(cuda_lib, kind):
+    """The dense quadratic objective on a pair of CTAs per node (a two-CTA
+    cluster splitting the objective's products, per-lane partial sums exchanged
+    through distributed shared memory) gives the nodes of one CTA per node bit
+    for bit, and the oracle's on a sample."""
+    if kind == "portfolio":
+        inst = instances.portfolio(assets=100)
+        alg = O.algorithm(A.ALG_FRANK_WOLFE, A.LS_QUADRATIC_EXACT)
+        N, iters = 64, 60
+        lb, ub = instances.portfolio_node_batch(100, 10, N, seed=17)
+    elif kind == "box":
+        inst = instances.box_qp(n=64, seed=23)
+        alg = O.algorithm(A.ALG_DICG, A.LS_SECANT)
+        N, iters = 40, 40
+        lb = np.zeros((N, 64))
+        ub = np.ones((N, 64))
+        rng = np.random.default_rng(3)
+        for i in range(N):
+            fix = rng.choice(64, 4, replace=False)
+            lb[i, fix[:2]] = 1.0
+            ub[i, fix[2:]] = 0.0
+    else:   # the secant line search: objective values through the pair's exchanged sums
+        inst = instances.portfolio(assets=100)
+        alg = O.algorithm(A.ALG_FRANK_WOLFE, A.LS_SECANT)
+        N, iters = 32, 30
+        lb, ub = instances.portfolio_node_batch(100, 10, N, seed=19)
+    try:
+        shape(cuda_lib, inst, alg, -1, 0)
+        a = run(inst, alg, lb, ub, iters, N)
+        shape(cuda_lib, inst, alg, -1, 3)
+        b = run(inst, alg, lb, ub, iters, N)
+    finally:
+        shape(cuda_lib, inst, alg, -1, 0)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    S = 2
+    o = O.relax(inst.objective, inst.lmo, alg, lb[:S].copy(), lb[:S], ub[:S], 1e-6, np.zeros(S, np.int32),
+                np.zeros(S, np.uint8), iters, np.ones(lb.shape[1], np.uint8))
+    for k in ("x", "gap", "value", "status", "iterations"):
+        assert np.array_equal(b[k][:S], o[k]), k
