@@ -36,7 +36,7 @@ def _dev(a, dtype=None):
     return torch.from_numpy(np.array(a, dtype=dtype, order="C", copy=True)).cuda()   # a writable copy
 
 
-def test_config1_box_bqp64_whole_tree_equals_the_oracle(cuda_lib):
+def test_box_bqp64_whole_tree_equals_the_oracle(cuda_lib):
     inst = instances.box_qp(n=64)
     s = inst.settings
     s.num_streams = 1
@@ -52,7 +52,7 @@ def test_config1_box_bqp64_whole_tree_equals_the_oracle(cuda_lib):
     assert abs(0.5 * x @ Q @ x + c @ x - g.objective) <= 1e-9 * abs(g.objective)
 
 
-def test_config2_gnp36_plain_equals_oracle_and_mixed_finds_the_isomorphism(cuda_lib):
+def test_gnp36_plain_equals_oracle_and_mixed_finds_the_isomorphism(cuda_lib):
     inst = instances.birkhoff_gnp(order=36)
     s = inst.settings
     s.num_streams = 1
@@ -72,7 +72,7 @@ def test_config2_gnp36_plain_equals_oracle_and_mixed_finds_the_isomorphism(cuda_
     assert np.array_equal(Am @ X, X @ Bm)
 
 
-def test_config3_portfolio_first_640_nodes_equal_the_oracle(cuda_lib):
+def test_portfolio100_first_640_nodes_equal_the_oracle(cuda_lib):
     inst = instances.portfolio()
     s = inst.settings
     s.num_streams = 1
@@ -84,7 +84,7 @@ def test_config3_portfolio_first_640_nodes_equal_the_oracle(cuda_lib):
     _same(g, o)
 
 
-def test_config4_order120_fp64_relaxation_bit_exact(cuda_lib):
+def test_regular120_fp64_relaxation_bit_exact(cuda_lib):
     inst = instances.birkhoff_regular_perturbed(order=120)
     m, N = 120, 8
     n = m * m
@@ -117,7 +117,7 @@ def _order400_fixed_pairs(inst, rows_per_node):
 
 
 @pytest.mark.parametrize("precision", [A.PRECISION_MIXED, A.PRECISION_FP64])
-def test_config5_order400_nodes_with_five_correct_pairs_reach_the_isomorphism(cuda_lib, precision):
+def test_regular400_nodes_with_five_correct_pairs_reach_the_isomorphism(cuda_lib, precision):
     inst = instances.birkhoff_regular_isomorphic(order=400)
     m = 400
     lb, ub = _order400_fixed_pairs(inst, [range(5), range(100, 105)])
@@ -137,7 +137,7 @@ def test_config5_order400_nodes_with_five_correct_pairs_reach_the_isomorphism(cu
         assert np.array_equal(Am @ X, X @ Bm)
 
 
-def test_config5_order400_mixed_certificate_equals_the_oracle(cuda_lib):
+def test_regular400_mixed_certificate_equals_the_oracle(cuda_lib):
     """The mixed iterations steer; the certificate at the iterate they return
     is FP64 and must be the oracle's to the last bit."""
     inst = instances.birkhoff_regular_isomorphic(order=400)
