@@ -38,6 +38,8 @@ __global__ void __launch_bounds__(kThreads, 1) grad_fp64_kernel(gbx_objective o,
     c.A = o.A;
     c.B = o.B;
     c.R = ws + (size_t)k * o.n;
+    c.pr = -1;   // one CTA per gradient: no pair exchange
+    c.xch = nullptr;
     obj_grad(c, x + (size_t)k * o.n, g + (size_t)k * o.n);
 }
 

@@ -140,8 +140,8 @@ struct Ctx {
     // a node on a pair of CTAs (a two-CTA cluster, dense quadratic objective):
     // this CTA's rank (-1: one CTA per node) and the 256-double buffer through
     // which the pair exchanges per-lane partial sums
-    int pr;
-    double* xch;
+    int pr = -1;
+    double* xch = nullptr;
 };
 
 // ---- the pair's exchange: the peer's copy of a shared-memory object, a
