@@ -858,6 +858,54 @@ def run_gradient(args):
                       "tflops_algorithmic": N * 8.0 * m ** 3 / (t / 1000.0) / 1e12}), flush=True)
 
 
+def run_lmo(args):
+    """--mode lmo: the batched box LMO (gbx_lmo_batch) alone, for profiling
+    its HBM stream: --cases rows of --lmo-n variables, --lmo-mode 0 (forward:
+    direction, lb, ub in, the vertex out, 32 bytes per variable) or 1 (in-face:
+    x in as well, 40 bytes). Every array is larger than L2 at the default
+    sizes (4096 x 8192 doubles = 268 MB), so no flush is needed between calls.
+    One JSON line (not the benchmark's line) with the algorithmic GB/s against
+    the measured copy bandwidth; the result is checked against the same
+    formula in numpy on a sample of rows. The timed region is one call of the
+    Python API: the output's allocation and zero fill (8 more bytes per
+    variable), the kernel, and the call's stream synchronisation; the
+    kernel's own duration is what ncu reports for box_lmo_stream_kernel."""
+    import torch
+    from gpuboscia_gb300 import api
+    N, n, mode = args.cases, args.lmo_n, args.lmo_mode
+    rng = np.random.Generator(np.random.PCG64(13))
+    d = torch.from_numpy(rng.standard_normal((N, n))).cuda()
+    lb = torch.from_numpy(rng.integers(-1, 1, (N, n)).astype(np.float64)).cuda()
+    ub = lb + 1.0
+    x = (lb + torch.from_numpy(rng.random((N, n))).cuda().round()) if mode == 1 else None
+    lmo = api.BoxLMO()
+    call = lambda: api.lmo_batch(lmo, mode, d, lb, ub, x=x)
+    for _ in range(max(args.warmup, 3)):
+        out, _ = call()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        out, _ = call()
+        b.record()
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    rows = slice(0, min(N, 64))
+    want = np.where(d[rows].cpu().numpy() > 0.0, lb[rows].cpu().numpy(), ub[rows].cpu().numpy())
+    if mode == 1:   # x sits on a bound everywhere here: the in-face vertex keeps it
+        want = x[rows].cpu().numpy()
+    ok = bool(np.array_equal(out[rows].cpu().numpy(), want))
+    t = statistics.mean(ms)
+    per = 40 if mode == 1 else 32
+    gbs = N * n * per / (t / 1000.0) / 1e9
+    hbm, _, kind = load_peaks()
+    print(json.dumps({"mode": "lmo", "lmo": "box", "lmo_mode": mode, "cases": N, "n": n, "ms": t,
+                      "bytes_per_variable": per, "gbs_algorithmic": gbs, "hbm_peak_gbs": hbm,
+                      "peak_kind": kind, "frac": gbs / hbm, "sample_rows_equal": ok,
+                      "l2": "every array larger than L2 (no flush)"}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -892,17 +940,23 @@ def main():
     ap.add_argument("--solve", default=None, choices=sorted(PAIR_CONFIGS),
                     help="only solve the held-out graph pairs with this time-to-gap configuration "
                          "(one JSON line; for profiling the search)")
-    ap.add_argument("--mode", default=None, choices=["bnb", "relax", "gradient"],
+    ap.add_argument("--mode", default=None, choices=["bnb", "relax", "gradient", "lmo"],
                     help="override the workload's measurement (relax: one relaxation launch per step; "
-                         "gradient: the batched gradient entry points alone, for profiling)")
+                         "gradient: the batched gradient entry points alone; lmo: the batched box LMO "
+                         "alone; both for profiling)")
     ap.add_argument("--order", type=int, default=128, help="gradient mode: graph order")
     ap.add_argument("--cases", type=int, default=4096, help="gradient mode: points per call")
     ap.add_argument("--gradient", default="f32", choices=["f32", "mixed"], help="gradient mode: entry point")
+    ap.add_argument("--lmo-n", type=int, default=8192, help="lmo mode: variables per row")
+    ap.add_argument("--lmo-mode", type=int, default=0, choices=[0, 1], help="lmo mode: forward (0) or in-face (1)")
     args = ap.parse_args()
-    if args.mode == "gradient":
+    if args.mode in ("gradient", "lmo"):
         from gpuboscia_gb300 import build
         build.build()
-        run_gradient(args)
+        if args.mode == "lmo":
+            run_lmo(args)
+        else:
+            run_gradient(args)
         return
     if args.solve:
         from gpuboscia_gb300 import build

@@ -231,6 +231,9 @@ int launch_relax(const Params& p, void* stream, std::string* err);
 int launch_lmo_batch(const gbx_lmo& l, int cases, int mode, const double* dir,
                      const double* x, const double* lb, const double* ub, double* out,
                      double* out_step, void* stream, std::string* err);
+// the box LMO over cases*n elements in HBM as one vectorised stream (lmo_stream.cu)
+int launch_box_lmo_stream(int mode, size_t total, const double* dir, const double* x, const double* lb,
+                          const double* ub, double* out, cudaStream_t st, std::string* err);
 int launch_gradient_batch(const gbx_objective& o, int precision, int cases, const double* x, double* g,
                           cudaStream_t st, std::string* err);
 int scorer_param_count(int F, int H);

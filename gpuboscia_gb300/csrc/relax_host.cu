@@ -440,10 +440,14 @@ int launch_lmo_batch(const gbx_lmo& l, int cases, int mode, const double* dir,
                      const double* x, const double* lb, const double* ub, double* out,
                      double* out_step, void* stream, std::string* err) {
     if (cases == 0) return GBX_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // the box oracles are element-wise: one stream over the whole batch; the
+    // DICG maximum step (a per-case reduction) stays with the per-case kernel
+    if (l.kind == GBX_LMO_BOX && !out_step)
+        return launch_box_lmo_stream(mode, (size_t)cases * l.n, dir, x, lb, ub, out, st, err);
     Layout L;
     int rc = probe_layout(l, &L, err);
     if (rc) return rc;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     switch (l.kind) {
     case GBX_LMO_BOX: return probe_one<GBX_LMO_BOX>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);
     case GBX_LMO_SIMPLEX: return probe_one<GBX_LMO_SIMPLEX>(l, L, cases, mode, dir, x, lb, ub, out, out_step, st, err);

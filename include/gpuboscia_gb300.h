@@ -242,7 +242,10 @@ int gbx_relax_set_nodes_per_sm(const gbx_objective* obj, const gbx_lmo* lmo, con
  * the minimal face of x. All arrays are device [cases*n]; x may be NULL for
  * mode 0. out_step (device [cases], may be NULL) receives, for mode 1, the
  * DICG maximum step of x - gamma*(out - fwd) where fwd is the forward vertex
- * of -direction (dicg_maximum_step_local + dicg_sum_maximum_step). */
+ * of -direction (dicg_maximum_step_local + dicg_sum_maximum_step). The box
+ * LMO without out_step runs as one element stream over all cases (16-byte
+ * accesses when every buffer is 16-byte aligned); the other sets and the
+ * maximum step take one CTA per case. */
 int gbx_lmo_batch(const gbx_lmo* lmo, int cases, int mode,
                   const double* direction, const double* x,
                   const double* lb, const double* ub, double* out,

@@ -227,6 +227,45 @@ def test_box_simplex_lmo_bitwise(cuda_lib, kind):
             assert np.array_equal(gs.cpu().numpy(), os_)
 
 
+def _t_at(a, offset):
+    """A device copy of `a` that starts `offset` doubles into its allocation
+    (offset 1: the buffer is 8-byte but not 16-byte aligned)."""
+    import torch
+    flat = torch.zeros(a.size + offset, dtype=torch.float64, device="cuda")
+    flat[offset:] = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64).ravel()).cuda()
+    return flat[offset:].view(*a.shape)
+
+
+@pytest.mark.parametrize("cases,n,offset", [(1, 1, 0), (3, 7, 0), (3, 7, 1), (5, 4099, 0), (64, 4099, 1),
+                                            (512, 2048, 0)])
+def test_box_lmo_stream_bitwise(cuda_lib, cases, n, offset):
+    """Without the DICG step, a batch of box LMO calls runs as one stream over
+    cases*n elements: 16-byte accesses when every buffer is 16-byte aligned,
+    one double at a time otherwise, and a lone last element when the count is
+    odd. Forward and in-face vertices equal the oracle's bit for bit,
+    including directions of -0.0 and iterates just inside and just outside the
+    in-face tolerance 1e-6 + 1e-4 |bound|."""
+    rng = np.random.default_rng(29 + n + offset)
+    d = rng.standard_normal((cases, n))
+    d.flat[::5] = 0.0
+    d.flat[1::11] = -0.0
+    lb = rng.integers(-2, 1, (cases, n)).astype(float)
+    ub = lb + rng.integers(0, 3, (cases, n))
+    x = lb + rng.random((cases, n)) * (ub - lb)
+    pick = rng.random((cases, n))
+    x = np.where(pick < 0.15, ub, x)
+    x = np.where((pick >= 0.15) & (pick < 0.3), lb, x)
+    x = np.where((pick >= 0.3) & (pick < 0.4), ub - 0.5e-6, x)          # inside the upper tolerance
+    x = np.where((pick >= 0.4) & (pick < 0.5), lb + 2e-6 + 1e-4 * np.abs(lb), x)   # outside the lower one
+    for mode in (0, 1):
+        g, step = api.lmo_batch(api.BoxLMO(), mode, _t_at(d, offset), _t_at(lb, offset), _t_at(ub, offset),
+                                x=_t_at(x, offset))
+        assert step is None
+        o, _ = O.lmo_call(api.BoxLMO(), mode, d, lb, ub, x=x)
+        assert np.array_equal(g.cpu().numpy(), o), mode
+        assert np.array_equal(np.signbit(g.cpu().numpy()), np.signbit(o)), mode
+
+
 def test_node_feasibility_matches_oracle(cuda_lib):
     order = 6
     n = order * order
