@@ -153,6 +153,30 @@ def main():
         br.append(dict(x=x, k=k, lb=ol[:cnt * n].reshape(cnt, n).tolist(), ub=ou[:cnt * n].reshape(cnt, n).tolist()))
     doc["branch_pow2"] = br
 
+    # the box oracles at the edges of the in-face tolerance 1e-6 + 1e-4 |bound|
+    # and with signed-zero directions (own generator: the cases above stay as they were)
+    re_ = np.random.default_rng(4242)
+    be = []
+    for s in range(8):
+        n = 48
+        g = frac(re_, n)
+        g[::4] = 0.0
+        g[2::8] = -0.0
+        lb = re_.integers(-3, 2, n).astype(float)
+        ub = lb + re_.integers(0, 3, n)
+        tu = 1e-6 + 1e-4 * np.abs(ub)
+        tl = 1e-6 + 1e-4 * np.abs(lb)
+        pick = re_.integers(0, 8, n)
+        x = np.choose(pick, [ub, lb, ub - 0.5 * tu, lb + 0.5 * tl, ub - tu, lb + tl, ub - 2.0 * tu,
+                             lb + 2.0 * tl])
+        fwd = np.zeros(n)
+        R.ref_box_lmo(0, n, g.ctypes.data, None, lb.ctypes.data, ub.ctypes.data, fwd.ctypes.data, None)
+        face = np.zeros(n)
+        R.ref_box_lmo(1, n, g.ctypes.data, x.ctypes.data, lb.ctypes.data, ub.ctypes.data, face.ctypes.data, None)
+        be.append(dict(g=g.tolist(), lb=lb.tolist(), ub=ub.tolist(), x=x.tolist(), forward=fwd.tolist(),
+                       inface=face.tolist()))
+    doc["box_edges"] = be
+
     out = HERE / "reference_cpu.json"
     out.write_text(json.dumps(doc, allow_nan=True, separators=(",", ":")))
     print(out, out.stat().st_size, "bytes")

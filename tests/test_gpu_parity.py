@@ -266,6 +266,21 @@ def test_box_lmo_stream_bitwise(cuda_lib, cases, n, offset):
         assert np.array_equal(np.signbit(g.cpu().numpy()), np.signbit(o)), mode
 
 
+def test_box_lmo_stream_equals_reference_golden(cuda_lib):
+    """The committed outputs of the reference's own box oracles at the edges
+    of the in-face tolerance (tests/golden/reference_cpu.json, box_edges):
+    the stream kernel reproduces them bit for bit, all cases in one batch."""
+    import json
+    import pathlib
+    cases = json.loads((pathlib.Path(__file__).parent / "golden" / "reference_cpu.json").read_text())["box_edges"]
+    g, lb, ub, x, fwd, face = (np.array([c[k] for c in cases]) for k in ("g", "lb", "ub", "x", "forward", "inface"))
+    for mode, want in ((0, fwd), (1, face)):
+        out, _ = api.lmo_batch(api.BoxLMO(), mode, _t(g), _t(lb), _t(ub), x=_t(x))
+        got = out.cpu().numpy()
+        assert np.array_equal(got, want), mode
+        assert np.array_equal(np.signbit(got), np.signbit(want)), mode
+
+
 def test_node_feasibility_matches_oracle(cuda_lib):
     order = 6
     n = order * order

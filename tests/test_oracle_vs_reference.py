@@ -38,6 +38,22 @@ def test_box_lmo_matches_reference():
         assert step[0] == max(0.0, c["step"])
 
 
+def test_box_lmo_tolerance_edges_match_reference():
+    """BoxLMO::compute_v_cpu / compute_inface_v_cpu (lmo.cuh:225-262) with
+    iterates on, just inside, exactly at and just beyond the in-face
+    tolerance 1e-6 + 1e-4 |bound| of either bound, and directions of +0.0 and
+    -0.0: the oracle's vertices equal the reference's bit for bit (sign bits
+    included)."""
+    for c in GOLDEN["box_edges"]:
+        g, lb, ub, x = (np.array([c[k]]) for k in ("g", "lb", "ub", "x"))
+        fwd, _ = O.lmo_call(api.BoxLMO(), 0, g, lb, ub)
+        assert np.array_equal(fwd[0], c["forward"])
+        assert np.array_equal(np.signbit(fwd[0]), np.signbit(c["forward"]))
+        face, _ = O.lmo_call(api.BoxLMO(), 1, g, lb, ub, x=x)
+        assert np.array_equal(face[0], c["inface"])
+        assert np.array_equal(np.signbit(face[0]), np.signbit(c["inface"]))
+
+
 def test_simplex_lmo_matches_reference():
     for c in GOLDEN["simplex"]:
         lmo = api.UnitSimplexLMO(c["rhs"], c["ints"], bool(c["equality"]))
