@@ -2,7 +2,8 @@
 types, as a reference program would call them) compiled with the host
 compiler and linked against the in-tree library: the reference's
 examples/minimal.cu answer and a graph pair, on the host and the device
-frontier (tests/cpp/minimal_gpu.cpp)."""
+frontier (tests/cpp/minimal_gpu.cpp); and the host engine's scheduling order
+(tests/cpp/scheduling_gpu.cpp)."""
 import pathlib
 import subprocess
 
@@ -11,18 +12,27 @@ import pytest
 ROOT = pathlib.Path(__file__).resolve().parent.parent
 
 
-@pytest.fixture(scope="module")
-def exe(tmp_path_factory):
+def _program(tmp_path_factory, name):
     from gpuboscia_gb300 import build
     lib = build.build()
     cuda = build._cuda_home()
-    out = tmp_path_factory.mktemp("cppgpu") / "minimal_gpu"
+    out = tmp_path_factory.mktemp("cppgpu") / name
     cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-I", str(cuda / "include"),
-           str(ROOT / "tests" / "cpp" / "minimal_gpu.cpp"), "-o", str(out),
+           str(ROOT / "tests" / "cpp" / f"{name}.cpp"), "-o", str(out),
            "-L", str(lib.parent), "-lgpuboscia_gb300", "-Wl,-rpath," + str(lib.parent),
            "-L", str(cuda / "lib64"), "-lcudart", "-Wl,-rpath," + str(cuda / "lib64"), "-lpthread"]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     return out
+
+
+@pytest.fixture(scope="module")
+def exe(tmp_path_factory):
+    return _program(tmp_path_factory, "minimal_gpu")
+
+
+@pytest.fixture(scope="module")
+def scheduling_exe(tmp_path_factory):
+    return _program(tmp_path_factory, "scheduling_gpu")
 
 
 def test_dropin_program_compiles_and_links(exe):
@@ -32,5 +42,20 @@ def test_dropin_program_compiles_and_links(exe):
 @pytest.mark.gpu
 def test_dropin_program_runs(cuda_lib, exe):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "0 failed" in r.stdout
+
+
+def test_scheduling_program_compiles_and_links(scheduling_exe):
+    assert scheduling_exe.exists()
+
+
+@pytest.mark.gpu
+def test_scheduling_order_as_the_reference_asserts(cuda_lib, scheduling_exe):
+    """tests/test_pipeline.cu:723-836: a completed slot is refilled before its
+    batch is post-processed, and with an empty frontier the children are
+    dispatched before the root's post-processing (root branched once, optimum
+    and bound kept)."""
+    r = subprocess.run([str(scheduling_exe)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "0 failed" in r.stdout
