@@ -120,3 +120,46 @@ def test_live_random_birkhoff_against_reference():
             R.ref_birkhoff_lmo(order, 0, cost.ctypes.data, None, lb.ctypes.data, ub.ctypes.data, out.ctypes.data)
             ours, _ = O.lmo_call(lmo, 0, cost[None], lb[None], ub[None])
             assert np.array_equal(ours[0], out)
+
+
+@pytest.mark.skipif(O.ref() is None, reason="reference tree not available at build time")
+def test_live_birkhoff_inface_forced_forbidden_against_reference():
+    """BirkhoffLMO::compute_v_cpu / compute_inface_v_cpu (lmo.cuh:958-1171) on
+    heavy ties (costs in quarters, some -0.0), forbidden entries, a few forced
+    pairs and iterates that mix up to three permutations: the oracle's
+    forward and in-face vertices equal the reference's bit for bit."""
+    R = O.ref()
+    rng = np.random.default_rng(5)
+    calls = 0
+    for _ in range(300):
+        order = int(rng.choice([3, 4, 5, 6, 7, 8, 12, 16]))
+        n = order * order
+        cost = rng.integers(-3, 4, n) / 4.0
+        cost[rng.random(n) < 0.1] = -0.0
+        lb, ub = np.zeros(n), np.ones(n)
+        p = rng.permutation(order)
+        forbid = rng.random(n) < 0.25
+        forbid[np.arange(order) * order + p] = False
+        ub[forbid] = 0.0
+        for i in range(order):
+            if rng.random() < 0.15:
+                lb[i * order + p[i]] = 1.0
+        x = np.zeros(n)
+        for w in rng.dirichlet(np.ones(3)):
+            q = p.copy()
+            a, b = rng.choice(order, 2, replace=False)
+            q[a], q[b] = p[b], p[a]
+            allowed = all(ub[i * order + q[i]] > 0 for i in range(order)) and lb[a * order + p[a]] == 0 \
+                and lb[b * order + p[b]] == 0
+            for i, col in enumerate(q if allowed else p):
+                x[i * order + col] += w
+        lmo = api.BirkhoffLMO(order)
+        for mode in (0, 1):
+            out = np.zeros(n)
+            rc = R.ref_birkhoff_lmo(order, mode, cost.ctypes.data, x.ctypes.data if mode else None, lb.ctypes.data,
+                                    ub.ctypes.data, out.ctypes.data)
+            assert rc == 0
+            ours, _ = O.lmo_call(lmo, mode, cost[None], lb[None], ub[None], x=x[None] if mode else None)
+            assert np.array_equal(ours[0], out), (order, mode)
+            calls += 1
+    assert calls == 600
