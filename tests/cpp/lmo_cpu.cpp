@@ -65,8 +65,9 @@ int main() {
         } else if (kind == "birkhoff") {
             int order;
             std::cin >> order;
-            if (!(birkhoff<3>(order) || birkhoff<5>(order) || birkhoff<7>(order) || birkhoff<8>(order)
-                  || birkhoff<12>(order) || birkhoff<36>(order))) {
+            if (!(birkhoff<3>(order) || birkhoff<4>(order) || birkhoff<5>(order) || birkhoff<6>(order)
+                  || birkhoff<7>(order) || birkhoff<8>(order) || birkhoff<12>(order) || birkhoff<16>(order)
+                  || birkhoff<36>(order))) {
                 std::printf("unsupported order %d\n", order);
                 return 1;
             }

@@ -115,6 +115,78 @@ def test_host_lmo_oracles_match_the_reference_outputs(tmp_path):
         assert all(_eq(a, b) for a, b in zip(g, w)), (i, g, w)
 
 
+def test_host_lmo_oracles_live_against_the_reference(tmp_path):
+    """The drop-in headers' CPU oracles against the reference's own CPU
+    functions (oracle/_ref, built where the reference tree was present) on
+    fresh random cases: bounded and equality simplices with integral and
+    fractional right-hand sides, tie-heavy gradients and forced integer
+    coordinates (forward vertex, in-face vertex, DICG maximum step), and
+    Birkhoff orders 3-16 with forbidden entries and forced pairs."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    import numpy as np
+    import _oracle as O
+    R = O.ref()
+    if R is None:
+        pytest.skip("reference tree not available at build time")
+    exe = tmp_path / "lmo_cpu"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
+                    str(ROOT / "tests" / "cpp" / "lmo_cpu.cpp"), "-o", str(exe)], check=True)
+    rng = np.random.default_rng(23)
+    lines, want = [], []
+    for c in range(400):
+        n = int(rng.integers(2, 30))
+        eq = int(rng.integers(0, 2))
+        ints = sorted(rng.choice(n, int(rng.integers(0, n + 1)), replace=False).tolist())
+        rhs = float(rng.integers(1, 10)) + (0.5 if c % 2 else 0.0)
+        g = rng.integers(-2, 3, n) / 8.0
+        lb = np.zeros(n)
+        ub = np.where(np.isin(np.arange(n), ints), rng.integers(1, 4, n), rhs).astype(float)
+        for j in ints[:2]:
+            lb[j] = 1.0 if lb.sum() + 1 <= rhs else 0.0
+        x = lb.copy()
+        rest = rhs - lb.sum() if eq else (rhs - lb.sum()) * rng.random()
+        for j in rng.permutation(n):
+            add = min(ub[j] - x[j], rest)
+            x[j] += add
+            rest -= add
+        iv = np.array(ints, dtype=np.int32)
+        fwd, face, step = np.zeros(n), np.zeros(n), np.zeros(1)
+        ip = iv.ctypes.data if ints else None
+        R.ref_simplex_lmo(eq, 0, n, rhs, ip, len(ints), g.ctypes.data, None, lb.ctypes.data, ub.ctypes.data,
+                          fwd.ctypes.data, None)
+        R.ref_simplex_lmo(eq, 1, n, rhs, ip, len(ints), g.ctypes.data, x.ctypes.data, lb.ctypes.data,
+                          ub.ctypes.data, face.ctypes.data, step.ctypes.data)
+        lines.append(f"simplex {eq} {rhs!r} {n} {len(ints)} {' '.join(map(str, ints))} "
+                     f"{_fmt(g)} {_fmt(lb)} {_fmt(ub)} {_fmt(x)}")
+        want.append(list(fwd) + list(face) + [float(step[0])])
+    for _ in range(100):
+        order = int(rng.choice([3, 4, 5, 6, 7, 8, 12, 16]))
+        n = order * order
+        cost = rng.integers(-3, 4, n) / 4.0
+        lb, ub = np.zeros(n), np.ones(n)
+        p = rng.permutation(order)
+        forbid = rng.random(n) < 0.25
+        forbid[np.arange(order) * order + p] = False
+        ub[forbid] = 0.0
+        lb[np.arange(order) * order + p] = (rng.random(order) < 0.15).astype(float)
+        x = np.zeros(n)
+        x[np.arange(order) * order + p] = 1.0
+        fwd, face = np.zeros(n), np.zeros(n)
+        R.ref_birkhoff_lmo(order, 0, cost.ctypes.data, None, lb.ctypes.data, ub.ctypes.data, fwd.ctypes.data)
+        zl, on = np.zeros(n), np.ones(n)
+        R.ref_birkhoff_lmo(order, 1, cost.ctypes.data, x.ctypes.data, zl.ctypes.data, on.ctypes.data,
+                           face.ctypes.data)
+        lines.append(f"birkhoff {order} {_fmt(cost)} {_fmt(lb)} {_fmt(ub)} {_fmt(x)}")
+        want.append(list(fwd) + list(face))
+    r = subprocess.run([str(exe)], input="\n".join(lines) + "\n", capture_output=True, text=True, check=True)
+    got = [[float(t) for t in line.split()] for line in r.stdout.splitlines()]
+    assert len(got) == len(want) == 500
+    for i, (gv, w) in enumerate(zip(got, want)):
+        assert len(gv) == len(w), i
+        assert all(_eq(a, b) for a, b in zip(gv, w)), (i, lines[i], gv, w)
+
+
 # the reference's public header names (include/gpuboscia/ of the reference)
 REFERENCE_HEADERS = [
     "algorithms.cuh", "atomic_incumbent.h", "bnb.h", "branching.h", "concurrent_queue.h",
