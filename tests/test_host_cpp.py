@@ -62,6 +62,45 @@ def test_host_rules_match_reference_fixture(exe):
         assert float(out[k]) == e
 
 
+def test_host_rules_live_against_the_reference(exe):
+    """gap_utils.h (absolute and relative gap, the tolerance test, the
+    certified Frank-Wolfe bound, the depth schedule) and the closed-form
+    quadratic-exact step against the reference's own functions (oracle/_ref)
+    on random values mixed with zeros, signed infinities and NaN."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    import numpy as np
+    import _oracle as O
+    R = O.ref()
+    if R is None:
+        pytest.skip("reference tree not available at build time")
+    rng = np.random.default_rng(31)
+    special = [0.0, -0.0, 1.0, -1.0, 1e-300, -1e-300, 1e300, math.inf, -math.inf, math.nan]
+
+    def value():
+        return float(rng.choice(special)) if rng.random() < 0.3 else float(rng.normal() * 10.0 ** rng.integers(-8, 9))
+
+    pairs = [(value(), value()) for _ in range(400)]
+    tols = [(float(rng.choice([0.0, 1e-6, 0.01])), float(rng.choice([0.0, 1e-6, 0.105]))) for _ in pairs]
+    out = _table(exe, [f"gap {b!r} {i!r} {ta!r} {tr!r}" for (b, i), (ta, tr) in zip(pairs, tols)])
+    for k, ((b, i), (ta, tr)) in enumerate(zip(pairs, tols)):
+        a, r, w = out[k].split()
+        assert _eq(float(a), R.ref_gap_absolute(b, i)), (b, i)
+        assert _eq(float(r), R.ref_gap_relative(b, i)), (b, i)
+        assert int(w) == R.ref_gap_within_tolerance(b, i, ta, tr), (b, i, ta, tr)
+    triples = [(value(), value(), value()) for _ in range(300)]
+    out = _table(exe, [f"cert {a!r} {b!r} {c!r}" for a, b, c in triples])
+    for k, (a, b, c) in enumerate(triples):
+        assert _eq(float(out[k]), R.ref_certified_fw_lower_bound(a, b, c)), (a, b, c)
+    depths = [int(d) for d in rng.integers(-2, 2000, 100)]
+    out = _table(exe, [f"depth {d}" for d in depths])
+    for k, d in enumerate(depths):
+        assert float(out[k]) == R.ref_depth_dependent_tolerance(1e-3, 0.8, 1e-6, d), d
+    out = _table(exe, [f"quad {g!r} {c!r} {m!r}" for g, c, m in triples])
+    for k, (g, c, m) in enumerate(triples):
+        assert _eq(float(out[k]), R.ref_quadratic_exact_step(g, c, m)), (g, c, m)
+
+
 def test_logger_header_drives_like_the_examples(tmp_path):
     """include/gpuboscia/logger.h: the examples' Logger / LoggerParams /
     SolutionStats calls compile warning-free; rows are throttled by the node
