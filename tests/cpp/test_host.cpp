@@ -164,6 +164,26 @@ int main(int argc, char** argv) {
                 std::printf("%.17g\n", depth_dependent_tolerance(1e-3, 0.8, 1e-6, (int)a));
             } else if (op == "quad" && num(a) && num(b) && num(c)) {
                 std::printf("%.17g\n", quadratic_exact_step(a, b, c));
+            } else if (op == "branch") {   // branch n k tol n_int ints[n_int] lb[n] ub[n] x[n]
+                int n = 0, k = 0, n_int = 0;
+                double tol = 0;
+                std::cin >> n >> k;
+                num(tol);
+                std::cin >> n_int;
+                std::vector<int> ints(n_int);
+                for (int& i : ints) std::cin >> i;
+                std::vector<double> lb(n), ub(n), x(n);
+                for (auto* v : {&lb, &ub, &x})
+                    for (double& e : *v) num(e);
+                Node parent(0, -1, 0, lb, ub);
+                int next = 1;
+                const auto ch = branch_pow2(parent, next, x, ints, k, tol);
+                std::printf("%d", (int)ch.size());   // then each child's lb and ub
+                for (const auto& c2 : ch) {
+                    for (double e : c2.lb) std::printf(" %.17g", e);
+                    for (double e : c2.ub) std::printf(" %.17g", e);
+                }
+                std::printf("\n");
             }
         }
         return 0;

@@ -101,6 +101,45 @@ def test_host_rules_live_against_the_reference(exe):
         assert _eq(float(out[k]), R.ref_quadratic_exact_step(g, c, m)), (g, c, m)
 
 
+def test_branch_pow2_live_against_the_reference(exe):
+    """branching.h's branch_pow2 (the reference's branching.h:80-118) against
+    the reference's own function on random nodes: k from 0 to 4, iterates
+    with ties in fractionality, near-integral values around the tolerance,
+    bounds already narrowed, and more than 16 candidates (where std::sort's
+    order among equal fractionalities is no longer the index order); the
+    children (count, order, bounds) are equal."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    import numpy as np
+    import _oracle as O
+    R = O.ref()
+    if R is None:
+        pytest.skip("reference tree not available at build time")
+    rng = np.random.default_rng(37)
+    lines, want = [], []
+    for _ in range(300):
+        n = int(rng.integers(1, 40))
+        k = int(rng.integers(0, 5))
+        tol = float(rng.choice([1e-6, 1e-3]))
+        ints = sorted(rng.choice(n, int(rng.integers(0, n + 1)), replace=False).tolist())
+        lb = rng.integers(-2, 2, n).astype(float)
+        ub = lb + rng.integers(0, 4, n)
+        x = lb + (ub - lb) * rng.integers(0, 9, n) / 8.0
+        near = rng.random(n) < 0.2
+        x[near] = np.round(x[near]) + rng.choice([-1, 1], near.sum()) * tol * rng.choice([0.5, 2.0], near.sum())
+        iv = np.array(ints, dtype=np.int32)
+        olb, oub = np.zeros(16 * n), np.zeros(16 * n)
+        cnt = R.ref_branch_pow2(n, lb.ctypes.data, ub.ctypes.data, x.ctypes.data, iv.ctypes.data if ints else None,
+                                len(ints), k, tol, olb.ctypes.data, oub.ctypes.data)
+        kids = [v for c in range(cnt) for v in list(olb[c * n:(c + 1) * n]) + list(oub[c * n:(c + 1) * n])]
+        lines.append(f"branch {n} {k} {tol!r} {len(ints)} {' '.join(map(str, ints))} {_fmt(lb)} {_fmt(ub)} {_fmt(x)}")
+        want.append([float(cnt)] + kids)
+    out = _table(exe, lines)
+    for i, w in enumerate(want):
+        got = [float(t) for t in out[i].split()]
+        assert got == w, (lines[i], got, w)
+
+
 def test_logger_header_drives_like_the_examples(tmp_path):
     """include/gpuboscia/logger.h: the examples' Logger / LoggerParams /
     SolutionStats calls compile warning-free; rows are throttled by the node
