@@ -140,6 +140,56 @@ def test_branch_pow2_live_against_the_reference(exe):
         assert got == w, (lines[i], got, w)
 
 
+def test_queue_and_bound_set_match_the_reference_implementation(tmp_path):
+    """concurrent_queue.h here against the reference's own header: one script
+    of random operations (pushes with few distinct bounds, so ties are the
+    rule; pop_batch and pop_full_batch with cutoffs that drop part of the
+    frontier and return short batches; discard_children; best bounds and the
+    bound set's inserts and erasures) run through the same driver compiled
+    against each. The outputs (which nodes leave in which order) are equal."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    import random
+    from _refdata import reference_path
+    ref_include = reference_path("include")
+    if not (ref_include / "gpuboscia" / "concurrent_queue.h").is_file():
+        pytest.skip("reference tree not available")
+    src = ROOT / "tests" / "cpp" / "queue_ops.cpp"
+    exes = []
+    for name, inc in (("ours", ROOT / "include"), ("ref", ref_include)):
+        out = tmp_path / name
+        subprocess.run(["g++", "-std=c++17", "-O1", "-I", str(inc), str(src), "-o", str(out)], check=True)
+        exes.append(out)
+    rng = random.Random(43)
+    ops, next_id, bounds_held = [], 0, []
+    for _ in range(6000):
+        r = rng.random()
+        if r < 0.45:
+            ops.append(f"push {next_id} {rng.randrange(0, 40)} {rng.choice([-3.0, -2.5, -2.0, -1.0, 0.0, 0.5])!r}")
+            next_id += 1
+        elif r < 0.6:
+            ops.append(f"pop {rng.randrange(0, 9)} {rng.choice([-2.0, 0.0, 0.5, 1e300])!r}")
+        elif r < 0.72:
+            ops.append(f"full {rng.randrange(1, 9)} {rng.choice([-2.0, 0.0, 0.5, 1e300])!r}")
+        elif r < 0.76:
+            ops.append(f"discard {rng.randrange(0, 40)}")
+        elif r < 0.82:
+            ops.append(f"best {rng.choice([-2.0, 0.5, 1e300])!r}")
+        elif r < 0.92:
+            b = rng.choice([-3.0, -2.0, 0.0, 1.5])
+            bounds_held.append(b)
+            ops.append(f"bins {b!r}")
+        elif r < 0.97:
+            ops.append(f"berase {rng.choice(bounds_held or [0.0])!r}")
+        else:
+            ops.append(f"bbest {rng.choice([-2.5, 0.0, 1e300])!r}")
+    script = "\n".join(ops) + "\n"
+    ours, ref = (subprocess.run([str(e)], input=script, capture_output=True, text=True, check=True).stdout
+                 for e in exes)
+    assert ours.count("\n") > 1500
+    assert ours == ref
+
+
 def test_logger_header_drives_like_the_examples(tmp_path):
     """include/gpuboscia/logger.h: the examples' Logger / LoggerParams /
     SolutionStats calls compile warning-free; rows are throttled by the node
