@@ -190,6 +190,53 @@ def test_queue_and_bound_set_match_the_reference_implementation(tmp_path):
     assert ours == ref
 
 
+def test_incumbent_and_root_point_checks_match_the_reference_implementation(tmp_path):
+    """atomic_incumbent.h and tree.h's validate_root_initial_point here
+    against the reference's headers: one random script (incumbent updates
+    with ties, NaN and infinities; root points for box, bounded and equality
+    simplices, a caller's validator and an LMO without a point check, with
+    wrong lengths, bad tolerances, non-finite entries and bound violations)
+    run through the same driver compiled against each (the reference's
+    lmo.cuh through nvcc). The outputs, messages included, are equal."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    import random
+    from _refdata import reference_path
+    from gpuboscia_gb300 import build
+    ref_include = reference_path("include")
+    if not (ref_include / "gpuboscia" / "tree.h").is_file():
+        pytest.skip("reference tree not available")
+    src = ROOT / "tests" / "cpp" / "root_point_ops.cpp"
+    ours, ref = tmp_path / "ours", tmp_path / "ref"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", str(ROOT / "include"), str(src), "-o", str(ours)], check=True)
+    cu = tmp_path / "root_point_ops.cu"
+    cu.write_text(src.read_text())
+    subprocess.run([str(build._cuda_home() / "bin" / "nvcc"), "-std=c++17", "-O1", "-I", str(ref_include), str(cu),
+                    "-o", str(ref)], check=True)
+    rng = random.Random(47)
+    vals = [0.0, 0.25, 0.5, 1.0, 2.0, -1.0, float("nan"), float("inf"), -float("inf"), 1e-10, -1e-10]
+    lines = []
+    for _ in range(3000):
+        if rng.random() < 0.3:
+            lines.append(f"inc {rng.choice(vals + [3.0, 3.0, 1.5])!r}")
+            continue
+        kind = rng.choice(["box", "simplex", "eqsimplex", "accept", "reject", "none"])
+        n = rng.randrange(1, 6)
+        m = n if rng.random() < 0.85 else rng.choice([0, n + 1, max(0, n - 1)])
+        tol = rng.choice([1e-9, 0.0, 1e-3, -1.0, float("nan"), float("inf")])
+        lb = [rng.choice([0.0, 0.0, -1.0, float("nan")]) for _ in range(n)]
+        ub = [rng.choice([1.0, 1.0, 2.0, -2.0, float("nan")]) for _ in range(n)]
+        x = [rng.choice(vals) for _ in range(m)]
+        head = f"root {kind}" + (f" {rng.choice([1.0, 1.5, 2.0])!r}" if "simplex" in kind else "")
+        lines.append(f"{head} {n} {m} {tol!r} " + " ".join(repr(v) for v in lb + ub + x))
+    script = "\n".join(lines) + "\n"
+    a, b = (subprocess.run([str(e)], input=script, capture_output=True, text=True, check=True).stdout
+            for e in (ours, ref))
+    assert a.count("\n") == len(lines)
+    assert "ok" in a and "violates the LMO" in a and "dimensions or tolerance" in a and "requires LMO" in a
+    assert a == b
+
+
 def test_logger_header_drives_like_the_examples(tmp_path):
     """include/gpuboscia/logger.h: the examples' Logger / LoggerParams /
     SolutionStats calls compile warning-free; rows are throttled by the node
