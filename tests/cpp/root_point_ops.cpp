@@ -1,10 +1,13 @@
-// The incumbent and the root-point checks driven by a script on stdin, for a
-// differential check of two implementations of atomic_incumbent.h and
-// tree.h's validate_root_initial_point (the same source compiled against each):
+// The incumbent, the root-point checks and the node feasibility predicates
+// driven by a script on stdin, for a differential check of two
+// implementations of atomic_incumbent.h, tree.h's validate_root_initial_point
+// and bnb.h (the same source compiled against each):
 //   inc value                 -> try_update(value, {value}): result, get(), get_x()
 //   root kind n tol lb[n] ub[n] x[m]   (m given first: "root kind n m tol ...")
 //        kind: box | simplex rhs | eqsimplex rhs | accept | reject | none
 //        -> "ok" or the exception's message
+//   intfeas n k tol x[n] ints[k]        -> bnb.h is_integer_feasible
+//   nodefeas n k tol lb[n] ub[n] ints[k] -> bnb.h is_node_feasible
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -14,6 +17,7 @@
 #include <vector>
 
 #include <gpuboscia/atomic_incumbent.h>
+#include <gpuboscia/bnb.h>
 #include <gpuboscia/lmo.cuh>
 #include <gpuboscia/problem.h>
 #include <gpuboscia/tree.h>
@@ -52,6 +56,22 @@ int main() {
             const bool r = inc.try_update(v, {v});
             const auto x = inc.get_x();
             std::printf("%d %.17g %s\n", r ? 1 : 0, inc.get(), x.empty() ? "none" : std::to_string(x[0]).c_str());
+        } else if (op == "intfeas" || op == "nodefeas") {
+            int n = 0, k = 0;
+            std::cin >> n >> k;
+            const double tol = num();
+            const auto a = nums(n);
+            const auto b = op == "nodefeas" ? nums(n) : std::vector<double>{};
+            std::vector<int> ints(k);
+            for (int& i : ints) std::cin >> i;
+            bool r;
+            if (op == "intfeas") {
+                r = is_integer_feasible(a, ints, tol);
+            } else {
+                Node nd(0, -1, 0, a, b);
+                r = is_node_feasible(nd, ints, tol);
+            }
+            std::printf("%d\n", r ? 1 : 0);
         } else if (op == "root") {
             std::string kind;
             std::cin >> kind;

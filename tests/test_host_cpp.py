@@ -191,12 +191,13 @@ def test_queue_and_bound_set_match_the_reference_implementation(tmp_path):
 
 
 def test_incumbent_and_root_point_checks_match_the_reference_implementation(tmp_path):
-    """atomic_incumbent.h and tree.h's validate_root_initial_point here
-    against the reference's headers: one random script (incumbent updates
-    with ties, NaN and infinities; root points for box, bounded and equality
-    simplices, a caller's validator and an LMO without a point check, with
-    wrong lengths, bad tolerances, non-finite entries and bound violations)
-    run through the same driver compiled against each (the reference's
+    """atomic_incumbent.h, tree.h's validate_root_initial_point and bnb.h's
+    feasibility predicates here against the reference's headers: one random
+    script (incumbent updates with ties, NaN and infinities; root points for
+    box, bounded and equality simplices, a caller's validator and an LMO
+    without a point check, with wrong lengths, bad tolerances, non-finite
+    entries and bound violations; integer and node feasibility with indices
+    out of range, NaN and values at the tolerance) run through the same driver compiled against each (the reference's
     lmo.cuh through nvcc). The outputs, messages included, are equal."""
     import sys
     sys.path.insert(0, str(ROOT / "tests"))
@@ -229,6 +230,17 @@ def test_incumbent_and_root_point_checks_match_the_reference_implementation(tmp_
         x = [rng.choice(vals) for _ in range(m)]
         head = f"root {kind}" + (f" {rng.choice([1.0, 1.5, 2.0])!r}" if "simplex" in kind else "")
         lines.append(f"{head} {n} {m} {tol!r} " + " ".join(repr(v) for v in lb + ub + x))
+    for _ in range(2000):
+        n = rng.randrange(1, 7)
+        ints = [rng.randrange(-1, n + 1) for _ in range(rng.randrange(0, n + 1))]
+        tol = rng.choice([1e-9, 1e-6, 0.0, 0.3])
+        a = [rng.choice([0.0, 0.5, 1.0, 1e-7, 1.0 - 1e-7, 2.9999999999, float("nan"), -0.25]) for _ in range(n)]
+        tail = " ".join(map(str, ints))
+        if rng.random() < 0.5:
+            lines.append(f"intfeas {n} {len(ints)} {tol!r} " + " ".join(repr(v) for v in a) + " " + tail)
+        else:
+            b = [v + rng.choice([0.0, 1.0, -1e-10, 0.5, -0.5]) for v in a]
+            lines.append(f"nodefeas {n} {len(ints)} {tol!r} " + " ".join(repr(v) for v in a + b) + " " + tail)
     script = "\n".join(lines) + "\n"
     a, b = (subprocess.run([str(e)], input=script, capture_output=True, text=True, check=True).stdout
             for e in (ours, ref))
