@@ -249,6 +249,24 @@ def test_incumbent_and_root_point_checks_match_the_reference_implementation(tmp_
     assert a == b
 
 
+def test_reference_root_point_test_compiles_and_passes_unchanged(tmp_path):
+    """The reference's own CPU test of the root-point checks
+    (tests/test_root_initial_point.cpp of the reference), compiled unchanged
+    against the drop-in headers with g++: it accepts and rejects the same
+    points and prints its success line."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _refdata import reference_path
+    src = reference_path("tests", "test_root_initial_point.cpp")
+    if not src.is_file():
+        pytest.skip("reference tree not available")
+    exe = tmp_path / "root_point"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Root initial-point validation passed" in r.stdout
+
+
 def test_logger_header_drives_like_the_examples(tmp_path):
     """include/gpuboscia/logger.h: the examples' Logger / LoggerParams /
     SolutionStats calls compile warning-free; rows are throttled by the node
