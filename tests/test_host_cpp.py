@@ -1,5 +1,8 @@
 """The C++ drop-in headers on the CPU: the reference's test_cpu.cpp assertions
-(tests/cpp/test_host.cpp) and the host rules against the reference fixtures."""
+(tests/cpp/test_host.cpp), the host rules against the reference fixtures, and,
+where the reference tree is present, live and differential checks against the
+reference's own CPU functions and headers (random cases and operation scripts
+through the same drivers compiled against each)."""
 import json
 import math
 import pathlib
