@@ -219,3 +219,66 @@ def test_equality_simplex_convergence_matrix():
         assert 0 < r["iterations"][0] <= 20000
         if expect:
             assert r["status"][0] in (A.NODE_FRACTIONAL_CONVERGED, A.NODE_INTEGRAL_CONVERGED)
+
+
+def _equality_points(lb, ub, rhs):
+    """Every integer point of {lb <= p <= ub, sum p = rhs}, in the order of
+    the reference's enumerate_integer_equality_points_rec (test_pipeline.cu:
+    409-427: coordinate by coordinate, values ascending)."""
+    out = []
+
+    def rec(j, remaining, point):
+        if j == len(lb):
+            if remaining == 0:
+                out.append(list(point))
+            return
+        value = int(math.ceil(lb[j]))
+        while value <= int(math.floor(ub[j])) and value <= remaining:
+            rec(j + 1, remaining - value, point + [float(value)])
+            value += 1
+
+    rec(0, rhs, [])
+    return out
+
+
+def test_equality_simplex_against_enumeration():
+    """test_pipeline.cu:525-643: EqualitySimplexLMO<6>, rhs 8, all six
+    coordinates integer with bounds lb = (0,1,0,0,1,0), ub = (3,3,2,4,3,4);
+    twelve gradients sin(0.71 (s+1)(j+2)) + 0.17 j - 0.03 s at iterates
+    mixing two enumerated points. The forward vertex attains the enumerated
+    minimum of <g, p>; the in-face vertex of -g attains the maximum over the
+    points on x's face; both are feasible with mass 8; the DICG maximum step
+    along a - v equals the independent ratio formula (1e-10 each)."""
+    n, rhs = 6, 8
+    one_lb = [0.0, 1.0, 0.0, 0.0, 1.0, 0.0]
+    one_ub = [3.0, 3.0, 2.0, 4.0, 3.0, 4.0]
+    feasible = _equality_points(one_lb, one_ub, rhs)
+    assert feasible
+    lmo = api.UnitSimplexLMO(float(rhs), list(range(n)), True)
+    for sample in range(12):
+        p = feasible[(sample * 7 + 1) % len(feasible)]
+        q = feasible[(sample * 13 + len(feasible) // 2) % len(feasible)]
+        alpha = 0.0 if sample % 3 == 0 else (0.35 if sample % 3 == 1 else 0.73)
+        g = np.array([math.sin(0.71 * (sample + 1) * (j + 2)) + 0.17 * j - 0.03 * sample for j in range(n)])
+        x = np.array([(1.0 - alpha) * p[j] + alpha * q[j] for j in range(n)])
+        lb, ub = np.array(one_lb), np.array(one_ub)
+        v, _ = O.lmo_call(lmo, 0, g[None], lb[None], ub[None])
+        a, step = O.lmo_call(lmo, 1, -g[None], lb[None], ub[None], x=x[None], want_step=True)
+        v, a = v[0], a[0]
+        forward_truth = min(float(np.dot(g, pt)) for pt in feasible)
+        face = [pt for pt in feasible
+                if all(not ((abs(x[j] - one_lb[j]) <= 1e-12 and pt[j] != one_lb[j])
+                            or (abs(x[j] - one_ub[j]) <= 1e-12 and pt[j] != one_ub[j])) for j in range(n))]
+        away_truth = max(float(np.dot(g, pt)) for pt in face)
+        assert abs(float(np.dot(g, v)) - forward_truth) <= 1e-10, sample
+        assert abs(float(np.dot(g, a)) - away_truth) <= 1e-10, sample
+        assert np.all(v >= lb - 1e-10) and np.all(v <= ub + 1e-10) and abs(v.sum() - rhs) <= 1e-10
+        assert np.all(a >= lb - 1e-10) and np.all(a <= ub + 1e-10) and abs(a.sum() - rhs) <= 1e-10
+        expected = 1.0
+        for j in range(n):
+            d = a[j] - v[j]
+            if d > 1e-6:
+                expected = min(expected, (x[j] - one_lb[j]) / d)
+            elif d < -1e-6:
+                expected = min(expected, (one_ub[j] - x[j]) / -d)
+        assert abs(step[0] - expected) <= 1e-10, (sample, step[0], expected)
