@@ -270,6 +270,32 @@ def test_reference_root_point_test_compiles_and_passes_unchanged(tmp_path):
     assert "Root initial-point validation passed" in r.stdout
 
 
+def test_interface_defaults_match_the_reference(tmp_path):
+    """Settings, Result, DeviceResidentConfig and LineSearchOptions defaults,
+    the enums' values and name strings, and the scheduling event types: one
+    driver (tests/cpp/defaults_dump.cpp) naming only the reference's fields,
+    compiled against the drop-in headers with g++ and against the reference's
+    gpuboscia.cuh with nvcc, prints the same lines."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _refdata import reference_path
+    from gpuboscia_gb300 import build
+    ref_include = reference_path("include")
+    if not (ref_include / "gpuboscia" / "gpuboscia.cuh").is_file():
+        pytest.skip("reference tree not available")
+    src = ROOT / "tests" / "cpp" / "defaults_dump.cpp"
+    ours, ref = tmp_path / "ours", tmp_path / "ref"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-I", CUDA_INCLUDE,
+                    str(src), "-o", str(ours)], check=True)
+    cu = tmp_path / "defaults_dump.cu"
+    cu.write_text(src.read_text())
+    subprocess.run([str(build._cuda_home() / "bin" / "nvcc"), "-std=c++17", "-O1", "-I", str(ref_include), str(cu),
+                    "-o", str(ref)], check=True)
+    a, b = (subprocess.run([str(e)], capture_output=True, text=True, check=True).stdout for e in (ours, ref))
+    assert a.count("\n") >= 40
+    assert a == b
+
+
 def test_logger_header_drives_like_the_examples(tmp_path):
     """include/gpuboscia/logger.h: the examples' Logger / LoggerParams /
     SolutionStats calls compile warning-free; rows are throttled by the node
