@@ -59,3 +59,27 @@ def test_scheduling_order_as_the_reference_asserts(cuda_lib, scheduling_exe):
     r = subprocess.run([str(scheduling_exe)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "0 failed" in r.stdout
+
+
+@pytest.mark.parametrize("example", ["minimal", "weighted_clique"])
+def test_reference_example_compiles_and_links_unchanged(tmp_path, example):
+    """The reference's own examples/minimal.cu and examples/weighted_clique.cu,
+    unchanged, compile with nvcc against the drop-in headers and link against
+    the library (their models run on the GPU in tests/cpp/minimal_gpu.cpp and
+    test_gpu_weighted_clique.py). examples/main.cu is compiled and run in
+    test_user_objective.py; examples/sparse_sharpe.cu defines its own device
+    LMO, which the precompiled kernels do not take."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _refdata import reference_path
+    from gpuboscia_gb300 import build
+    src = reference_path("examples", f"{example}.cu")
+    if not src.is_file():
+        pytest.skip("reference tree not available")
+    lib = build.build()
+    cuda = build._cuda_home()
+    out = tmp_path / example
+    subprocess.run([str(cuda / "bin" / "nvcc"), "-std=c++17", "-O1", build.ARCH, "-I", str(ROOT / "include"),
+                    str(src), "-o", str(out), "-L", str(lib.parent), "-lgpuboscia_gb300"],
+                   check=True, capture_output=True, text=True)
+    assert out.exists()
