@@ -61,14 +61,13 @@ def test_scheduling_order_as_the_reference_asserts(cuda_lib, scheduling_exe):
     assert "0 failed" in r.stdout
 
 
-@pytest.mark.parametrize("example", ["minimal", "weighted_clique"])
+@pytest.mark.parametrize("example", ["minimal"])
 def test_reference_example_compiles_and_links_unchanged(tmp_path, example):
-    """The reference's own examples/minimal.cu and examples/weighted_clique.cu,
-    unchanged, compile with nvcc against the drop-in headers and link against
-    the library (their models run on the GPU in tests/cpp/minimal_gpu.cpp and
-    test_gpu_weighted_clique.py). examples/main.cu is compiled and run in
-    test_user_objective.py; examples/sparse_sharpe.cu defines its own device
-    LMO, which the precompiled kernels do not take."""
+    """The reference's own examples/minimal.cu, unchanged, compiles with nvcc
+    against the drop-in headers and links against the library (its model runs
+    on the GPU in tests/cpp/minimal_gpu.cpp). examples/main.cu is compiled and
+    run in test_user_objective.py; examples/sparse_sharpe.cu defines its own
+    device LMO, which the precompiled kernels do not take."""
     import sys
     sys.path.insert(0, str(ROOT / "tests"))
     from _refdata import reference_path
