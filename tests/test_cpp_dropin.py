@@ -82,3 +82,32 @@ def test_reference_example_compiles_and_links_unchanged(tmp_path, example):
                     str(src), "-o", str(out), "-L", str(lib.parent), "-lgpuboscia_gb300"],
                    check=True, capture_output=True, text=True)
     assert out.exists()
+
+
+def test_reference_consumer_programs_build_unchanged(tmp_path):
+    """The reference's package-consumer tests (tests/consumer and
+    tests/consumer_cuda of the reference), unchanged, against the drop-in
+    headers: the two host translation units build with g++ -Wall -Werror and
+    the program exits 0 (branch_pow2, quadratic_exact_step and gap_absolute
+    from both units); examples/minimal.cu and consumer_cuda/second.cu build
+    together with nvcc in separable compilation and link against the library
+    (no duplicate definitions across the units)."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _refdata import reference_path
+    from gpuboscia_gb300 import build
+    host = [reference_path("tests", "consumer", f) for f in ("main.cpp", "second.cpp")]
+    cuda_units = [reference_path("examples", "minimal.cu"), reference_path("tests", "consumer_cuda", "second.cu")]
+    if not all(p.is_file() for p in host + cuda_units):
+        pytest.skip("reference tree not available")
+    out = tmp_path / "consumer"
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I", str(ROOT / "include")] + [str(p) for p in host]
+                   + ["-o", str(out)], check=True)
+    assert subprocess.run([str(out)]).returncode == 0
+    lib = build.build()
+    cuda = build._cuda_home()
+    out2 = tmp_path / "consumer_cuda"
+    subprocess.run([str(cuda / "bin" / "nvcc"), "-std=c++17", "-O1", "-rdc=true", build.ARCH, "-I", str(ROOT / "include")]
+                   + [str(p) for p in cuda_units] + ["-o", str(out2), "-L", str(lib.parent), "-lgpuboscia_gb300"],
+                   check=True, capture_output=True, text=True)
+    assert out2.exists()
