@@ -282,3 +282,86 @@ def test_equality_simplex_against_enumeration():
             elif d < -1e-6:
                 expected = min(expected, (one_ub[j] - x[j]) / -d)
         assert abs(step[0] - expected) <= 1e-10, (sample, step[0], expected)
+
+
+def _exhaustive_assignment(order, cost, lb, ub, face=None):
+    """exhaustive_assignment_cost (test_pipeline.cu:165-191): the least cost
+    over permutations within the bounds (and on x's face when given)."""
+    best = math.inf
+    for perm in itertools.permutations(range(order)):
+        ok = True
+        for r in range(order):
+            for c in range(order):
+                e = r * order + c
+                sel = 1.0 if perm[r] == c else 0.0
+                if not (sel >= lb[e] - 1e-12 and sel <= ub[e] + 1e-12 and (face is None or sel == 0.0
+                                                                           or face[e] > 1e-9)):
+                    ok = False
+                    break
+            if not ok:
+                break
+        if ok:
+            best = min(best, sum(cost[r * order + perm[r]] for r in range(order)))
+    return best
+
+
+def test_birkhoff_forward_against_exhaustive_search():
+    """test_pipeline.cu:193-300: order 7, twenty cost matrices
+    sin(0.37 (s+1)(e+2)) + 0.013 e + 0.001 s, arcs off a cyclic matching
+    forbidden where (11 r + 7 c + 3 s) mod 5 = 0, one matching arc forced in
+    two cases out of three. The vertex is a permutation within the bounds and
+    its cost is the exhaustive minimum (1e-10)."""
+    order = 7
+    n = order * order
+    lmo = api.BirkhoffLMO(order)
+    for s in range(20):
+        cost = np.array([math.sin(0.37 * (s + 1) * (e + 2)) + 0.013 * e + 0.001 * s for e in range(n)])
+        lb, ub = np.zeros(n), np.ones(n)
+        for r in range(order):
+            for c in range(order):
+                if c != (r + s) % order and (r * 11 + c * 7 + s * 3) % 5 == 0:
+                    ub[r * order + c] = 0.0
+        if s % 3 != 0:
+            fr = s % order
+            lb[fr * order + (fr + s) % order] = 1.0
+        v, _ = O.lmo_call(lmo, 0, cost[None], lb[None], ub[None])
+        P = v[0].reshape(order, order)
+        assert np.array_equal(P.sum(0), np.ones(order)) and np.array_equal(P.sum(1), np.ones(order))
+        assert np.all(v[0] >= lb - 1e-12) and np.all(v[0] <= ub + 1e-12)
+        assert abs(float(cost @ v[0]) - _exhaustive_assignment(order, cost, lb, ub)) <= 1e-10, s
+
+
+def test_birkhoff_dicg_face_and_step():
+    """test_pipeline.cu:301-407: order 7, twelve iterates mixing two shifted
+    permutations (weights 1 or 0.63/0.37), directions cos(0.29 (s+2)(e+1)) +
+    0.017 e. The in-face vertex stays on x's minimal face and attains the
+    exhaustive minimum over that face; the DICG maximum step along
+    inface(d) - forward(-d) is BirkhoffLMO::dicg_maximum_step_cpu's
+    (lmo.cuh:982-996) within 1e-10."""
+    order = 7
+    n = order * order
+    lmo = api.BirkhoffLMO(order)
+    lb, ub = np.zeros(n), np.ones(n)
+    for s in range(12):
+        sa = s % order
+        sb = (sa + 1 + s % (order - 1)) % order
+        alpha = 0.0 if s % 4 == 0 else 0.37
+        x = np.zeros(n)
+        for r in range(order):
+            x[r * order + (r + sa) % order] += 1.0 - alpha
+            x[r * order + (r + sb) % order] += alpha
+        d = np.array([math.cos(0.29 * (s + 2) * (e + 1)) + 0.017 * e for e in range(n)])
+        a, step = O.lmo_call(lmo, 1, d[None], lb[None], ub[None], x=x[None], want_step=True)
+        fwd, _ = O.lmo_call(lmo, 0, -d[None], lb[None], ub[None])
+        a, fwd = a[0], fwd[0]
+        assert all((x[e] > 1e-9 or abs(a[e]) <= 1e-12) and (x[e] < 1 - 1e-9 or abs(a[e] - 1) <= 1e-12)
+                   for e in range(n)), s
+        assert abs(float(d @ a) - _exhaustive_assignment(order, d, lb, ub, face=x)) <= 1e-10, s
+        pair = a - fwd
+        gamma = 1.0
+        for e in range(n):
+            if pair[e] > 0.0:
+                gamma = min(gamma, (x[e] - lb[e]) / pair[e])
+            elif pair[e] < 0.0:
+                gamma = min(gamma, (ub[e] - x[e]) / -pair[e])
+        assert abs(step[0] - max(0.0, gamma)) <= 1e-10, (s, step[0], gamma)
