@@ -365,3 +365,28 @@ def test_birkhoff_dicg_face_and_step():
             elif pair[e] < 0.0:
                 gamma = min(gamma, (ub[e] - x[e]) / -pair[e])
         assert abs(step[0] - max(0.0, gamma)) <= 1e-10, (s, step[0], gamma)
+
+
+@pytest.mark.parametrize("kind", [A.ALG_FRANK_WOLFE, A.ALG_DICG])
+def test_wide_infeasible_nodes_rejected_first(kind):
+    """test_pipeline.cu:1539-1574: 65 coordinates, a box with the last lower
+    bound 2 above its upper bound 1, an integer coordinate confined to
+    [1.2, 1.8], a simplex whose lower bounds 0.02 sum past the right-hand
+    side 1, and an equality simplex whose upper bounds 0.01 cannot reach it:
+    each node is infeasible, with no iteration and no incumbent candidate."""
+    n = 65
+    obj = api.ILSObjective(np.eye(n), np.zeros(n), 0.0)
+    alg = O.algorithm(kind, A.LS_OPEN_LOOP)
+    lb, ub = np.zeros(n), np.ones(n)
+    lb[-1] = 2.0
+    cases = [(lb.copy(), ub.copy(), np.zeros(n, np.uint8), api.BoxLMO())]
+    lb[-1], ub[-1] = 1.2, 1.8
+    flags = np.zeros(n, np.uint8)
+    flags[-1] = 1
+    cases.append((lb.copy(), ub.copy(), flags, api.BoxLMO()))
+    cases.append((np.full(n, 0.02), np.ones(n), np.zeros(n, np.uint8), api.UnitSimplexLMO(1.0, [])))
+    cases.append((np.zeros(n), np.full(n, 0.01), np.zeros(n, np.uint8), api.EqualitySimplexLMO(1.0, [])))
+    for lo, hi, fl, lmo in cases:
+        r = O.relax(obj, lmo, alg, [lo], [lo], [hi], 1e-12, max_iters=1, flags=fl)
+        assert r["status"][0] == A.NODE_INFEASIBLE and r["iterations"][0] == 0
+        assert r["best_vertex_val"][0] >= 1e299
