@@ -111,3 +111,31 @@ def test_reference_consumer_programs_build_unchanged(tmp_path):
                    + [str(p) for p in cuda_units] + ["-o", str(out2), "-L", str(lib.parent), "-lgpuboscia_gb300"],
                    check=True, capture_output=True, text=True)
     assert out2.exists()
+
+
+def test_solver_api_surface_matches_the_reference(tmp_path):
+    """tests/cpp/solver_api.cpp uses every public member of the reference's
+    DeviceResidentHybridSolver (both constructor forms, push, the progress and
+    scheduling callbacks, solve, every accessor) and both solve entry points
+    with the reference's own types. It compiles and links against the
+    reference's headers (nvcc) and against the drop-in headers and library
+    (g++ -Wall -Werror)."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _refdata import reference_path
+    from gpuboscia_gb300 import build
+    ref_include = reference_path("include")
+    if not (ref_include / "gpuboscia" / "device_resident_solver.cuh").is_file():
+        pytest.skip("reference tree not available")
+    lib = build.build()
+    cuda = build._cuda_home()
+    src = ROOT / "tests" / "cpp" / "solver_api.cpp"
+    ours = tmp_path / "ours"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-I",
+                    str(cuda / "include"), str(src), "-o", str(ours), "-L", str(lib.parent), "-lgpuboscia_gb300",
+                    "-L", str(cuda / "lib64"), "-lcudart", "-lpthread"], check=True)
+    cu = tmp_path / "solver_api.cu"
+    cu.write_text(src.read_text())
+    subprocess.run([str(cuda / "bin" / "nvcc"), "-std=c++17", "-O1", build.ARCH, "-I", str(ref_include), str(cu),
+                    "-o", str(tmp_path / "ref")], check=True, capture_output=True, text=True)
+    assert ours.exists() and (tmp_path / "ref").exists()
