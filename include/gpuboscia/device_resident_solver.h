@@ -57,6 +57,12 @@
                                      std::to_string(__LINE__) + " - " + cudaGetErrorString(_e)); \
     } while (0)
 
+// The reference's name for the same check (device_resident_solver.cuh:114-122),
+// for programs that use it around their own CUDA calls.
+#ifndef DRS_CUDA_CHECK
+#define DRS_CUDA_CHECK(call) GBX_CUDA_CHECK(call)
+#endif
+
 // Per-node status bytes of a relaxation (device_resident_solver.cuh:192-202):
 // the C ABI's GBX_NODE_* values under the reference's names.
 enum DRSNodeState : uint8_t {

@@ -5,5 +5,6 @@
 #pragma once
 #include "gpuboscia.h"
 #ifdef __CUDACC__
+#include "multiblock.cuh"
 #include "user_relax.cuh"
 #endif

@@ -61,18 +61,22 @@ def test_scheduling_order_as_the_reference_asserts(cuda_lib, scheduling_exe):
     assert "0 failed" in r.stdout
 
 
-@pytest.mark.parametrize("example", ["minimal"])
-def test_reference_example_compiles_and_links_unchanged(tmp_path, example):
-    """The reference's own examples/minimal.cu, unchanged, compiles with nvcc
-    against the drop-in headers and links against the library (its model runs
-    on the GPU in tests/cpp/minimal_gpu.cpp). examples/main.cu is compiled and
-    run in test_user_objective.py; examples/sparse_sharpe.cu defines its own
-    device LMO, which the precompiled kernels do not take."""
+@pytest.mark.parametrize("where,name", [("examples", "minimal.cu"), ("tests", "test_root_initial_point.cu")])
+def test_reference_example_compiles_and_links_unchanged(tmp_path, where, name):
+    """The reference's own examples/minimal.cu and tests/test_root_initial_point.cu
+    (a device objective with the optional grad_multiblock member, the
+    reference's DRS_CUDA_CHECK and DRS_HAS_MULTIBLOCK_ATOMICS), unchanged,
+    compile with nvcc against the drop-in headers and link against the
+    library (minimal.cu's model runs on the GPU in tests/cpp/minimal_gpu.cpp).
+    examples/main.cu is compiled and run in test_user_objective.py;
+    examples/sparse_sharpe.cu defines its own device LMO, which the
+    precompiled kernels do not take."""
     import sys
     sys.path.insert(0, str(ROOT / "tests"))
     from _refdata import reference_path
     from gpuboscia_gb300 import build
-    src = reference_path("examples", f"{example}.cu")
+    src = reference_path(where, name)
+    example = name.split(".")[0]
     if not src.is_file():
         pytest.skip("reference tree not available")
     lib = build.build()
