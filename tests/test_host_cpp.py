@@ -440,6 +440,27 @@ def test_every_reference_header_name_compiles_alone(tmp_path, name):
                     "-I", CUDA_INCLUDE, str(src)], check=True)
 
 
+def test_every_reference_header_name_compiles_alone_under_nvcc(tmp_path):
+    """The same one-include programs as CUDA translation units (the way the
+    reference's users compile them): each compiles with nvcc for sm_103a,
+    which also brings in the device-side names (MultiBlockContext, the
+    template relaxation of user objectives)."""
+    import concurrent.futures as cf
+    from gpuboscia_gb300 import build
+    nvcc = str(build._cuda_home() / "bin" / "nvcc")
+
+    def one(name):
+        src = tmp_path / f"{name.replace('.', '_')}.cu"
+        src.write_text(f"#include <gpuboscia/{name}>\nint main() {{ return 0; }}\n")
+        r = subprocess.run([nvcc, "-std=c++17", build.ARCH, "-I", str(ROOT / "include"), "-c", str(src), "-o",
+                            str(src.with_suffix(".o"))], capture_output=True, text=True)
+        return name, r.returncode, r.stderr[-2000:]
+
+    with cf.ThreadPoolExecutor(max_workers=8) as ex:
+        for name, rc, err in ex.map(one, REFERENCE_HEADERS):
+            assert rc == 0, (name, err)
+
+
 def test_node_selection_policies(tmp_path):
     src = tmp_path / "sel.cpp"
     src.write_text(r'''
