@@ -83,7 +83,12 @@ int ref_birkhoff_lmo(int order, int mode, const double* cost, const double* x,
     case 8: return birkhoff<8>(mode, cost, x, lb, ub, out);
     case 12: return birkhoff<12>(mode, cost, x, lb, ub, out);
     case 16: return birkhoff<16>(mode, cost, x, lb, ub, out);
+    case 32: return birkhoff<32>(mode, cost, x, lb, ub, out);
+    case 33: return birkhoff<33>(mode, cost, x, lb, ub, out);
     case 36: return birkhoff<36>(mode, cost, x, lb, ub, out);
+    case 97: return birkhoff<97>(mode, cost, x, lb, ub, out);
+    case 120: return birkhoff<120>(mode, cost, x, lb, ub, out);
+    case 129: return birkhoff<129>(mode, cost, x, lb, ub, out);
     default: return -1;
     }
 }

@@ -163,3 +163,38 @@ def test_live_birkhoff_inface_forced_forbidden_against_reference():
             assert np.array_equal(ours[0], out), (order, mode)
             calls += 1
     assert calls == 600
+
+
+@pytest.mark.skipif(O.ref() is None, reason="reference tree not available at build time")
+@pytest.mark.parametrize("order", [32, 33, 97, 120, 129])
+def test_live_large_order_birkhoff_against_reference(order):
+    """The orders of the reference's LMO benchmark check (32, 33, 97, 129)
+    and the order-120 workload: forward and in-face vertices under 30 %
+    forbidden arcs, a few forced pairs and tied costs, bit-identical to the
+    reference's CPU Hungarian."""
+    R = O.ref()
+    rng = np.random.default_rng(order)
+    n = order * order
+    lmo = api.BirkhoffLMO(order)
+    for _ in range(4):
+        cost = rng.integers(-8, 9, n) / 4.0
+        lb, ub = np.zeros(n), np.ones(n)
+        p = rng.permutation(order)
+        forbid = rng.random(n) < 0.3
+        forbid[np.arange(order) * order + p] = False
+        ub[forbid] = 0.0
+        lb[np.arange(order) * order + p] = (rng.random(order) < 0.05).astype(float)
+        x = np.zeros(n)
+        for w in (0.6, 0.4):
+            q = p.copy()
+            a, b = rng.choice(order, 2, replace=False)
+            if ub[a * order + p[b]] > 0 and ub[b * order + p[a]] > 0 and lb[a * order + p[a]] == 0 \
+                    and lb[b * order + p[b]] == 0:
+                q[a], q[b] = p[b], p[a]
+            x[np.arange(order) * order + q] += w
+        for mode in (0, 1):
+            out = np.zeros(n)
+            assert R.ref_birkhoff_lmo(order, mode, cost.ctypes.data, x.ctypes.data if mode else None,
+                                      lb.ctypes.data, ub.ctypes.data, out.ctypes.data) == 0
+            ours, _ = O.lmo_call(lmo, mode, cost[None], lb[None], ub[None], x=x[None] if mode else None)
+            assert np.array_equal(ours[0], out), mode
