@@ -89,6 +89,7 @@ int ref_birkhoff_lmo(int order, int mode, const double* cost, const double* x,
     case 97: return birkhoff<97>(mode, cost, x, lb, ub, out);
     case 120: return birkhoff<120>(mode, cost, x, lb, ub, out);
     case 129: return birkhoff<129>(mode, cost, x, lb, ub, out);
+    case 400: return birkhoff<400>(mode, cost, x, lb, ub, out);
     default: return -1;
     }
 }

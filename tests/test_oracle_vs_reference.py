@@ -166,10 +166,10 @@ def test_live_birkhoff_inface_forced_forbidden_against_reference():
 
 
 @pytest.mark.skipif(O.ref() is None, reason="reference tree not available at build time")
-@pytest.mark.parametrize("order", [32, 33, 97, 120, 129])
+@pytest.mark.parametrize("order", [32, 33, 97, 120, 129, 400])
 def test_live_large_order_birkhoff_against_reference(order):
     """The orders of the reference's LMO benchmark check (32, 33, 97, 129)
-    and the order-120 workload: forward and in-face vertices under 30 %
+    and the order-120 and order-400 workloads: forward and in-face vertices under 30 %
     forbidden arcs, a few forced pairs and tied costs, bit-identical to the
     reference's CPU Hungarian."""
     R = O.ref()
