@@ -837,7 +837,7 @@ public:
                                DeviceResidentConfig cfg = {}, LMO lmo = {},
                                double time_limit_seconds = std::numeric_limits<double>::infinity(),
                                Heuristic = {})
-        : BnBEngine(check_size(prob), objective_descriptor(obj), lmo.spec(prob.n_vars), alg.descriptor(),
+        : BnBEngine(prob, objective_descriptor(obj), lmo.spec(prob.n_vars), alg.descriptor(),
                     std::move(branch_sel), cfg, time_limit_seconds, hooks_for(obj)) {}
 
 private:
@@ -855,10 +855,5 @@ private:
     static gpuboscia::RelaxHooks hooks_for(const DeviceObjective& obj) {
         if constexpr (gpuboscia::HasDescriptor<DeviceObjective>::value) return {};
         else return gpuboscia::UserRelax<DeviceObjective>::hooks(obj);
-    }
-    static const Problem& check_size(const Problem& prob) {
-        if (prob.n_vars != DeviceObjective::n_vars)
-            throw std::runtime_error("DeviceObjective::n_vars does not match Problem::n_vars");
-        return prob;
     }
 };

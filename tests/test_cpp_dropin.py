@@ -143,3 +143,34 @@ def test_solver_api_surface_matches_the_reference(tmp_path):
     subprocess.run([str(cuda / "bin" / "nvcc"), "-std=c++17", "-O1", build.ARCH, "-I", str(ref_include), str(cu),
                     "-o", str(tmp_path / "ref")], check=True, capture_output=True, text=True)
     assert ours.exists() and (tmp_path / "ref").exists()
+
+
+def test_configuration_checks_match_the_reference(tmp_path):
+    """The solver constructor's checks on its configuration (counts,
+    integer indices, tolerances, time limit, objective size), which run
+    before any CUDA call: tests/cpp/config_checks.cpp builds the solver with
+    20 bad configurations against the reference's headers (nvcc) and against
+    the drop-in (g++), and the exception type, message and the order in which
+    two failing checks are reported are the same."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _refdata import reference_path
+    from gpuboscia_gb300 import build
+    ref_include = reference_path("include")
+    if not (ref_include / "gpuboscia" / "device_resident_solver.cuh").is_file():
+        pytest.skip("reference tree not available")
+    lib = build.build()
+    cuda = build._cuda_home()
+    src = ROOT / "tests" / "cpp" / "config_checks.cpp"
+    ours, ref = tmp_path / "ours", tmp_path / "ref"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-I",
+                    str(cuda / "include"), str(src), "-o", str(ours), "-L", str(lib.parent), "-lgpuboscia_gb300",
+                    "-Wl,-rpath," + str(lib.parent), "-L", str(cuda / "lib64"), "-lcudart",
+                    "-Wl,-rpath," + str(cuda / "lib64"), "-lpthread"], check=True)
+    cu = tmp_path / "config_checks.cu"
+    cu.write_text(src.read_text())
+    subprocess.run([str(cuda / "bin" / "nvcc"), "-std=c++17", "-O1", build.ARCH, "-I", str(ref_include), str(cu),
+                    "-o", str(ref)], check=True, capture_output=True, text=True)
+    a, b = (subprocess.run([str(e)], capture_output=True, text=True, check=True).stdout for e in (ours, ref))
+    assert a.count("\n") == 20 and "accepted" not in a
+    assert a == b
