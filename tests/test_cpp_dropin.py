@@ -174,3 +174,31 @@ def test_configuration_checks_match_the_reference(tmp_path):
     a, b = (subprocess.run([str(e)], capture_output=True, text=True, check=True).stdout for e in (ours, ref))
     assert a.count("\n") == 20 and "accepted" not in a
     assert a == b
+
+
+def test_solve_argument_checks_match_the_reference(tmp_path):
+    """gpuboscia::solve's checks (algorithm and line-search combinations,
+    quadratic-exact without curvature support, the root point, the solver's
+    configuration) and the order in which they are reported:
+    tests/cpp/solve_checks.cpp, compiled with nvcc against the reference's
+    headers and against the drop-in, prints the same 14 lines."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _refdata import reference_path
+    from gpuboscia_gb300 import build
+    ref_include = reference_path("include")
+    if not (ref_include / "gpuboscia" / "gpuboscia.cuh").is_file():
+        pytest.skip("reference tree not available")
+    lib = build.build()
+    nvcc = str(build._cuda_home() / "bin" / "nvcc")
+    cu = tmp_path / "solve_checks.cu"
+    cu.write_text((ROOT / "tests" / "cpp" / "solve_checks.cpp").read_text())
+    ours, ref = tmp_path / "ours", tmp_path / "ref"
+    subprocess.run([nvcc, "-std=c++17", "-O1", build.ARCH, "-I", str(ROOT / "include"), str(cu), "-o", str(ours),
+                    "-L", str(lib.parent), "-lgpuboscia_gb300", "-Xlinker", "-rpath", "-Xlinker", str(lib.parent)],
+                   check=True, capture_output=True, text=True)
+    subprocess.run([nvcc, "-std=c++17", "-O1", build.ARCH, "-I", str(ref_include), str(cu), "-o", str(ref)],
+                   check=True, capture_output=True, text=True)
+    a, b = (subprocess.run([str(e)], capture_output=True, text=True, check=True).stdout for e in (ours, ref))
+    assert a.count("\n") == 14 and "returned" not in a
+    assert a == b
