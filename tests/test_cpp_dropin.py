@@ -12,6 +12,15 @@ import pytest
 ROOT = pathlib.Path(__file__).resolve().parent.parent
 
 
+def _compile_all(cmds):
+    """Runs the compile commands side by side (each nvcc front end is single
+    threaded) and fails on the first that does not succeed."""
+    import concurrent.futures as cf
+    with cf.ThreadPoolExecutor(max_workers=len(cmds)) as ex:
+        for r in ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), cmds):
+            assert r.returncode == 0, r.stderr[-3000:]
+
+
 def _program(tmp_path_factory, name):
     from gpuboscia_gb300 import build
     lib = build.build()
@@ -117,88 +126,76 @@ def test_reference_consumer_programs_build_unchanged(tmp_path):
     assert out2.exists()
 
 
-def test_solver_api_surface_matches_the_reference(tmp_path):
+@pytest.fixture(scope="module")
+def differential_programs(tmp_path_factory):
+    """The differential drivers of tests/cpp, each built against the
+    reference's headers (nvcc) and against the drop-in headers and library,
+    all six compiles side by side. Skips without the reference tree."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _refdata import reference_path
+    from gpuboscia_gb300 import build
+    ref_include = reference_path("include")
+    if not (ref_include / "gpuboscia" / "device_resident_solver.cuh").is_file():
+        pytest.skip("reference tree not available")
+    lib = build.build()
+    cuda = build._cuda_home()
+    nvcc = str(cuda / "bin" / "nvcc")
+    out = tmp_path_factory.mktemp("differential")
+    link = ["-L", str(lib.parent), "-lgpuboscia_gb300", "-L", str(cuda / "lib64"), "-lcudart", "-lpthread"]
+    rpath = ["-Wl,-rpath," + str(lib.parent), "-Wl,-rpath," + str(cuda / "lib64")]
+    cmds, exes = [], {}
+    for name, ours_with_nvcc in (("solver_api", False), ("config_checks", False), ("solve_checks", True)):
+        src = ROOT / "tests" / "cpp" / f"{name}.cpp"
+        cu = out / f"{name}.cu"
+        cu.write_text(src.read_text())
+        exes[name] = (out / f"{name}_ours", out / f"{name}_ref")
+        if ours_with_nvcc:   # a device objective of its own: nvcc on both sides
+            cmds.append([nvcc, "-std=c++17", "-O1", build.ARCH, "-I", str(ROOT / "include"), str(cu), "-o",
+                         str(exes[name][0]), "-L", str(lib.parent), "-lgpuboscia_gb300", "-Xlinker", "-rpath",
+                         "-Xlinker", str(lib.parent)])
+        else:
+            cmds.append(["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-I",
+                         str(cuda / "include"), str(src), "-o", str(exes[name][0])] + link + rpath)
+        cmds.append([nvcc, "-std=c++17", "-O1", build.ARCH, "-I", str(ref_include), str(cu), "-o",
+                     str(exes[name][1])])
+    _compile_all(cmds)
+    return exes
+
+
+def _both_outputs(exes):
+    return [subprocess.run([str(e)], capture_output=True, text=True, check=True).stdout for e in exes]
+
+
+def test_solver_api_surface_matches_the_reference(differential_programs):
     """tests/cpp/solver_api.cpp uses every public member of the reference's
     DeviceResidentHybridSolver (both constructor forms, push, the progress and
     scheduling callbacks, solve, every accessor) and both solve entry points
     with the reference's own types. It compiles and links against the
     reference's headers (nvcc) and against the drop-in headers and library
     (g++ -Wall -Werror)."""
-    import sys
-    sys.path.insert(0, str(ROOT / "tests"))
-    from _refdata import reference_path
-    from gpuboscia_gb300 import build
-    ref_include = reference_path("include")
-    if not (ref_include / "gpuboscia" / "device_resident_solver.cuh").is_file():
-        pytest.skip("reference tree not available")
-    lib = build.build()
-    cuda = build._cuda_home()
-    src = ROOT / "tests" / "cpp" / "solver_api.cpp"
-    ours = tmp_path / "ours"
-    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-I",
-                    str(cuda / "include"), str(src), "-o", str(ours), "-L", str(lib.parent), "-lgpuboscia_gb300",
-                    "-L", str(cuda / "lib64"), "-lcudart", "-lpthread"], check=True)
-    cu = tmp_path / "solver_api.cu"
-    cu.write_text(src.read_text())
-    subprocess.run([str(cuda / "bin" / "nvcc"), "-std=c++17", "-O1", build.ARCH, "-I", str(ref_include), str(cu),
-                    "-o", str(tmp_path / "ref")], check=True, capture_output=True, text=True)
-    assert ours.exists() and (tmp_path / "ref").exists()
+    ours, ref = differential_programs["solver_api"]
+    assert ours.exists() and ref.exists()
 
 
-def test_configuration_checks_match_the_reference(tmp_path):
+def test_configuration_checks_match_the_reference(differential_programs):
     """The solver constructor's checks on its configuration (counts,
     integer indices, tolerances, time limit, objective size), which run
     before any CUDA call: tests/cpp/config_checks.cpp builds the solver with
     20 bad configurations against the reference's headers (nvcc) and against
     the drop-in (g++), and the exception type, message and the order in which
     two failing checks are reported are the same."""
-    import sys
-    sys.path.insert(0, str(ROOT / "tests"))
-    from _refdata import reference_path
-    from gpuboscia_gb300 import build
-    ref_include = reference_path("include")
-    if not (ref_include / "gpuboscia" / "device_resident_solver.cuh").is_file():
-        pytest.skip("reference tree not available")
-    lib = build.build()
-    cuda = build._cuda_home()
-    src = ROOT / "tests" / "cpp" / "config_checks.cpp"
-    ours, ref = tmp_path / "ours", tmp_path / "ref"
-    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-I",
-                    str(cuda / "include"), str(src), "-o", str(ours), "-L", str(lib.parent), "-lgpuboscia_gb300",
-                    "-Wl,-rpath," + str(lib.parent), "-L", str(cuda / "lib64"), "-lcudart",
-                    "-Wl,-rpath," + str(cuda / "lib64"), "-lpthread"], check=True)
-    cu = tmp_path / "config_checks.cu"
-    cu.write_text(src.read_text())
-    subprocess.run([str(cuda / "bin" / "nvcc"), "-std=c++17", "-O1", build.ARCH, "-I", str(ref_include), str(cu),
-                    "-o", str(ref)], check=True, capture_output=True, text=True)
-    a, b = (subprocess.run([str(e)], capture_output=True, text=True, check=True).stdout for e in (ours, ref))
+    a, b = _both_outputs(differential_programs["config_checks"])
     assert a.count("\n") == 20 and "accepted" not in a
     assert a == b
 
 
-def test_solve_argument_checks_match_the_reference(tmp_path):
+def test_solve_argument_checks_match_the_reference(differential_programs):
     """gpuboscia::solve's checks (algorithm and line-search combinations,
     quadratic-exact without curvature support, the root point, the solver's
     configuration) and the order in which they are reported:
     tests/cpp/solve_checks.cpp, compiled with nvcc against the reference's
     headers and against the drop-in, prints the same 14 lines."""
-    import sys
-    sys.path.insert(0, str(ROOT / "tests"))
-    from _refdata import reference_path
-    from gpuboscia_gb300 import build
-    ref_include = reference_path("include")
-    if not (ref_include / "gpuboscia" / "gpuboscia.cuh").is_file():
-        pytest.skip("reference tree not available")
-    lib = build.build()
-    nvcc = str(build._cuda_home() / "bin" / "nvcc")
-    cu = tmp_path / "solve_checks.cu"
-    cu.write_text((ROOT / "tests" / "cpp" / "solve_checks.cpp").read_text())
-    ours, ref = tmp_path / "ours", tmp_path / "ref"
-    subprocess.run([nvcc, "-std=c++17", "-O1", build.ARCH, "-I", str(ROOT / "include"), str(cu), "-o", str(ours),
-                    "-L", str(lib.parent), "-lgpuboscia_gb300", "-Xlinker", "-rpath", "-Xlinker", str(lib.parent)],
-                   check=True, capture_output=True, text=True)
-    subprocess.run([nvcc, "-std=c++17", "-O1", build.ARCH, "-I", str(ref_include), str(cu), "-o", str(ref)],
-                   check=True, capture_output=True, text=True)
-    a, b = (subprocess.run([str(e)], capture_output=True, text=True, check=True).stdout for e in (ours, ref))
+    a, b = _both_outputs(differential_programs["solve_checks"])
     assert a.count("\n") == 14 and "returned" not in a
     assert a == b
